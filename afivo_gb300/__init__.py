@@ -1,0 +1,434 @@
+"""afivo_gb300: GB300 (sm_103a) FAS multigrid for Poisson problems on
+quadtree/octree block grids, behind the C ABI of include/afivo_gb300.h.
+
+This module is the Python host side of that ABI. Its names follow the Afivo
+reference's Fortran API for this path:
+
+=========================  ===============================================
+here                       reference (src/...)
+=========================  ===============================================
+``a2_init`` / ``a3_init``  ``a$D_init`` (m_aX_core.f90:24-131)
+``Tree.set_base``          ``a$D_set_base`` (m_aX_core.f90:152-235)
+``Tree.adjust_refinement`` ``a$D_adjust_refinement`` (m_aX_core.f90:452-541)
+``Forest``                 the device copy of one or more ``a$D_t`` trees
+``mg2_init_mg``            ``mg$D_init_mg`` (m_aX_mg.f90:130-154)
+``mg2_fas_vcycle``         ``mg$D_fas_vcycle`` (m_aX_mg.f90:208-255)
+``mg2_fas_fmg``            ``mg$D_fas_fmg`` (m_aX_mg.f90:164-203)
+``a2_gc_tree``             ``a$D_gc_tree`` (m_aX_gc.f90:28-46)
+``a2_tree_max_abs_cc``     ``a$D_tree_max_cc``/``min_cc`` (m_aX_utils.f90:468-571)
+=========================  ===============================================
+
+Errors: every C call returns a status; a negative status raises AfivoError
+with the library's message (the reference calls ``stop`` instead).
+The CUDA library must have been built (``afivo_gb300.build.build()``); there is
+no CPU fallback.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libafivo_gb300.so")
+
+AFV_OK = 0
+AFV_ERR_INVALID, AFV_ERR_CUDA, AFV_ERR_NOMEM = -1, -2, -3
+AFV_ERR_UNSUPPORTED, AFV_ERR_TIMEOUT, AFV_ERR_STATE, AFV_ERR_BUDGET = -4, -5, -6, -7
+AFV_RM_REF, AFV_KEEP_REF, AFV_DO_REF = -1, 0, 1
+AFV_PHI, AFV_RHS, AFV_TMP = 0, 1, 2
+AFV_BC_DIRICHLET, AFV_BC_NEUMANN = -1, -2
+AFV_REF_UNIFORM, AFV_REF_SOURCE, AFV_REF_RANDOM, AFV_REF_RANDOM_RM = 0, 1, 2, 3
+AFV_PREC_FP64, AFV_PREC_MIXED = 0, 1
+KERNEL_KINDS = ("sweep", "fill", "restrict", "coarse_rhs", "correct", "residual", "defect",
+                "accumulate")
+
+# Refinement flags under the reference's names (src/m_aX_t.f90:17-24)
+a5_rm_ref, a5_keep_ref, a5_do_ref = AFV_RM_REF, AFV_KEEP_REF, AFV_DO_REF
+a5_bc_dirichlet, a5_bc_neumann = AFV_BC_DIRICHLET, AFV_BC_NEUMANN
+
+
+class AfivoError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"afivo_gb300 error {code}: {msg}")
+        self.code = code
+
+
+class BoxView(ctypes.Structure):
+    _fields_ = [("id", ctypes.c_int), ("lvl", ctypes.c_int), ("n_cell", ctypes.c_int),
+                ("dim", ctypes.c_int), ("ix", ctypes.c_int * 3), ("dr", ctypes.c_double),
+                ("r_min", ctypes.c_double * 3), ("pass_", ctypes.c_int)]
+
+
+REF_FN = ctypes.CFUNCTYPE(None, ctypes.POINTER(BoxView), ctypes.POINTER(ctypes.c_int),
+                          ctypes.c_void_p)
+
+
+class RefCrit(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int), ("lvl_max", ctypes.c_int), ("thr", ctypes.c_double),
+                ("prob", ctypes.c_double), ("seed", ctypes.c_ulonglong),
+                ("src_lpl", ctypes.c_int), ("n_gauss", ctypes.c_int),
+                ("gauss", ctypes.POINTER(ctypes.c_double))]
+
+
+class MgOpts(ctypes.Structure):
+    """The mg$D_t options of src/m_aX_mg.f90:20-52 (cycle counts)."""
+    _fields_ = [("n_cycle_down", ctypes.c_int), ("n_cycle_up", ctypes.c_int),
+                ("n_cycle_base", ctypes.c_int)]
+
+    def __init__(self, n_cycle_down=-1, n_cycle_up=-1, n_cycle_base=-1):
+        super().__init__(n_cycle_down, n_cycle_up, n_cycle_base)
+
+
+class ForestOpts(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int), ("mixed_buffers", ctypes.c_int)]
+
+
+_lib = None
+
+
+def lib():
+    """Load the in-tree CUDA library; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is missing: build it with afivo_gb300.build.build()")
+        L = ctypes.CDLL(LIB_PATH)
+        P = ctypes.c_void_p
+        I = ctypes.c_int
+        Dd = ctypes.c_double
+        ip = ctypes.POINTER(I)
+        dp = ctypes.POINTER(Dd)
+        llp = ctypes.POINTER(ctypes.c_longlong)
+        sig = {
+            "afv_last_error": (ctypes.c_char_p, []),
+            "afv_version": (I, []),
+            "afv_tree_create": (I, [I, I, Dd, dp, I, I, Dd, ctypes.POINTER(P)]),
+            "afv_tree_set_base": (I, [P, I, ip, ip]),
+            "afv_tree_adjust_refinement": (I, [P, REF_FN, P, ip, ip]),
+            "afv_tree_adjust_builtin": (I, [P, ctypes.POINTER(RefCrit), ip, ip]),
+            "afv_tree_refine_builtin": (I, [P, ctypes.POINTER(RefCrit), I, ip]),
+            "afv_tree_destroy": (None, [P]),
+            "afv_tree_get_info": (I, [P, ip]),
+            "afv_tree_export": (I, [P, ip, ip, ip, ip, ip, ip, dp, dp, ip]),
+            "afv_tree_level": (I, [P, I, ip, ip, ip, ip]),
+            "afv_forest_create": (I, [I, ctypes.POINTER(P), ctypes.POINTER(ForestOpts),
+                                      ctypes.POINTER(P)]),
+            "afv_forest_destroy": (None, [P]),
+            "afv_forest_get_info": (I, [P, llp]),
+            "afv_forest_set_var": (I, [P, I, I, dp, I]),
+            "afv_forest_get_var": (I, [P, I, I, dp, I]),
+            "afv_forest_set_source": (I, [P, I, I, I, dp]),
+            "afv_forest_set_bc": (I, [P, I, I, I, I, dp]),
+            "afv_forest_zero": (I, [P, I]),
+            "afv_forest_sync": (I, [P]),
+            "afv_forest_get_stream": (I, [P, ctypes.POINTER(P)]),
+            "afv_mg_init": (I, [ctypes.POINTER(MgOpts)]),
+            "afv_mg_fas_vcycle": (I, [P, ctypes.POINTER(MgOpts), I, I]),
+            "afv_mg_fas_fmg": (I, [P, ctypes.POINTER(MgOpts), I, I]),
+            "afv_gc_tree": (I, [P]),
+            "afv_tree_max_abs_cc": (I, [P, I, I, dp]),
+            "afv_mg_solve": (I, [P, ctypes.POINTER(MgOpts), I, Dd, I, ip, dp]),
+            "afv_mg_gsrb_level": (I, [P, I, I]),
+            "afv_fill_gc_level": (I, [P, I]),
+            "afv_mg_update_coarse": (I, [P, I]),
+            "afv_mg_correct_children": (I, [P, I]),
+            "afv_mg_residual_all": (I, [P]),
+            "afv_forest_profile": (I, [P, I]),
+            "afv_forest_profile_read": (I, [P, I, llp, dp, dp]),
+        }
+        for name, (res, args) in sig.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _check(rc):
+    if rc != AFV_OK:
+        raise AfivoError(rc, lib().afv_last_error().decode())
+    return rc
+
+
+def _ip(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _crit(kind, lvl_max, thr=0.0, prob=0.0, seed=0, gauss=None, lpl=False):
+    g = None if gauss is None else np.ascontiguousarray(gauss, dtype=np.float64)
+    c = RefCrit(kind, lvl_max, thr, prob, seed, int(lpl), 0, None)
+    if g is not None:
+        c.gauss = _dp(g)
+    return c, g
+
+
+class Tree:
+    """Host tree of NxN(xN) boxes, the reference's a$D_t (src/m_aX_t.f90:189-207)."""
+
+    def __init__(self, dim, n_cell, dr, r_min=None, lvl_limit=30, coarsen_to=-1,
+                 mem_limit_gb=64.0):
+        self.dim = dim
+        rm = np.zeros(dim) if r_min is None else np.ascontiguousarray(r_min, dtype=np.float64)
+        h = ctypes.c_void_p()
+        _check(lib().afv_tree_create(dim, n_cell, float(dr), _dp(rm), lvl_limit, coarsen_to,
+                                     float(mem_limit_gb), ctypes.byref(h)))
+        self.h = h
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.afv_tree_destroy(self.h)
+            self.h = None
+
+    def set_base(self, ix_list, nb_list):
+        ix = np.ascontiguousarray(np.asarray(ix_list, dtype=np.int32).reshape(-1, self.dim))
+        nb = np.ascontiguousarray(np.asarray(nb_list, dtype=np.int32).reshape(-1, 2 * self.dim))
+        _check(lib().afv_tree_set_base(self.h, ix.shape[0], _ip(ix), _ip(nb)))
+        return self
+
+    def adjust_refinement(self, ref_fn):
+        """One a$D_adjust_refinement pass with a Python ref_subr(box, flag) -> flag."""
+        def cb(view_p, flag_p, _user):
+            v = view_p.contents
+            flag_p[0] = int(ref_fn(v, flag_p[0]))
+        c = REF_FN(cb)
+        na, nr = ctypes.c_int(0), ctypes.c_int(0)
+        _check(lib().afv_tree_adjust_refinement(self.h, c, None, ctypes.byref(na), ctypes.byref(nr)))
+        return na.value, nr.value
+
+    def adjust_builtin(self, kind, lvl_max, thr=0.0, prob=0.0, seed=0, gauss=None, lpl=False):
+        c, _keep = _crit(kind, lvl_max, thr, prob, seed, gauss, lpl)
+        if gauss is not None:
+            c.n_gauss = len(gauss) // (2 + self.dim)
+        na, nr = ctypes.c_int(0), ctypes.c_int(0)
+        _check(lib().afv_tree_adjust_builtin(self.h, ctypes.byref(c), ctypes.byref(na),
+                                             ctypes.byref(nr)))
+        return na.value, nr.value
+
+    def refine_builtin(self, kind, lvl_max, thr=0.0, prob=0.0, seed=0, gauss=None, lpl=False,
+                       max_passes=100):
+        c, _keep = _crit(kind, lvl_max, thr, prob, seed, gauss, lpl)
+        if gauss is not None:
+            c.n_gauss = len(gauss) // (2 + self.dim)
+        n = ctypes.c_int(0)
+        _check(lib().afv_tree_refine_builtin(self.h, ctypes.byref(c), max_passes, ctypes.byref(n)))
+        return n.value
+
+    def info(self):
+        out = np.zeros(8, np.int32)
+        _check(lib().afv_tree_get_info(self.h, _ip(out)))
+        keys = ("dim", "n_cell", "min_lvl", "highest_lvl", "highest_id", "n_boxes", "n_leaves",
+                "lvl_limit")
+        return dict(zip(keys, (int(x) for x in out)))
+
+    @property
+    def min_lvl(self):
+        return self.info()["min_lvl"]
+
+    @property
+    def highest_lvl(self):
+        return self.info()["highest_lvl"]
+
+    def boxes(self):
+        n, D = self.info()["highest_id"], self.dim
+        out = dict(lvl=np.zeros(n, np.int32), ix=np.zeros((n, D), np.int32),
+                   parent=np.zeros(n, np.int32), children=np.zeros((n, 2 ** D), np.int32),
+                   neighbors=np.zeros((n, 2 * D), np.int32), n_cell=np.zeros(n, np.int32),
+                   dr=np.zeros(n), r_min=np.zeros((n, D)), in_use=np.zeros(n, np.int32))
+        _check(lib().afv_tree_export(self.h, _ip(out["lvl"]), _ip(out["ix"]), _ip(out["parent"]),
+                                     _ip(out["children"]), _ip(out["neighbors"]),
+                                     _ip(out["n_cell"]), _dp(out["dr"]), _dp(out["r_min"]),
+                                     _ip(out["in_use"])))
+        return out
+
+    def level(self, lvl):
+        sz = np.zeros(3, np.int32)
+        _check(lib().afv_tree_level(self.h, lvl, _ip(sz), None, None, None))
+        ids, lv, pa = (np.zeros(max(int(s), 1), np.int32) for s in sz)
+        _check(lib().afv_tree_level(self.h, lvl, _ip(sz), _ip(ids), _ip(lv), _ip(pa)))
+        return ids[:sz[0]].copy(), lv[:sz[1]].copy(), pa[:sz[2]].copy()
+
+    def n_cell_at(self, lvl):
+        nc = self.info()["n_cell"]
+        return nc if lvl >= 1 else nc >> (1 - lvl)
+
+    def leaf_cells(self):
+        i = self.info()
+        return i["n_leaves"] * i["n_cell"] ** self.dim
+
+
+def a2_init(n_cell, dr, r_min=None, lvl_limit=30, coarsen_to=-1, mem_limit_gb=64.0):
+    """a2_init (src/m_aX_core.f90:24-131) for phi, rhs and tmp."""
+    return Tree(2, n_cell, dr, r_min, lvl_limit, coarsen_to, mem_limit_gb)
+
+
+def a3_init(n_cell, dr, r_min=None, lvl_limit=30, coarsen_to=-1, mem_limit_gb=64.0):
+    """a3_init (src/m_aX_core.f90:24-131) for phi, rhs and tmp."""
+    return Tree(3, n_cell, dr, r_min, lvl_limit, coarsen_to, mem_limit_gb)
+
+
+class Forest:
+    """One or more trees resident on a GPU, swept together by every launch."""
+
+    def __init__(self, trees, device=0, mixed=False):
+        self.trees = list(trees)
+        self.dim = self.trees[0].dim
+        arr = (ctypes.c_void_p * len(self.trees))(*[t.h for t in self.trees])
+        opts = ForestOpts(device, int(mixed))
+        h = ctypes.c_void_p()
+        _check(lib().afv_forest_create(len(self.trees), arr, ctypes.byref(opts), ctypes.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.afv_forest_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def info(self):
+        out = np.zeros(8, np.int64)
+        _check(lib().afv_forest_get_info(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong))))
+        keys = ("n_trees", "dim", "n_cell", "min_lvl", "max_lvl", "n_boxes", "leaf_cells", "bytes")
+        return dict(zip(keys, (int(x) for x in out)))
+
+    def _n_values(self, tree, interior):
+        t = self.trees[tree]
+        n = 0
+        for lvl in range(t.min_lvl, t.highest_lvl + 1):
+            ids, _, _ = t.level(lvl)
+            nc = t.n_cell_at(lvl)
+            n += len(ids) * ((nc if interior else nc + 2) ** self.dim)
+        return n
+
+    def set_var(self, tree, var, values, interior_only=False):
+        a = np.ascontiguousarray(values, dtype=np.float64).ravel()
+        if a.size != self._n_values(tree, interior_only):
+            raise ValueError("values do not match the tree's box layout")
+        _check(lib().afv_forest_set_var(self.h, tree, var, _dp(a), int(interior_only)))
+
+    def get_var(self, tree, var, interior_only=False, out=None):
+        n = self._n_values(tree, interior_only)
+        a = np.empty(n) if out is None else out
+        _check(lib().afv_forest_get_var(self.h, tree, var, _dp(a), int(interior_only)))
+        return a
+
+    def set_source(self, tree, gauss, lpl=False):
+        g = np.ascontiguousarray(gauss, dtype=np.float64)
+        _check(lib().afv_forest_set_source(self.h, tree, int(lpl), g.size // (2 + self.dim), _dp(g)))
+
+    def set_bc(self, tree, bc_type=AFV_BC_DIRICHLET, gauss=None, lpl=False):
+        if gauss is None:
+            _check(lib().afv_forest_set_bc(self.h, tree, bc_type, 0, 0, None))
+        else:
+            g = np.ascontiguousarray(gauss, dtype=np.float64)
+            _check(lib().afv_forest_set_bc(self.h, tree, bc_type, int(lpl),
+                                           g.size // (2 + self.dim), _dp(g)))
+
+    def zero(self, var):
+        _check(lib().afv_forest_zero(self.h, var))
+
+    def sync(self):
+        _check(lib().afv_forest_sync(self.h))
+
+    def stream(self):
+        """The cudaStream_t (as an int) that orders this forest's work."""
+        s = ctypes.c_void_p()
+        _check(lib().afv_forest_get_stream(self.h, ctypes.byref(s)))
+        return s.value or 0
+
+    def launches(self):
+        return self.profile_read(-1)[0]
+
+    def vcycle(self, mg=None, highest_lvl=None, set_residual=True):
+        mg = mg or MgOpts()
+        hl = self.info()["max_lvl"] if highest_lvl is None else highest_lvl
+        _check(lib().afv_mg_fas_vcycle(self.h, ctypes.byref(mg), hl, int(set_residual)))
+
+    def fmg(self, mg=None, set_residual=True, have_guess=False):
+        mg = mg or MgOpts()
+        _check(lib().afv_mg_fas_fmg(self.h, ctypes.byref(mg), int(set_residual), int(have_guess)))
+
+    def gc_tree(self):
+        _check(lib().afv_gc_tree(self.h))
+
+    def max_abs(self, tree, var):
+        out = ctypes.c_double(0)
+        _check(lib().afv_tree_max_abs_cc(self.h, tree, var, ctypes.byref(out)))
+        return out.value
+
+    def solve(self, precision=AFV_PREC_FP64, tol=1e-8, max_cycles=50, mg=None, check=True):
+        mg = mg or MgOpts()
+        n = len(self.trees)
+        cyc = np.zeros(n, np.int32)
+        rel = np.zeros(n)
+        rc = lib().afv_mg_solve(self.h, ctypes.byref(mg), precision, float(tol), max_cycles,
+                                _ip(cyc), _dp(rel))
+        if check and rc != AFV_OK:
+            _check(rc)
+        return cyc, rel, rc
+
+    # single operators
+    def gsrb_level(self, lvl, n_cycle):
+        _check(lib().afv_mg_gsrb_level(self.h, lvl, n_cycle))
+
+    def fill_gc_level(self, lvl):
+        _check(lib().afv_fill_gc_level(self.h, lvl))
+
+    def update_coarse(self, lvl):
+        _check(lib().afv_mg_update_coarse(self.h, lvl))
+
+    def correct_children(self, lvl_parent):
+        _check(lib().afv_mg_correct_children(self.h, lvl_parent))
+
+    def residual_all(self):
+        _check(lib().afv_mg_residual_all(self.h))
+
+    # event profiler
+    def profile(self, mask):
+        _check(lib().afv_forest_profile(self.h, mask))
+
+    def profile_read(self, kind):
+        n, ms, b = ctypes.c_longlong(0), ctypes.c_double(0), ctypes.c_double(0)
+        _check(lib().afv_forest_profile_read(self.h, kind, ctypes.byref(n), ctypes.byref(ms),
+                                             ctypes.byref(b)))
+        return n.value, ms.value, b.value
+
+
+def mg2_init_mg(mg=None):
+    """mg$D_init_mg (src/m_aX_mg.f90:130-154): negative cycle counts become 2."""
+    mg = mg or MgOpts()
+    _check(lib().afv_mg_init(ctypes.byref(mg)))
+    return mg
+
+
+mg3_init_mg = mg2_init_mg
+
+
+def mg2_fas_vcycle(forest, mg, highest_lvl, set_residual):
+    forest.vcycle(mg, highest_lvl, set_residual)
+
+
+def mg2_fas_fmg(forest, mg, set_residual, have_guess):
+    forest.fmg(mg, set_residual, have_guess)
+
+
+mg3_fas_vcycle, mg3_fas_fmg = mg2_fas_vcycle, mg2_fas_fmg
+
+
+def a2_gc_tree(forest):
+    forest.gc_tree()
+
+
+a3_gc_tree = a2_gc_tree
+
+
+def a2_tree_max_abs_cc(forest, tree, var):
+    return forest.max_abs(tree, var)
+
+
+a3_tree_max_abs_cc = a2_tree_max_abs_cc

@@ -1,0 +1,155 @@
+// Device-resident forest: the plan's tables and the cell data on one GPU, and
+// the multigrid drivers that sweep it (one launch per level and operator for
+// all trees at once).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "plan.hpp"
+
+namespace afv {
+
+template <class T>
+struct Arrays {
+  T* phi = nullptr;  // ghosted
+  T* rhs = nullptr;  // interior
+  T* tmp = nullptr;  // ghosted
+};
+
+struct DevMeta {
+  int* nb = nullptr;
+  int* parent = nullptr;
+  int* first_child = nullptr;
+  int* tree = nullptr;
+  int* qd = nullptr;
+  double* dr = nullptr;
+  long long* offg = nullptr;
+  long long* offi = nullptr;
+  int* bctype = nullptr;
+  long long* bcoff = nullptr;
+  double* bcval = nullptr;
+  int* active = nullptr;  // [n_trees]
+};
+
+struct MgOpts {
+  int n_down = 2, n_up = 2, n_base = 2;
+};
+
+// Kernel kinds for the event profiler (afv_forest_profile).
+enum ProfKind {
+  kProfSweep = 0,
+  kProfFill,
+  kProfRestrict,
+  kProfCoarseRhs,
+  kProfCorrect,
+  kProfResidual,
+  kProfDefect,
+  kProfAccumulate,
+  kProfOther,
+  kProfKinds
+};
+
+struct ProfEntry {
+  cudaEvent_t start, stop;
+  int kind;
+  double bytes;  // algorithmic bytes of the launch
+};
+
+struct SolveStats {
+  std::vector<int> cycles;
+  std::vector<double> rel_res;
+  int status = 0;
+};
+
+class Forest {
+ public:
+  Plan plan;
+  int device = 0;
+  int n_sm = 148;
+  cudaStream_t stream = nullptr;
+  DevMeta meta;
+  Arrays<double> d64;
+  Arrays<float> d32;
+  double* base_phi64 = nullptr;  // FP64 copy of the coarsest level for the mixed cycle
+  double* base_rhs64 = nullptr;
+  bool mixed = false;
+  // level lists on the device
+  int* d_lists = nullptr;
+  std::vector<int> leaves_off, parents_off;  // offsets in d_lists per level
+  int all_leaves_off = 0;
+  // per-tree reductions
+  unsigned long long* d_norm = nullptr;  // [n_trees]
+  double* d_fmax = nullptr;              // [n_trees]
+  int* d_count = nullptr;                // [1]
+  int* h_count = nullptr;                // pinned
+  unsigned long long* h_norm = nullptr;  // pinned [n_trees]
+  double* d_stage = nullptr;             // staging for host exchange
+  long long stage_elems = 0;
+  int* d_stage_slots = nullptr;
+  long long bytes = 0;
+  std::vector<int> host_active;
+  // event profiler: when enabled, launches of the selected kinds (bit mask)
+  // are bracketed by CUDA events on the forest's stream
+  int prof_mask = 0;
+  long long n_launches = 0;  // every kernel launched on the stream
+  std::vector<ProfEntry> prof;
+  std::vector<cudaEvent_t> event_pool;
+  cudaEvent_t prof_begin(int kind);
+  void prof_end(cudaEvent_t start, int kind, double bytes);
+  int prof_read(int kind, long long* launches, double* ms, double* bytes);
+  void prof_reset();
+
+  ~Forest();
+  int create(const std::vector<const HostTree*>& trees, const afv_forest_opts* opts, std::string& err);
+  int upload_bc(std::string& err);
+
+  // Host exchange in the reference's box layout.
+  int set_var(int tree, int var, const double* host, int interior_only, std::string& err);
+  int get_var(int tree, int var, double* host, int interior_only, std::string& err);
+
+  // Activity masks.
+  int set_active_all(int v);
+  int set_active_host(const std::vector<int>& a);
+
+  // Multigrid (FP64 state).
+  int gsrb_level(int lvl, int n_cycle, std::string& err);
+  int fill_level(int lvl, std::string& err);
+  int update_coarse(int lvl, std::string& err);
+  int correct_children(int lvl_parent, std::string& err);
+  int residual_all(unsigned long long* norm, std::string& err);
+  int vcycle(const MgOpts& mg, int highest, bool set_residual, std::string& err);
+  int fmg(const MgOpts& mg, bool set_residual, bool have_guess, std::string& err);
+  int gc_tree(std::string& err);
+  int max_abs(int tree, int var, double* out, std::string& err);
+  int solve(const MgOpts& mg, int precision, double tol, int max_cycles, SolveStats& st,
+            std::string& err);
+
+  // Generic-precision pieces.
+  template <class T> void sweep(const Arrays<T>& a, int lvl, int n, bool pull, bool homog);
+  template <class T> void fill(const Arrays<T>& a, int lvl, bool homog);
+  template <class T> void restrict_res(const Arrays<T>& a, int lvl, bool with_res);
+  template <class T> void coarse_rhs(const Arrays<T>& a, int lvl_parent, bool copy_tmp);
+  template <class T> void correct(const Arrays<T>& a, int lvl_parent);
+  template <class T> void residual(const Arrays<T>& a, int lvl, unsigned long long* norm, bool store);
+  template <class T> void gsrb_boxes(const Arrays<T>& a, int lvl, int n_cycle, bool homog);
+  template <class T> void update_coarse_t(const Arrays<T>& a, int lvl, bool homog, bool copy_tmp);
+  template <class T> void vcycle_t(const Arrays<T>& a, const MgOpts& mg, int highest, bool homog,
+                                   bool base64);
+  void fill_all64(bool homog);
+  void restrict_tree_phi64();
+
+  int check(std::string& err, const char* where);
+  int lvl_n(int l) const {
+    return (l < plan.min_lvl || l > plan.max_lvl) ? 0 : plan.lvl_n[plan.L(l)];
+  }
+  int* leaves_list(int l) { return d_lists + leaves_off[plan.L(l)]; }
+  int* parents_list(int l) { return d_lists + parents_off[plan.L(l)]; }
+  int n_leaves(int l) const { return (int)plan.leaves[plan.L(l)].size(); }
+  int n_parents(int l) const {
+    return (l < plan.min_lvl || l > plan.max_lvl) ? 0 : (int)plan.parents[plan.L(l)].size();
+  }
+};
+
+}  // namespace afv

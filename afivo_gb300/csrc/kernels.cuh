@@ -1,0 +1,834 @@
+// Device kernels of the FAS multigrid path (sm_103a). Templated on the
+// dimension D, the block size NC of the level they sweep and the arithmetic
+// type T (double for the FP64 path, float for the inner cycles of the mixed
+// path).
+//
+// Storage: every variable is one flat device array shared by all levels and
+// trees; slot s keeps phi/tmp at offg[s] as a (NC+2)^D box with one ghost
+// layer, x fastest (the reference's cc(0:nc+1, ...) arrays,
+// src/m_aX_core.f90:360-369), and rhs at offi[s] as an NC^D interior-only box
+// (rhs ghost cells are never read by the reference's path).
+//
+// Floating-point order follows the reference expression by expression; the
+// library is compiled with -fmad=false so that no multiply-add is fused.
+#pragma once
+#include <cstdint>
+
+namespace afv {
+namespace dev {
+
+constexpr int kThreads = 256;
+constexpr int kSmemCap = 48 * 1024;
+
+// Neighbour codes of a slot face.
+constexpr int kNbRefinement = -1;  // no box at this level: coarse neighbour
+constexpr int kNbPhysical = -2;    // physical boundary
+
+struct BoxSet {
+  const int* list;  // slot list, or nullptr for the range [lo, lo+n)
+  int lo;
+  int n;
+};
+
+struct Meta {
+  const int* nb;           // [slot*2D + face]
+  const int* parent;       // [slot]
+  const int* first_child;  // [slot]
+  const int* tree;         // [slot]
+  const int* qd;           // [slot] child-number bits within the parent (lvl >= 2), else -1
+  const double* dr;        // [slot]
+  const long long* offg;   // [slot] offset of the ghosted box
+  const long long* offi;   // [slot] offset of the interior box
+  const int* bctype;       // [slot*2D + face] 0 Dirichlet, 1 Neumann
+  const long long* bcoff;  // [slot*2D + face] offset of the face values in bcval, -1 = zero
+  const double* bcval;
+  const int* active;       // [tree] nonzero if the tree takes part in this launch
+};
+
+__device__ __forceinline__ int box_at(const BoxSet& s, int i) { return s.list ? s.list[i] : s.lo + i; }
+
+template <int D, int NC>
+struct Geo {
+  static constexpr int NG = NC + 2;
+  static constexpr int SG = D == 2 ? NG * NG : NG * NG * NG;
+  static constexpr int SI = D == 2 ? NC * NC : NC * NC * NC;
+  static constexpr int NF = D == 2 ? NC : NC * NC;
+  static constexpr int NNB = 2 * D;
+  __host__ __device__ static constexpr int g(int i, int j, int k) { return i + NG * (j + NG * k); }
+  __host__ __device__ static constexpr int in(int i, int j, int k) {
+    return (i - 1) + NC * ((j - 1) + NC * (k - 1 < 0 ? 0 : k - 1));
+  }
+};
+
+template <class T> struct Vec;
+template <> struct Vec<double> { using type = double2; static constexpr int w = 2; };
+template <> struct Vec<float> { using type = float4; static constexpr int w = 4; };
+
+template <int SG, int PER_BOX, class T>
+__host__ __device__ constexpr int boxes_per_cta(int staged) {
+  int by_threads = kThreads / PER_BOX;
+  int by_smem = kSmemCap / (SG * (int)sizeof(T) * staged);
+  int b = by_threads < by_smem ? by_threads : by_smem;
+  return b < 1 ? 1 : b;
+}
+
+// Face cell (a, c) of face f (0-based: lowx, highx, lowy, highy, lowz, highz):
+// ghost position, the adjacent interior cell, and the matching boundary cell
+// of the neighbour across the face. a, c run over 1..NC in the tangential
+// directions (x before y before z).
+template <int D, int NC>
+struct Face {
+  int gi, gj, gk;  // ghost cell
+  int ai, aj, ak;  // adjacent interior cell
+  int ni, nj, nk;  // neighbour's cell copied into the ghost (sides_from_nb)
+  __device__ __forceinline__ Face(int f, int a, int c) {
+    int dim = f >> 1, hi = f & 1;
+    int t[3] = {a, c, 1};
+    int p[3], q[3], r[3];
+    int k = 0;
+    for (int d = 0; d < 3; ++d) {
+      if (d >= D) {
+        p[d] = q[d] = r[d] = 0;
+      } else if (d == dim) {
+        p[d] = hi ? NC + 1 : 0;
+        q[d] = hi ? NC : 1;
+        r[d] = hi ? 1 : NC;
+      } else {
+        p[d] = q[d] = r[d] = t[k++];
+      }
+    }
+    gi = p[0]; gj = p[1]; gk = p[2];
+    ai = q[0]; aj = q[1]; ak = q[2];
+    ni = r[0]; nj = r[1]; nk = r[2];
+  }
+};
+
+// Ghost value of one face cell of box s, from the state of the level before
+// this call. own(i,j,k) reads the box's own cells.
+//  - neighbour box: copy of its boundary cell, src/m_aX_gc.f90:381-415
+//  - refinement boundary: mg$D_sides_rb, src/m_aX_mg.f90:262-350, after the
+//    zeroth-order injection of the parent's value (a$D_gc_prolong0,
+//    src/m_aX_gc.f90:135-151 and a$D_prolong0, src/m_aX_prolong.f90:39-108)
+//  - physical boundary: bc_to_gc, src/m_aX_gc.f90:71-132 with the sampled
+//    boundary value b of the sides_bc hook
+template <int D, int NC, class T, class Own>
+__device__ __forceinline__ T ghost_value(const Meta& m, const T* __restrict__ phi, int s, int f,
+                                         int a, int c, bool homog, Own own) {
+  using G = Geo<D, NC>;
+  Face<D, NC> F(f, a, c);
+  int code = m.nb[s * G::NNB + f];
+  if (code >= 0) {
+    return phi[m.offg[code] + G::g(F.ni, F.nj, F.nk)];
+  }
+  if (code == kNbRefinement) {
+    // Injection from the parent (levels >= 2 only; the parent has the same NC).
+    int p = m.parent[s];
+    int qd = m.qd[s];
+    int lo[3], idx[3] = {F.gi, F.gj, F.gk};
+    for (int d = 0; d < 3; ++d) lo[d] = (d < D) ? ((qd >> d) & 1) * (NC >> 1) : 0;
+    int pc[3];
+    for (int d = 0; d < 3; ++d) pc[d] = (d < D) ? lo[d] + ((idx[d] + 1) >> 1) : 0;
+    T g0 = phi[m.offg[p] + G::g(pc[0], pc[1], pc[2])];
+    int dim = f >> 1;
+    int ix = (f & 1) ? NC : 1;
+    int dix = (f & 1) ? -1 : 1;
+    (void)ix;
+    if constexpr (D == 2) {
+      if (dim == 0) {
+        int i = F.ai, j = F.aj;
+        int dj = -1 + 2 * (j & 1);
+        return (T)0.5 * g0 + own(i, j, 0) - (T)0.25 * (own(i + dix, j, 0) + own(i, j + dj, 0));
+      } else {
+        int i = F.ai, j = F.aj;
+        int di = -1 + 2 * (i & 1);
+        return (T)0.5 * g0 + own(i, j, 0) - (T)0.25 * (own(i + di, j, 0) + own(i, j + dix, 0));
+      }
+    } else {
+      int i = F.ai, j = F.aj, k = F.ak;
+      int di = (dim == 0) ? dix : -1 + 2 * (i & 1);
+      int dj = (dim == 1) ? dix : -1 + 2 * (j & 1);
+      int dk = (dim == 2) ? dix : -1 + 2 * (k & 1);
+      return (T)0.5 * g0 + (T)0.75 * own(i, j, k) - (T)0.25 * own(i + di, j + dj, k + dk);
+    }
+  }
+  // Physical boundary: y = c2 * b + c1 * x
+  T b = 0;
+  long long bo = m.bcoff[s * G::NNB + f];
+  if (!homog && bo >= 0) {
+    int lin = (D == 2) ? (a - 1) : (a - 1) + NC * (c - 1);
+    b = (T)m.bcval[bo + lin];
+  }
+  T x = own(F.ai, F.aj, F.ak);
+  if (m.bctype[s * G::NNB + f] == 0) {
+    return (T)2 * b + (T)(-1) * x;
+  } else {
+    T c2 = (T)m.dr[s] * (T)((f & 1) ? 1 : -1);
+    return c2 * b + (T)1 * x;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// GSRB half-sweep (mg$D_box_gsrb_lpl, src/m_aX_mg.f90:718-760) on every box of
+// a level, for red/black counter n. With pull = 1 the ghost cells this colour
+// needs are first recomputed from the neighbours' current state (the
+// a$D_gc_box call that the reference makes after the previous half-sweep,
+// src/m_aX_mg.f90:412-417); they are the neighbours' cells of the other colour,
+// which no block writes during this sweep, so blocks may update in place.
+// With pull = 0 the stored ghost cells are used, as in the first half-sweep.
+// ---------------------------------------------------------------------------
+template <int D, int NC, class T>
+__global__ void __launch_bounds__(kThreads)
+k_sweep(Meta m, BoxSet bs, T* __restrict__ phi, const T* __restrict__ rhs, int n, int pull,
+        int homog) {
+  using G = Geo<D, NC>;
+  constexpr int PER_BOX = G::SI / 2;
+  constexpr int BPC = boxes_per_cta<G::SG, PER_BOX, T>(1);
+  using V = typename Vec<T>::type;
+  constexpr int VW = Vec<T>::w;
+  __shared__ __align__(16) T sm[BPC * G::SG];
+  __shared__ int s_slot[BPC];
+  __shared__ int s_act[BPC];
+
+  const int groups = (bs.n + BPC - 1) / BPC;
+  for (int grp = blockIdx.x; grp < groups; grp += gridDim.x) {
+    const int nbox = min(BPC, bs.n - grp * BPC);
+    if (threadIdx.x < BPC) {
+      int s = threadIdx.x < nbox ? box_at(bs, grp * BPC + threadIdx.x) : -1;
+      s_slot[threadIdx.x] = s;
+      s_act[threadIdx.x] = (s >= 0) ? m.active[m.tree[s]] : 0;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < nbox * (G::SG / VW); e += blockDim.x) {
+      int b = e / (G::SG / VW), q = e % (G::SG / VW);
+      reinterpret_cast<V*>(sm + b * G::SG)[q] =
+          reinterpret_cast<const V*>(phi + m.offg[s_slot[b]])[q];
+    }
+    __syncthreads();
+    if (pull) {
+      for (int e = threadIdx.x; e < nbox * G::NNB * G::NF; e += blockDim.x) {
+        int b = e / (G::NNB * G::NF);
+        int r = e % (G::NNB * G::NF);
+        int f = r / G::NF, lin = r % G::NF;
+        int a = lin % NC + 1, c = lin / NC + 1;
+        Face<D, NC> F(f, a, c);
+        if (((F.ai + F.aj + F.ak + n) & 1) != 0) continue;  // neighbour cell of this colour: not needed
+        if (!s_act[b]) continue;
+        const T* bx = sm + b * G::SG;
+        auto own = [&](int i, int j, int k) { return bx[G::g(i, j, k)]; };
+        T v = ghost_value<D, NC, T>(m, phi, s_slot[b], f, a, c, homog != 0, own);
+        sm[b * G::SG + G::g(F.gi, F.gj, F.gk)] = v;
+      }
+      __syncthreads();
+    }
+    {
+      int b = threadIdx.x / PER_BOX, q = threadIdx.x % PER_BOX;
+      if (b < nbox && s_act[b]) {
+        int s = s_slot[b];
+        const T* bx = sm + b * G::SG;
+        T dx2 = (T)(m.dr[s] * m.dr[s]);
+        int p = q % (NC / 2);
+        if constexpr (D == 2) {
+          int j = q / (NC / 2) + 1;
+          int i = 2 * p + 1 + ((1 + j + n) & 1);
+          T f = rhs[m.offi[s] + G::in(i, j, 1)];
+          T v = (T)0.25 * (bx[G::g(i + 1, j, 0)] + bx[G::g(i - 1, j, 0)] + bx[G::g(i, j + 1, 0)] +
+                           bx[G::g(i, j - 1, 0)] - dx2 * f);
+          phi[m.offg[s] + G::g(i, j, 0)] = v;
+        } else {
+          int j = (q / (NC / 2)) % NC + 1;
+          int k = q / ((NC / 2) * NC) + 1;
+          int i = 2 * p + 1 + ((1 + j + k + n) & 1);
+          const T sixth = (T)(1 / 6.0);
+          T f = rhs[m.offi[s] + G::in(i, j, k)];
+          T v = sixth * (bx[G::g(i + 1, j, k)] + bx[G::g(i - 1, j, k)] + bx[G::g(i, j + 1, k)] +
+                         bx[G::g(i, j - 1, k)] + bx[G::g(i, j, k + 1)] + bx[G::g(i, j, k - 1)] -
+                         dx2 * f);
+          phi[m.offg[s] + G::g(i, j, k)] = v;
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Ghost fill of every face of every box of a level (a$D_gc_box per box,
+// src/m_aX_gc.f90:50-69, as called by fill_gc_phi, src/m_aX_mg.f90:352-365).
+// Writes only ghost cells and reads only interior cells (own, neighbours')
+// and the parent's stored cells, so all boxes fill concurrently.
+// ---------------------------------------------------------------------------
+template <int D, int NC, class T>
+__global__ void __launch_bounds__(kThreads)
+k_fill(Meta m, BoxSet bs, T* __restrict__ phi, int homog) {
+  using G = Geo<D, NC>;
+  const long long total = (long long)bs.n * G::NNB * G::NF;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    int bi = (int)(e / (G::NNB * G::NF));
+    int r = (int)(e % (G::NNB * G::NF));
+    int f = r / G::NF, lin = r % G::NF;
+    int a = lin % NC + 1, c = lin / NC + 1;
+    int s = box_at(bs, bi);
+    if (!m.active[m.tree[s]]) continue;
+    const T* bx = phi + m.offg[s];
+    auto own = [&](int i, int j, int k) { return bx[G::g(i, j, k)]; };
+    T v = ghost_value<D, NC, T>(m, phi, s, f, a, c, homog != 0, own);
+    Face<D, NC> F(f, a, c);
+    phi[m.offg[s] + G::g(F.gi, F.gj, F.gk)] = v;
+  }
+}
+
+// Laplacian of mg$D_box_lpl (src/m_aX_mg.f90:763-797) at (i,j,k) of a staged box.
+template <int D, int NC, class T>
+__device__ __forceinline__ T lpl_at(const T* bx, int i, int j, int k, T inv_dr_sq) {
+  using G = Geo<D, NC>;
+  if constexpr (D == 2) {
+    return inv_dr_sq * (bx[G::g(i - 1, j, 0)] + bx[G::g(i + 1, j, 0)] + bx[G::g(i, j - 1, 0)] +
+                        bx[G::g(i, j + 1, 0)] - (T)4 * bx[G::g(i, j, 0)]);
+  } else {
+    return inv_dr_sq * (bx[G::g(i - 1, j, k)] + bx[G::g(i + 1, j, k)] + bx[G::g(i, j - 1, k)] +
+                        bx[G::g(i, j + 1, k)] + bx[G::g(i, j, k - 1)] + bx[G::g(i, j, k + 1)] -
+                        (T)6 * bx[G::g(i, j, k)]);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Residual and restriction to the parent: the per-box body of update_coarse
+// and set_coarse_phi_rhs (src/m_aX_mg.f90:444-465, :495-504): residual_box
+// (:545-559) then a$D_restrict_box of tmp and phi (src/m_aX_restrict.f90:67-132).
+// The residual is kept in registers; the fine box's tmp is not written, which
+// is what the reference's save/restore of tmp leaves behind (:452-462).
+// SUB = the fine level is <= 1 (the parent is a sub-level box of half the size
+// covering the same region, src/m_aX_t.f90:366-373).
+// ---------------------------------------------------------------------------
+template <int D, int NC, bool SUB, class T>
+__global__ void __launch_bounds__(kThreads)
+k_restrict_res(Meta m, BoxSet bs, T* __restrict__ phi, const T* __restrict__ rhs,
+               T* __restrict__ tmp, int with_res) {
+  using G = Geo<D, NC>;
+  constexpr int H = NC / 2;
+  constexpr int PNC = SUB ? NC / 2 : NC;
+  using GP = Geo<D, PNC>;
+  constexpr int PER_BOX = D == 2 ? H * H : H * H * H;
+  constexpr int BPC = boxes_per_cta<G::SG, PER_BOX, T>(1);
+  using V = typename Vec<T>::type;
+  constexpr int VW = Vec<T>::w;
+  __shared__ __align__(16) T sm[BPC * G::SG];
+  __shared__ int s_slot[BPC];
+  __shared__ int s_act[BPC];
+  const int groups = (bs.n + BPC - 1) / BPC;
+  for (int grp = blockIdx.x; grp < groups; grp += gridDim.x) {
+    const int nbox = min(BPC, bs.n - grp * BPC);
+    if (threadIdx.x < BPC) {
+      int s = threadIdx.x < nbox ? box_at(bs, grp * BPC + threadIdx.x) : -1;
+      s_slot[threadIdx.x] = s;
+      s_act[threadIdx.x] = (s >= 0) ? m.active[m.tree[s]] : 0;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < nbox * (G::SG / VW); e += blockDim.x) {
+      int b = e / (G::SG / VW), q = e % (G::SG / VW);
+      reinterpret_cast<V*>(sm + b * G::SG)[q] =
+          reinterpret_cast<const V*>(phi + m.offg[s_slot[b]])[q];
+    }
+    __syncthreads();
+    int b = threadIdx.x / PER_BOX, q = threadIdx.x % PER_BOX;
+    if (b < nbox && s_act[b]) {
+      int s = s_slot[b];
+      const T* bx = sm + b * G::SG;
+      const T* f = rhs + m.offi[s];
+      T inv = (T)1 / (T)(m.dr[s] * m.dr[s]);
+      if constexpr (sizeof(T) == 8) inv = 1 / (m.dr[s] * m.dr[s]);
+      int ic = q % H + 1, jc = (q / H) % H + 1, kc = (D == 3) ? q / (H * H) + 1 : 0;
+      int off[3] = {0, 0, 0};
+      if (!SUB) {
+        int qd = m.qd[s];
+        for (int d = 0; d < D; ++d) off[d] = ((qd >> d) & 1) * H;
+      }
+      T sr = 0, sp = 0;
+      int kk_n = (D == 3) ? 2 : 1;
+      for (int kk = 0; kk < kk_n; ++kk)
+        for (int jj = 0; jj < 2; ++jj)
+          for (int ii = 0; ii < 2; ++ii) {
+            int i = 2 * ic - 1 + ii, j = 2 * jc - 1 + jj, k = (D == 3) ? 2 * kc - 1 + kk : 0;
+            if (with_res) {
+              T r = f[G::in(i, j, D == 3 ? k : 1)] - lpl_at<D, NC, T>(bx, i, j, k, inv);
+              sr = sr + r;
+            }
+            sp = sp + bx[G::g(i, j, k)];
+          }
+      const T w = (D == 2) ? (T)0.25 : (T)0.125;
+      int p = m.parent[s];
+      long long po = m.offg[p] + GP::g(off[0] + ic, off[1] + jc, (D == 3) ? off[2] + kc : 0);
+      if (with_res) tmp[po] = w * sr;
+      phi[po] = w * sp;
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Coarse right-hand side on the parents of a level after restriction
+// (src/m_aX_mg.f90:472-479 and :510-515): rhs = L(phi) + tmp over the interior,
+// then, for update_coarse, tmp = phi over the whole box including its ghosts
+// (a$D_box_copy_cc, src/m_aX_utils.f90:331-339).
+// ---------------------------------------------------------------------------
+template <int D, int NC, class T>
+__global__ void __launch_bounds__(kThreads)
+k_coarse_rhs(Meta m, BoxSet bs, const T* __restrict__ phi, T* __restrict__ rhs,
+             T* __restrict__ tmp, int copy_tmp) {
+  using G = Geo<D, NC>;
+  constexpr int PER_BOX = G::SI < kThreads ? G::SI : kThreads;
+  constexpr int BPC = boxes_per_cta<G::SG, PER_BOX, T>(1);
+  using V = typename Vec<T>::type;
+  constexpr int VW = Vec<T>::w;
+  __shared__ __align__(16) T sm[BPC * G::SG];
+  __shared__ int s_slot[BPC];
+  __shared__ int s_act[BPC];
+  const int groups = (bs.n + BPC - 1) / BPC;
+  for (int grp = blockIdx.x; grp < groups; grp += gridDim.x) {
+    const int nbox = min(BPC, bs.n - grp * BPC);
+    if (threadIdx.x < BPC) {
+      int s = threadIdx.x < nbox ? box_at(bs, grp * BPC + threadIdx.x) : -1;
+      s_slot[threadIdx.x] = s;
+      s_act[threadIdx.x] = (s >= 0) ? m.active[m.tree[s]] : 0;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < nbox * (G::SG / VW); e += blockDim.x) {
+      int b = e / (G::SG / VW), q = e % (G::SG / VW);
+      reinterpret_cast<V*>(sm + b * G::SG)[q] =
+          reinterpret_cast<const V*>(phi + m.offg[s_slot[b]])[q];
+    }
+    __syncthreads();
+    int b = threadIdx.x / PER_BOX, q0 = threadIdx.x % PER_BOX;
+    if (b < nbox && s_act[b]) {
+      int s = s_slot[b];
+      const T* bx = sm + b * G::SG;
+      T inv = (T)1 / (T)(m.dr[s] * m.dr[s]);
+      if constexpr (sizeof(T) == 8) inv = 1 / (m.dr[s] * m.dr[s]);
+      for (int q = q0; q < G::SI; q += PER_BOX) {
+        int i = q % NC + 1, j = (q / NC) % NC + 1, k = (D == 3) ? q / (NC * NC) + 1 : 0;
+        T l = lpl_at<D, NC, T>(bx, i, j, k, inv);
+        long long gi = m.offg[s] + G::g(i, j, k);
+        rhs[m.offi[s] + q] = l + tmp[gi];
+      }
+    }
+    __syncthreads();
+    if (copy_tmp) {
+      for (int e = threadIdx.x; e < nbox * (G::SG / VW); e += blockDim.x) {
+        int b2 = e / (G::SG / VW), q = e % (G::SG / VW);
+        if (!s_act[b2]) continue;
+        reinterpret_cast<V*>(tmp + m.offg[s_slot[b2]])[q] =
+            reinterpret_cast<const V*>(sm + b2 * G::SG)[q];
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// correct_children (src/m_aX_mg.f90:368-395): per parent, tmp = phi - tmp over
+// the whole box, then every child gets phi += prolong2(tmp)
+// (mg$D_box_corr_lpl :708-715, a$D_prolong2 with add, src/m_aX_prolong.f90:
+// 243-348). One thread per parent interior cell; that cell feeds the 2^D fine
+// cells of the child whose quadrant contains it. SUB = the children are on a
+// level <= 1 (one child, twice the cells per direction, no offset).
+// ---------------------------------------------------------------------------
+template <int D, int NC, bool SUB, class T>
+__global__ void __launch_bounds__(kThreads)
+k_correct(Meta m, BoxSet bs, T* __restrict__ phi, T* __restrict__ tmp) {
+  using G = Geo<D, NC>;  // parent geometry
+  constexpr int CNC = SUB ? 2 * NC : NC;
+  using GC = Geo<D, CNC>;
+  constexpr int PER_BOX = G::SI < kThreads ? G::SI : kThreads;
+  constexpr int BPC = boxes_per_cta<G::SG, PER_BOX, T>(1);
+  using V = typename Vec<T>::type;
+  constexpr int VW = Vec<T>::w;
+  __shared__ __align__(16) T sm[BPC * G::SG];
+  __shared__ int s_slot[BPC];
+  __shared__ int s_act[BPC];
+  const int groups = (bs.n + BPC - 1) / BPC;
+  for (int grp = blockIdx.x; grp < groups; grp += gridDim.x) {
+    const int nbox = min(BPC, bs.n - grp * BPC);
+    if (threadIdx.x < BPC) {
+      int s = threadIdx.x < nbox ? box_at(bs, grp * BPC + threadIdx.x) : -1;
+      s_slot[threadIdx.x] = s;
+      s_act[threadIdx.x] = (s >= 0) ? m.active[m.tree[s]] : 0;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < nbox * (G::SG / VW); e += blockDim.x) {
+      int b = e / (G::SG / VW), q = e % (G::SG / VW);
+      if (!s_act[b]) continue;
+      long long o = m.offg[s_slot[b]];
+      V p = reinterpret_cast<const V*>(phi + o)[q];
+      V t = reinterpret_cast<const V*>(tmp + o)[q];
+      V r;
+      if constexpr (VW == 2) {
+        r.x = p.x - t.x;
+        r.y = p.y - t.y;
+      } else {
+        r.x = p.x - t.x;
+        r.y = p.y - t.y;
+        r.z = p.z - t.z;
+        r.w = p.w - t.w;
+      }
+      reinterpret_cast<V*>(sm + b * G::SG)[q] = r;
+      reinterpret_cast<V*>(tmp + o)[q] = r;
+    }
+    __syncthreads();
+    int b = threadIdx.x / PER_BOX, q0 = threadIdx.x % PER_BOX;
+    if (b < nbox && s_act[b]) {
+      int s = s_slot[b];
+      const T* t = sm + b * G::SG;
+      constexpr int H = NC / 2;
+      for (int q = q0; q < G::SI; q += PER_BOX) {
+        int ic = q % NC + 1, jc = (q / NC) % NC + 1, kc = (D == 3) ? q / (NC * NC) + 1 : 0;
+        int child, li, lj, lk;
+        if (SUB) {
+          child = m.first_child[s];
+          li = ic;
+          lj = jc;
+          lk = kc;
+        } else {
+          int qx = (ic - 1) / H, qy = (jc - 1) / H, qz = (D == 3) ? (kc - 1) / H : 0;
+          child = m.first_child[s] + qx + 2 * qy + 4 * qz;
+          li = ic - qx * H;
+          lj = jc - qy * H;
+          lk = (D == 3) ? kc - qz * H : 0;
+        }
+        T* c = phi + m.offg[child];
+        int i_f = 2 * li - 1, j_f = 2 * lj - 1;
+        T f0 = t[G::g(ic, jc, kc)];
+        T fx = (T)0.125 * (t[G::g(ic + 1, jc, kc)] - t[G::g(ic - 1, jc, kc)]);
+        T fy = (T)0.125 * (t[G::g(ic, jc + 1, kc)] - t[G::g(ic, jc - 1, kc)]);
+        T fxx = (T)0.03125 * (t[G::g(ic - 1, jc, kc)] - (T)2 * f0 + t[G::g(ic + 1, jc, kc)]);
+        T fyy = (T)0.03125 * (t[G::g(ic, jc - 1, kc)] - (T)2 * f0 + t[G::g(ic, jc + 1, kc)]);
+        if constexpr (D == 2) {
+          T f2 = fxx + fyy;
+          long long o00 = GC::g(i_f, j_f, 0), o10 = GC::g(i_f + 1, j_f, 0);
+          long long o01 = GC::g(i_f, j_f + 1, 0), o11 = GC::g(i_f + 1, j_f + 1, 0);
+          c[o00] = f0 - fx - fy + f2 + c[o00];
+          c[o10] = f0 + fx - fy + f2 + c[o10];
+          c[o01] = f0 - fx + fy + f2 + c[o01];
+          c[o11] = f0 + fx + fy + f2 + c[o11];
+        } else {
+          int k_f = 2 * lk - 1;
+          T fz = (T)0.125 * (t[G::g(ic, jc, kc + 1)] - t[G::g(ic, jc, kc - 1)]);
+          T fzz = (T)0.03125 * (t[G::g(ic, jc, kc - 1)] - (T)2 * f0 + t[G::g(ic, jc, kc + 1)]);
+          T f2 = fxx + fyy + fzz;
+#pragma unroll
+          for (int cz = 0; cz < 2; ++cz)
+#pragma unroll
+            for (int cy = 0; cy < 2; ++cy)
+#pragma unroll
+              for (int cx = 0; cx < 2; ++cx) {
+                long long o = GC::g(i_f + cx, j_f + cy, k_f + cz);
+                // f0 -/+ fx -/+ fy -/+ fz + f2 + old, in this order
+                T v = f0;
+                v = cx ? v + fx : v - fx;
+                v = cy ? v + fy : v - fy;
+                v = cz ? v + fz : v - fz;
+                c[o] = v + f2 + c[o];
+              }
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Block-segment max of non-negative values followed by one atomicMax per
+// segment of SEG threads (SEG a power of two); the bit pattern of a
+// non-negative double orders like its value.
+template <int SEG>
+__device__ __forceinline__ void seg_atomic_max(unsigned long long* dst, double v) {
+  unsigned lane = threadIdx.x & 31;
+  constexpr int W = SEG < 32 ? SEG : 32;
+#pragma unroll
+  for (int o = W / 2; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  if ((lane & (W - 1)) == 0 && dst) atomicMax(dst, (unsigned long long)__double_as_longlong(v));
+}
+
+// ---------------------------------------------------------------------------
+// Residual tmp = rhs - L(phi) on every box of a set (residual_box,
+// src/m_aX_mg.f90:545-559), and optionally max |tmp| over the leaf boxes per
+// tree (a$D_tree_max_cc / a$D_tree_min_cc, src/m_aX_utils.f90:468-571).
+// ---------------------------------------------------------------------------
+template <int D, int NC, class T>
+__global__ void __launch_bounds__(kThreads)
+k_residual(Meta m, BoxSet bs, const T* __restrict__ phi, const T* __restrict__ rhs,
+           T* __restrict__ tmp, unsigned long long* __restrict__ norm_per_tree, int store) {
+  using G = Geo<D, NC>;
+  constexpr int PER_BOX = G::SI < kThreads ? G::SI : kThreads;
+  constexpr int BPC = kThreads / PER_BOX;
+  const int groups = (bs.n + BPC - 1) / BPC;
+  for (int grp = blockIdx.x; grp < groups; grp += gridDim.x) {
+    int b = threadIdx.x / PER_BOX, q0 = threadIdx.x % PER_BOX;
+    int bi = grp * BPC + b;
+    double mx = 0;
+    int tr = -1;
+    bool leaf = false;
+    if (bi < bs.n) {
+      int s = box_at(bs, bi);
+      tr = m.tree[s];
+      if (m.active[tr]) {
+        leaf = m.first_child[s] < 0;
+        const T* bx = phi + m.offg[s];
+        T inv = (T)1 / (T)(m.dr[s] * m.dr[s]);
+        if constexpr (sizeof(T) == 8) inv = 1 / (m.dr[s] * m.dr[s]);
+        for (int q = q0; q < G::SI; q += PER_BOX) {
+          int i = q % NC + 1, j = (q / NC) % NC + 1, k = (D == 3) ? q / (NC * NC) + 1 : 0;
+          T r = rhs[m.offi[s] + q] - lpl_at<D, NC, T>(bx, i, j, k, inv);
+          if (store) tmp[m.offg[s] + G::g(i, j, k)] = r;
+          mx = fmax(mx, fabs((double)r));
+        }
+      } else {
+        tr = -1;
+      }
+    }
+    if (norm_per_tree) {
+      // all threads of a PER_BOX segment belong to the same box
+      seg_atomic_max<PER_BOX>((tr >= 0 && leaf) ? norm_per_tree + tr : nullptr,
+                              (tr >= 0 && leaf) ? mx : 0.0);
+    }
+  }
+}
+
+// max |v| over the interiors of a set of boxes (variable in interior layout or
+// ghosted layout), per tree.
+template <int D, int NC, class T>
+__global__ void __launch_bounds__(kThreads)
+k_maxabs(Meta m, BoxSet bs, const T* __restrict__ v, int ghosted,
+         unsigned long long* __restrict__ norm_per_tree) {
+  using G = Geo<D, NC>;
+  constexpr int PER_BOX = G::SI < kThreads ? G::SI : kThreads;
+  constexpr int BPC = kThreads / PER_BOX;
+  const int groups = (bs.n + BPC - 1) / BPC;
+  for (int grp = blockIdx.x; grp < groups; grp += gridDim.x) {
+    int b = threadIdx.x / PER_BOX, q0 = threadIdx.x % PER_BOX;
+    int bi = grp * BPC + b;
+    double mx = 0;
+    int tr = -1;
+    if (bi < bs.n) {
+      int s = box_at(bs, bi);
+      tr = m.tree[s];
+      if (!m.active[tr]) tr = -1;
+      if (tr >= 0) {
+        for (int q = q0; q < G::SI; q += PER_BOX) {
+          int i = q % NC + 1, j = (q / NC) % NC + 1, k = (D == 3) ? q / (NC * NC) + 1 : 0;
+          T x = ghosted ? v[m.offg[s] + G::g(i, j, k)] : v[m.offi[s] + q];
+          mx = fmax(mx, fabs((double)x));
+        }
+      }
+    }
+    seg_atomic_max<PER_BOX>(tr >= 0 ? norm_per_tree + tr : nullptr, tr >= 0 ? mx : 0.0);
+  }
+}
+
+// Elementwise operations over whole boxes (ghosts included), as the
+// reference's full-array utilities do: a$D_box_clear_cc, a$D_box_copy_cc
+// (src/m_aX_utils.f90:262-270, :331-339).
+template <int D, int NC, class T>
+__global__ void __launch_bounds__(kThreads)
+k_box_op(Meta m, BoxSet bs, T* __restrict__ dst, const T* __restrict__ src, int op) {
+  using G = Geo<D, NC>;
+  using V = typename Vec<T>::type;
+  constexpr int VW = Vec<T>::w;
+  constexpr int NV = G::SG / VW;
+  const long long total = (long long)bs.n * NV;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    int bi = (int)(e / NV), q = (int)(e % NV);
+    int s = box_at(bs, bi);
+    if (!m.active[m.tree[s]]) continue;
+    V* d = reinterpret_cast<V*>(dst + m.offg[s]) + q;
+    if (op == 0) {
+      V z;
+      if constexpr (VW == 2) {
+        z.x = 0; z.y = 0;
+      } else {
+        z.x = 0; z.y = 0; z.z = 0; z.w = 0;
+      }
+      *d = z;
+    } else {
+      *d = reinterpret_cast<const V*>(src + m.offg[s])[q];
+    }
+  }
+}
+
+// Restriction of an interior-layout variable (rhs) to the parent, the
+// init_phi_rhs step of src/m_aX_mg.f90:530-541 (a$D_restrict_box).
+template <int D, int NC, bool SUB, class T>
+__global__ void __launch_bounds__(kThreads)
+k_restrict_interior(Meta m, BoxSet bs, T* __restrict__ v) {
+  constexpr int H = NC / 2;
+  constexpr int PNC = SUB ? NC / 2 : NC;
+  constexpr int PER_BOX = D == 2 ? H * H : H * H * H;
+  using G = Geo<D, NC>;
+  using GP = Geo<D, PNC>;
+  const long long total = (long long)bs.n * PER_BOX;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    int bi = (int)(e / PER_BOX), q = (int)(e % PER_BOX);
+    int s = box_at(bs, bi);
+    if (!m.active[m.tree[s]]) continue;
+    int ic = q % H + 1, jc = (q / H) % H + 1, kc = (D == 3) ? q / (H * H) + 1 : 1;
+    int off[3] = {0, 0, 0};
+    if (!SUB) {
+      int qd = m.qd[s];
+      for (int d = 0; d < D; ++d) off[d] = ((qd >> d) & 1) * H;
+    }
+    const T* f = v + m.offi[s];
+    T acc = 0;
+    int kk_n = (D == 3) ? 2 : 1;
+    for (int kk = 0; kk < kk_n; ++kk)
+      for (int jj = 0; jj < 2; ++jj)
+        for (int ii = 0; ii < 2; ++ii)
+          acc = acc + f[G::in(2 * ic - 1 + ii, 2 * jc - 1 + jj, D == 3 ? 2 * kc - 1 + kk : 1)];
+    const T w = (D == 2) ? (T)0.25 : (T)0.125;
+    int p = m.parent[s];
+    v[m.offi[p] + GP::in(off[0] + ic, off[1] + jc, D == 3 ? off[2] + kc : 1)] = w * acc;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Mixed precision: FP64 defect on the leaves written as the FP32 right-hand
+// side, and the FP64 accumulate of the FP32 correction.
+// ---------------------------------------------------------------------------
+template <int D, int NC>
+__global__ void __launch_bounds__(kThreads)
+k_defect(Meta m, BoxSet bs, const double* __restrict__ u, const double* __restrict__ f,
+         float* __restrict__ r32, unsigned long long* __restrict__ norm_per_tree) {
+  using G = Geo<D, NC>;
+  constexpr int PER_BOX = G::SI < kThreads ? G::SI : kThreads;
+  constexpr int BPC = kThreads / PER_BOX;
+  const int groups = (bs.n + BPC - 1) / BPC;
+  for (int grp = blockIdx.x; grp < groups; grp += gridDim.x) {
+    int b = threadIdx.x / PER_BOX, q0 = threadIdx.x % PER_BOX;
+    int bi = grp * BPC + b;
+    double mx = 0;
+    int tr = -1;
+    if (bi < bs.n) {
+      int s = box_at(bs, bi);
+      tr = m.tree[s];
+      if (!m.active[tr]) tr = -1;
+      if (tr >= 0) {
+        const double* bx = u + m.offg[s];
+        double inv = 1 / (m.dr[s] * m.dr[s]);
+        for (int q = q0; q < G::SI; q += PER_BOX) {
+          int i = q % NC + 1, j = (q / NC) % NC + 1, k = (D == 3) ? q / (NC * NC) + 1 : 0;
+          double r = f[m.offi[s] + q] - lpl_at<D, NC, double>(bx, i, j, k, inv);
+          r32[m.offi[s] + q] = (float)r;
+          mx = fmax(mx, fabs(r));
+        }
+      }
+    }
+    seg_atomic_max<PER_BOX>(tr >= 0 ? norm_per_tree + tr : nullptr, tr >= 0 ? mx : 0.0);
+  }
+}
+
+template <int D, int NC>
+__global__ void __launch_bounds__(kThreads)
+k_accumulate(Meta m, BoxSet bs, double* __restrict__ u, const float* __restrict__ e) {
+  using G = Geo<D, NC>;
+  const long long total = (long long)bs.n * G::SI;
+  for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < total;
+       x += (long long)gridDim.x * blockDim.x) {
+    int bi = (int)(x / G::SI), q = (int)(x % G::SI);
+    int s = box_at(bs, bi);
+    if (!m.active[m.tree[s]]) continue;
+    int i = q % NC + 1, j = (q / NC) % NC + 1, k = (D == 3) ? q / (NC * NC) + 1 : 0;
+    long long o = m.offg[s] + G::g(i, j, k);
+    u[o] = u[o] + (double)e[o];
+  }
+}
+
+// Precision conversion over whole boxes (the coarsest level of the mixed
+// cycle is smoothed in FP64).
+template <class TD, class TS>
+__global__ void k_convert(TD* __restrict__ dst, const TS* __restrict__ src, long long n) {
+  for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < n;
+       x += (long long)gridDim.x * blockDim.x)
+    dst[x] = (TD)src[x];
+}
+
+// Scatter / gather between the reference's host box layout (boxes in
+// level-list order, each (nc+2)^D, or nc^D when packed) and slot storage.
+// host_interior: the host buffer holds only interiors. dev_ghosted: the device
+// variable has ghost cells (phi, tmp) or not (rhs).
+template <int D, int NC, class T>
+__global__ void k_scatter(Meta m, const int* __restrict__ slots, int n,
+                          const double* __restrict__ src, T* __restrict__ dst, int host_interior,
+                          int dev_ghosted) {
+  using G = Geo<D, NC>;
+  const int per = host_interior ? G::SI : G::SG;
+  const long long total = (long long)n * per;
+  for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < total;
+       x += (long long)gridDim.x * blockDim.x) {
+    int bi = (int)(x / per), q = (int)(x % per);
+    int s = slots[bi];
+    int i, j, k;
+    if (host_interior) {
+      i = q % NC + 1;
+      j = (q / NC) % NC + 1;
+      k = (D == 3) ? q / (NC * NC) + 1 : 0;
+    } else {
+      i = q % G::NG;
+      j = (q / G::NG) % G::NG;
+      k = (D == 3) ? q / (G::NG * G::NG) : 0;
+    }
+    bool interior = i >= 1 && i <= NC && j >= 1 && j <= NC && (D == 2 || (k >= 1 && k <= NC));
+    if (dev_ghosted) {
+      dst[m.offg[s] + G::g(i, j, k)] = (T)src[x];
+    } else if (interior) {
+      dst[m.offi[s] + G::in(i, j, D == 3 ? k : 1)] = (T)src[x];
+    }
+  }
+}
+
+template <int D, int NC, class T>
+__global__ void k_gather(Meta m, const int* __restrict__ slots, int n, const T* __restrict__ src,
+                         double* __restrict__ dst, int host_interior, int dev_ghosted) {
+  using G = Geo<D, NC>;
+  const int per = host_interior ? G::SI : G::SG;
+  const long long total = (long long)n * per;
+  for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < total;
+       x += (long long)gridDim.x * blockDim.x) {
+    int bi = (int)(x / per), q = (int)(x % per);
+    int s = slots[bi];
+    int i, j, k;
+    if (host_interior) {
+      i = q % NC + 1;
+      j = (q / NC) % NC + 1;
+      k = (D == 3) ? q / (NC * NC) + 1 : 0;
+    } else {
+      i = q % G::NG;
+      j = (q / G::NG) % G::NG;
+      k = (D == 3) ? q / (G::NG * G::NG) : 0;
+    }
+    bool interior = i >= 1 && i <= NC && j >= 1 && j <= NC && (D == 2 || (k >= 1 && k <= NC));
+    double v = 0;
+    if (dev_ghosted)
+      v = (double)src[m.offg[s] + G::g(i, j, k)];
+    else if (interior)
+      v = (double)src[m.offi[s] + G::in(i, j, D == 3 ? k : 1)];
+    dst[x] = v;
+  }
+}
+
+// Per-tree convergence bookkeeping on the device: a tree stays active while
+// max|r| > tol * max|f|; counts the cycles applied to active trees.
+__global__ void k_check(int n_trees, const unsigned long long* __restrict__ rnorm,
+                        const double* __restrict__ fmax, double tol, int* __restrict__ active,
+                        int* __restrict__ n_active_out) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n_trees) {
+    double r = __longlong_as_double((long long)rnorm[t]);
+    int a = active[t];
+    if (a && !(r > tol * fmax[t])) a = 0;
+    active[t] = a;
+    if (a) atomicAdd(n_active_out, 1);
+  }
+}
+
+}  // namespace dev
+}  // namespace afv

@@ -1,0 +1,830 @@
+// Device forest and the FAS multigrid drivers: allocations, uploads, the
+// kernel launches per level, and the V-cycle / FMG / solve schedules of
+// src/m_aX_mg.f90, with all trees of the forest swept by each launch.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <type_traits>
+
+#include "forest.hpp"
+#include "kernels.cuh"
+
+namespace afv {
+
+using dev::BoxSet;
+using dev::Meta;
+template <int N> using IC = std::integral_constant<int, N>;
+
+// Calls f(IC<D>, IC<NC>) for the supported (dimension, block size) pairs.
+template <class F>
+static bool with_nc(int D, int nc, F&& f) {
+  if (D == 2) {
+    switch (nc) {
+      case 2: f(IC<2>{}, IC<2>{}); return true;
+      case 4: f(IC<2>{}, IC<4>{}); return true;
+      case 8: f(IC<2>{}, IC<8>{}); return true;
+      case 16: f(IC<2>{}, IC<16>{}); return true;
+    }
+  } else {
+    switch (nc) {
+      case 2: f(IC<3>{}, IC<2>{}); return true;
+      case 4: f(IC<3>{}, IC<4>{}); return true;
+      case 8: f(IC<3>{}, IC<8>{}); return true;
+    }
+  }
+  return false;
+}
+
+static Meta meta_of(const DevMeta& d) {
+  Meta m;
+  m.nb = d.nb;
+  m.parent = d.parent;
+  m.first_child = d.first_child;
+  m.tree = d.tree;
+  m.qd = d.qd;
+  m.dr = d.dr;
+  m.offg = d.offg;
+  m.offi = d.offi;
+  m.bctype = d.bctype;
+  m.bcoff = d.bcoff;
+  m.bcval = d.bcval;
+  m.active = d.active;
+  return m;
+}
+
+static int grid_for(long long units, int n_sm) {
+  long long cap = (long long)n_sm * 16;
+  return (int)std::max(1LL, std::min(units, cap));
+}
+
+template <class T>
+static int dmalloc(T** p, long long n, long long& bytes) {
+  size_t b = (size_t)std::max(1LL, n) * sizeof(T);
+  if (cudaMalloc((void**)p, b) != cudaSuccess) return AFV_ERR_NOMEM;
+  bytes += (long long)b;
+  return AFV_OK;
+}
+
+template <class T>
+static int dupload(T** p, const std::vector<T>& v, long long& bytes) {
+  int rc = dmalloc(p, (long long)v.size(), bytes);
+  if (rc) return rc;
+  if (!v.empty() && cudaMemcpy(*p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice) != cudaSuccess)
+    return AFV_ERR_CUDA;
+  return AFV_OK;
+}
+
+Forest::~Forest() {
+  cudaSetDevice(device);
+  if (stream) cudaStreamSynchronize(stream);
+  void* ptrs[] = {meta.nb, meta.parent, meta.first_child, meta.tree, meta.qd, meta.dr, meta.offg,
+                  meta.offi, meta.bctype, meta.bcoff, meta.bcval, meta.active, d64.phi, d64.rhs,
+                  d64.tmp, d32.phi, d32.rhs, d32.tmp, base_phi64, base_rhs64, d_lists, d_norm,
+                  d_fmax, d_count, d_stage, d_stage_slots};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  for (const ProfEntry& p : prof) {
+    cudaEventDestroy(p.start);
+    cudaEventDestroy(p.stop);
+  }
+  for (cudaEvent_t e : event_pool) cudaEventDestroy(e);
+  if (h_count) cudaFreeHost(h_count);
+  if (h_norm) cudaFreeHost(h_norm);
+  if (stream) cudaStreamDestroy(stream);
+}
+
+int Forest::check(std::string& err, const char* where) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    err = std::string(where) + ": " + cudaGetErrorString(e);
+    return AFV_ERR_CUDA;
+  }
+  return AFV_OK;
+}
+
+cudaEvent_t Forest::prof_begin(int kind) {
+  ++n_launches;
+  if (!(prof_mask & (1 << kind))) return nullptr;
+  cudaEvent_t e;
+  if (!event_pool.empty()) {
+    e = event_pool.back();
+    event_pool.pop_back();
+  } else {
+    cudaEventCreate(&e);
+  }
+  cudaEventRecord(e, stream);
+  return e;
+}
+
+void Forest::prof_end(cudaEvent_t start, int kind, double b) {
+  if (!start) return;
+  cudaEvent_t e;
+  if (!event_pool.empty()) {
+    e = event_pool.back();
+    event_pool.pop_back();
+  } else {
+    cudaEventCreate(&e);
+  }
+  cudaEventRecord(e, stream);
+  prof.push_back(ProfEntry{start, e, kind, b});
+}
+
+int Forest::prof_read(int kind, long long* launches, double* ms, double* b) {
+  cudaStreamSynchronize(stream);
+  long long n = 0;
+  double t = 0, by = 0;
+  for (const ProfEntry& p : prof) {
+    if (p.kind != kind) continue;
+    float x = 0;
+    cudaEventElapsedTime(&x, p.start, p.stop);
+    t += x;
+    by += p.bytes;
+    ++n;
+  }
+  *launches = n;
+  *ms = t;
+  *b = by;
+  return AFV_OK;
+}
+
+void Forest::prof_reset() {
+  cudaStreamSynchronize(stream);
+  for (const ProfEntry& p : prof) {
+    event_pool.push_back(p.start);
+    event_pool.push_back(p.stop);
+  }
+  prof.clear();
+}
+
+// Brackets one launch with profiler events.
+struct ProfScope {
+  Forest* f;
+  int kind;
+  double bytes;
+  cudaEvent_t e;
+  ProfScope(Forest* f_, int k, double b) : f(f_), kind(k), bytes(b) { e = f->prof_begin(k); }
+  ~ProfScope() { f->prof_end(e, kind, bytes); }
+};
+
+int Forest::create(const std::vector<const HostTree*>& trees, const afv_forest_opts* opts,
+                   std::string& err) {
+  int rc = build_plan(trees, plan, err);
+  if (rc) return rc;
+  device = opts ? opts->device : 0;
+  mixed = opts ? opts->mixed_buffers != 0 : false;
+  if (cudaSetDevice(device) != cudaSuccess) return err = "cudaSetDevice failed", AFV_ERR_CUDA;
+  cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, device);
+  if (cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking) != cudaSuccess)
+    return err = "cudaStreamCreate failed", AFV_ERR_CUDA;
+  const Plan& p = plan;
+  bytes = 0;
+#define UP(field, vec) \
+  if ((rc = dupload(&meta.field, p.vec, bytes))) return err = "device allocation failed", rc;
+  UP(nb, nb);
+  UP(parent, parent);
+  UP(first_child, first_child);
+  UP(tree, tree);
+  UP(qd, qd);
+  UP(dr, dr);
+  UP(offg, offg);
+  UP(offi, offi);
+  UP(bctype, bctype);
+#undef UP
+  if ((rc = upload_bc(err))) return rc;
+  std::vector<int> act(p.n_trees, 1);
+  if ((rc = dupload(&meta.active, act, bytes))) return err = "device allocation failed", rc;
+  host_active = act;
+
+  if (dmalloc(&d64.phi, p.n_elem_g, bytes) || dmalloc(&d64.tmp, p.n_elem_g, bytes) ||
+      dmalloc(&d64.rhs, p.n_elem_i, bytes))
+    return err = "device allocation of the FP64 state failed", AFV_ERR_NOMEM;
+  cudaMemset(d64.phi, 0, p.n_elem_g * sizeof(double));
+  cudaMemset(d64.tmp, 0, p.n_elem_g * sizeof(double));
+  cudaMemset(d64.rhs, 0, p.n_elem_i * sizeof(double));
+  if (mixed) {
+    if (dmalloc(&d32.phi, p.n_elem_g, bytes) || dmalloc(&d32.tmp, p.n_elem_g, bytes) ||
+        dmalloc(&d32.rhs, p.n_elem_i, bytes))
+      return err = "device allocation of the FP32 state failed", AFV_ERR_NOMEM;
+    cudaMemset(d32.phi, 0, p.n_elem_g * sizeof(float));
+    cudaMemset(d32.tmp, 0, p.n_elem_g * sizeof(float));
+    cudaMemset(d32.rhs, 0, p.n_elem_i * sizeof(float));
+    int l0 = p.min_lvl;
+    long long ng = (long long)p.lvl_n[p.L(l0)] * (long long)std::pow(p.nc_at(l0) + 2, p.dim);
+    long long ni = (long long)p.lvl_n[p.L(l0)] * (long long)std::pow(p.nc_at(l0), p.dim);
+    if (dmalloc(&base_phi64, ng, bytes) || dmalloc(&base_rhs64, ni, bytes))
+      return err = "device allocation failed", AFV_ERR_NOMEM;
+  }
+  // level lists
+  std::vector<int> lists;
+  int nlev = p.max_lvl - p.min_lvl + 1;
+  leaves_off.assign(nlev, 0);
+  parents_off.assign(nlev, 0);
+  for (int k = 0; k < nlev; ++k) {
+    leaves_off[k] = (int)lists.size();
+    lists.insert(lists.end(), p.leaves[k].begin(), p.leaves[k].end());
+    parents_off[k] = (int)lists.size();
+    lists.insert(lists.end(), p.parents[k].begin(), p.parents[k].end());
+  }
+  all_leaves_off = (int)lists.size();
+  lists.insert(lists.end(), p.all_leaves.begin(), p.all_leaves.end());
+  if ((rc = dupload(&d_lists, lists, bytes))) return err = "device allocation failed", rc;
+  if (dmalloc(&d_norm, p.n_trees, bytes) || dmalloc(&d_fmax, p.n_trees, bytes) ||
+      dmalloc(&d_count, 1, bytes))
+    return err = "device allocation failed", AFV_ERR_NOMEM;
+  if (cudaMallocHost((void**)&h_count, sizeof(int)) != cudaSuccess ||
+      cudaMallocHost((void**)&h_norm, sizeof(unsigned long long) * p.n_trees) != cudaSuccess)
+    return err = "pinned allocation failed", AFV_ERR_NOMEM;
+  if (cudaDeviceSynchronize() != cudaSuccess) return check(err, "forest create");
+  return AFV_OK;
+}
+
+int Forest::upload_bc(std::string& err) {
+  long long b = 0;
+  if (meta.bcoff) cudaFree(meta.bcoff);
+  if (meta.bcval) cudaFree(meta.bcval);
+  meta.bcoff = nullptr;
+  meta.bcval = nullptr;
+  if (dupload(&meta.bcoff, plan.bcoff, b) || dupload(&meta.bcval, plan.bcval, b))
+    return err = "device allocation failed", AFV_ERR_NOMEM;
+  if (cudaMemcpy(meta.bctype, plan.bctype.data(), plan.bctype.size() * sizeof(int),
+                 cudaMemcpyHostToDevice) != cudaSuccess)
+    return err = "bc upload failed", AFV_ERR_CUDA;
+  return AFV_OK;
+}
+
+int Forest::set_active_all(int v) {
+  std::vector<int> a(plan.n_trees, v);
+  return set_active_host(a);
+}
+
+int Forest::set_active_host(const std::vector<int>& a) {
+  host_active = a;
+  cudaMemcpyAsync(meta.active, host_active.data(), sizeof(int) * a.size(), cudaMemcpyHostToDevice,
+                  stream);
+  cudaStreamSynchronize(stream);
+  return AFV_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Host exchange
+// ---------------------------------------------------------------------------
+
+
+// Copies between the host layout and slot storage go level by level: the
+// host buffer is the concatenation, over the tree's levels, of its boxes in
+// level-list order.
+static int exchange(Forest& F, int t, int var, double* host, int interior_only, bool to_dev,
+                    std::string& err) {
+  const Plan& p = F.plan;
+  if (t < 0 || t >= p.n_trees) return err = "tree index out of range", AFV_ERR_INVALID;
+  if (var < AFV_PHI || var > AFV_TMP) return err = "unknown variable", AFV_ERR_INVALID;
+  const std::vector<int>& order = p.host_order[t];
+  const int D = p.dim;
+  // sizes per box follow the level of each slot
+  long long total = 0;
+  for (int s : order) {
+    int nc = p.nc_at(p.lvl[s]);
+    total += interior_only ? (long long)std::pow(nc, D) : (long long)std::pow(nc + 2, D);
+  }
+  if (F.stage_elems < total || !F.d_stage) {
+    if (F.d_stage) cudaFree(F.d_stage);
+    if (F.d_stage_slots) cudaFree(F.d_stage_slots);
+    F.d_stage = nullptr;
+    F.d_stage_slots = nullptr;
+    if (cudaMalloc((void**)&F.d_stage, sizeof(double) * std::max(1LL, total)) != cudaSuccess)
+      return err = "staging allocation failed", AFV_ERR_NOMEM;
+    F.stage_elems = total;
+  }
+  if (!F.d_stage_slots) {
+    size_t maxn = 0;
+    for (const auto& o : p.host_order) maxn = std::max(maxn, o.size());
+    if (cudaMalloc((void**)&F.d_stage_slots, sizeof(int) * std::max<size_t>(1, maxn)) != cudaSuccess)
+      return err = "staging allocation failed", AFV_ERR_NOMEM;
+  }
+  cudaStream_t st = F.stream;
+  cudaMemcpyAsync(F.d_stage_slots, order.data(), sizeof(int) * order.size(), cudaMemcpyHostToDevice, st);
+  if (to_dev)
+    cudaMemcpyAsync(F.d_stage, host, sizeof(double) * total, cudaMemcpyHostToDevice, st);
+  Meta m = meta_of(F.meta);
+  bool ghosted = var != AFV_RHS;
+  double* dvar = var == AFV_PHI ? F.d64.phi : var == AFV_RHS ? F.d64.rhs : F.d64.tmp;
+  // runs of consecutive boxes with the same level
+  size_t i = 0;
+  long long off = 0;
+  while (i < order.size()) {
+    int l = p.lvl[order[i]];
+    size_t j = i;
+    while (j < order.size() && p.lvl[order[j]] == l) ++j;
+    int n = (int)(j - i);
+    int nc = p.nc_at(l);
+    long long per = interior_only ? (long long)std::pow(nc, D) : (long long)std::pow(nc + 2, D);
+    with_nc(D, nc, [&](auto d_, auto nc_) {
+      constexpr int DD = decltype(d_)::value, NC = decltype(nc_)::value;
+      int grid = grid_for((n * per + 255) / 256, F.n_sm);
+      ProfScope ps(&F, kProfOther, 16.0 * n * per);
+      if (to_dev)
+        dev::k_scatter<DD, NC, double><<<grid, 256, 0, st>>>(m, F.d_stage_slots + i, n, F.d_stage + off,
+                                                            dvar, interior_only, ghosted);
+      else
+        dev::k_gather<DD, NC, double><<<grid, 256, 0, st>>>(m, F.d_stage_slots + i, n, dvar,
+                                                           F.d_stage + off, interior_only, ghosted);
+    });
+    off += n * per;
+    i = j;
+  }
+  if (!to_dev) cudaMemcpyAsync(host, F.d_stage, sizeof(double) * total, cudaMemcpyDeviceToHost, st);
+  if (cudaStreamSynchronize(st) != cudaSuccess) return F.check(err, "host exchange");
+  return F.check(err, "host exchange");
+}
+
+}  // namespace afv
+
+namespace afv {
+
+int forest_set_var(Forest& F, int t, int var, const double* host, int interior_only, std::string& err) {
+  return exchange(F, t, var, const_cast<double*>(host), interior_only, true, err);
+}
+int forest_get_var(Forest& F, int t, int var, double* host, int interior_only, std::string& err) {
+  return exchange(F, t, var, host, interior_only, false, err);
+}
+
+int Forest::get_var(int t, int var, double* host, int interior_only, std::string& err) {
+  return forest_get_var(*this, t, var, host, interior_only, err);
+}
+int Forest::set_var(int t, int var, const double* host, int interior_only, std::string& err) {
+  return forest_set_var(*this, t, var, host, interior_only, err);
+}
+
+// ---------------------------------------------------------------------------
+// Level operators
+// ---------------------------------------------------------------------------
+
+template <class T>
+void Forest::sweep(const Arrays<T>& a, int lvl, int n, bool pull, bool homog) {
+  int nbx = lvl_n(lvl);
+  if (!nbx) return;
+  BoxSet bs{nullptr, plan.lvl_lo[plan.L(lvl)], nbx};
+  Meta m = meta_of(meta);
+  with_nc(plan.dim, plan.nc_at(lvl), [&](auto d_, auto nc_) {
+    constexpr int D = decltype(d_)::value, NC = decltype(nc_)::value;
+    using G = dev::Geo<D, NC>;
+    constexpr int BPC = dev::boxes_per_cta<G::SG, G::SI / 2, T>(1);
+    int grid = grid_for((nbx + BPC - 1) / BPC, n_sm);
+    // read phi and f, write phi over the interior
+    ProfScope ps(this, kProfSweep, 3.0 * nbx * G::SI * sizeof(T));
+    dev::k_sweep<D, NC, T><<<grid, dev::kThreads, 0, stream>>>(m, bs, a.phi, a.rhs, n, pull ? 1 : 0,
+                                                              homog ? 1 : 0);
+  });
+}
+
+template <class T>
+void Forest::fill(const Arrays<T>& a, int lvl, bool homog) {
+  int nbx = lvl_n(lvl);
+  if (!nbx) return;
+  BoxSet bs{nullptr, plan.lvl_lo[plan.L(lvl)], nbx};
+  Meta m = meta_of(meta);
+  with_nc(plan.dim, plan.nc_at(lvl), [&](auto d_, auto nc_) {
+    constexpr int D = decltype(d_)::value, NC = decltype(nc_)::value;
+    using G = dev::Geo<D, NC>;
+    long long items = (long long)nbx * G::NNB * G::NF;
+    int grid = grid_for((items + dev::kThreads - 1) / dev::kThreads, n_sm);
+    // read the neighbour face value, write the ghost value
+    ProfScope ps(this, kProfFill, 2.0 * items * sizeof(T));
+    dev::k_fill<D, NC, T><<<grid, dev::kThreads, 0, stream>>>(m, bs, a.phi, homog ? 1 : 0);
+  });
+}
+
+template <class T>
+void Forest::restrict_res(const Arrays<T>& a, int lvl, bool with_res) {
+  int nbx = lvl_n(lvl);
+  if (!nbx || lvl <= plan.min_lvl) return;
+  BoxSet bs{nullptr, plan.lvl_lo[plan.L(lvl)], nbx};
+  Meta m = meta_of(meta);
+  bool sub = lvl <= 1;
+  with_nc(plan.dim, plan.nc_at(lvl), [&](auto d_, auto nc_) {
+    constexpr int D = decltype(d_)::value, NC = decltype(nc_)::value;
+    using G = dev::Geo<D, NC>;
+    constexpr int H = NC / 2;
+    constexpr int PER_BOX = D == 2 ? H * H : H * H * H;
+    constexpr int BPC = dev::boxes_per_cta<G::SG, PER_BOX, T>(1);
+    int grid = grid_for((nbx + BPC - 1) / BPC, n_sm);
+    // read phi, f; write the parent's phi and tmp (2 values per 2^D fine cells)
+    ProfScope ps(this, kProfRestrict,
+                 (2.0 + 2.0 / (1 << D)) * nbx * G::SI * sizeof(T));
+    if (sub)
+      dev::k_restrict_res<D, NC, true, T><<<grid, dev::kThreads, 0, stream>>>(m, bs, a.phi, a.rhs, a.tmp,
+                                                                             with_res ? 1 : 0);
+    else
+      dev::k_restrict_res<D, NC, false, T><<<grid, dev::kThreads, 0, stream>>>(m, bs, a.phi, a.rhs,
+                                                                              a.tmp, with_res ? 1 : 0);
+  });
+}
+
+template <class T>
+void Forest::coarse_rhs(const Arrays<T>& a, int lp, bool copy_tmp) {
+  int np = n_parents(lp);
+  if (!np) return;
+  BoxSet bs{parents_list(lp), 0, np};
+  Meta m = meta_of(meta);
+  with_nc(plan.dim, plan.nc_at(lp), [&](auto d_, auto nc_) {
+    constexpr int D = decltype(d_)::value, NC = decltype(nc_)::value;
+    using G = dev::Geo<D, NC>;
+    constexpr int PER_BOX = G::SI < dev::kThreads ? G::SI : dev::kThreads;
+    constexpr int BPC = dev::boxes_per_cta<G::SG, PER_BOX, T>(1);
+    int grid = grid_for((np + BPC - 1) / BPC, n_sm);
+    // read phi, tmp; write rhs, tmp
+    ProfScope ps(this, kProfCoarseRhs, 4.0 * np * G::SI * sizeof(T));
+    dev::k_coarse_rhs<D, NC, T><<<grid, dev::kThreads, 0, stream>>>(m, bs, a.phi, a.rhs, a.tmp,
+                                                                   copy_tmp ? 1 : 0);
+  });
+}
+
+template <class T>
+void Forest::correct(const Arrays<T>& a, int lp) {
+  int np = n_parents(lp);
+  if (!np) return;
+  BoxSet bs{parents_list(lp), 0, np};
+  Meta m = meta_of(meta);
+  bool sub = lp + 1 <= 1;
+  with_nc(plan.dim, plan.nc_at(lp), [&](auto d_, auto nc_) {
+    constexpr int D = decltype(d_)::value, NC = decltype(nc_)::value;
+    using G = dev::Geo<D, NC>;
+    constexpr int PER_BOX = G::SI < dev::kThreads ? G::SI : dev::kThreads;
+    constexpr int BPC = dev::boxes_per_cta<G::SG, PER_BOX, T>(1);
+    int grid = grid_for((np + BPC - 1) / BPC, n_sm);
+    // parent: read phi, tmp, write tmp; children: read and write phi
+    ProfScope ps(this, kProfCorrect, (3.0 + 2.0 * (1 << D)) * np * G::SI * sizeof(T));
+    if (sub) {
+      if constexpr (!(D == 2 && NC == 16) && !(D == 3 && NC == 8))
+        dev::k_correct<D, NC, true, T><<<grid, dev::kThreads, 0, stream>>>(m, bs, a.phi, a.tmp);
+    } else {
+      dev::k_correct<D, NC, false, T><<<grid, dev::kThreads, 0, stream>>>(m, bs, a.phi, a.tmp);
+    }
+  });
+}
+
+template <class T>
+void Forest::residual(const Arrays<T>& a, int lvl, unsigned long long* norm, bool store) {
+  int nbx = lvl_n(lvl);
+  if (!nbx) return;
+  BoxSet bs{nullptr, plan.lvl_lo[plan.L(lvl)], nbx};
+  Meta m = meta_of(meta);
+  with_nc(plan.dim, plan.nc_at(lvl), [&](auto d_, auto nc_) {
+    constexpr int D = decltype(d_)::value, NC = decltype(nc_)::value;
+    using G = dev::Geo<D, NC>;
+    constexpr int PER_BOX = G::SI < dev::kThreads ? G::SI : dev::kThreads;
+    constexpr int BPC = dev::kThreads / PER_BOX;
+    int grid = grid_for((nbx + BPC - 1) / BPC, n_sm);
+    ProfScope ps(this, kProfResidual, (store ? 3.0 : 2.0) * nbx * G::SI * sizeof(T));
+    dev::k_residual<D, NC, T><<<grid, dev::kThreads, 0, stream>>>(m, bs, a.phi, a.rhs, a.tmp, norm,
+                                                                 store ? 1 : 0);
+  });
+}
+
+// gsrb_boxes, src/m_aX_mg.f90:397-420: 2*n_cycle half-sweeps, each followed by
+// a ghost fill. The fill after half-sweep n is folded into half-sweep n+1
+// (pull); the last one is a separate launch.
+template <class T>
+void Forest::gsrb_boxes(const Arrays<T>& a, int lvl, int n_cycle, bool homog) {
+  if (!lvl_n(lvl) || n_cycle <= 0) return;
+  for (int n = 1; n <= 2 * n_cycle; ++n) sweep(a, lvl, n, n > 1, homog);
+  fill(a, lvl, homog);
+}
+
+// update_coarse (copy_tmp) and set_coarse_phi_rhs (no copy),
+// src/m_aX_mg.f90:424-517.
+template <class T>
+void Forest::update_coarse_t(const Arrays<T>& a, int lvl, bool homog, bool copy_tmp) {
+  restrict_res(a, lvl, true);
+  fill(a, lvl - 1, homog);
+  coarse_rhs(a, lvl - 1, copy_tmp);
+}
+
+// mg$D_fas_vcycle, src/m_aX_mg.f90:208-255 (without the residual branch).
+// base64: smooth the coarsest level in FP64 (mixed cycle).
+template <class T>
+void Forest::vcycle_t(const Arrays<T>& a, const MgOpts& mg, int highest, bool homog, bool base64) {
+  const int l0 = plan.min_lvl;
+  for (int l = highest; l >= l0 + 1; --l) {
+    gsrb_boxes(a, l, mg.n_down, homog);
+    update_coarse_t(a, l, homog, true);
+  }
+  if (base64 && !std::is_same<T, double>::value) {
+    long long ng = 0, ni = 0;
+    int nb0 = lvl_n(l0);
+    ng = (long long)nb0 * (long long)std::pow(plan.nc_at(l0) + 2, plan.dim);
+    ni = (long long)nb0 * (long long)std::pow(plan.nc_at(l0), plan.dim);
+    int g1 = grid_for((ng + 255) / 256, n_sm), g2 = grid_for((ni + 255) / 256, n_sm);
+    {
+      ProfScope ps(this, kProfOther, (8.0 + sizeof(T)) * ng);
+      dev::k_convert<double, T><<<g1, 256, 0, stream>>>(base_phi64, a.phi, ng);
+    }
+    {
+      ProfScope ps(this, kProfOther, (8.0 + sizeof(T)) * ni);
+      dev::k_convert<double, T><<<g2, 256, 0, stream>>>(base_rhs64, a.rhs, ni);
+    }
+    Arrays<double> b{base_phi64, base_rhs64, nullptr};
+    gsrb_boxes(b, l0, mg.n_base, homog);
+    {
+      ProfScope ps(this, kProfOther, (8.0 + sizeof(T)) * ng);
+      dev::k_convert<T, double><<<g1, 256, 0, stream>>>(a.phi, base_phi64, ng);
+    }
+  } else {
+    gsrb_boxes(a, l0, mg.n_base, homog);
+  }
+  for (int l = l0 + 1; l <= highest; ++l) {
+    correct(a, l - 1);
+    fill(a, l, homog);
+    gsrb_boxes(a, l, mg.n_up, homog);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// FP64 entry points
+// ---------------------------------------------------------------------------
+
+int Forest::gsrb_level(int lvl, int n_cycle, std::string& err) {
+  gsrb_boxes(d64, lvl, n_cycle, false);
+  return check(err, "gsrb_level");
+}
+int Forest::fill_level(int lvl, std::string& err) {
+  fill(d64, lvl, false);
+  return check(err, "fill_level");
+}
+int Forest::update_coarse(int lvl, std::string& err) {
+  if (lvl <= plan.min_lvl || lvl > plan.max_lvl) return err = "level out of range", AFV_ERR_INVALID;
+  update_coarse_t(d64, lvl, false, true);
+  return check(err, "update_coarse");
+}
+int Forest::correct_children(int lp, std::string& err) {
+  if (lp < plan.min_lvl || lp >= plan.max_lvl) return err = "level out of range", AFV_ERR_INVALID;
+  correct(d64, lp);
+  return check(err, "correct_children");
+}
+int Forest::residual_all(unsigned long long* norm, std::string& err) {
+  for (int l = plan.min_lvl; l <= plan.max_lvl; ++l) residual(d64, l, norm, true);
+  return check(err, "residual");
+}
+
+int Forest::vcycle(const MgOpts& mg, int highest, bool set_residual, std::string& err) {
+  if (highest < plan.min_lvl) return err = "highest_lvl below the coarsest level", AFV_ERR_INVALID;
+  highest = std::min(highest, plan.max_lvl);
+  vcycle_t(d64, mg, highest, false, false);
+  if (set_residual)
+    for (int l = plan.min_lvl; l <= highest; ++l) residual(d64, l, nullptr, true);
+  return check(err, "vcycle");
+}
+
+int Forest::gc_tree(std::string& err) {
+  for (int l = plan.min_lvl; l <= plan.max_lvl; ++l) fill(d64, l, false);
+  return check(err, "gc_tree");
+}
+
+// mg$D_fas_fmg, src/m_aX_mg.f90:164-203, for every tree of the forest. Trees
+// of different depth finish at their own highest level: at FMG step lvl only
+// trees with highest_lvl >= lvl take part.
+int Forest::fmg(const MgOpts& mg, bool set_residual, bool have_guess, std::string& err) {
+  const int l0 = plan.min_lvl;
+  std::vector<int> all(plan.n_trees, 1);
+  set_active_host(all);
+  Meta m = meta_of(meta);
+  if (have_guess) {
+    for (int l = plan.max_lvl; l >= l0 + 1; --l) {
+      // set_coarse_phi_rhs(l): trees with highest == l first fill level l.
+      std::vector<int> top(plan.n_trees, 0);
+      bool any = false;
+      for (int t = 0; t < plan.n_trees; ++t)
+        if (plan.tree_highest[t] == l) top[t] = 1, any = true;
+      if (any) {
+        set_active_host(top);
+        fill(d64, l, false);
+        set_active_host(all);
+      }
+      update_coarse_t(d64, l, false, false);
+    }
+  } else {
+    // init_phi_rhs: phi = 0 on levels > min_lvl, rhs restricted downwards.
+    for (int l = plan.max_lvl; l >= l0 + 1; --l) {
+      int nbx = lvl_n(l);
+      if (!nbx) continue;
+      BoxSet bs{nullptr, plan.lvl_lo[plan.L(l)], nbx};
+      bool sub = l <= 1;
+      with_nc(plan.dim, plan.nc_at(l), [&](auto d_, auto nc_) {
+        constexpr int D = decltype(d_)::value, NC = decltype(nc_)::value;
+        using G = dev::Geo<D, NC>;
+        constexpr int VW = dev::Vec<double>::w;
+        long long items = (long long)nbx * (G::SG / VW);
+        {
+          ProfScope ps(this, kProfOther, 8.0 * nbx * G::SG);
+          dev::k_box_op<D, NC, double><<<grid_for((items + 255) / 256, n_sm), 256, 0, stream>>>(
+              m, bs, d64.phi, nullptr, 0);
+        }
+        constexpr int H = NC / 2;
+        long long it2 = (long long)nbx * (D == 2 ? H * H : H * H * H);
+        ProfScope ps(this, kProfOther, 8.0 * nbx * G::SI * (1.0 + 1.0 / (1 << D)));
+        if (sub)
+          dev::k_restrict_interior<D, NC, true, double>
+              <<<grid_for((it2 + 255) / 256, n_sm), 256, 0, stream>>>(m, bs, d64.rhs);
+        else
+          dev::k_restrict_interior<D, NC, false, double>
+              <<<grid_for((it2 + 255) / 256, n_sm), 256, 0, stream>>>(m, bs, d64.rhs);
+      });
+    }
+  }
+  for (int l = l0; l <= plan.max_lvl; ++l) {
+    std::vector<int> act(plan.n_trees, 0);
+    for (int t = 0; t < plan.n_trees; ++t) act[t] = plan.tree_highest[t] >= l;
+    set_active_host(act);
+    int nbx = lvl_n(l);
+    if (nbx) {
+      BoxSet bs{nullptr, plan.lvl_lo[plan.L(l)], nbx};
+      with_nc(plan.dim, plan.nc_at(l), [&](auto d_, auto nc_) {
+        constexpr int D = decltype(d_)::value, NC = decltype(nc_)::value;
+        using G = dev::Geo<D, NC>;
+        constexpr int VW = dev::Vec<double>::w;
+        long long items = (long long)nbx * (G::SG / VW);
+        ProfScope ps(this, kProfOther, 16.0 * nbx * G::SG);
+        dev::k_box_op<D, NC, double><<<grid_for((items + 255) / 256, n_sm), 256, 0, stream>>>(
+            m, bs, d64.tmp, d64.phi, 1);
+      });
+    }
+    if (l > l0) {
+      correct(d64, l - 1);
+      fill(d64, l, false);
+    }
+    vcycle_t(d64, mg, l, false, false);
+    if (set_residual) {
+      std::vector<int> fin(plan.n_trees, 0);
+      bool any = false;
+      for (int t = 0; t < plan.n_trees; ++t)
+        if (plan.tree_highest[t] == l) fin[t] = 1, any = true;
+      if (any) {
+        set_active_host(fin);
+        for (int k = l0; k <= l; ++k) residual(d64, k, nullptr, true);
+      }
+    }
+  }
+  set_active_host(all);
+  return check(err, "fmg");
+}
+
+int Forest::max_abs(int t, int var, double* out, std::string& err) {
+  if (t < 0 || t >= plan.n_trees) return err = "tree index out of range", AFV_ERR_INVALID;
+  std::vector<int> act(plan.n_trees, 0);
+  act[t] = 1;
+  std::vector<int> saved = host_active;
+  set_active_host(act);
+  cudaMemsetAsync(d_norm, 0, sizeof(unsigned long long) * plan.n_trees, stream);
+  Meta m = meta_of(meta);
+  for (int l = plan.min_lvl; l <= plan.max_lvl; ++l) {
+    int nl = n_leaves(l);
+    if (!nl) continue;
+    BoxSet bs{leaves_list(l), 0, nl};
+    const double* v = var == AFV_PHI ? d64.phi : var == AFV_RHS ? d64.rhs : d64.tmp;
+    with_nc(plan.dim, plan.nc_at(l), [&](auto d_, auto nc_) {
+      constexpr int D = decltype(d_)::value, NC = decltype(nc_)::value;
+      using G = dev::Geo<D, NC>;
+      constexpr int PER_BOX = G::SI < dev::kThreads ? G::SI : dev::kThreads;
+      constexpr int BPC = dev::kThreads / PER_BOX;
+      ProfScope ps(this, kProfOther, 8.0 * nl * G::SI);
+      dev::k_maxabs<D, NC, double><<<grid_for((nl + BPC - 1) / BPC, n_sm), dev::kThreads, 0, stream>>>(
+          m, bs, v, var != AFV_RHS, d_norm);
+    });
+  }
+  cudaMemcpyAsync(h_norm, d_norm, sizeof(unsigned long long) * plan.n_trees, cudaMemcpyDeviceToHost,
+                  stream);
+  cudaStreamSynchronize(stream);
+  std::memcpy(out, &h_norm[t], sizeof(double));
+  set_active_host(saved);
+  return check(err, "max_abs");
+}
+
+// Ghost fill of the FP64 state on all levels, coarse to fine.
+void Forest::fill_all64(bool homog) {
+  for (int l = plan.min_lvl; l <= plan.max_lvl; ++l) fill(d64, l, homog);
+}
+
+// a$D_restrict_tree for phi (src/m_aX_restrict.f90:54-64), then ghost cells.
+void Forest::restrict_tree_phi64() {
+  for (int l = plan.max_lvl; l >= plan.min_lvl + 1; --l) restrict_res(d64, l, false);
+  fill_all64(false);
+}
+
+// Solve every tree to max|f - L phi| <= tol * max|f| over its leaves.
+int Forest::solve(const MgOpts& mg, int precision, double tol, int max_cycles, SolveStats& st,
+                  std::string& err) {
+  const int nt = plan.n_trees;
+  if (precision == AFV_PREC_MIXED && !mixed)
+    return err = "forest created without mixed_buffers", AFV_ERR_STATE;
+  st.cycles.assign(nt, 0);
+  st.rel_res.assign(nt, 0.0);
+  Meta m = meta_of(meta);
+  set_active_all(1);
+  // max |f| over the leaves of every tree
+  cudaMemsetAsync(d_norm, 0, sizeof(unsigned long long) * nt, stream);
+  for (int l = plan.min_lvl; l <= plan.max_lvl; ++l) {
+    int nl = n_leaves(l);
+    if (!nl) continue;
+    BoxSet bs{leaves_list(l), 0, nl};
+    with_nc(plan.dim, plan.nc_at(l), [&](auto d_, auto nc_) {
+      constexpr int D = decltype(d_)::value, NC = decltype(nc_)::value;
+      using G = dev::Geo<D, NC>;
+      constexpr int PER_BOX = G::SI < dev::kThreads ? G::SI : dev::kThreads;
+      constexpr int BPC = dev::kThreads / PER_BOX;
+      ProfScope ps(this, kProfOther, 8.0 * nl * G::SI);
+      dev::k_maxabs<D, NC, double><<<grid_for((nl + BPC - 1) / BPC, n_sm), dev::kThreads, 0, stream>>>(
+          m, bs, d64.rhs, 0, d_norm);
+    });
+  }
+  cudaMemcpyAsync(d_fmax, d_norm, sizeof(double) * nt, cudaMemcpyDeviceToDevice, stream);
+  std::vector<double> fmax(nt);
+  cudaMemcpyAsync(fmax.data(), d_norm, sizeof(double) * nt, cudaMemcpyDeviceToHost, stream);
+  cudaStreamSynchronize(stream);
+  std::vector<int> done_cycles(nt, 0);
+
+  auto residual_check = [&](bool mixed_path) -> int {
+    cudaMemsetAsync(d_norm, 0, sizeof(unsigned long long) * nt, stream);
+    if (mixed_path) {
+      fill_all64(false);
+      int nl = (int)plan.all_leaves.size();
+      BoxSet bs{d_lists + all_leaves_off, 0, nl};
+      with_nc(plan.dim, plan.nc, [&](auto d_, auto nc_) {
+        constexpr int D = decltype(d_)::value, NC = decltype(nc_)::value;
+        using G = dev::Geo<D, NC>;
+        constexpr int PER_BOX = G::SI < dev::kThreads ? G::SI : dev::kThreads;
+        constexpr int BPC = dev::kThreads / PER_BOX;
+        // read u (8 B), f (8 B); write r (4 B)
+        ProfScope ps(this, kProfDefect, 20.0 * nl * G::SI);
+        dev::k_defect<D, NC><<<grid_for((nl + BPC - 1) / BPC, n_sm), dev::kThreads, 0, stream>>>(
+            m, bs, d64.phi, d64.rhs, d32.rhs, d_norm);
+      });
+    } else {
+      for (int l = plan.min_lvl; l <= plan.max_lvl; ++l) residual(d64, l, d_norm, true);
+    }
+    cudaMemsetAsync(d_count, 0, sizeof(int), stream);
+    {
+      ProfScope ps(this, kProfOther, 20.0 * nt);
+      dev::k_check<<<(nt + 255) / 256, 256, 0, stream>>>(nt, d_norm, d_fmax, tol, meta.active,
+                                                         d_count);
+    }
+    cudaMemcpyAsync(h_count, d_count, sizeof(int), cudaMemcpyDeviceToHost, stream);
+    cudaMemcpyAsync(h_norm, d_norm, sizeof(unsigned long long) * nt, cudaMemcpyDeviceToHost, stream);
+    cudaMemcpyAsync(host_active.data(), meta.active, sizeof(int) * nt, cudaMemcpyDeviceToHost, stream);
+    cudaStreamSynchronize(stream);
+    return *h_count;
+  };
+
+  std::vector<unsigned long long> final_r(nt, 0);
+  auto record = [&](const std::vector<int>& was_active) {
+    for (int t = 0; t < nt; ++t)
+      if (was_active[t]) final_r[t] = h_norm[t];
+  };
+  std::vector<int> was(nt, 1);
+  int n_active = residual_check(precision == AFV_PREC_MIXED);
+  record(was);
+  int cyc = 0;
+  while (n_active > 0 && cyc < max_cycles) {
+    for (int t = 0; t < nt; ++t) done_cycles[t] += host_active[t] ? 1 : 0;
+    if (precision == AFV_PREC_MIXED) {
+      cudaMemsetAsync(d32.phi, 0, sizeof(float) * plan.n_elem_g, stream);
+      vcycle_t(d32, mg, plan.max_lvl, true, true);
+      int nl = (int)plan.all_leaves.size();
+      BoxSet bs{d_lists + all_leaves_off, 0, nl};
+      with_nc(plan.dim, plan.nc, [&](auto d_, auto nc_) {
+        constexpr int D = decltype(d_)::value, NC = decltype(nc_)::value;
+        using G = dev::Geo<D, NC>;
+        long long items = (long long)nl * G::SI;
+        // read e (4 B), read and write u (16 B)
+        ProfScope ps(this, kProfAccumulate, 20.0 * items);
+        dev::k_accumulate<D, NC><<<grid_for((items + 255) / 256, n_sm), 256, 0, stream>>>(m, bs, d64.phi,
+                                                                                       d32.phi);
+      });
+    } else {
+      vcycle_t(d64, mg, plan.max_lvl, false, false);
+    }
+    ++cyc;
+    was = host_active;
+    n_active = residual_check(precision == AFV_PREC_MIXED);
+    record(was);
+    if (int rc = check(err, "solve")) return rc;
+  }
+  if (precision == AFV_PREC_MIXED) {
+    set_active_all(1);
+    restrict_tree_phi64();
+    // residual on every box, as the FP64 path leaves it
+    for (int l = plan.min_lvl; l <= plan.max_lvl; ++l) residual(d64, l, nullptr, true);
+  }
+  set_active_all(1);
+  for (int t = 0; t < nt; ++t) {
+    double r;
+    std::memcpy(&r, &final_r[t], sizeof(double));
+    st.cycles[t] = done_cycles[t];
+    st.rel_res[t] = fmax[t] > 0 ? r / fmax[t] : r;
+  }
+  if (int rc = check(err, "solve")) return rc;
+  st.status = n_active > 0 ? AFV_ERR_TIMEOUT : AFV_OK;
+  if (n_active > 0) err = "not converged within max_cycles";
+  return st.status;
+}
+
+}  // namespace afv

@@ -1,0 +1,353 @@
+"""Benchmark of the FAS multigrid hot path on GB300.
+
+Workload (one step): solve the 3-D adaptive Poisson problem
+poisson3d_nc8_gauss4_seed2 -- 8^3-cell boxes, Dirichlet 0, four seeded
+Gaussians, 1.564e7 leaf cells -- from phi = 0 to a relative residual of 1e-8
+(max |f - L phi| / max |f| over leaf cells), with FP32 V-cycles inside FP64
+defect correction. The metric is V-cycle unknowns/s: leaf cells x V-cycles /
+solve time. The same solve with FP64 V-cycles is timed beside it.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+--impl reference times the CPU oracle (the C++/OpenMP restatement of the
+reference's solver, oracle/) on all host cores, FP64 V-cycles on the same
+tree, one V-cycle per step. Under torchrun each rank solves its own replica
+(one tree does not shard; there is no data-path collective).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+TOL = 1e-8
+
+
+def dist_setup(n_gpus):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        backend = "nccl" if os.environ.get("AFV_BENCH_BACKEND", "nccl") == "nccl" else "gloo"
+        dist.init_process_group(backend)
+    return rank, world, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+class Clocks:
+    """nvidia-smi samples of SM clocks and throttle reasons during a region."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        self.out = ""
+        if self.p is not None:
+            time.sleep(0.3)
+            self.p.terminate()
+            try:
+                self.out, _ = self.p.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.p.kill()
+                self.out = ""
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in (self.out or "").splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[3:7]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def load_traffic():
+    p = os.path.join(ROOT, "profiles", "roofline_traffic.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f)
+    return None
+
+
+def build_workload(spec):
+    from afivo_gb300 import workloads as W
+    t0 = time.time()
+    tree = W.build_tree(spec)
+    return tree, time.time() - t0
+
+
+def cpu_baseline_sample(spec, threads, cycles=2):
+    """Oracle FP64 V-cycles on the same tree, timed on the host cores."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle as O
+    from helpers import oracle_tree
+    O.build()
+    O.set_threads(threads)
+    ot = oracle_tree(spec)
+    ot.fill_gauss(O.I_RHS, spec["gauss"], lpl=True)
+    ot.mg_init()
+    leaves = sum(len(ot.level(l)[1]) for l in range(ot.min_lvl, ot.highest_lvl + 1))
+    cells = leaves * spec["n_cell"] ** spec["dim"]
+    ot.vcycle(set_residual=False)  # warm-up
+    t0 = time.perf_counter()
+    for _ in range(cycles):
+        ot.vcycle(set_residual=False)
+    dt = time.perf_counter() - t0
+    return cells * cycles / dt, dt, cells
+
+
+def run_reference(args, spec):
+    rank, world, local = dist_setup(args.gpus)
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle as O
+    from helpers import oracle_tree
+    O.build()
+    cores = os.cpu_count() or 1
+    O.set_threads(cores)
+    ot = oracle_tree(spec)
+    ot.fill_gauss(O.I_RHS, spec["gauss"], lpl=True)
+    ot.mg_init()
+    leaves = sum(len(ot.level(l)[1]) for l in range(ot.min_lvl, ot.highest_lvl + 1))
+    cells = leaves * spec["n_cell"] ** spec["dim"]
+    for _ in range(args.warmup):
+        ot.vcycle(set_residual=False)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ot.vcycle(set_residual=False)
+    dt = time.perf_counter() - t0
+    value = cells * args.steps / dt
+    line = {
+        "impl": "reference", "metric": "V-cycle unknowns/s", "value": value, "unit": "unknowns/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": spec["name"], "leaf_cells": cells, "cycle": "FAS V(2,2), FP64"},
+        "cpu_baseline": {"value": value, "unit": "unknowns/s", "cores": cores, "kind": "port",
+                         "sample": f"{args.steps} FP64 V-cycles of the full tree (oracle, "
+                                   f"C++/OpenMP restatement of the reference solver)"},
+        "e2e": {"value": value, "unit": "unknowns/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--small", action="store_true", help="smaller tree (quick checks)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    from afivo_gb300 import workloads as W
+    spec = W.c2_poisson_3d(thr=3e-3, lvl_max=7) if args.small else W.c2_poisson_3d()
+    if args.impl == "reference":
+        return run_reference(args, spec)
+
+    rank, world, local = dist_setup(args.gpus)
+    import torch
+    torch.cuda.set_device(local)
+    from afivo_gb300 import build as B
+    B.build()
+    import afivo_gb300 as afv
+
+    tree, t_build = build_workload(spec)
+    forest = afv.Forest([tree], device=local, mixed=True)
+    info = forest.info()
+    cells = info["leaf_cells"]
+    forest.set_source(0, spec["gauss"], lpl=True)
+    ext = torch.cuda.ExternalStream(forest.stream())
+
+    def solve(prec):
+        forest.zero(afv.AFV_PHI)
+        cyc, rel, rc = forest.solve(prec, tol=TOL, max_cycles=60, check=False)
+        if rc != 0:
+            raise RuntimeError(f"solve did not converge: rc={rc} rel={rel[0]:.3e}")
+        return int(cyc[0]), float(rel[0])
+
+    def timed(prec, steps, mask=0):
+        forest.profile(mask)
+        cycles, rels, per = [], [], []
+        barrier(world)
+        torch.cuda.synchronize()
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        l0 = forest.launches()
+        ev0.record(ext)
+        for _ in range(steps):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(ext)
+            c, r = solve(prec)
+            e1.record(ext)
+            e1.synchronize()
+            per.append(e0.elapsed_time(e1))
+            cycles.append(c)
+            rels.append(r)
+        ev1.record(ext)
+        torch.cuda.synchronize()
+        barrier(world)
+        ms = ev0.elapsed_time(ev1)
+        return ms, cycles, rels, per, forest.launches() - l0
+
+    # warm-up
+    for _ in range(args.warmup):
+        solve(afv.AFV_PREC_MIXED)
+        solve(afv.AFV_PREC_FP64)
+
+    with Clocks(local) as clk:
+        ms, cyc, rels, per, launches = timed(afv.AFV_PREC_MIXED, args.steps, mask=1 << 0)
+    sweep_n, sweep_ms, sweep_bytes = forest.profile_read(0)
+    ms = max_over_ranks(ms, world)
+    total_cycles = sum_over_ranks(float(sum(cyc)), world)
+    value = cells * total_cycles / (ms / 1e3)
+
+    ms64, cyc64, rels64, per64, _ = timed(afv.AFV_PREC_FP64, max(1, args.steps // 2))
+    ms64 = max_over_ranks(ms64, world)
+    value64 = cells * sum_over_ranks(float(sum(cyc64)), world) / (ms64 / 1e3)
+
+    # per-kernel breakdown of one mixed solve (separate pass, all kinds profiled)
+    _, _, _, _, _ = timed(afv.AFV_PREC_MIXED, 1, mask=0xFF)
+    breakdown = {}
+    for k, name in enumerate(afv.KERNEL_KINDS):
+        n, kms, kb = forest.profile_read(k)
+        if n:
+            breakdown[name] = {"launches": n, "ms": round(kms, 4),
+                               "GB/s": round(kb / (kms / 1e3) / 1e9, 1) if kms > 0 else None}
+    forest.profile(0)
+
+    # end to end through the C ABI with host buffers
+    from afivo_gb300 import lib  # noqa: F401
+    n_in = forest._n_values(0, True)
+    host_rhs = torch.empty(n_in, dtype=torch.float64, pin_memory=True)
+    host_phi = torch.empty(n_in, dtype=torch.float64, pin_memory=True)
+    forest.get_var(0, afv.AFV_RHS, interior_only=True, out=host_rhs.numpy())
+    e2e_ms, e2e_cycles = [], 0
+    barrier(world)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        forest.set_var(0, afv.AFV_RHS, host_rhs.numpy(), interior_only=True)
+        c, _r = solve(afv.AFV_PREC_MIXED)
+        forest.get_var(0, afv.AFV_PHI, interior_only=True, out=host_phi.numpy())
+        e2e_cycles += c
+    torch.cuda.synchronize()
+    e2e_s = max_over_ranks(time.perf_counter() - t0, world)
+    e2e_value = cells * sum_over_ranks(float(e2e_cycles), world) / e2e_s
+
+    peak, peak_kind = load_peaks()
+    achieved = sweep_bytes / (sweep_ms / 1e3) / 1e9 if sweep_ms > 0 else None
+    traffic = load_traffic()
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cores = os.cpu_count() or 1
+        v, dt, _ = cpu_baseline_sample(spec, cores, cycles=2)
+        cpu = {"value": v, "unit": "unknowns/s", "cores": cores, "kind": "port",
+               "sample": f"2 FP64 V-cycles of the full tree on the oracle ({dt:.1f} s)"}
+    if rank != 0:
+        return
+    line = {
+        "metric": "V-cycle unknowns/s (mixed FP32/FP64, to 1e-8 rel. residual)",
+        "value": value, "unit": "unknowns/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+        "config": {"workload": spec["name"], "leaf_cells": cells, "boxes": info["n_boxes"],
+                   "levels": [info["min_lvl"], info["max_lvl"]], "tol": TOL,
+                   "cycle": "FAS V(2,2); FP32 cycles in FP64 defect correction",
+                   "l2": "inputs larger than L2 (device state %.0f MB)" % (info["bytes"] / 2 ** 20),
+                   "tree_build_s": round(t_build, 2)},
+        "solve": {"cycles": cyc, "rel_res": max(rels), "ms_p50": float(np.percentile(per, 50)),
+                  "ms_p99": float(np.percentile(per, 99))},
+        "fp64": {"value": value64, "unit": "unknowns/s", "cycles": cyc64, "rel_res": max(rels64),
+                 "ms_per_solve": ms64 / len(cyc64)},
+        "mixed_vs_fp64_solve_speedup": (ms64 / len(cyc64)) / (ms / args.steps),
+        "roofline": {"bound": "hbm", "kernel": "k_sweep<3,8,float>", "achieved": achieved,
+                     "peak": peak, "unit": "GB/s",
+                     "frac": (achieved / peak) if achieved else None,
+                     "peak_kind": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
+                     "launches": sweep_n, "ms": sweep_ms,
+                     "traffic": traffic.get("dram_bytes_per_launch") if traffic else None},
+        "kernels": breakdown,
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_value, "unit": "unknowns/s", "h2d_bytes_per_step": n_in * 8,
+                "d2h_bytes_per_step": n_in * 8},
+        "clocks": clk.summary(),
+        "gpu_launches": launches,
+    }
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,228 @@
+/*
+ * afivo_gb300 — C ABI of a GB300 (sm_103a) FAS multigrid solver for Poisson
+ * problems on quadtree/octree block grids.
+ *
+ * Every entry point here replaces one routine of the Afivo reference's Fortran
+ * API for this path; the citation beside each names it (file:line, paths
+ * relative to the reference project). The Fortran module
+ * fortran/m_afivo_gb300.f90 binds these functions through iso_c_binding
+ * under the reference's own routine names.
+ *
+ * Conventions
+ *  - Every function returns AFV_OK (0) or a negative AFV_ERR_* code; it never
+ *    aborts the process (the reference calls `stop`). afv_last_error() gives
+ *    the message of the calling thread's last failure.
+ *  - Box ids, levels, ix indices and neighbour codes follow the reference:
+ *    ids are 1-based, ix is 1-based, a neighbour id > 0 is a box, 0 means no
+ *    box (refinement boundary) and < 0 a physical boundary
+ *    (src/m_aX_t.f90:32-33, src/m_aX_gc.f90:58-67).
+ *  - Host cell data is exchanged as the reference stores it: per box an array
+ *    cc(0:nc+1, 0:nc+1[, 0:nc+1]) with x fastest, boxes in the order of the
+ *    tree's level lists (lvls(min_lvl)%ids, ..., lvls(highest_lvl)%ids).
+ *  - Device calls are ordered on the forest's CUDA stream. Calls on one
+ *    forest are not re-entrant (like the reference's routines on one tree).
+ */
+#ifndef AFIVO_GB300_H
+#define AFIVO_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. */
+enum {
+  AFV_OK = 0,
+  AFV_ERR_INVALID = -1,     /* bad argument or malformed tree            */
+  AFV_ERR_CUDA = -2,        /* a CUDA runtime call failed                */
+  AFV_ERR_NOMEM = -3,       /* host or device allocation failed          */
+  AFV_ERR_UNSUPPORTED = -4, /* valid request this build does not support */
+  AFV_ERR_TIMEOUT = -5,     /* a bounded device wait gave up             */
+  AFV_ERR_STATE = -6,       /* call out of order (e.g. before set_base)  */
+  AFV_ERR_BUDGET = -7       /* over the memory budget (box_limit, HBM)   */
+};
+
+/* Refinement flags, src/m_aX_t.f90:17-24. */
+enum { AFV_RM_REF = -1, AFV_KEEP_REF = 0, AFV_DO_REF = 1 };
+
+/* Cell-centred variables of a forest (mg%i_phi, mg%i_rhs, mg%i_tmp). */
+enum { AFV_PHI = 0, AFV_RHS = 1, AFV_TMP = 2 };
+
+/* Boundary-condition types, src/m_aX_t.f90:45-49. */
+enum { AFV_BC_DIRICHLET = -1, AFV_BC_NEUMANN = -2 };
+
+/* Built-in refinement criteria (afv_ref_crit.kind). */
+enum {
+  AFV_REF_UNIFORM = 0,  /* do_ref while lvl < lvl_max                        */
+  AFV_REF_SOURCE = 1,   /* do_ref if any cell centre has |f|*dr^2 > thr      */
+  AFV_REF_RANDOM = 2,   /* do_ref with probability prob (keyed, seeded)      */
+  AFV_REF_RANDOM_RM = 3 /* as RANDOM, and rm_ref otherwise                   */
+};
+
+/* Solver precisions (afv_mg_solve). */
+enum { AFV_PREC_FP64 = 0, AFV_PREC_MIXED = 1 };
+
+typedef struct afv_tree afv_tree;     /* host tree, the reference's a$D_t   */
+typedef struct afv_forest afv_forest; /* device-resident set of trees       */
+
+/* What a refinement callback sees of a box (box$D_t, src/m_aX_t.f90:153-177). */
+typedef struct {
+  int id, lvl, n_cell, dim;
+  int ix[3];
+  double dr;
+  double r_min[3];
+  int pass; /* number of adjust_refinement calls made before this one */
+} afv_box_view;
+
+/* The reference's ref_subr hook, src/m_aX_t.f90:231-236. */
+typedef void (*afv_ref_fn)(const afv_box_view* box, int* ref_flag, void* user);
+
+/* Parameters of a built-in criterion. Sources are sums of Gaussians
+ * a*exp(-|r-c|^2/s^2) (src_lpl = 0) or their Laplacian (src_lpl = 1), in the
+ * form of examples/m_gaussians.f90:64-102; gauss holds n_gauss records of
+ * (a, s, c_1..c_dim). */
+typedef struct {
+  int kind;
+  int lvl_max;
+  double thr;
+  double prob;
+  unsigned long long seed;
+  int src_lpl;
+  int n_gauss;
+  const double* gauss;
+} afv_ref_crit;
+
+/* Multigrid options, the mg$D_t type of src/m_aX_mg.f90:20-52. Negative cycle
+ * counts mean the reference defaults (2), src/m_aX_mg.f90:142-144. */
+typedef struct {
+  int n_cycle_down;
+  int n_cycle_up;
+  int n_cycle_base;
+} afv_mg_opts;
+
+typedef struct {
+  int device;         /* CUDA device ordinal                                 */
+  int mixed_buffers;  /* 1: also allocate the FP32 state for AFV_PREC_MIXED  */
+} afv_forest_opts;
+
+/* ---- errors -------------------------------------------------------------- */
+const char* afv_last_error(void);
+int afv_version(void);
+
+/* ---- tree build (host) --------------------------------------------------- */
+
+/* a$D_init, src/m_aX_core.f90:24-131 (n_var_cell is fixed to phi, rhs, tmp;
+ * coarsen_to <= 0 means no coarse sub-levels). */
+int afv_tree_create(int dim, int n_cell, double dr, const double* r_min, int lvl_limit,
+                    int coarsen_to, double mem_limit_gb, afv_tree** out);
+/* a$D_set_base, src/m_aX_core.f90:152-235. ix_list: n_boxes*dim, nb_list:
+ * n_boxes*2*dim, both box-major. */
+int afv_tree_set_base(afv_tree* t, int n_boxes, const int* ix_list, const int* nb_list);
+/* a$D_adjust_refinement, src/m_aX_core.f90:452-541 (one pass, at most one
+ * level per call); n_add / n_rm are ref_info%n_add / ref_info%n_rm. */
+int afv_tree_adjust_refinement(afv_tree* t, afv_ref_fn fn, void* user, int* n_add, int* n_rm);
+/* a$D_adjust_refinement with a built-in criterion. */
+int afv_tree_adjust_builtin(afv_tree* t, const afv_ref_crit* crit, int* n_add, int* n_rm);
+/* The examples' "do; adjust_refinement; if (n_add == 0) exit" loop
+ * (examples/poisson_basic_2d.f90:59-68). */
+int afv_tree_refine_builtin(afv_tree* t, const afv_ref_crit* crit, int max_passes,
+                            int* n_passes);
+/* a$D_destroy, src/m_aX_core.f90:135-148. */
+void afv_tree_destroy(afv_tree* t);
+/* out[8] = dim, n_cell, min_lvl, highest_lvl, highest_id, boxes in use,
+ * leaves, lvl_limit (a$D_print_info, src/m_aX_t.f90:303-329). */
+int afv_tree_get_info(const afv_tree* t, int* out8);
+/* Per-id topology (rows id-1, ids 1..highest_id) of box$D_t. */
+int afv_tree_export(const afv_tree* t, int* lvl, int* ix, int* parent, int* children,
+                    int* neighbors, int* n_cell, double* dr, double* r_min, int* in_use);
+/* lvls(lvl)%ids / %leaves / %parents (lvl_t, src/m_aX_t.f90:181-185);
+ * sizes3 receives the three lengths; the list pointers may be NULL. */
+int afv_tree_level(const afv_tree* t, int lvl, int* sizes3, int* ids, int* leaves, int* parents);
+
+/* ---- device forest ----------------------------------------------------------- */
+
+/* Uploads the topology of n_trees trees (same dim, n_cell, coarsen_to) and
+ * allocates their cell data on the device, zero-initialised. One forest is
+ * swept by one kernel launch per level and operator. */
+int afv_forest_create(int n_trees, afv_tree* const* trees, const afv_forest_opts* opts,
+                      afv_forest** out);
+void afv_forest_destroy(afv_forest* f);
+/* out[8] = n_trees, dim, n_cell, min_lvl, max_lvl, boxes, leaf cells, device bytes. */
+int afv_forest_get_info(const afv_forest* f, long long* out8);
+/* Copy one variable of one tree to or from the host, in the reference's box
+ * layout (see conventions). interior_only = 1 packs only cc(1:nc,...) per box. */
+int afv_forest_set_var(afv_forest* f, int tree, int var, const double* host, int interior_only);
+int afv_forest_get_var(afv_forest* f, int tree, int var, double* host, int interior_only);
+/* Fill rhs of one tree with a Gaussian source at the cell centres. */
+int afv_forest_set_source(afv_forest* f, int tree, int src_lpl, int n_gauss, const double* gauss);
+/* Boundary values on physical faces of one tree: the sides_bc hook of the
+ * reference (src/m_aX_t.f90:276-282) sampled once. bc_type is AFV_BC_*; the
+ * boundary value is 0 when n_gauss == 0, else the Gaussian source at the face
+ * centres (examples/poisson_basic_2d.f90:167-203). */
+int afv_forest_set_bc(afv_forest* f, int tree, int bc_type, int src_lpl, int n_gauss,
+                      const double* gauss);
+int afv_forest_zero(afv_forest* f, int var);
+int afv_forest_sync(afv_forest* f);
+/* No counterpart in the reference: the cudaStream_t that orders this
+ * forest's work, for callers that time it or order their own work after it. */
+int afv_forest_get_stream(afv_forest* f, void** stream);
+
+/* ---- multigrid ------------------------------------------------------------------- */
+
+/* mg$D_init_mg, src/m_aX_mg.f90:130-154. */
+int afv_mg_init(afv_mg_opts* mg);
+/* mg$D_fas_vcycle, src/m_aX_mg.f90:208-255 (all trees of the forest). */
+int afv_mg_fas_vcycle(afv_forest* f, const afv_mg_opts* mg, int highest_lvl, int set_residual);
+/* mg$D_fas_fmg, src/m_aX_mg.f90:164-203. */
+int afv_mg_fas_fmg(afv_forest* f, const afv_mg_opts* mg, int set_residual, int have_guess);
+/* a$D_gc_tree(tree, i_phi, mg%sides_rb, mg%sides_bc), src/m_aX_gc.f90:28-46. */
+int afv_gc_tree(afv_forest* f);
+/* max(|a$D_tree_min_cc|, |a$D_tree_max_cc|) over leaf interiors,
+ * src/m_aX_utils.f90:468-571. */
+int afv_tree_max_abs_cc(afv_forest* f, int tree, int var, double* out);
+/* Solve every tree to max|rhs - L phi| <= tol * max|rhs| over its leaves,
+ * from the current phi, with FP64 V-cycles (AFV_PREC_FP64) or FP64 defect
+ * correction around FP32 V-cycles (AFV_PREC_MIXED). cycles[t] and rel_res[t]
+ * (n_trees entries, may be NULL) receive per-tree results. Returns
+ * AFV_ERR_TIMEOUT if a tree is not converged after max_cycles. */
+int afv_mg_solve(afv_forest* f, const afv_mg_opts* mg, int precision, double tol, int max_cycles,
+                 int* cycles, double* rel_res);
+
+/* Single operators of the V-cycle, one level of every tree. */
+/* gsrb_boxes, src/m_aX_mg.f90:397-420 */
+int afv_mg_gsrb_level(afv_forest* f, int lvl, int n_cycle);
+/* fill_gc_phi, src/m_aX_mg.f90:352-365 */
+int afv_fill_gc_level(afv_forest* f, int lvl);
+/* update_coarse, src/m_aX_mg.f90:424-480 */
+int afv_mg_update_coarse(afv_forest* f, int lvl);
+/* correct_children, src/m_aX_mg.f90:368-395 (parents at lvl_parent) */
+int afv_mg_correct_children(afv_forest* f, int lvl_parent);
+/* residual_box on every box of every level, src/m_aX_mg.f90:243-254 */
+int afv_mg_residual_all(afv_forest* f);
+
+/* ---- measurement ------------------------------------------------------------ */
+
+/* Kernel kinds of the event profiler. */
+enum {
+  AFV_KERNEL_SWEEP = 0,     /* GSRB half-sweep (with the pulled ghost fill)  */
+  AFV_KERNEL_FILL = 1,      /* ghost fill of a level                         */
+  AFV_KERNEL_RESTRICT = 2,  /* residual + restriction to the parents         */
+  AFV_KERNEL_COARSE_RHS = 3,
+  AFV_KERNEL_CORRECT = 4,   /* coarse correction with prolong2               */
+  AFV_KERNEL_RESIDUAL = 5,
+  AFV_KERNEL_DEFECT = 6,    /* FP64 defect of the mixed path                 */
+  AFV_KERNEL_ACCUMULATE = 7 /* FP64 accumulate of the FP32 correction        */
+};
+/* No counterpart in the reference (it has no GPU path): bracket every launch
+ * of the kinds in mask (bit k = kind k) with CUDA events on the forest's
+ * stream; mask = 0 switches it off and drops the records. */
+int afv_forest_profile(afv_forest* f, int mask);
+/* Launch count, summed event time (ms) and summed algorithmic bytes of the
+ * launches of one kind since profiling was switched on. kind = -1 gives the
+ * number of kernels launched on the forest's stream since it was created. */
+int afv_forest_profile_read(afv_forest* f, int kind, long long* launches, double* ms,
+                            double* algorithmic_bytes);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* AFIVO_GB300_H */

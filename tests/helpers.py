@@ -1,0 +1,98 @@
+"""Shared setup for parity tests: build the same tree with the library and
+with the CPU oracle, feed both the same inputs, and compare per (level, ix)."""
+import numpy as np
+
+import oracle as O
+from afivo_gb300 import workloads as W
+
+
+def oracle_tree(spec, max_passes=100):
+    t = O.OracleTree(spec["dim"], spec["n_cell"], spec["dr"], spec["ix"], spec["nb"],
+                     coarsen_to=spec["coarsen_to"])
+    if "target_cells" in spec:
+        for _ in range(max_passes):
+            if leaf_boxes(t) * spec["n_cell"] ** spec["dim"] >= spec["target_cells"]:
+                break
+            t.adjust_refinement(O.REF_RANDOM, spec["lvl_max"], prob=spec["prob"], seed=spec["seed"])
+    else:
+        t.refine_until_done(spec["crit"], spec["lvl_max"], thr=spec.get("thr", 0.0),
+                            prob=spec.get("prob", 0.0), seed=spec.get("seed", 0),
+                            gauss=spec.get("gauss"), lpl=spec.get("lpl", False))
+    return t
+
+
+def leaf_boxes(t):
+    return sum(len(t.level(l)[1]) for l in range(t.min_lvl, t.highest_lvl + 1))
+
+
+def oracle_var(t, iv, n_cell):
+    """Concatenation over levels of the oracle's boxes (the library's host layout)."""
+    parts = [t.get_level(l, iv, n_cell).ravel() for l in range(t.min_lvl, t.highest_lvl + 1)]
+    return np.concatenate(parts)
+
+
+def split_boxes(flat, t, n_cell, dim):
+    """Split a host-layout array into per-level box arrays."""
+    out = {}
+    off = 0
+    for l in range(t.min_lvl, t.highest_lvl + 1):
+        n = len(t.level(l)[0])
+        nc = n_cell if l >= 1 else n_cell >> (1 - l)
+        sz = n * (nc + 2) ** dim
+        out[l] = flat[off:off + sz].reshape((n,) + (nc + 2,) * dim)
+        off += sz
+    return out
+
+
+def face_mask(nc, dim):
+    """Interior plus face ghost cells (corners and edges excluded)."""
+    g = nc + 2
+    idx = np.indices((g,) * dim)
+    inner = [(a >= 1) & (a <= nc) for a in idx]
+    n_out = sum((~m).astype(int) for m in inner)
+    return n_out <= 1
+
+
+def interior_mask(nc, dim):
+    g = nc + 2
+    idx = np.indices((g,) * dim)
+    m = np.ones((g,) * dim, bool)
+    for a in idx:
+        m &= (a >= 1) & (a <= nc)
+    return m
+
+
+def compare_var(gpu_flat, ora_flat, t, n_cell, dim, interior_only):
+    """Max relative difference over the compared cells of all boxes."""
+    g = split_boxes(gpu_flat, t, n_cell, dim)
+    o = split_boxes(ora_flat, t, n_cell, dim)
+    worst = 0.0
+    scale = max(np.abs(ora_flat).max(), 1e-300)
+    for l in g:
+        nc = n_cell if l >= 1 else n_cell >> (1 - l)
+        m = interior_mask(nc, dim) if interior_only else face_mask(nc, dim)
+        d = np.abs(g[l] - o[l])[:, m]
+        if d.size:
+            worst = max(worst, float(d.max()) / scale)
+    return worst
+
+
+def setup_pair(afv, spec, mixed=False, bc_gauss=False):
+    """Library forest + oracle tree with identical trees and right-hand sides."""
+    ot = oracle_tree(spec)
+    pt = W.build_tree(spec)
+    if spec.get("gauss") is not None:
+        ot.fill_gauss(O.I_RHS, spec["gauss"], lpl=spec.get("lpl", False))
+    else:
+        rng = np.random.default_rng(3)
+        for l in range(ot.min_lvl, ot.highest_lvl + 1):
+            a = ot.get_level(l, O.I_RHS, spec["n_cell"]).copy()
+            a[...] = rng.standard_normal(a.shape)
+            ot.set_level(l, O.I_RHS, a)
+    bc_kind = O.BC_DIRICHLET_GAUSS if bc_gauss else O.BC_DIRICHLET_ZERO
+    ot.mg_init(bc_kind=bc_kind, bc_gauss=spec["gauss"] if bc_gauss else None)
+    f = afv.Forest([pt], mixed=mixed)
+    f.set_var(0, afv.AFV_RHS, oracle_var(ot, O.I_RHS, spec["n_cell"]))
+    if bc_gauss:
+        f.set_bc(0, afv.AFV_BC_DIRICHLET, gauss=spec["gauss"], lpl=False)
+    return f, ot, pt

@@ -1,0 +1,214 @@
+"""GPU parity: the sm_103a kernels against the CPU oracle on the same trees,
+right-hand sides and cycle schedules. The FP64 path must agree within
+1e-13 relative (max |gpu - oracle| / max |oracle|) after every V-cycle; the
+tree and index work is compared bit for bit in test_tree_build.py."""
+import numpy as np
+import pytest
+
+import oracle as O
+from helpers import compare_var, oracle_tree, oracle_var, setup_pair
+from afivo_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-13  # FP64 parity bar per cycle
+
+
+def assert_state(afv, f, ot, spec, tol=TOL, tree=0, what=("phi", "tmp", "rhs")):
+    nc, dim = spec["n_cell"], spec["dim"]
+    out = {}
+    if "phi" in what:
+        out["phi"] = compare_var(f.get_var(tree, afv.AFV_PHI), oracle_var(ot, O.I_PHI, nc), ot, nc,
+                                 dim, False)
+    if "tmp" in what:
+        out["tmp"] = compare_var(f.get_var(tree, afv.AFV_TMP), oracle_var(ot, O.I_TMP, nc), ot, nc,
+                                 dim, True)
+    if "rhs" in what:
+        out["rhs"] = compare_var(f.get_var(tree, afv.AFV_RHS), oracle_var(ot, O.I_RHS, nc), ot, nc,
+                                 dim, True)
+    for k, v in out.items():
+        assert v <= tol, (k, out)
+    return out
+
+
+def test_vcycle_c1_every_cycle(gpu):
+    spec = W.c1_poisson_2d()
+    f, ot, _ = setup_pair(gpu, spec)
+    for _ in range(10):
+        ot.vcycle(set_residual=True)
+        f.vcycle(set_residual=True)
+        assert_state(gpu, f, ot, spec)
+
+
+def test_single_operators_c1(gpu):
+    spec = W.c1_poisson_2d()
+    f, ot, _ = setup_pair(gpu, spec)
+    ot.vcycle()
+    f.vcycle()
+    top = ot.highest_lvl
+    # gsrb_boxes on the finest level (includes refinement-boundary ghosts)
+    ot.gsrb_level(top, 2)
+    f.gsrb_level(top, 2)
+    assert_state(gpu, f, ot, spec, what=("phi",))
+    ot.update_coarse(top)
+    f.update_coarse(top)
+    assert_state(gpu, f, ot, spec, what=("phi", "rhs"))
+    ot.gsrb_level(top - 1, 1)
+    f.gsrb_level(top - 1, 1)
+    ot.correct_children(top - 1)
+    f.correct_children(top - 1)
+    ot.fill_gc_level(top)
+    f.fill_gc_level(top)
+    assert_state(gpu, f, ot, spec, what=("phi",))
+
+
+def test_fmg_c1(gpu):
+    spec = W.c1_poisson_2d()
+    f, ot, _ = setup_pair(gpu, spec)
+    for i in range(3):
+        ot.fmg(set_residual=True, have_guess=i > 0)
+        f.fmg(set_residual=True, have_guess=i > 0)
+        assert_state(gpu, f, ot, spec)
+    # residual norm over the leaves (a$D_tree_max_cc / a$D_tree_min_cc)
+    r_o = ot.max_abs_residual()
+    r_g = f.max_abs(0, gpu.AFV_TMP)
+    assert abs(r_o - r_g) <= TOL * max(r_o, 1e-300)
+
+
+def test_vcycle_3d(gpu):
+    spec = W.c2_poisson_3d(thr=3e-3, lvl_max=6)
+    f, ot, _ = setup_pair(gpu, spec)
+    for _ in range(4):
+        ot.vcycle()
+        f.vcycle()
+        assert_state(gpu, f, ot, spec)
+
+
+def test_fmg_3d(gpu):
+    spec = W.c2_poisson_3d(thr=3e-3, lvl_max=6)
+    f, ot, _ = setup_pair(gpu, spec)
+    for i in range(2):
+        ot.fmg(set_residual=True, have_guess=i > 0)
+        f.fmg(set_residual=True, have_guess=i > 0)
+        assert_state(gpu, f, ot, spec)
+
+
+def test_dirichlet_values(gpu):
+    """Non-zero boundary values from the sides_bc hook
+    (examples/poisson_basic_2d.f90:167-203)."""
+    spec = W.c1_poisson_2d()
+    f, ot, _ = setup_pair(gpu, spec, bc_gauss=True)
+    for i in range(2):
+        ot.fmg(set_residual=True, have_guess=i > 0)
+        f.fmg(set_residual=True, have_guess=i > 0)
+        assert_state(gpu, f, ot, spec)
+    ot.vcycle()
+    f.vcycle()
+    assert_state(gpu, f, ot, spec)
+
+
+def test_neumann(gpu):
+    spec = dict(W.c3_uniform_2d(4), nb=[[-1] * 4], n_cell=8, dr=1 / 8, name="neumann")
+    ot = oracle_tree(spec)
+    pt = W.build_tree(spec)
+    rng = np.random.default_rng(7)
+    for l in range(ot.min_lvl, ot.highest_lvl + 1):
+        a = ot.get_level(l, O.I_RHS, 8).copy()
+        a[...] = rng.standard_normal(a.shape)
+        ot.set_level(l, O.I_RHS, a)
+    ot.mg_init(bc_kind=O.BC_NEUMANN_ZERO)
+    f = gpu.Forest([pt])
+    f.set_var(0, gpu.AFV_RHS, oracle_var(ot, O.I_RHS, 8))
+    f.set_bc(0, gpu.AFV_BC_NEUMANN)
+    for _ in range(3):
+        ot.vcycle()
+        f.vcycle()
+        assert_state(gpu, f, ot, spec)
+
+
+def test_periodic_uniform_2d(gpu):
+    spec = W.c3_uniform_2d(4)
+    f, ot, _ = setup_pair(gpu, spec)
+    for _ in range(4):
+        ot.vcycle()
+        f.vcycle()
+        assert_state(gpu, f, ot, spec)
+
+
+def test_forest_matches_single_trees(gpu):
+    """Several trees of different depth in one forest give, per tree, the same
+    bits as the tree alone and the oracle's values."""
+    specs = W.c4_random_2d(4, small=True)
+    trees = [W.build_tree(s) for s in specs]
+    ots = []
+    forest = gpu.Forest(trees)
+    alone = []
+    for k, s in enumerate(specs):
+        ot = oracle_tree(s)
+        ot.fill_gauss(O.I_RHS, s["gauss"], lpl=True)
+        ot.mg_init()
+        ots.append(ot)
+        rhs = oracle_var(ot, O.I_RHS, 8)
+        forest.set_var(k, gpu.AFV_RHS, rhs)
+        f1 = gpu.Forest([W.build_tree(s)])
+        f1.set_var(0, gpu.AFV_RHS, rhs)
+        alone.append(f1)
+    for _ in range(3):
+        forest.vcycle()
+        for f1 in alone:
+            f1.vcycle()
+        for ot in ots:
+            ot.vcycle()
+    for k, s in enumerate(specs):
+        a = forest.get_var(k, gpu.AFV_PHI)
+        b = alone[k].get_var(0, gpu.AFV_PHI)
+        # Each tree alone is a forest whose highest level may be lower than the
+        # forest's; the V-cycle of a tree starts at its own highest level.
+        assert np.array_equal(a, b)
+        assert_state(gpu, forest, ots[k], s, tree=k)
+
+
+def test_fp64_solve_matches_oracle_cycle_count(gpu):
+    spec = W.c1_poisson_2d()
+    f, ot, _ = setup_pair(gpu, spec)
+    fmax = ot.max_abs(O.I_RHS)
+    ot.residual_all()
+    n = 0
+    while ot.max_abs_residual() > 1e-8 * fmax:
+        ot.vcycle()
+        n += 1
+    cyc, rel, rc = f.solve(gpu.AFV_PREC_FP64, tol=1e-8, max_cycles=40)
+    assert rc == 0 and cyc[0] == n and rel[0] <= 1e-8
+    assert_state(gpu, f, ot, spec)
+
+
+def test_mixed_solve_reaches_tolerance(gpu):
+    spec = W.c1_poisson_2d()
+    f, ot, _ = setup_pair(gpu, spec, mixed=True)
+    cyc, rel, rc = f.solve(gpu.AFV_PREC_MIXED, tol=1e-8, max_cycles=60)
+    assert rc == 0 and rel[0] <= 1e-8
+    # error against the FP64 oracle solution solved to 1e-12
+    for _ in range(40):
+        ot.vcycle()
+    ref = oracle_var(ot, O.I_PHI, 8)
+    got = f.get_var(0, gpu.AFV_PHI)
+    err = compare_var(got, ref, ot, 8, 2, True)
+    assert err < 1e-6, err
+
+
+def test_mixed_batch_alone_vs_mix(gpu):
+    """Continuous-batching invariant: a tree solved inside a forest gets the
+    same bits as solved alone (inactive trees are masked out per launch)."""
+    specs = W.c4_random_2d(3, small=True)
+    forest = gpu.Forest([W.build_tree(s) for s in specs], mixed=True)
+    outs = []
+    for k, s in enumerate(specs):
+        forest.set_source(k, s["gauss"], lpl=True)
+    cyc_f, rel_f, _ = forest.solve(gpu.AFV_PREC_MIXED, tol=1e-8, max_cycles=60)
+    for k, s in enumerate(specs):
+        f1 = gpu.Forest([W.build_tree(s)], mixed=True)
+        f1.set_source(0, s["gauss"], lpl=True)
+        c1, r1, _ = f1.solve(gpu.AFV_PREC_MIXED, tol=1e-8, max_cycles=60)
+        assert c1[0] == cyc_f[k]
+        assert np.array_equal(f1.get_var(0, gpu.AFV_PHI), forest.get_var(k, gpu.AFV_PHI))
+        outs.append(r1[0])
+    assert max(outs) <= 1e-8
