@@ -34,6 +34,7 @@ LIB_PATH = os.path.join(_HERE, "_lib", "libafivo_gb300.so")
 AFV_OK = 0
 AFV_ERR_INVALID, AFV_ERR_CUDA, AFV_ERR_NOMEM = -1, -2, -3
 AFV_ERR_UNSUPPORTED, AFV_ERR_TIMEOUT, AFV_ERR_STATE, AFV_ERR_BUDGET = -4, -5, -6, -7
+AFV_ERR_DIVERGED = -8
 AFV_RM_REF, AFV_KEEP_REF, AFV_DO_REF = -1, 0, 1
 AFV_PHI, AFV_RHS, AFV_TMP = 0, 1, 2
 AFV_BC_DIRICHLET, AFV_BC_NEUMANN = -1, -2

@@ -83,6 +83,7 @@ class Forest {
   unsigned long long* d_norm = nullptr;  // [n_trees]
   double* d_fmax = nullptr;              // [n_trees]
   int* d_count = nullptr;                // [1]
+  int* d_failed = nullptr;               // [n_trees] nonzero: residual not finite
   int* h_count = nullptr;                // pinned
   unsigned long long* h_norm = nullptr;  // pinned [n_trees]
   double* d_stage = nullptr;             // staging for host exchange
@@ -129,8 +130,10 @@ class Forest {
   // Generic-precision pieces.
   template <class T> void sweep(const Arrays<T>& a, int lvl, int n, bool pull, bool homog);
   template <class T> void fill(const Arrays<T>& a, int lvl, bool homog);
-  template <class T> void restrict_res(const Arrays<T>& a, int lvl, bool with_res);
-  template <class T> void coarse_rhs(const Arrays<T>& a, int lvl_parent, bool copy_tmp);
+  template <class T> void restrict_res(const Arrays<T>& a, int lvl, bool with_res, bool pull = false,
+                                       bool homog = false);
+  template <class T> void coarse_rhs(const Arrays<T>& a, int lvl_parent, bool copy_tmp,
+                                     bool pull = false, bool homog = false);
   template <class T> void correct(const Arrays<T>& a, int lvl_parent);
   template <class T> void residual(const Arrays<T>& a, int lvl, unsigned long long* norm, bool store);
   template <class T> void gsrb_boxes(const Arrays<T>& a, int lvl, int n_cycle, bool homog);

@@ -304,7 +304,7 @@ __device__ __forceinline__ T lpl_at(const T* bx, int i, int j, int k, T inv_dr_s
 template <int D, int NC, bool SUB, class T>
 __global__ void __launch_bounds__(kThreads)
 k_restrict_res(Meta m, BoxSet bs, T* __restrict__ phi, const T* __restrict__ rhs,
-               T* __restrict__ tmp, int with_res) {
+               T* __restrict__ tmp, int with_res, int pull, int homog) {
   using G = Geo<D, NC>;
   constexpr int H = NC / 2;
   constexpr int PNC = SUB ? NC / 2 : NC;
@@ -331,6 +331,23 @@ k_restrict_res(Meta m, BoxSet bs, T* __restrict__ phi, const T* __restrict__ rhs
           reinterpret_cast<const V*>(phi + m.offg[s_slot[b]])[q];
     }
     __syncthreads();
+    if (pull) {
+      // Ghost values of this level's current state; no block writes this level
+      // during the launch (restriction writes the parents' interiors).
+      for (int e = threadIdx.x; e < nbox * G::NNB * G::NF; e += blockDim.x) {
+        int b = e / (G::NNB * G::NF);
+        int r = e % (G::NNB * G::NF);
+        int f = r / G::NF, lin = r % G::NF;
+        int a = lin % NC + 1, c = lin / NC + 1;
+        if (!s_act[b]) continue;
+        const T* bx = sm + b * G::SG;
+        auto own = [&](int i, int j, int k) { return bx[G::g(i, j, k)]; };
+        T v = ghost_value<D, NC, T>(m, phi, s_slot[b], f, a, c, homog != 0, own);
+        Face<D, NC> F(f, a, c);
+        sm[b * G::SG + G::g(F.gi, F.gj, F.gk)] = v;
+      }
+      __syncthreads();
+    }
     int b = threadIdx.x / PER_BOX, q = threadIdx.x % PER_BOX;
     if (b < nbox && s_act[b]) {
       int s = s_slot[b];
@@ -374,8 +391,8 @@ k_restrict_res(Meta m, BoxSet bs, T* __restrict__ phi, const T* __restrict__ rhs
 // ---------------------------------------------------------------------------
 template <int D, int NC, class T>
 __global__ void __launch_bounds__(kThreads)
-k_coarse_rhs(Meta m, BoxSet bs, const T* __restrict__ phi, T* __restrict__ rhs,
-             T* __restrict__ tmp, int copy_tmp) {
+k_coarse_rhs(Meta m, BoxSet bs, T* __restrict__ phi, T* __restrict__ rhs,
+             T* __restrict__ tmp, int copy_tmp, int pull, int homog) {
   using G = Geo<D, NC>;
   constexpr int PER_BOX = G::SI < kThreads ? G::SI : kThreads;
   constexpr int BPC = boxes_per_cta<G::SG, PER_BOX, T>(1);
@@ -399,6 +416,25 @@ k_coarse_rhs(Meta m, BoxSet bs, const T* __restrict__ phi, T* __restrict__ rhs,
           reinterpret_cast<const V*>(phi + m.offg[s_slot[b]])[q];
     }
     __syncthreads();
+    if (pull) {
+      // The fill_gc_phi of the parent level (src/m_aX_mg.f90:467) for the boxes
+      // that need it here; the values are also stored as the boxes' ghosts.
+      for (int e = threadIdx.x; e < nbox * G::NNB * G::NF; e += blockDim.x) {
+        int b = e / (G::NNB * G::NF);
+        int r = e % (G::NNB * G::NF);
+        int f = r / G::NF, lin = r % G::NF;
+        int a = lin % NC + 1, c = lin / NC + 1;
+        if (!s_act[b]) continue;
+        const T* bx = sm + b * G::SG;
+        auto own = [&](int i, int j, int k) { return bx[G::g(i, j, k)]; };
+        T v = ghost_value<D, NC, T>(m, phi, s_slot[b], f, a, c, homog != 0, own);
+        Face<D, NC> F(f, a, c);
+        int gpos = G::g(F.gi, F.gj, F.gk);
+        sm[b * G::SG + gpos] = v;
+        phi[m.offg[s_slot[b]] + gpos] = v;
+      }
+      __syncthreads();
+    }
     int b = threadIdx.x / PER_BOX, q0 = threadIdx.x % PER_BOX;
     if (b < nbox && s_act[b]) {
       int s = s_slot[b];
@@ -536,6 +572,9 @@ k_correct(Meta m, BoxSet bs, T* __restrict__ phi, T* __restrict__ tmp) {
   }
 }
 
+// max that keeps a NaN once seen (fmax would drop it and hide a diverged solve)
+__device__ __forceinline__ double nanmax(double a, double b) { return (b > a || b != b) ? b : a; }
+
 // Block-segment max of non-negative values followed by one atomicMax per
 // segment of SEG threads (SEG a power of two); the bit pattern of a
 // non-negative double orders like its value.
@@ -544,7 +583,7 @@ __device__ __forceinline__ void seg_atomic_max(unsigned long long* dst, double v
   unsigned lane = threadIdx.x & 31;
   constexpr int W = SEG < 32 ? SEG : 32;
 #pragma unroll
-  for (int o = W / 2; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  for (int o = W / 2; o > 0; o >>= 1) v = nanmax(v, __shfl_xor_sync(0xffffffffu, v, o));
   if ((lane & (W - 1)) == 0 && dst) atomicMax(dst, (unsigned long long)__double_as_longlong(v));
 }
 
@@ -579,7 +618,7 @@ k_residual(Meta m, BoxSet bs, const T* __restrict__ phi, const T* __restrict__ r
           int i = q % NC + 1, j = (q / NC) % NC + 1, k = (D == 3) ? q / (NC * NC) + 1 : 0;
           T r = rhs[m.offi[s] + q] - lpl_at<D, NC, T>(bx, i, j, k, inv);
           if (store) tmp[m.offg[s] + G::g(i, j, k)] = r;
-          mx = fmax(mx, fabs((double)r));
+          mx = nanmax(mx, fabs((double)r));
         }
       } else {
         tr = -1;
@@ -616,7 +655,7 @@ k_maxabs(Meta m, BoxSet bs, const T* __restrict__ v, int ghosted,
         for (int q = q0; q < G::SI; q += PER_BOX) {
           int i = q % NC + 1, j = (q / NC) % NC + 1, k = (D == 3) ? q / (NC * NC) + 1 : 0;
           T x = ghosted ? v[m.offg[s] + G::g(i, j, k)] : v[m.offi[s] + q];
-          mx = fmax(mx, fabs((double)x));
+          mx = nanmax(mx, fabs((double)x));
         }
       }
     }
@@ -718,7 +757,7 @@ k_defect(Meta m, BoxSet bs, const double* __restrict__ u, const double* __restri
           int i = q % NC + 1, j = (q / NC) % NC + 1, k = (D == 3) ? q / (NC * NC) + 1 : 0;
           double r = f[m.offi[s] + q] - lpl_at<D, NC, double>(bx, i, j, k, inv);
           r32[m.offi[s] + q] = (float)r;
-          mx = fmax(mx, fabs(r));
+          mx = nanmax(mx, fabs(r));
         }
       }
     }
@@ -819,12 +858,17 @@ __global__ void k_gather(Meta m, const int* __restrict__ slots, int n, const T* 
 // max|r| > tol * max|f|; counts the cycles applied to active trees.
 __global__ void k_check(int n_trees, const unsigned long long* __restrict__ rnorm,
                         const double* __restrict__ fmax, double tol, int* __restrict__ active,
-                        int* __restrict__ n_active_out) {
+                        int* __restrict__ failed, int* __restrict__ n_active_out) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t < n_trees) {
     double r = __longlong_as_double((long long)rnorm[t]);
     int a = active[t];
-    if (a && !(r > tol * fmax[t])) a = 0;
+    if (a && !(r <= 1.0e300)) {  // NaN or overflow: stop this tree, report failure
+      a = 0;
+      failed[t] = 1;
+    } else if (a && r <= tol * fmax[t]) {
+      a = 0;
+    }
     active[t] = a;
     if (a) atomicAdd(n_active_out, 1);
   }

@@ -80,7 +80,7 @@ Forest::~Forest() {
   void* ptrs[] = {meta.nb, meta.parent, meta.first_child, meta.tree, meta.qd, meta.dr, meta.offg,
                   meta.offi, meta.bctype, meta.bcoff, meta.bcval, meta.active, d64.phi, d64.rhs,
                   d64.tmp, d32.phi, d32.rhs, d32.tmp, base_phi64, base_rhs64, d_lists, d_norm,
-                  d_fmax, d_count, d_stage, d_stage_slots};
+                  d_fmax, d_count, d_failed, d_stage, d_stage_slots};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (const ProfEntry& p : prof) {
@@ -229,7 +229,7 @@ int Forest::create(const std::vector<const HostTree*>& trees, const afv_forest_o
   lists.insert(lists.end(), p.all_leaves.begin(), p.all_leaves.end());
   if ((rc = dupload(&d_lists, lists, bytes))) return err = "device allocation failed", rc;
   if (dmalloc(&d_norm, p.n_trees, bytes) || dmalloc(&d_fmax, p.n_trees, bytes) ||
-      dmalloc(&d_count, 1, bytes))
+      dmalloc(&d_count, 1, bytes) || dmalloc(&d_failed, p.n_trees, bytes))
     return err = "device allocation failed", AFV_ERR_NOMEM;
   if (cudaMallocHost((void**)&h_count, sizeof(int)) != cudaSuccess ||
       cudaMallocHost((void**)&h_norm, sizeof(unsigned long long) * p.n_trees) != cudaSuccess)
@@ -395,7 +395,7 @@ void Forest::fill(const Arrays<T>& a, int lvl, bool homog) {
 }
 
 template <class T>
-void Forest::restrict_res(const Arrays<T>& a, int lvl, bool with_res) {
+void Forest::restrict_res(const Arrays<T>& a, int lvl, bool with_res, bool pull, bool homog) {
   int nbx = lvl_n(lvl);
   if (!nbx || lvl <= plan.min_lvl) return;
   BoxSet bs{nullptr, plan.lvl_lo[plan.L(lvl)], nbx};
@@ -412,16 +412,16 @@ void Forest::restrict_res(const Arrays<T>& a, int lvl, bool with_res) {
     ProfScope ps(this, kProfRestrict,
                  (2.0 + 2.0 / (1 << D)) * nbx * G::SI * sizeof(T));
     if (sub)
-      dev::k_restrict_res<D, NC, true, T><<<grid, dev::kThreads, 0, stream>>>(m, bs, a.phi, a.rhs, a.tmp,
-                                                                             with_res ? 1 : 0);
+      dev::k_restrict_res<D, NC, true, T><<<grid, dev::kThreads, 0, stream>>>(
+          m, bs, a.phi, a.rhs, a.tmp, with_res ? 1 : 0, pull ? 1 : 0, homog ? 1 : 0);
     else
-      dev::k_restrict_res<D, NC, false, T><<<grid, dev::kThreads, 0, stream>>>(m, bs, a.phi, a.rhs,
-                                                                              a.tmp, with_res ? 1 : 0);
+      dev::k_restrict_res<D, NC, false, T><<<grid, dev::kThreads, 0, stream>>>(
+          m, bs, a.phi, a.rhs, a.tmp, with_res ? 1 : 0, pull ? 1 : 0, homog ? 1 : 0);
   });
 }
 
 template <class T>
-void Forest::coarse_rhs(const Arrays<T>& a, int lp, bool copy_tmp) {
+void Forest::coarse_rhs(const Arrays<T>& a, int lp, bool copy_tmp, bool pull, bool homog) {
   int np = n_parents(lp);
   if (!np) return;
   BoxSet bs{parents_list(lp), 0, np};
@@ -434,8 +434,8 @@ void Forest::coarse_rhs(const Arrays<T>& a, int lp, bool copy_tmp) {
     int grid = grid_for((np + BPC - 1) / BPC, n_sm);
     // read phi, tmp; write rhs, tmp
     ProfScope ps(this, kProfCoarseRhs, 4.0 * np * G::SI * sizeof(T));
-    dev::k_coarse_rhs<D, NC, T><<<grid, dev::kThreads, 0, stream>>>(m, bs, a.phi, a.rhs, a.tmp,
-                                                                   copy_tmp ? 1 : 0);
+    dev::k_coarse_rhs<D, NC, T><<<grid, dev::kThreads, 0, stream>>>(
+        m, bs, a.phi, a.rhs, a.tmp, copy_tmp ? 1 : 0, pull ? 1 : 0, homog ? 1 : 0);
   });
 }
 
@@ -501,13 +501,24 @@ void Forest::update_coarse_t(const Arrays<T>& a, int lvl, bool homog, bool copy_
 }
 
 // mg$D_fas_vcycle, src/m_aX_mg.f90:208-255 (without the residual branch).
+// The reference's ghost fills are folded into the kernels that follow them:
+// a half-sweep pulls the ghosts its colour needs, the restriction pulls the
+// fine level's ghosts, and the coarse right-hand side pulls (and stores) the
+// ghosts of the parents after restriction. Each of these reads the same values
+// the reference's fill would have stored, so results are unchanged. Only the
+// first half-sweep on the top level reads stored ghosts (valid on input), and
+// every level ends the cycle with a stored ghost fill (valid on output).
 // base64: smooth the coarsest level in FP64 (mixed cycle).
 template <class T>
 void Forest::vcycle_t(const Arrays<T>& a, const MgOpts& mg, int highest, bool homog, bool base64) {
   const int l0 = plan.min_lvl;
+  auto sweeps = [&](const auto& arr, int l, int n_cycle) {
+    for (int n = 1; n <= 2 * n_cycle; ++n) sweep(arr, l, n, n > 1 || l != highest, homog);
+  };
   for (int l = highest; l >= l0 + 1; --l) {
-    gsrb_boxes(a, l, mg.n_down, homog);
-    update_coarse_t(a, l, homog, true);
+    sweeps(a, l, mg.n_down);
+    restrict_res(a, l, true, true, homog);
+    coarse_rhs(a, l - 1, true, true, homog);
   }
   if (base64 && !std::is_same<T, double>::value) {
     long long ng = 0, ni = 0;
@@ -524,18 +535,24 @@ void Forest::vcycle_t(const Arrays<T>& a, const MgOpts& mg, int highest, bool ho
       dev::k_convert<double, T><<<g2, 256, 0, stream>>>(base_rhs64, a.rhs, ni);
     }
     Arrays<double> b{base_phi64, base_rhs64, nullptr};
-    gsrb_boxes(b, l0, mg.n_base, homog);
+    if (mg.n_base > 0) {
+      sweeps(b, l0, mg.n_base);
+      fill(b, l0, homog);
+    }
     {
       ProfScope ps(this, kProfOther, (8.0 + sizeof(T)) * ng);
       dev::k_convert<T, double><<<g1, 256, 0, stream>>>(a.phi, base_phi64, ng);
     }
-  } else {
-    gsrb_boxes(a, l0, mg.n_base, homog);
+  } else if (mg.n_base > 0) {
+    sweeps(a, l0, mg.n_base);
+    fill(a, l0, homog);
   }
   for (int l = l0 + 1; l <= highest; ++l) {
     correct(a, l - 1);
+    if (mg.n_up > 0) {
+      for (int n = 1; n <= 2 * mg.n_up; ++n) sweep(a, l, n, true, homog);
+    }
     fill(a, l, homog);
-    gsrb_boxes(a, l, mg.n_up, homog);
   }
 }
 
@@ -741,10 +758,15 @@ int Forest::solve(const MgOpts& mg, int precision, double tol, int max_cycles, S
   cudaMemcpyAsync(fmax.data(), d_norm, sizeof(double) * nt, cudaMemcpyDeviceToHost, stream);
   cudaStreamSynchronize(stream);
   std::vector<int> done_cycles(nt, 0);
+  cudaMemsetAsync(d_failed, 0, sizeof(int) * nt, stream);
 
   auto residual_check = [&](bool mixed_path) -> int {
     cudaMemsetAsync(d_norm, 0, sizeof(unsigned long long) * nt, stream);
     if (mixed_path) {
+      // Parents hold the restriction of their children, as at the fixed point
+      // of the FAS cycle: coarse leaves next to a refined region see them
+      // through their ghost cells.
+      for (int l = plan.max_lvl; l >= plan.min_lvl + 1; --l) restrict_res(d64, l, false);
       fill_all64(false);
       int nl = (int)plan.all_leaves.size();
       BoxSet bs{d_lists + all_leaves_off, 0, nl};
@@ -765,7 +787,7 @@ int Forest::solve(const MgOpts& mg, int precision, double tol, int max_cycles, S
     {
       ProfScope ps(this, kProfOther, 20.0 * nt);
       dev::k_check<<<(nt + 255) / 256, 256, 0, stream>>>(nt, d_norm, d_fmax, tol, meta.active,
-                                                         d_count);
+                                                         d_failed, d_count);
     }
     cudaMemcpyAsync(h_count, d_count, sizeof(int), cudaMemcpyDeviceToHost, stream);
     cudaMemcpyAsync(h_norm, d_norm, sizeof(unsigned long long) * nt, cudaMemcpyDeviceToHost, stream);
@@ -822,8 +844,15 @@ int Forest::solve(const MgOpts& mg, int precision, double tol, int max_cycles, S
     st.rel_res[t] = fmax[t] > 0 ? r / fmax[t] : r;
   }
   if (int rc = check(err, "solve")) return rc;
-  st.status = n_active > 0 ? AFV_ERR_TIMEOUT : AFV_OK;
-  if (n_active > 0) err = "not converged within max_cycles";
+  std::vector<int> failed(nt, 0);
+  cudaMemcpy(failed.data(), d_failed, sizeof(int) * nt, cudaMemcpyDeviceToHost);
+  int n_failed = 0;
+  for (int t = 0; t < nt; ++t) n_failed += failed[t] != 0;
+  st.status = n_failed ? AFV_ERR_DIVERGED : n_active > 0 ? AFV_ERR_TIMEOUT : AFV_OK;
+  if (n_failed)
+    err = std::to_string(n_failed) + " tree(s) diverged (non-finite residual)";
+  else if (n_active > 0)
+    err = "not converged within max_cycles";
   return st.status;
 }
 

@@ -38,7 +38,8 @@ enum {
   AFV_ERR_UNSUPPORTED = -4, /* valid request this build does not support */
   AFV_ERR_TIMEOUT = -5,     /* a bounded device wait gave up             */
   AFV_ERR_STATE = -6,       /* call out of order (e.g. before set_base)  */
-  AFV_ERR_BUDGET = -7       /* over the memory budget (box_limit, HBM)   */
+  AFV_ERR_BUDGET = -7,      /* over the memory budget (box_limit, HBM)   */
+  AFV_ERR_DIVERGED = -8     /* a solve produced a non-finite residual    */
 };
 
 /* Refinement flags, src/m_aX_t.f90:17-24. */
@@ -183,7 +184,8 @@ int afv_tree_max_abs_cc(afv_forest* f, int tree, int var, double* out);
  * from the current phi, with FP64 V-cycles (AFV_PREC_FP64) or FP64 defect
  * correction around FP32 V-cycles (AFV_PREC_MIXED). cycles[t] and rel_res[t]
  * (n_trees entries, may be NULL) receive per-tree results. Returns
- * AFV_ERR_TIMEOUT if a tree is not converged after max_cycles. */
+ * AFV_ERR_TIMEOUT if a tree is not converged after max_cycles and
+ * AFV_ERR_DIVERGED if a tree's residual stopped being finite. */
 int afv_mg_solve(afv_forest* f, const afv_mg_opts* mg, int precision, double tol, int max_cycles,
                  int* cycles, double* rel_res);
 
