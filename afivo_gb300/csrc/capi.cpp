@@ -254,6 +254,7 @@ int afv_forest_set_bc(afv_forest* f, int tree, int bc_type, int src_lpl, int n_g
     bc.src_lpl = src_lpl;
     bc.gauss.assign(gauss ? gauss : nullptr, gauss ? gauss + (size_t)n_gauss * (2 + p.dim) : nullptr);
     afv::plan_fill_bc(p, tree);
+    afv::plan_build_desc(p);
     return f->f.upload_bc(err);
   });
 }

@@ -31,6 +31,9 @@ struct DevMeta {
   long long* bcoff = nullptr;
   double* bcval = nullptr;
   int* active = nullptr;  // [n_trees]
+  long long* nbo = nullptr;
+  SlotDesc* desc = nullptr;
+  int* err = nullptr;  // device error word (bounded waits)
 };
 
 struct MgOpts {
@@ -80,7 +83,8 @@ class Forest {
   std::vector<int> leaves_off, parents_off;  // offsets in d_lists per level
   int all_leaves_off = 0;
   // per-tree reductions
-  unsigned long long* d_norm = nullptr;  // [n_trees]
+  unsigned long long* d_norm = nullptr;  // [n_trees * kStripes] striped per-tree maxima
+  unsigned long long* d_red = nullptr;   // [n_trees] reduced maxima
   double* d_fmax = nullptr;              // [n_trees]
   int* d_count = nullptr;                // [1]
   int* d_failed = nullptr;               // [n_trees] nonzero: residual not finite
@@ -144,6 +148,9 @@ class Forest {
   void restrict_tree_phi64();
 
   int check(std::string& err, const char* where);
+  int check_device_error(std::string& err);  // reads and clears the device error word
+  void norm_reset();
+  void norm_fold();  // d_norm -> d_red
   int lvl_n(int l) const {
     return (l < plan.min_lvl || l > plan.max_lvl) ? 0 : plan.lvl_n[plan.L(l)];
   }

@@ -14,6 +14,8 @@
 #pragma once
 #include <cstdint>
 
+#include "desc.hpp"
+
 namespace afv {
 namespace dev {
 
@@ -43,6 +45,9 @@ struct Meta {
   const long long* bcoff;  // [slot*2D + face] offset of the face values in bcval, -1 = zero
   const double* bcval;
   const int* active;       // [tree] nonzero if the tree takes part in this launch
+  const long long* nbo;    // [slot*2D + face] offg of the neighbour (box code >= 0) or of the parent (refinement boundary)
+  const SlotDesc* desc;    // [slot]
+  int* err;                // device error word: nonzero after a bounded wait gave up
 };
 
 __device__ __forceinline__ int box_at(const BoxSet& s, int i) { return s.list ? s.list[i] : s.lo + i; }
@@ -82,24 +87,26 @@ struct Face {
   int ai, aj, ak;  // adjacent interior cell
   int ni, nj, nk;  // neighbour's cell copied into the ghost (sides_from_nb)
   __device__ __forceinline__ Face(int f, int a, int c) {
-    int dim = f >> 1, hi = f & 1;
-    int t[3] = {a, c, 1};
-    int p[3], q[3], r[3];
-    int k = 0;
-    for (int d = 0; d < 3; ++d) {
-      if (d >= D) {
-        p[d] = q[d] = r[d] = 0;
-      } else if (d == dim) {
-        p[d] = hi ? NC + 1 : 0;
-        q[d] = hi ? NC : 1;
-        r[d] = hi ? 1 : NC;
-      } else {
-        p[d] = q[d] = r[d] = t[k++];
-      }
+    const int hi = f & 1;
+    const int gn = hi ? NC + 1 : 0, an = hi ? NC : 1, nn = hi ? 1 : NC;
+    const int cz = (D == 3) ? c : 0;
+    switch (f >> 1) {
+      case 0:
+        gi = gn; ai = an; ni = nn;
+        gj = aj = nj = a;
+        gk = ak = nk = cz;
+        break;
+      case 1:
+        gj = gn; aj = an; nj = nn;
+        gi = ai = ni = a;
+        gk = ak = nk = cz;
+        break;
+      default:
+        gk = gn; ak = an; nk = nn;
+        gi = ai = ni = a;
+        gj = aj = nj = c;
+        break;
     }
-    gi = p[0]; gj = p[1]; gk = p[2];
-    ai = q[0]; aj = q[1]; ak = q[2];
-    ni = r[0]; nj = r[1]; nk = r[2];
   }
 };
 
@@ -118,21 +125,18 @@ __device__ __forceinline__ T ghost_value(const Meta& m, const T* __restrict__ ph
   Face<D, NC> F(f, a, c);
   int code = m.nb[s * G::NNB + f];
   if (code >= 0) {
-    return phi[m.offg[code] + G::g(F.ni, F.nj, F.nk)];
+    return phi[m.nbo[s * G::NNB + f] + G::g(F.ni, F.nj, F.nk)];
   }
   if (code == kNbRefinement) {
     // Injection from the parent (levels >= 2 only; the parent has the same NC).
-    int p = m.parent[s];
-    int qd = m.qd[s];
-    int lo[3], idx[3] = {F.gi, F.gj, F.gk};
-    for (int d = 0; d < 3; ++d) lo[d] = (d < D) ? ((qd >> d) & 1) * (NC >> 1) : 0;
-    int pc[3];
-    for (int d = 0; d < 3; ++d) pc[d] = (d < D) ? lo[d] + ((idx[d] + 1) >> 1) : 0;
-    T g0 = phi[m.offg[p] + G::g(pc[0], pc[1], pc[2])];
+    const int qd = m.qd[s];
+    const int h = NC >> 1;
+    const int pi = (qd & 1) * h + ((F.gi + 1) >> 1);
+    const int pj = ((qd >> 1) & 1) * h + ((F.gj + 1) >> 1);
+    const int pk = (D == 3) ? ((qd >> 2) & 1) * h + ((F.gk + 1) >> 1) : 0;
+    T g0 = phi[m.nbo[s * G::NNB + f] + G::g(pi, pj, pk)];
     int dim = f >> 1;
-    int ix = (f & 1) ? NC : 1;
     int dix = (f & 1) ? -1 : 1;
-    (void)ix;
     if constexpr (D == 2) {
       if (dim == 0) {
         int i = F.ai, j = F.aj;
@@ -168,86 +172,298 @@ __device__ __forceinline__ T ghost_value(const Meta& m, const T* __restrict__ ph
 }
 
 // ---------------------------------------------------------------------------
-// GSRB half-sweep (mg$D_box_gsrb_lpl, src/m_aX_mg.f90:718-760) on every box of
-// a level, for red/black counter n. With pull = 1 the ghost cells this colour
-// needs are first recomputed from the neighbours' current state (the
-// a$D_gc_box call that the reference makes after the previous half-sweep,
-// src/m_aX_mg.f90:412-417); they are the neighbours' cells of the other colour,
-// which no block writes during this sweep, so blocks may update in place.
-// With pull = 0 the stored ghost cells are used, as in the first half-sweep.
+// Bulk copies (TMA, cp.async.bulk) into shared memory, completed on mbarriers.
+// Every wait is bounded by a clock budget; a kernel that gives up records it in
+// the error word and drains its own copies before it returns.
+// ---------------------------------------------------------------------------
+constexpr long long kWaitLimitCycles = 4000000000LL;  // about two seconds
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void fence_proxy_async() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes,
+                                         unsigned long long* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+__device__ __forceinline__ bool mbar_test(unsigned long long* bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned parity) {
+  const long long t0 = clock64();
+  while (!mbar_test(bar, parity)) {
+    if (clock64() - t0 > kWaitLimitCycles) return false;
+  }
+  return true;
+}
+
+// The cell (a, c) on face f whose adjacent interior cell is updated by
+// half-sweep n (the ghosts that sweep reads); m enumerates them.
+template <int D, int NC>
+__device__ __forceinline__ void needed_face_cell(int f, int m, int n, int& a, int& c) {
+  const int an = (f & 1) ? NC : 1;
+  if constexpr (D == 2) {
+    c = 1;
+    a = 2 * m + 1 + ((1 + an + n) & 1);
+  } else {
+    c = m / (NC / 2) + 1;
+    a = 2 * (m % (NC / 2)) + 1 + ((1 + an + c + n) & 1);
+  }
+}
+
+template <int D, int NC, class T>
+struct SweepCfg {
+  using G = Geo<D, NC>;
+  static constexpr int S = 3;                   // pipeline stages
+  static constexpr int PER_BOX = G::SI / 2;     // one thread per updated cell
+  static constexpr int BOX_B = (int)sizeof(SlotDesc) + (G::SG + G::SI) * (int)sizeof(T);
+  static constexpr int BPC_T = kThreads / PER_BOX;
+  static constexpr int BPC_S = 46 * 1024 / (S * BOX_B);
+  static constexpr int BPC = BPC_T < BPC_S ? BPC_T : BPC_S;
+  static constexpr int NEED = 2 * D * (G::NF / 2);  // ghost cells one colour reads
+  static constexpr int ITEMS = (BPC * NEED + kThreads - 1) / kThreads;
+  static constexpr int DESC_B = BPC * (int)sizeof(SlotDesc);
+  static constexpr int PHI_B = BPC * G::SG * (int)sizeof(T);
+  static constexpr int RHS_B = BPC * G::SI * (int)sizeof(T);
+  static constexpr int STAGE_B = DESC_B + PHI_B + RHS_B;
+  static_assert(BPC >= 1, "box too large for the sweep pipeline");
+  static_assert(PHI_B % 16 == 0 && RHS_B % 16 == 0 && DESC_B % 16 == 0, "bulk copy sizes");
+};
+
+// ---------------------------------------------------------------------------
+// GSRB half-sweep on every box of one level (mg$D_box_gsrb_lpl,
+// src/m_aX_mg.f90:718-760), persistent and pipelined: each block streams its
+// groups of consecutive boxes through an S-stage ring in shared memory (one
+// bulk copy each for the descriptors, phi and rhs of a group), and loads the
+// ghost values of the next group into registers while the current one is
+// being updated.
+//
+// With pull = 1 the ghost cells this colour reads are the values of the
+// a$D_gc_box fill the reference runs after the previous half-sweep
+// (src/m_aX_mg.f90:412-417): neighbours' cells of the other colour, which no
+// block writes during this sweep, so all blocks update in place. With
+// pull = 0 the stored ghost cells are used (first half-sweep).
 // ---------------------------------------------------------------------------
 template <int D, int NC, class T>
 __global__ void __launch_bounds__(kThreads)
-k_sweep(Meta m, BoxSet bs, T* __restrict__ phi, const T* __restrict__ rhs, int n, int pull,
-        int homog) {
+k_sweep_tma(Meta m, int lo, int nbx, T* __restrict__ phi, const T* __restrict__ rhs, int n, int pull,
+            int homog) {
+  using C = SweepCfg<D, NC, T>;
   using G = Geo<D, NC>;
-  constexpr int PER_BOX = G::SI / 2;
-  constexpr int BPC = boxes_per_cta<G::SG, PER_BOX, T>(1);
-  using V = typename Vec<T>::type;
-  constexpr int VW = Vec<T>::w;
-  __shared__ __align__(16) T sm[BPC * G::SG];
-  __shared__ int s_slot[BPC];
-  __shared__ int s_act[BPC];
+  constexpr int S = C::S;
+  __shared__ __align__(128) unsigned char smem[S * C::STAGE_B];
+  __shared__ __align__(8) unsigned long long bar[S];
+  __shared__ int s_act[C::BPC];
 
-  const int groups = (bs.n + BPC - 1) / BPC;
-  for (int grp = blockIdx.x; grp < groups; grp += gridDim.x) {
-    const int nbox = min(BPC, bs.n - grp * BPC);
-    if (threadIdx.x < BPC) {
-      int s = threadIdx.x < nbox ? box_at(bs, grp * BPC + threadIdx.x) : -1;
-      s_slot[threadIdx.x] = s;
-      s_act[threadIdx.x] = (s >= 0) ? m.active[m.tree[s]] : 0;
-    }
-    __syncthreads();
-    for (int e = threadIdx.x; e < nbox * (G::SG / VW); e += blockDim.x) {
-      int b = e / (G::SG / VW), q = e % (G::SG / VW);
-      reinterpret_cast<V*>(sm + b * G::SG)[q] =
-          reinterpret_cast<const V*>(phi + m.offg[s_slot[b]])[q];
-    }
-    __syncthreads();
-    if (pull) {
-      for (int e = threadIdx.x; e < nbox * G::NNB * G::NF; e += blockDim.x) {
-        int b = e / (G::NNB * G::NF);
-        int r = e % (G::NNB * G::NF);
-        int f = r / G::NF, lin = r % G::NF;
-        int a = lin % NC + 1, c = lin / NC + 1;
-        Face<D, NC> F(f, a, c);
-        if (((F.ai + F.aj + F.ak + n) & 1) != 0) continue;  // neighbour cell of this colour: not needed
-        if (!s_act[b]) continue;
-        const T* bx = sm + b * G::SG;
-        auto own = [&](int i, int j, int k) { return bx[G::g(i, j, k)]; };
-        T v = ghost_value<D, NC, T>(m, phi, s_slot[b], f, a, c, homog != 0, own);
-        sm[b * G::SG + G::g(F.gi, F.gj, F.gk)] = v;
+  const int groups = (nbx + C::BPC - 1) / C::BPC;
+  if ((int)blockIdx.x >= groups) return;
+  const int my_groups = (groups - 1 - (int)blockIdx.x) / (int)gridDim.x + 1;
+
+  if (threadIdx.x == 0) {
+    for (int st = 0; st < S; ++st) mbar_init(&bar[st], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+
+  auto group_first = [&](int k) { return ((int)blockIdx.x + k * (int)gridDim.x) * C::BPC; };
+  auto group_n = [&](int k) { return min(C::BPC, nbx - group_first(k)); };
+  auto issue = [&](int k) {  // one thread
+    const int first = group_first(k), nb = group_n(k), s0 = lo + first;
+    unsigned char* sp = smem + (k % S) * C::STAGE_B;
+    const unsigned bytes = nb * (unsigned)C::BOX_B;
+    fence_proxy_async();
+    mbar_expect_tx(&bar[k % S], bytes);
+    bulk_g2s(sp, m.desc + s0, nb * (unsigned)sizeof(SlotDesc), &bar[k % S]);
+    bulk_g2s(sp + C::DESC_B, phi + m.offg[s0], nb * (unsigned)(G::SG * sizeof(T)), &bar[k % S]);
+    bulk_g2s(sp + C::DESC_B + C::PHI_B, rhs + m.offi[s0], nb * (unsigned)(G::SI * sizeof(T)),
+             &bar[k % S]);
+  };
+
+  int issued = 0;  // groups issued so far (by thread 0; uniform count)
+  if (threadIdx.x == 0)
+    for (int k = 0; k < S - 1 && k < my_groups; ++k) issue(k);
+  issued = min(S - 1, my_groups);
+
+  T cur[C::ITEMS], nxt[C::ITEMS];
+  int cur_act = 0, nxt_act = 0;
+
+  // Ghost sources of group k (its stage has landed): neighbour cells, parent
+  // cells for refinement boundaries, or boundary values.
+  auto prefetch = [&](int k, T* val, int& act) {
+    const unsigned char* sp = smem + (k % S) * C::STAGE_B;
+    const SlotDesc* dsc = reinterpret_cast<const SlotDesc*>(sp);
+    const int nb = group_n(k);
+    act = ((int)threadIdx.x < nb) ? m.active[dsc[threadIdx.x].tree] : 0;
+#pragma unroll
+    for (int j = 0; j < C::ITEMS; ++j) {
+      const int e = threadIdx.x + j * kThreads;
+      val[j] = (T)0;
+      if (!pull || e >= nb * C::NEED) continue;
+      const int b = e / C::NEED, r = e % C::NEED;
+      const int f = r / (G::NF / 2), mm = r % (G::NF / 2);
+      int a, c;
+      needed_face_cell<D, NC>(f, mm, n, a, c);
+      const Face<D, NC> F(f, a, c);
+      const SlotDesc& d = dsc[b];
+      const int code = d.code[f];
+      const long long o = d.nbo[f];
+      if (code >= 0) {
+        val[j] = phi[o + G::g(F.ni, F.nj, F.nk)];
+      } else if (code == -1) {
+        const int h = NC >> 1, qd = d.qd;
+        const int pi = (qd & 1) * h + ((F.gi + 1) >> 1);
+        const int pj = ((qd >> 1) & 1) * h + ((F.gj + 1) >> 1);
+        const int pk = (D == 3) ? ((qd >> 2) & 1) * h + ((F.gk + 1) >> 1) : 0;
+        val[j] = phi[o + G::g(pi, pj, pk)];
+      } else if (o >= 0 && !homog) {
+        const int lin = (D == 2) ? (a - 1) : (a - 1) + NC * (c - 1);
+        val[j] = (T)m.bcval[o + lin];
       }
-      __syncthreads();
     }
-    {
-      int b = threadIdx.x / PER_BOX, q = threadIdx.x % PER_BOX;
-      if (b < nbox && s_act[b]) {
-        int s = s_slot[b];
-        const T* bx = sm + b * G::SG;
-        T dx2 = (T)(m.dr[s] * m.dr[s]);
-        int p = q % (NC / 2);
-        if constexpr (D == 2) {
-          int j = q / (NC / 2) + 1;
-          int i = 2 * p + 1 + ((1 + j + n) & 1);
-          T f = rhs[m.offi[s] + G::in(i, j, 1)];
-          T v = (T)0.25 * (bx[G::g(i + 1, j, 0)] + bx[G::g(i - 1, j, 0)] + bx[G::g(i, j + 1, 0)] +
-                           bx[G::g(i, j - 1, 0)] - dx2 * f);
-          phi[m.offg[s] + G::g(i, j, 0)] = v;
+  };
+
+  auto abort_cta = [&](int waited) {
+    if (threadIdx.x == 0) {
+      atomicExch(m.err, 1);
+      for (int k = waited; k < issued; ++k) mbar_wait_bounded(&bar[k % S], (k / S) & 1);
+    }
+    __syncthreads();
+  };
+
+  {
+    const bool ok = mbar_wait_bounded(&bar[0], 0);
+    if (__syncthreads_or(!ok)) {
+      abort_cta(0);
+      return;
+    }
+  }
+  prefetch(0, cur, cur_act);
+
+  for (int k = 0; k < my_groups; ++k) {
+    const int st = k % S;
+    unsigned char* sp = smem + st * C::STAGE_B;
+    const SlotDesc* dsc = reinterpret_cast<const SlotDesc*>(sp);
+    T* sphi = reinterpret_cast<T*>(sp + C::DESC_B);
+    const T* srhs = reinterpret_cast<const T*>(sp + C::DESC_B + C::PHI_B);
+    const int nb = group_n(k);
+
+    if (k + S - 1 < my_groups) {
+      if (threadIdx.x == 0) issue(k + S - 1);
+      ++issued;
+    }
+    if (k + 1 < my_groups) {
+      const bool ok = mbar_wait_bounded(&bar[(k + 1) % S], ((k + 1) / S) & 1);
+      if (__syncthreads_or(!ok)) {
+        abort_cta(k + 1);
+        return;
+      }
+      prefetch(k + 1, nxt, nxt_act);
+    }
+
+    // ghost cells of this colour (values of the state after the previous sweep)
+    if ((int)threadIdx.x < nb) s_act[threadIdx.x] = cur_act;
+    if (pull) {
+#pragma unroll
+      for (int j = 0; j < C::ITEMS; ++j) {
+        const int e = threadIdx.x + j * kThreads;
+        if (e >= nb * C::NEED) continue;
+        const int b = e / C::NEED, r = e % C::NEED;
+        const int f = r / (G::NF / 2), mm = r % (G::NF / 2);
+        int a, c;
+        needed_face_cell<D, NC>(f, mm, n, a, c);
+        const Face<D, NC> F(f, a, c);
+        const SlotDesc& d = dsc[b];
+        const int code = d.code[f];
+        const T* bx = sphi + b * G::SG;
+        auto own = [&](int i, int jj, int kk) { return bx[G::g(i, jj, kk)]; };
+        T v;
+        if (code >= 0) {
+          v = cur[j];
+        } else if (code == -1) {
+          const T g0 = cur[j];
+          const int dim = f >> 1, dix = (f & 1) ? -1 : 1;
+          const int i = F.ai, jj = F.aj, kk = F.ak;
+          if constexpr (D == 2) {
+            if (dim == 0) {
+              const int dj = -1 + 2 * (jj & 1);
+              v = (T)0.5 * g0 + own(i, jj, 0) - (T)0.25 * (own(i + dix, jj, 0) + own(i, jj + dj, 0));
+            } else {
+              const int di = -1 + 2 * (i & 1);
+              v = (T)0.5 * g0 + own(i, jj, 0) - (T)0.25 * (own(i + di, jj, 0) + own(i, jj + dix, 0));
+            }
+          } else {
+            const int di = (dim == 0) ? dix : -1 + 2 * (i & 1);
+            const int dj = (dim == 1) ? dix : -1 + 2 * (jj & 1);
+            const int dk = (dim == 2) ? dix : -1 + 2 * (kk & 1);
+            v = (T)0.5 * g0 + (T)0.75 * own(i, jj, kk) - (T)0.25 * own(i + di, jj + dj, kk + dk);
+          }
         } else {
-          int j = (q / (NC / 2)) % NC + 1;
-          int k = q / ((NC / 2) * NC) + 1;
-          int i = 2 * p + 1 + ((1 + j + k + n) & 1);
+          const T b = cur[j];
+          const T x = own(F.ai, F.aj, F.ak);
+          if (code == -2) {
+            v = (T)2 * b + (T)(-1) * x;
+          } else {
+            const T c2 = (T)d.dr * (T)((f & 1) ? 1 : -1);
+            v = c2 * b + (T)1 * x;
+          }
+        }
+        sphi[b * G::SG + G::g(F.gi, F.gj, F.gk)] = v;
+      }
+    }
+    __syncthreads();
+    {
+      const int b = threadIdx.x / C::PER_BOX, q = threadIdx.x % C::PER_BOX;
+      if (b < nb && s_act[b]) {
+        const T* bx = sphi + b * G::SG;
+        const T* f = srhs + b * G::SI;
+        const SlotDesc& d = dsc[b];
+        const T dx2 = (T)(d.dr * d.dr);
+        const int p = q % (NC / 2);
+        if constexpr (D == 2) {
+          const int j = q / (NC / 2) + 1;
+          const int i = 2 * p + 1 + ((1 + j + n) & 1);
+          const T v = (T)0.25 * (bx[G::g(i + 1, j, 0)] + bx[G::g(i - 1, j, 0)] + bx[G::g(i, j + 1, 0)] +
+                                 bx[G::g(i, j - 1, 0)] - dx2 * f[G::in(i, j, 1)]);
+          phi[d.offg + G::g(i, j, 0)] = v;
+        } else {
+          const int j = (q / (NC / 2)) % NC + 1;
+          const int kk = q / ((NC / 2) * NC) + 1;
+          const int i = 2 * p + 1 + ((1 + j + kk + n) & 1);
           const T sixth = (T)(1 / 6.0);
-          T f = rhs[m.offi[s] + G::in(i, j, k)];
-          T v = sixth * (bx[G::g(i + 1, j, k)] + bx[G::g(i - 1, j, k)] + bx[G::g(i, j + 1, k)] +
-                         bx[G::g(i, j - 1, k)] + bx[G::g(i, j, k + 1)] + bx[G::g(i, j, k - 1)] -
-                         dx2 * f);
-          phi[m.offg[s] + G::g(i, j, k)] = v;
+          const T v = sixth * (bx[G::g(i + 1, j, kk)] + bx[G::g(i - 1, j, kk)] + bx[G::g(i, j + 1, kk)] +
+                               bx[G::g(i, j - 1, kk)] + bx[G::g(i, j, kk + 1)] + bx[G::g(i, j, kk - 1)] -
+                               dx2 * f[G::in(i, j, kk)]);
+          phi[d.offg + G::g(i, j, kk)] = v;
         }
       }
     }
     __syncthreads();
+#pragma unroll
+    for (int j = 0; j < C::ITEMS; ++j) cur[j] = nxt[j];
+    cur_act = nxt_act;
   }
 }
 
@@ -575,16 +791,51 @@ k_correct(Meta m, BoxSet bs, T* __restrict__ phi, T* __restrict__ tmp) {
 // max that keeps a NaN once seen (fmax would drop it and hide a diverged solve)
 __device__ __forceinline__ double nanmax(double a, double b) { return (b > a || b != b) ? b : a; }
 
-// Block-segment max of non-negative values followed by one atomicMax per
-// segment of SEG threads (SEG a power of two); the bit pattern of a
-// non-negative double orders like its value.
-template <int SEG>
-__device__ __forceinline__ void seg_atomic_max(unsigned long long* dst, double v) {
-  unsigned lane = threadIdx.x & 31;
-  constexpr int W = SEG < 32 ? SEG : 32;
+// Per-tree maxima are accumulated in kStripes slots per tree (box index
+// modulo kStripes) so that boxes of one tree do not all contend for one
+// address; k_stripe_reduce folds them. The bit pattern of a non-negative
+// double orders like its value, and a NaN orders above every number.
+constexpr int kStripes = 64;
+
+__device__ __forceinline__ unsigned long long dbits(double v) {
+  return (unsigned long long)__double_as_longlong(v);
+}
+
+// Max over the PER_BOX threads of each box (PER_BOX a power of two), then one
+// atomicMax per box into dst (uniform per box, may be null).
+template <int PER_BOX>
+__device__ __forceinline__ void box_max_atomic(double v, unsigned long long* dst, double* red) {
+  constexpr int W = PER_BOX < 32 ? PER_BOX : 32;
 #pragma unroll
   for (int o = W / 2; o > 0; o >>= 1) v = nanmax(v, __shfl_xor_sync(0xffffffffu, v, o));
-  if ((lane & (W - 1)) == 0 && dst) atomicMax(dst, (unsigned long long)__double_as_longlong(v));
+  if constexpr (PER_BOX <= 32) {
+    if ((threadIdx.x & (W - 1)) == 0 && dst) atomicMax(dst, dbits(v));
+  } else {
+    constexpr int WPB = PER_BOX / 32;
+    const int warp = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) red[warp] = v;
+    __syncthreads();
+    if ((threadIdx.x % PER_BOX) == 0 && dst) {
+      double mm = red[warp];
+#pragma unroll
+      for (int w = 1; w < WPB; ++w) mm = nanmax(mm, red[warp + w]);
+      atomicMax(dst, dbits(mm));
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void k_stripe_reduce(int n_trees, const unsigned long long* __restrict__ norm,
+                                unsigned long long* __restrict__ out) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n_trees) {
+    unsigned long long m = 0;
+    for (int k = 0; k < kStripes; ++k) {
+      unsigned long long v = norm[(size_t)t * kStripes + k];
+      m = v > m ? v : m;
+    }
+    out[t] = m;
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -599,6 +850,7 @@ k_residual(Meta m, BoxSet bs, const T* __restrict__ phi, const T* __restrict__ r
   using G = Geo<D, NC>;
   constexpr int PER_BOX = G::SI < kThreads ? G::SI : kThreads;
   constexpr int BPC = kThreads / PER_BOX;
+  __shared__ double red[kThreads / 32];
   const int groups = (bs.n + BPC - 1) / BPC;
   for (int grp = blockIdx.x; grp < groups; grp += gridDim.x) {
     int b = threadIdx.x / PER_BOX, q0 = threadIdx.x % PER_BOX;
@@ -626,8 +878,9 @@ k_residual(Meta m, BoxSet bs, const T* __restrict__ phi, const T* __restrict__ r
     }
     if (norm_per_tree) {
       // all threads of a PER_BOX segment belong to the same box
-      seg_atomic_max<PER_BOX>((tr >= 0 && leaf) ? norm_per_tree + tr : nullptr,
-                              (tr >= 0 && leaf) ? mx : 0.0);
+      box_max_atomic<PER_BOX>(
+          mx, (tr >= 0 && leaf) ? norm_per_tree + (size_t)tr * kStripes + (bi & (kStripes - 1)) : nullptr,
+          red);
     }
   }
 }
@@ -641,6 +894,7 @@ k_maxabs(Meta m, BoxSet bs, const T* __restrict__ v, int ghosted,
   using G = Geo<D, NC>;
   constexpr int PER_BOX = G::SI < kThreads ? G::SI : kThreads;
   constexpr int BPC = kThreads / PER_BOX;
+  __shared__ double red[kThreads / 32];
   const int groups = (bs.n + BPC - 1) / BPC;
   for (int grp = blockIdx.x; grp < groups; grp += gridDim.x) {
     int b = threadIdx.x / PER_BOX, q0 = threadIdx.x % PER_BOX;
@@ -659,7 +913,8 @@ k_maxabs(Meta m, BoxSet bs, const T* __restrict__ v, int ghosted,
         }
       }
     }
-    seg_atomic_max<PER_BOX>(tr >= 0 ? norm_per_tree + tr : nullptr, tr >= 0 ? mx : 0.0);
+    box_max_atomic<PER_BOX>(
+        mx, tr >= 0 ? norm_per_tree + (size_t)tr * kStripes + (bi & (kStripes - 1)) : nullptr, red);
   }
 }
 
@@ -740,6 +995,7 @@ k_defect(Meta m, BoxSet bs, const double* __restrict__ u, const double* __restri
   using G = Geo<D, NC>;
   constexpr int PER_BOX = G::SI < kThreads ? G::SI : kThreads;
   constexpr int BPC = kThreads / PER_BOX;
+  __shared__ double red[kThreads / 32];
   const int groups = (bs.n + BPC - 1) / BPC;
   for (int grp = blockIdx.x; grp < groups; grp += gridDim.x) {
     int b = threadIdx.x / PER_BOX, q0 = threadIdx.x % PER_BOX;
@@ -761,7 +1017,8 @@ k_defect(Meta m, BoxSet bs, const double* __restrict__ u, const double* __restri
         }
       }
     }
-    seg_atomic_max<PER_BOX>(tr >= 0 ? norm_per_tree + tr : nullptr, tr >= 0 ? mx : 0.0);
+    box_max_atomic<PER_BOX>(
+        mx, tr >= 0 ? norm_per_tree + (size_t)tr * kStripes + (bi & (kStripes - 1)) : nullptr, red);
   }
 }
 
@@ -861,7 +1118,7 @@ __global__ void k_check(int n_trees, const unsigned long long* __restrict__ rnor
                         int* __restrict__ failed, int* __restrict__ n_active_out) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t < n_trees) {
-    double r = __longlong_as_double((long long)rnorm[t]);
+    double r = __longlong_as_double((long long)rnorm[t]);  // reduced over stripes
     int a = active[t];
     if (a && !(r <= 1.0e300)) {  // NaN or overflow: stop this tree, report failure
       a = 0;

@@ -1,6 +1,7 @@
 #include "plan.hpp"
 
 #include <algorithm>
+#include <cstring>
 #include <numeric>
 
 namespace afv {
@@ -180,6 +181,16 @@ int build_plan(const std::vector<const HostTree*>& trees, Plan& p, std::string& 
       }
     }
   }
+  // Offsets of the box each ghost face reads from.
+  p.nbo.assign((size_t)N * NNB, -1);
+  for (int sl = 0; sl < N; ++sl)
+    for (int f = 0; f < NNB; ++f) {
+      int code = p.nb[(size_t)sl * NNB + f];
+      if (code >= 0)
+        p.nbo[(size_t)sl * NNB + f] = p.offg[code];
+      else if (code == -1)
+        p.nbo[(size_t)sl * NNB + f] = p.offg[p.parent[sl]];
+    }
   // per-level leaf / parent lists in slot order
   for (int l = p.min_lvl; l <= max_lvl; ++l) {
     for (int k = 0; k < p.lvl_n[p.L(l)]; ++k) {
@@ -195,7 +206,39 @@ int build_plan(const std::vector<const HostTree*>& trees, Plan& p, std::string& 
     }
   }
   for (int t = 0; t < p.n_trees; ++t) plan_fill_bc(p, t);
+  plan_build_desc(p);
   return AFV_OK;
+}
+
+void plan_build_desc(Plan& p) {
+  const int NNB = 2 * p.dim;
+  p.desc.assign(p.n_slots, SlotDesc());
+  for (int s = 0; s < p.n_slots; ++s) {
+    SlotDesc& d = p.desc[s];
+    std::memset(&d, 0, sizeof(d));
+    for (int f = 0; f < 6; ++f) {
+      d.code[f] = -2;
+      d.nbo[f] = -1;
+    }
+    for (int f = 0; f < NNB; ++f) {
+      size_t k = (size_t)s * NNB + f;
+      int code = p.nb[k];
+      if (code >= -1) {
+        d.code[f] = code;
+        d.nbo[f] = p.nbo[k];
+      } else {
+        d.code[f] = p.bctype[k] ? -3 : -2;
+        d.nbo[f] = p.bcoff[k];
+      }
+    }
+    d.qd = p.qd[s];
+    d.tree = p.tree[s];
+    d.dr = p.dr[s];
+    d.offg = p.offg[s];
+    d.offi = p.offi[s];
+    d.first_child = p.first_child[s];
+    d.parent = p.parent[s];
+  }
 }
 
 void plan_fill_bc(Plan& p, int t) {

@@ -11,6 +11,7 @@
 #include <string>
 #include <vector>
 
+#include "desc.hpp"
 #include "host_tree.hpp"
 
 namespace afv {
@@ -35,6 +36,7 @@ struct Plan {
   std::vector<double> dr;
   std::vector<double> r_min;     // [s*D+d]
   std::vector<long long> offg, offi;
+  std::vector<long long> nbo;    // [s*2D+f] offg of the neighbour / of the parent at a refinement boundary
   std::vector<int> bctype;       // [s*2D+f]
   std::vector<long long> bcoff;  // [s*2D+f]
   std::vector<double> bcval;
@@ -48,6 +50,7 @@ struct Plan {
   std::vector<int> tree_highest;
   std::vector<long long> tree_leaf_cells;
   std::vector<BcSpec> bc;
+  std::vector<SlotDesc> desc;   // per slot, see desc.hpp
 
   int nc_at(int l) const { return l >= 1 ? nc : (nc >> (1 - l)); }
   int L(int l) const { return l - min_lvl; }
@@ -58,5 +61,8 @@ int build_plan(const std::vector<const HostTree*>& trees, Plan& p, std::string& 
 
 // (Re)compute the boundary value records of one tree from its BcSpec.
 void plan_fill_bc(Plan& p, int tree);
+
+// (Re)build the per-slot descriptors (after the tables or the boundary values change).
+void plan_build_desc(Plan& p);
 
 }  // namespace afv

@@ -49,6 +49,9 @@ static Meta meta_of(const DevMeta& d) {
   m.bcoff = d.bcoff;
   m.bcval = d.bcval;
   m.active = d.active;
+  m.nbo = d.nbo;
+  m.desc = d.desc;
+  m.err = d.err;
   return m;
 }
 
@@ -78,8 +81,9 @@ Forest::~Forest() {
   cudaSetDevice(device);
   if (stream) cudaStreamSynchronize(stream);
   void* ptrs[] = {meta.nb, meta.parent, meta.first_child, meta.tree, meta.qd, meta.dr, meta.offg,
-                  meta.offi, meta.bctype, meta.bcoff, meta.bcval, meta.active, d64.phi, d64.rhs,
-                  d64.tmp, d32.phi, d32.rhs, d32.tmp, base_phi64, base_rhs64, d_lists, d_norm,
+                  meta.offi, meta.bctype, meta.bcoff, meta.bcval, meta.active, meta.nbo, meta.desc,
+                  meta.err, d64.phi, d64.rhs,
+                  d64.tmp, d32.phi, d32.rhs, d32.tmp, base_phi64, base_rhs64, d_lists, d_norm, d_red,
                   d_fmax, d_count, d_failed, d_stage, d_stage_slots};
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -91,6 +95,18 @@ Forest::~Forest() {
   if (h_count) cudaFreeHost(h_count);
   if (h_norm) cudaFreeHost(h_norm);
   if (stream) cudaStreamDestroy(stream);
+}
+
+int Forest::check_device_error(std::string& err) {
+  int h = 0;
+  cudaMemcpyAsync(&h, meta.err, sizeof(int), cudaMemcpyDeviceToHost, stream);
+  cudaStreamSynchronize(stream);
+  if (h) {
+    cudaMemsetAsync(meta.err, 0, sizeof(int), stream);
+    err = "a bounded device wait gave up (copy not completed in time)";
+    return AFV_ERR_TIMEOUT;
+  }
+  return AFV_OK;
 }
 
 int Forest::check(std::string& err, const char* where) {
@@ -189,7 +205,10 @@ int Forest::create(const std::vector<const HostTree*>& trees, const afv_forest_o
   UP(offg, offg);
   UP(offi, offi);
   UP(bctype, bctype);
+  UP(nbo, nbo);
 #undef UP
+  if (dmalloc(&meta.err, 1, bytes)) return err = "device allocation failed", AFV_ERR_NOMEM;
+  cudaMemset(meta.err, 0, sizeof(int));
   if ((rc = upload_bc(err))) return rc;
   std::vector<int> act(p.n_trees, 1);
   if ((rc = dupload(&meta.active, act, bytes))) return err = "device allocation failed", rc;
@@ -228,7 +247,8 @@ int Forest::create(const std::vector<const HostTree*>& trees, const afv_forest_o
   all_leaves_off = (int)lists.size();
   lists.insert(lists.end(), p.all_leaves.begin(), p.all_leaves.end());
   if ((rc = dupload(&d_lists, lists, bytes))) return err = "device allocation failed", rc;
-  if (dmalloc(&d_norm, p.n_trees, bytes) || dmalloc(&d_fmax, p.n_trees, bytes) ||
+  if (dmalloc(&d_norm, (long long)p.n_trees * dev::kStripes, bytes) ||
+      dmalloc(&d_red, p.n_trees, bytes) || dmalloc(&d_fmax, p.n_trees, bytes) ||
       dmalloc(&d_count, 1, bytes) || dmalloc(&d_failed, p.n_trees, bytes))
     return err = "device allocation failed", AFV_ERR_NOMEM;
   if (cudaMallocHost((void**)&h_count, sizeof(int)) != cudaSuccess ||
@@ -236,6 +256,15 @@ int Forest::create(const std::vector<const HostTree*>& trees, const afv_forest_o
     return err = "pinned allocation failed", AFV_ERR_NOMEM;
   if (cudaDeviceSynchronize() != cudaSuccess) return check(err, "forest create");
   return AFV_OK;
+}
+
+void Forest::norm_reset() {
+  cudaMemsetAsync(d_norm, 0, sizeof(unsigned long long) * plan.n_trees * dev::kStripes, stream);
+}
+
+void Forest::norm_fold() {
+  ProfScope ps(this, kProfOther, 8.0 * plan.n_trees * dev::kStripes);
+  dev::k_stripe_reduce<<<(plan.n_trees + 255) / 256, 256, 0, stream>>>(plan.n_trees, d_norm, d_red);
 }
 
 int Forest::upload_bc(std::string& err) {
@@ -246,6 +275,11 @@ int Forest::upload_bc(std::string& err) {
   meta.bcval = nullptr;
   if (dupload(&meta.bcoff, plan.bcoff, b) || dupload(&meta.bcval, plan.bcval, b))
     return err = "device allocation failed", AFV_ERR_NOMEM;
+  if (!meta.desc && dmalloc(&meta.desc, (long long)plan.desc.size(), bytes))
+    return err = "device allocation failed", AFV_ERR_NOMEM;
+  if (cudaMemcpy(meta.desc, plan.desc.data(), plan.desc.size() * sizeof(SlotDesc),
+                 cudaMemcpyHostToDevice) != cudaSuccess)
+    return err = "descriptor upload failed", AFV_ERR_CUDA;
   if (cudaMemcpy(meta.bctype, plan.bctype.data(), plan.bctype.size() * sizeof(int),
                  cudaMemcpyHostToDevice) != cudaSuccess)
     return err = "bc upload failed", AFV_ERR_CUDA;
@@ -368,12 +402,18 @@ void Forest::sweep(const Arrays<T>& a, int lvl, int n, bool pull, bool homog) {
   with_nc(plan.dim, plan.nc_at(lvl), [&](auto d_, auto nc_) {
     constexpr int D = decltype(d_)::value, NC = decltype(nc_)::value;
     using G = dev::Geo<D, NC>;
-    constexpr int BPC = dev::boxes_per_cta<G::SG, G::SI / 2, T>(1);
-    int grid = grid_for((nbx + BPC - 1) / BPC, n_sm);
+    using C = dev::SweepCfg<D, NC, T>;
+    static int occ = 0;
+    if (!occ) {
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, dev::k_sweep_tma<D, NC, T>, dev::kThreads, 0);
+      if (occ < 1) occ = 1;
+    }
+    const long long groups = (nbx + C::BPC - 1) / C::BPC;
+    const int grid = (int)std::max(1LL, std::min(groups, (long long)n_sm * occ));
     // read phi and f, write phi over the interior
     ProfScope ps(this, kProfSweep, 3.0 * nbx * G::SI * sizeof(T));
-    dev::k_sweep<D, NC, T><<<grid, dev::kThreads, 0, stream>>>(m, bs, a.phi, a.rhs, n, pull ? 1 : 0,
-                                                              homog ? 1 : 0);
+    dev::k_sweep_tma<D, NC, T><<<grid, dev::kThreads, 0, stream>>>(
+        m, bs.lo, nbx, a.phi, a.rhs, n, pull ? 1 : 0, homog ? 1 : 0);
   });
 }
 
@@ -562,7 +602,8 @@ void Forest::vcycle_t(const Arrays<T>& a, const MgOpts& mg, int highest, bool ho
 
 int Forest::gsrb_level(int lvl, int n_cycle, std::string& err) {
   gsrb_boxes(d64, lvl, n_cycle, false);
-  return check(err, "gsrb_level");
+  if (int rc = check(err, "gsrb_level")) return rc;
+  return check_device_error(err);
 }
 int Forest::fill_level(int lvl, std::string& err) {
   fill(d64, lvl, false);
@@ -589,7 +630,8 @@ int Forest::vcycle(const MgOpts& mg, int highest, bool set_residual, std::string
   vcycle_t(d64, mg, highest, false, false);
   if (set_residual)
     for (int l = plan.min_lvl; l <= highest; ++l) residual(d64, l, nullptr, true);
-  return check(err, "vcycle");
+  if (int rc = check(err, "vcycle")) return rc;
+  return check_device_error(err);
 }
 
 int Forest::gc_tree(std::string& err) {
@@ -682,7 +724,8 @@ int Forest::fmg(const MgOpts& mg, bool set_residual, bool have_guess, std::strin
     }
   }
   set_active_host(all);
-  return check(err, "fmg");
+  if (int rc = check(err, "fmg")) return rc;
+  return check_device_error(err);
 }
 
 int Forest::max_abs(int t, int var, double* out, std::string& err) {
@@ -691,7 +734,7 @@ int Forest::max_abs(int t, int var, double* out, std::string& err) {
   act[t] = 1;
   std::vector<int> saved = host_active;
   set_active_host(act);
-  cudaMemsetAsync(d_norm, 0, sizeof(unsigned long long) * plan.n_trees, stream);
+  norm_reset();
   Meta m = meta_of(meta);
   for (int l = plan.min_lvl; l <= plan.max_lvl; ++l) {
     int nl = n_leaves(l);
@@ -708,7 +751,8 @@ int Forest::max_abs(int t, int var, double* out, std::string& err) {
           m, bs, v, var != AFV_RHS, d_norm);
     });
   }
-  cudaMemcpyAsync(h_norm, d_norm, sizeof(unsigned long long) * plan.n_trees, cudaMemcpyDeviceToHost,
+  norm_fold();
+  cudaMemcpyAsync(h_norm, d_red, sizeof(unsigned long long) * plan.n_trees, cudaMemcpyDeviceToHost,
                   stream);
   cudaStreamSynchronize(stream);
   std::memcpy(out, &h_norm[t], sizeof(double));
@@ -738,7 +782,7 @@ int Forest::solve(const MgOpts& mg, int precision, double tol, int max_cycles, S
   Meta m = meta_of(meta);
   set_active_all(1);
   // max |f| over the leaves of every tree
-  cudaMemsetAsync(d_norm, 0, sizeof(unsigned long long) * nt, stream);
+  norm_reset();
   for (int l = plan.min_lvl; l <= plan.max_lvl; ++l) {
     int nl = n_leaves(l);
     if (!nl) continue;
@@ -753,15 +797,16 @@ int Forest::solve(const MgOpts& mg, int precision, double tol, int max_cycles, S
           m, bs, d64.rhs, 0, d_norm);
     });
   }
-  cudaMemcpyAsync(d_fmax, d_norm, sizeof(double) * nt, cudaMemcpyDeviceToDevice, stream);
+  norm_fold();
+  cudaMemcpyAsync(d_fmax, d_red, sizeof(double) * nt, cudaMemcpyDeviceToDevice, stream);
   std::vector<double> fmax(nt);
-  cudaMemcpyAsync(fmax.data(), d_norm, sizeof(double) * nt, cudaMemcpyDeviceToHost, stream);
+  cudaMemcpyAsync(fmax.data(), d_red, sizeof(double) * nt, cudaMemcpyDeviceToHost, stream);
   cudaStreamSynchronize(stream);
   std::vector<int> done_cycles(nt, 0);
   cudaMemsetAsync(d_failed, 0, sizeof(int) * nt, stream);
 
   auto residual_check = [&](bool mixed_path) -> int {
-    cudaMemsetAsync(d_norm, 0, sizeof(unsigned long long) * nt, stream);
+    norm_reset();
     if (mixed_path) {
       // Parents hold the restriction of their children, as at the fixed point
       // of the FAS cycle: coarse leaves next to a refined region see them
@@ -784,13 +829,14 @@ int Forest::solve(const MgOpts& mg, int precision, double tol, int max_cycles, S
       for (int l = plan.min_lvl; l <= plan.max_lvl; ++l) residual(d64, l, d_norm, true);
     }
     cudaMemsetAsync(d_count, 0, sizeof(int), stream);
+    norm_fold();
     {
       ProfScope ps(this, kProfOther, 20.0 * nt);
-      dev::k_check<<<(nt + 255) / 256, 256, 0, stream>>>(nt, d_norm, d_fmax, tol, meta.active,
+      dev::k_check<<<(nt + 255) / 256, 256, 0, stream>>>(nt, d_red, d_fmax, tol, meta.active,
                                                          d_failed, d_count);
     }
     cudaMemcpyAsync(h_count, d_count, sizeof(int), cudaMemcpyDeviceToHost, stream);
-    cudaMemcpyAsync(h_norm, d_norm, sizeof(unsigned long long) * nt, cudaMemcpyDeviceToHost, stream);
+    cudaMemcpyAsync(h_norm, d_red, sizeof(unsigned long long) * nt, cudaMemcpyDeviceToHost, stream);
     cudaMemcpyAsync(host_active.data(), meta.active, sizeof(int) * nt, cudaMemcpyDeviceToHost, stream);
     cudaStreamSynchronize(stream);
     return *h_count;
@@ -829,6 +875,7 @@ int Forest::solve(const MgOpts& mg, int precision, double tol, int max_cycles, S
     n_active = residual_check(precision == AFV_PREC_MIXED);
     record(was);
     if (int rc = check(err, "solve")) return rc;
+    if (int rc = check_device_error(err)) return rc;
   }
   if (precision == AFV_PREC_MIXED) {
     set_active_all(1);
