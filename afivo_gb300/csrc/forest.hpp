@@ -19,20 +19,15 @@ struct Arrays {
 };
 
 struct DevMeta {
-  int* nb = nullptr;
   int* parent = nullptr;
   int* first_child = nullptr;
   int* tree = nullptr;
-  int* qd = nullptr;
-  double* dr = nullptr;
   long long* offg = nullptr;
   long long* offi = nullptr;
-  int* bctype = nullptr;
-  long long* bcoff = nullptr;
   double* bcval = nullptr;
   int* active = nullptr;  // [n_trees]
-  long long* nbo = nullptr;
   SlotDesc* desc = nullptr;
+  long long* nbo2 = nullptr;
   int* err = nullptr;  // device error word (bounded waits)
 };
 

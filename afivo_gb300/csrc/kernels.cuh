@@ -7,10 +7,12 @@
 // trees; slot s keeps phi/tmp at offg[s] as a (NC+2)^D box with one ghost
 // layer, x fastest (the reference's cc(0:nc+1, ...) arrays,
 // src/m_aX_core.f90:360-369), and rhs at offi[s] as an NC^D interior-only box
-// (rhs ghost cells are never read by the reference's path).
+// (rhs ghost cells are never read by the reference's path). A 128-byte
+// SlotDesc per slot (desc.hpp) holds the box's links and constants.
 //
 // Floating-point order follows the reference expression by expression; the
-// library is compiled with -fmad=false so that no multiply-add is fused.
+// library is compiled with -fmad=false so that no multiply-add is fused
+// (the mixed path's FP64 defect uses explicit fma() where stated).
 #pragma once
 #include <cstdint>
 
@@ -22,10 +24,6 @@ namespace dev {
 constexpr int kThreads = 256;
 constexpr int kSmemCap = 48 * 1024;
 
-// Neighbour codes of a slot face.
-constexpr int kNbRefinement = -1;  // no box at this level: coarse neighbour
-constexpr int kNbPhysical = -2;    // physical boundary
-
 struct BoxSet {
   const int* list;  // slot list, or nullptr for the range [lo, lo+n)
   int lo;
@@ -33,20 +31,15 @@ struct BoxSet {
 };
 
 struct Meta {
-  const int* nb;           // [slot*2D + face]
+  const int* tree;         // [slot]
   const int* parent;       // [slot]
   const int* first_child;  // [slot]
-  const int* tree;         // [slot]
-  const int* qd;           // [slot] child-number bits within the parent (lvl >= 2), else -1
-  const double* dr;        // [slot]
   const long long* offg;   // [slot] offset of the ghosted box
   const long long* offi;   // [slot] offset of the interior box
-  const int* bctype;       // [slot*2D + face] 0 Dirichlet, 1 Neumann
-  const long long* bcoff;  // [slot*2D + face] offset of the face values in bcval, -1 = zero
-  const double* bcval;
+  const double* bcval;     // boundary values (faces of physical boundaries)
   const int* active;       // [tree] nonzero if the tree takes part in this launch
-  const long long* nbo;    // [slot*2D + face] offg of the neighbour (box code >= 0) or of the parent (refinement boundary)
   const SlotDesc* desc;    // [slot]
+  const long long* nbo2;   // [slot*2D + face] refinement boundary: offg of the parent's neighbour
   int* err;                // device error word: nonzero after a bounded wait gave up
 };
 
@@ -60,14 +53,28 @@ struct Geo {
   static constexpr int NF = D == 2 ? NC : NC * NC;
   static constexpr int NNB = 2 * D;
   __host__ __device__ static constexpr int g(int i, int j, int k) { return i + NG * (j + NG * k); }
+  // interior index; k is ignored in 2-D
   __host__ __device__ static constexpr int in(int i, int j, int k) {
-    return (i - 1) + NC * ((j - 1) + NC * (k - 1 < 0 ? 0 : k - 1));
+    return (i - 1) + NC * ((j - 1) + (D == 3 ? NC * (k - 1) : 0));
   }
 };
 
 template <class T> struct Vec;
 template <> struct Vec<double> { using type = double2; static constexpr int w = 2; };
 template <> struct Vec<float> { using type = float4; static constexpr int w = 4; };
+
+// Per-precision constants of a slot.
+template <class T> struct Sc;
+template <> struct Sc<double> {
+  __device__ static double dr(const SlotDesc& d) { return d.dr; }
+  __device__ static double dx2(const SlotDesc& d) { return d.dx2; }
+  __device__ static double inv(const SlotDesc& d) { return d.inv_dx2; }
+};
+template <> struct Sc<float> {
+  __device__ static float dr(const SlotDesc& d) { return d.drf; }
+  __device__ static float dx2(const SlotDesc& d) { return d.dx2f; }
+  __device__ static float inv(const SlotDesc& d) { return d.inv_dx2f; }
+};
 
 template <int SG, int PER_BOX, class T>
 __host__ __device__ constexpr int boxes_per_cta(int staged) {
@@ -110,65 +117,79 @@ struct Face {
   }
 };
 
-// Ghost value of one face cell of box s, from the state of the level before
-// this call. own(i,j,k) reads the box's own cells.
-//  - neighbour box: copy of its boundary cell, src/m_aX_gc.f90:381-415
-//  - refinement boundary: mg$D_sides_rb, src/m_aX_mg.f90:262-350, after the
-//    zeroth-order injection of the parent's value (a$D_gc_prolong0,
-//    src/m_aX_gc.f90:135-151 and a$D_prolong0, src/m_aX_prolong.f90:39-108)
-//  - physical boundary: bc_to_gc, src/m_aX_gc.f90:71-132 with the sampled
-//    boundary value b of the sides_bc hook
-template <int D, int NC, class T, class Own>
-__device__ __forceinline__ T ghost_value(const Meta& m, const T* __restrict__ phi, int s, int f,
-                                         int a, int c, bool homog, Own own) {
-  using G = Geo<D, NC>;
-  Face<D, NC> F(f, a, c);
-  int code = m.nb[s * G::NNB + f];
-  if (code >= 0) {
-    return phi[m.nbo[s * G::NNB + f] + G::g(F.ni, F.nj, F.nk)];
-  }
-  if (code == kNbRefinement) {
-    // Injection from the parent (levels >= 2 only; the parent has the same NC).
-    const int qd = m.qd[s];
-    const int h = NC >> 1;
-    const int pi = (qd & 1) * h + ((F.gi + 1) >> 1);
-    const int pj = ((qd >> 1) & 1) * h + ((F.gj + 1) >> 1);
-    const int pk = (D == 3) ? ((qd >> 2) & 1) * h + ((F.gk + 1) >> 1) : 0;
-    T g0 = phi[m.nbo[s * G::NNB + f] + G::g(pi, pj, pk)];
-    int dim = f >> 1;
-    int dix = (f & 1) ? -1 : 1;
-    if constexpr (D == 2) {
-      if (dim == 0) {
-        int i = F.ai, j = F.aj;
-        int dj = -1 + 2 * (j & 1);
-        return (T)0.5 * g0 + own(i, j, 0) - (T)0.25 * (own(i + dix, j, 0) + own(i, j + dj, 0));
-      } else {
-        int i = F.ai, j = F.aj;
-        int di = -1 + 2 * (i & 1);
-        return (T)0.5 * g0 + own(i, j, 0) - (T)0.25 * (own(i + di, j, 0) + own(i, j + dix, 0));
-      }
-    } else {
-      int i = F.ai, j = F.aj, k = F.ak;
-      int di = (dim == 0) ? dix : -1 + 2 * (i & 1);
-      int dj = (dim == 1) ? dix : -1 + 2 * (j & 1);
-      int dk = (dim == 2) ? dix : -1 + 2 * (k & 1);
-      return (T)0.5 * g0 + (T)0.75 * own(i, j, k) - (T)0.25 * own(i + di, j + dj, k + dk);
+// Cell of the parent (or, two hops away, of the parent's neighbour) that the
+// zeroth-order injection a$D_prolong0 (src/m_aX_prolong.f90:88-94) copies into
+// ghost cell F of a box with child bits qd. With two_hop the parent's ghost
+// cell is replaced by the neighbour's boundary cell it holds.
+template <int D, int NC>
+__device__ __forceinline__ int parent_cell(const Face<D, NC>& F, int f, int qd, bool two_hop) {
+  const int h = NC >> 1;
+  int pi = (qd & 1) * h + ((F.gi + 1) >> 1);
+  int pj = ((qd >> 1) & 1) * h + ((F.gj + 1) >> 1);
+  int pk = (D == 3) ? ((qd >> 2) & 1) * h + ((F.gk + 1) >> 1) : 0;
+  if (two_hop) {  // ghost index 0 <- neighbour's NC, ghost index NC+1 <- neighbour's 1
+    const int mirror = (f & 1) ? 1 : NC;
+    switch (f >> 1) {
+      case 0: pi = mirror; break;
+      case 1: pj = mirror; break;
+      default: pk = mirror; break;
     }
   }
-  // Physical boundary: y = c2 * b + c1 * x
-  T b = 0;
-  long long bo = m.bcoff[s * G::NNB + f];
-  if (!homog && bo >= 0) {
-    int lin = (D == 2) ? (a - 1) : (a - 1) + NC * (c - 1);
-    b = (T)m.bcval[bo + lin];
-  }
-  T x = own(F.ai, F.aj, F.ak);
-  if (m.bctype[s * G::NNB + f] == 0) {
-    return (T)2 * b + (T)(-1) * x;
+  return Geo<D, NC>::g(pi, pj, pk);
+}
+
+// Ghost value from the injected parent value g0 and the box's own cells:
+// mg$D_sides_rb, src/m_aX_mg.f90:286-347 (2-D and 3-D forms).
+template <int D, int NC, class T, class Own>
+__device__ __forceinline__ T rb_value(const Face<D, NC>& F, int f, T g0, Own own) {
+  const int dim = f >> 1, dix = (f & 1) ? -1 : 1;
+  const int i = F.ai, j = F.aj, k = F.ak;
+  if constexpr (D == 2) {
+    if (dim == 0) {
+      const int dj = -1 + 2 * (j & 1);
+      return (T)0.5 * g0 + own(i, j, 0) - (T)0.25 * (own(i + dix, j, 0) + own(i, j + dj, 0));
+    } else {
+      const int di = -1 + 2 * (i & 1);
+      return (T)0.5 * g0 + own(i, j, 0) - (T)0.25 * (own(i + di, j, 0) + own(i, j + dix, 0));
+    }
   } else {
-    T c2 = (T)m.dr[s] * (T)((f & 1) ? 1 : -1);
-    return c2 * b + (T)1 * x;
+    const int di = (dim == 0) ? dix : -1 + 2 * (i & 1);
+    const int dj = (dim == 1) ? dix : -1 + 2 * (j & 1);
+    const int dk = (dim == 2) ? dix : -1 + 2 * (k & 1);
+    return (T)0.5 * g0 + (T)0.75 * own(i, j, k) - (T)0.25 * own(i + di, j + dj, k + dk);
   }
+}
+
+// Physical boundary, bc_to_gc (src/m_aX_gc.f90:71-132): y = c2 * b + c1 * x
+// with (c1, c2) = (-1, 2) for Dirichlet and (1, dr * (+-1)) for Neumann.
+template <class T>
+__device__ __forceinline__ T bc_value(int code, int f, T b, T x, T dr) {
+  if (code == kFaceDirichlet) return (T)2 * b + (T)(-1) * x;
+  const T c2 = dr * (T)((f & 1) ? 1 : -1);
+  return c2 * b + (T)1 * x;
+}
+
+// Ghost value of one face cell of a slot from the current state of its level
+// (own(i,j,k) reads the box's own cells): the value the reference's a$D_gc_box
+// (src/m_aX_gc.f90:50-69) stores there.
+//  - neighbour box: copy of its boundary cell (sides_from_nb, :381-415)
+//  - refinement boundary: parent injection + mg$D_sides_rb
+//  - physical boundary: bc_to_gc with the sampled sides_bc value
+template <int D, int NC, class T, class Own>
+__device__ __forceinline__ T ghost_value(const Meta& m, const SlotDesc& d, const T* __restrict__ phi,
+                                         int f, int a, int c, bool homog, Own own) {
+  using G = Geo<D, NC>;
+  const Face<D, NC> F(f, a, c);
+  const int code = d.code[f];
+  const long long o = d.nbo[f];
+  if (code >= 0) return phi[o + G::g(F.ni, F.nj, F.nk)];
+  if (code == kFaceRefinement) {
+    const T g0 = phi[o + parent_cell<D, NC>(F, f, d.qd, false)];
+    return rb_value<D, NC, T>(F, f, g0, own);
+  }
+  T b = 0;
+  if (!homog && o >= 0) b = (T)m.bcval[o + ((D == 2) ? (a - 1) : (a - 1) + NC * (c - 1))];
+  return bc_value<T>(code, f, b, own(F.ai, F.aj, F.ak), Sc<T>::dr(d));
 }
 
 // ---------------------------------------------------------------------------
@@ -237,29 +258,31 @@ __device__ __forceinline__ void needed_face_cell(int f, int m, int n, int& a, in
 template <int D, int NC, class T>
 struct SweepCfg {
   using G = Geo<D, NC>;
-  static constexpr int S = 3;                   // pipeline stages
+  static constexpr int S = 4;                   // pipeline stages
   static constexpr int PER_BOX = G::SI / 2;     // one thread per updated cell
   static constexpr int BOX_B = (int)sizeof(SlotDesc) + (G::SG + G::SI) * (int)sizeof(T);
   static constexpr int BPC_T = kThreads / PER_BOX;
-  static constexpr int BPC_S = 46 * 1024 / (S * BOX_B);
-  static constexpr int BPC = BPC_T < BPC_S ? BPC_T : BPC_S;
+  static constexpr int BPC_S = 56 * 1024 / (S * BOX_B);
+  static constexpr int BPC = BPC_T < BPC_S ? BPC_T : (BPC_S < 1 ? 1 : BPC_S);
   static constexpr int NEED = 2 * D * (G::NF / 2);  // ghost cells one colour reads
   static constexpr int ITEMS = (BPC * NEED + kThreads - 1) / kThreads;
   static constexpr int DESC_B = BPC * (int)sizeof(SlotDesc);
   static constexpr int PHI_B = BPC * G::SG * (int)sizeof(T);
   static constexpr int RHS_B = BPC * G::SI * (int)sizeof(T);
   static constexpr int STAGE_B = DESC_B + PHI_B + RHS_B;
-  static_assert(BPC >= 1, "box too large for the sweep pipeline");
+  static constexpr int SMEM_B = S * STAGE_B;  // dynamic shared memory
   static_assert(PHI_B % 16 == 0 && RHS_B % 16 == 0 && DESC_B % 16 == 0, "bulk copy sizes");
 };
 
 // ---------------------------------------------------------------------------
 // GSRB half-sweep on every box of one level (mg$D_box_gsrb_lpl,
-// src/m_aX_mg.f90:718-760), persistent and pipelined: each block streams its
+// src/m_aX_mg.f90:718-760), persistent and pipelined. Each block streams its
 // groups of consecutive boxes through an S-stage ring in shared memory (one
-// bulk copy each for the descriptors, phi and rhs of a group), and loads the
-// ghost values of the next group into registers while the current one is
-// being updated.
+// bulk copy each for the descriptors, phi and rhs of a group, issued two
+// groups ahead), and loads the ghost sources of the next group into registers
+// while the current group is updated. One block barrier per group: the stage
+// refilled at group k was last read at group k-2, which every thread finished
+// before the barrier of group k-1.
 //
 // With pull = 1 the ghost cells this colour reads are the values of the
 // a$D_gc_box fill the reference runs after the previous half-sweep
@@ -274,9 +297,10 @@ k_sweep_tma(Meta m, int lo, int nbx, T* __restrict__ phi, const T* __restrict__ 
   using C = SweepCfg<D, NC, T>;
   using G = Geo<D, NC>;
   constexpr int S = C::S;
-  __shared__ __align__(128) unsigned char smem[S * C::STAGE_B];
+  extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) unsigned long long bar[S];
-  __shared__ int s_act[C::BPC];
+  __shared__ int s_act[S][C::BPC];
+  __shared__ int s_abort;
 
   const int groups = (nbx + C::BPC - 1) / C::BPC;
   if ((int)blockIdx.x >= groups) return;
@@ -284,6 +308,7 @@ k_sweep_tma(Meta m, int lo, int nbx, T* __restrict__ phi, const T* __restrict__ 
 
   if (threadIdx.x == 0) {
     for (int st = 0; st < S; ++st) mbar_init(&bar[st], 1);
+    s_abort = 0;
     fence_mbar_init();
   }
   __syncthreads();
@@ -293,28 +318,17 @@ k_sweep_tma(Meta m, int lo, int nbx, T* __restrict__ phi, const T* __restrict__ 
   auto issue = [&](int k) {  // one thread
     const int first = group_first(k), nb = group_n(k), s0 = lo + first;
     unsigned char* sp = smem + (k % S) * C::STAGE_B;
-    const unsigned bytes = nb * (unsigned)C::BOX_B;
     fence_proxy_async();
-    mbar_expect_tx(&bar[k % S], bytes);
+    mbar_expect_tx(&bar[k % S], nb * (unsigned)C::BOX_B);
     bulk_g2s(sp, m.desc + s0, nb * (unsigned)sizeof(SlotDesc), &bar[k % S]);
     bulk_g2s(sp + C::DESC_B, phi + m.offg[s0], nb * (unsigned)(G::SG * sizeof(T)), &bar[k % S]);
     bulk_g2s(sp + C::DESC_B + C::PHI_B, rhs + m.offi[s0], nb * (unsigned)(G::SI * sizeof(T)),
              &bar[k % S]);
   };
-
-  int issued = 0;  // groups issued so far (by thread 0; uniform count)
-  if (threadIdx.x == 0)
-    for (int k = 0; k < S - 1 && k < my_groups; ++k) issue(k);
-  issued = min(S - 1, my_groups);
-
-  T cur[C::ITEMS], nxt[C::ITEMS];
-  int cur_act = 0, nxt_act = 0;
-
   // Ghost sources of group k (its stage has landed): neighbour cells, parent
-  // cells for refinement boundaries, or boundary values.
-  auto prefetch = [&](int k, T* val, int& act) {
-    const unsigned char* sp = smem + (k % S) * C::STAGE_B;
-    const SlotDesc* dsc = reinterpret_cast<const SlotDesc*>(sp);
+  // cells at refinement boundaries, or boundary values.
+  auto prefetch = [&](int k, T (&val)[C::ITEMS], int& act) {
+    const SlotDesc* dsc = reinterpret_cast<const SlotDesc*>(smem + (k % S) * C::STAGE_B);
     const int nb = group_n(k);
     act = ((int)threadIdx.x < nb) ? m.active[dsc[threadIdx.x].tree] : 0;
 #pragma unroll
@@ -330,61 +344,38 @@ k_sweep_tma(Meta m, int lo, int nbx, T* __restrict__ phi, const T* __restrict__ 
       const SlotDesc& d = dsc[b];
       const int code = d.code[f];
       const long long o = d.nbo[f];
-      if (code >= 0) {
+      if (code >= 0)
         val[j] = phi[o + G::g(F.ni, F.nj, F.nk)];
-      } else if (code == -1) {
-        const int h = NC >> 1, qd = d.qd;
-        const int pi = (qd & 1) * h + ((F.gi + 1) >> 1);
-        const int pj = ((qd >> 1) & 1) * h + ((F.gj + 1) >> 1);
-        const int pk = (D == 3) ? ((qd >> 2) & 1) * h + ((F.gk + 1) >> 1) : 0;
-        val[j] = phi[o + G::g(pi, pj, pk)];
-      } else if (o >= 0 && !homog) {
-        const int lin = (D == 2) ? (a - 1) : (a - 1) + NC * (c - 1);
-        val[j] = (T)m.bcval[o + lin];
-      }
+      else if (code == kFaceRefinement)
+        val[j] = phi[o + parent_cell<D, NC>(F, f, d.qd, false)];
+      else if (o >= 0 && !homog)
+        val[j] = (T)m.bcval[o + ((D == 2) ? (a - 1) : (a - 1) + NC * (c - 1))];
     }
   };
 
-  auto abort_cta = [&](int waited) {
-    if (threadIdx.x == 0) {
-      atomicExch(m.err, 1);
-      for (int k = waited; k < issued; ++k) mbar_wait_bounded(&bar[k % S], (k / S) & 1);
-    }
-    __syncthreads();
-  };
+  int issued = min(2, my_groups);
+  if (threadIdx.x == 0)
+    for (int k = 0; k < issued; ++k) issue(k);
 
-  {
-    const bool ok = mbar_wait_bounded(&bar[0], 0);
-    if (__syncthreads_or(!ok)) {
-      abort_cta(0);
-      return;
-    }
-  }
-  prefetch(0, cur, cur_act);
-
-  for (int k = 0; k < my_groups; ++k) {
+  // Returns false when the block has to stop (a bounded wait gave up).
+  auto body = [&](int k, T (&cur)[C::ITEMS], int& cur_act, T (&nxt)[C::ITEMS], int& nxt_act) -> bool {
     const int st = k % S;
     unsigned char* sp = smem + st * C::STAGE_B;
     const SlotDesc* dsc = reinterpret_cast<const SlotDesc*>(sp);
     T* sphi = reinterpret_cast<T*>(sp + C::DESC_B);
     const T* srhs = reinterpret_cast<const T*>(sp + C::DESC_B + C::PHI_B);
     const int nb = group_n(k);
-
-    if (k + S - 1 < my_groups) {
-      if (threadIdx.x == 0) issue(k + S - 1);
+    if (k + 2 < my_groups) {
+      if (threadIdx.x == 0) issue(k + 2);
       ++issued;
     }
     if (k + 1 < my_groups) {
-      const bool ok = mbar_wait_bounded(&bar[(k + 1) % S], ((k + 1) / S) & 1);
-      if (__syncthreads_or(!ok)) {
-        abort_cta(k + 1);
-        return;
-      }
-      prefetch(k + 1, nxt, nxt_act);
+      if (mbar_wait_bounded(&bar[(k + 1) % S], ((k + 1) / S) & 1))
+        prefetch(k + 1, nxt, nxt_act);
+      else
+        s_abort = 1;
     }
-
-    // ghost cells of this colour (values of the state after the previous sweep)
-    if ((int)threadIdx.x < nb) s_act[threadIdx.x] = cur_act;
+    if ((int)threadIdx.x < nb) s_act[st][threadIdx.x] = cur_act;
     if (pull) {
 #pragma unroll
       for (int j = 0; j < C::ITEMS; ++j) {
@@ -400,70 +391,66 @@ k_sweep_tma(Meta m, int lo, int nbx, T* __restrict__ phi, const T* __restrict__ 
         const T* bx = sphi + b * G::SG;
         auto own = [&](int i, int jj, int kk) { return bx[G::g(i, jj, kk)]; };
         T v;
-        if (code >= 0) {
+        if (code >= 0)
           v = cur[j];
-        } else if (code == -1) {
-          const T g0 = cur[j];
-          const int dim = f >> 1, dix = (f & 1) ? -1 : 1;
-          const int i = F.ai, jj = F.aj, kk = F.ak;
-          if constexpr (D == 2) {
-            if (dim == 0) {
-              const int dj = -1 + 2 * (jj & 1);
-              v = (T)0.5 * g0 + own(i, jj, 0) - (T)0.25 * (own(i + dix, jj, 0) + own(i, jj + dj, 0));
-            } else {
-              const int di = -1 + 2 * (i & 1);
-              v = (T)0.5 * g0 + own(i, jj, 0) - (T)0.25 * (own(i + di, jj, 0) + own(i, jj + dix, 0));
-            }
-          } else {
-            const int di = (dim == 0) ? dix : -1 + 2 * (i & 1);
-            const int dj = (dim == 1) ? dix : -1 + 2 * (jj & 1);
-            const int dk = (dim == 2) ? dix : -1 + 2 * (kk & 1);
-            v = (T)0.5 * g0 + (T)0.75 * own(i, jj, kk) - (T)0.25 * own(i + di, jj + dj, kk + dk);
-          }
-        } else {
-          const T b = cur[j];
-          const T x = own(F.ai, F.aj, F.ak);
-          if (code == -2) {
-            v = (T)2 * b + (T)(-1) * x;
-          } else {
-            const T c2 = (T)d.dr * (T)((f & 1) ? 1 : -1);
-            v = c2 * b + (T)1 * x;
-          }
-        }
+        else if (code == kFaceRefinement)
+          v = rb_value<D, NC, T>(F, f, cur[j], own);
+        else
+          v = bc_value<T>(code, f, cur[j], own(F.ai, F.aj, F.ak), Sc<T>::dr(d));
         sphi[b * G::SG + G::g(F.gi, F.gj, F.gk)] = v;
       }
     }
     __syncthreads();
-    {
-      const int b = threadIdx.x / C::PER_BOX, q = threadIdx.x % C::PER_BOX;
-      if (b < nb && s_act[b]) {
-        const T* bx = sphi + b * G::SG;
-        const T* f = srhs + b * G::SI;
-        const SlotDesc& d = dsc[b];
-        const T dx2 = (T)(d.dr * d.dr);
-        const int p = q % (NC / 2);
-        if constexpr (D == 2) {
-          const int j = q / (NC / 2) + 1;
-          const int i = 2 * p + 1 + ((1 + j + n) & 1);
-          const T v = (T)0.25 * (bx[G::g(i + 1, j, 0)] + bx[G::g(i - 1, j, 0)] + bx[G::g(i, j + 1, 0)] +
-                                 bx[G::g(i, j - 1, 0)] - dx2 * f[G::in(i, j, 1)]);
-          phi[d.offg + G::g(i, j, 0)] = v;
-        } else {
-          const int j = (q / (NC / 2)) % NC + 1;
-          const int kk = q / ((NC / 2) * NC) + 1;
-          const int i = 2 * p + 1 + ((1 + j + kk + n) & 1);
-          const T sixth = (T)(1 / 6.0);
-          const T v = sixth * (bx[G::g(i + 1, j, kk)] + bx[G::g(i - 1, j, kk)] + bx[G::g(i, j + 1, kk)] +
-                               bx[G::g(i, j - 1, kk)] + bx[G::g(i, j, kk + 1)] + bx[G::g(i, j, kk - 1)] -
-                               dx2 * f[G::in(i, j, kk)]);
-          phi[d.offg + G::g(i, j, kk)] = v;
-        }
+    if (s_abort) return false;
+    const int b = threadIdx.x / C::PER_BOX, q = threadIdx.x % C::PER_BOX;
+    if (b < nb && s_act[st][b]) {
+      const T* bx = sphi + b * G::SG;
+      const T* f = srhs + b * G::SI;
+      const SlotDesc& d = dsc[b];
+      const T dx2 = Sc<T>::dx2(d);
+      const int p = q % (NC / 2);
+      if constexpr (D == 2) {
+        const int j = q / (NC / 2) + 1;
+        const int i = 2 * p + 1 + ((1 + j + n) & 1);
+        const T v = (T)0.25 * (bx[G::g(i + 1, j, 0)] + bx[G::g(i - 1, j, 0)] + bx[G::g(i, j + 1, 0)] +
+                               bx[G::g(i, j - 1, 0)] - dx2 * f[G::in(i, j, 1)]);
+        phi[d.offg + G::g(i, j, 0)] = v;
+      } else {
+        const int j = (q / (NC / 2)) % NC + 1;
+        const int kk = q / ((NC / 2) * NC) + 1;
+        const int i = 2 * p + 1 + ((1 + j + kk + n) & 1);
+        const T sixth = (T)(1 / 6.0);
+        const T v = sixth * (bx[G::g(i + 1, j, kk)] + bx[G::g(i - 1, j, kk)] + bx[G::g(i, j + 1, kk)] +
+                             bx[G::g(i, j - 1, kk)] + bx[G::g(i, j, kk + 1)] + bx[G::g(i, j, kk - 1)] -
+                             dx2 * f[G::in(i, j, kk)]);
+        phi[d.offg + G::g(i, j, kk)] = v;
       }
     }
-    __syncthreads();
-#pragma unroll
-    for (int j = 0; j < C::ITEMS; ++j) cur[j] = nxt[j];
-    cur_act = nxt_act;
+    return true;
+  };
+
+  T ra[C::ITEMS], rb[C::ITEMS];
+  int act_a = 0, act_b = 0;
+  bool ok = mbar_wait_bounded(&bar[0], 0);
+  if (ok) prefetch(0, ra, act_a);
+  if (__syncthreads_or(!ok)) {
+    if (threadIdx.x == 0) {
+      atomicExch(m.err, 1);
+      for (int k = 0; k < issued; ++k) mbar_wait_bounded(&bar[k % S], (k / S) & 1);
+    }
+    return;
+  }
+  int k = 0;
+  for (; k < my_groups; k += 2) {
+    if (!body(k, ra, act_a, rb, act_b)) break;
+    if (k + 1 < my_groups && !body(k + 1, rb, act_b, ra, act_a)) {
+      k += 1;
+      break;
+    }
+  }
+  if (k < my_groups && threadIdx.x == 0) {  // gave up: drain this block's copies
+    atomicExch(m.err, 1);
+    for (int j = k + 1; j < issued; ++j) mbar_wait_bounded(&bar[j % S], (j / S) & 1);
   }
 }
 
@@ -485,12 +472,13 @@ k_fill(Meta m, BoxSet bs, T* __restrict__ phi, int homog) {
     int f = r / G::NF, lin = r % G::NF;
     int a = lin % NC + 1, c = lin / NC + 1;
     int s = box_at(bs, bi);
-    if (!m.active[m.tree[s]]) continue;
-    const T* bx = phi + m.offg[s];
+    const SlotDesc& d = m.desc[s];
+    if (!m.active[d.tree]) continue;
+    const T* bx = phi + d.offg;
     auto own = [&](int i, int j, int k) { return bx[G::g(i, j, k)]; };
-    T v = ghost_value<D, NC, T>(m, phi, s, f, a, c, homog != 0, own);
+    T v = ghost_value<D, NC, T>(m, d, phi, f, a, c, homog != 0, own);
     Face<D, NC> F(f, a, c);
-    phi[m.offg[s] + G::g(F.gi, F.gj, F.gk)] = v;
+    phi[d.offg + G::g(F.gi, F.gj, F.gk)] = v;
   }
 }
 
@@ -508,6 +496,53 @@ __device__ __forceinline__ T lpl_at(const T* bx, int i, int j, int k, T inv_dr_s
   }
 }
 
+// Loads a group of BPC boxes of a set into shared memory (whole ghosted
+// boxes, vectorised) and their slots into s_slot; returns the count.
+template <int D, int NC, class T, int BPC>
+__device__ __forceinline__ int stage_boxes(const Meta& m, const BoxSet& bs, int grp, const T* __restrict__ src,
+                                           T* sm, int* s_slot, int* s_act) {
+  using G = Geo<D, NC>;
+  using V = typename Vec<T>::type;
+  constexpr int VW = Vec<T>::w;
+  const int nbox = min(BPC, bs.n - grp * BPC);
+  if ((int)threadIdx.x < BPC) {
+    int s = (int)threadIdx.x < nbox ? box_at(bs, grp * BPC + threadIdx.x) : -1;
+    s_slot[threadIdx.x] = s;
+    s_act[threadIdx.x] = (s >= 0) ? m.active[m.tree[s]] : 0;
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < nbox * (G::SG / VW); e += blockDim.x) {
+    int b = e / (G::SG / VW), q = e % (G::SG / VW);
+    reinterpret_cast<V*>(sm + b * G::SG)[q] = reinterpret_cast<const V*>(src + m.offg[s_slot[b]])[q];
+  }
+  __syncthreads();
+  return nbox;
+}
+
+// Fills all face ghosts of the staged boxes from the level's current state.
+template <int D, int NC, class T>
+__device__ __forceinline__ void pull_all_ghosts(const Meta& m, const T* __restrict__ phi, T* sm,
+                                                const int* s_slot, const int* s_act, int nbox, bool homog,
+                                                T* store_to) {
+  using G = Geo<D, NC>;
+  for (int e = threadIdx.x; e < nbox * G::NNB * G::NF; e += blockDim.x) {
+    const int b = e / (G::NNB * G::NF);
+    const int r = e % (G::NNB * G::NF);
+    const int f = r / G::NF, lin = r % G::NF;
+    const int a = lin % NC + 1, c = lin / NC + 1;
+    if (!s_act[b]) continue;
+    const SlotDesc& d = m.desc[s_slot[b]];
+    const T* bx = sm + b * G::SG;
+    auto own = [&](int i, int j, int k) { return bx[G::g(i, j, k)]; };
+    const T v = ghost_value<D, NC, T>(m, d, phi, f, a, c, homog, own);
+    const Face<D, NC> F(f, a, c);
+    const int gpos = G::g(F.gi, F.gj, F.gk);
+    sm[b * G::SG + gpos] = v;
+    if (store_to) store_to[d.offg + gpos] = v;
+  }
+  __syncthreads();
+}
+
 // ---------------------------------------------------------------------------
 // Residual and restriction to the parent: the per-box body of update_coarse
 // and set_coarse_phi_rhs (src/m_aX_mg.f90:444-465, :495-504): residual_box
@@ -515,7 +550,8 @@ __device__ __forceinline__ T lpl_at(const T* bx, int i, int j, int k, T inv_dr_s
 // The residual is kept in registers; the fine box's tmp is not written, which
 // is what the reference's save/restore of tmp leaves behind (:452-462).
 // SUB = the fine level is <= 1 (the parent is a sub-level box of half the size
-// covering the same region, src/m_aX_t.f90:366-373).
+// covering the same region, src/m_aX_t.f90:366-373). With pull the fine
+// level's ghosts are recomputed here (no block writes that level).
 // ---------------------------------------------------------------------------
 template <int D, int NC, bool SUB, class T>
 __global__ void __launch_bounds__(kThreads)
@@ -527,71 +563,45 @@ k_restrict_res(Meta m, BoxSet bs, T* __restrict__ phi, const T* __restrict__ rhs
   using GP = Geo<D, PNC>;
   constexpr int PER_BOX = D == 2 ? H * H : H * H * H;
   constexpr int BPC = boxes_per_cta<G::SG, PER_BOX, T>(1);
-  using V = typename Vec<T>::type;
-  constexpr int VW = Vec<T>::w;
   __shared__ __align__(16) T sm[BPC * G::SG];
   __shared__ int s_slot[BPC];
   __shared__ int s_act[BPC];
   const int groups = (bs.n + BPC - 1) / BPC;
   for (int grp = blockIdx.x; grp < groups; grp += gridDim.x) {
-    const int nbox = min(BPC, bs.n - grp * BPC);
-    if (threadIdx.x < BPC) {
-      int s = threadIdx.x < nbox ? box_at(bs, grp * BPC + threadIdx.x) : -1;
-      s_slot[threadIdx.x] = s;
-      s_act[threadIdx.x] = (s >= 0) ? m.active[m.tree[s]] : 0;
-    }
-    __syncthreads();
-    for (int e = threadIdx.x; e < nbox * (G::SG / VW); e += blockDim.x) {
-      int b = e / (G::SG / VW), q = e % (G::SG / VW);
-      reinterpret_cast<V*>(sm + b * G::SG)[q] =
-          reinterpret_cast<const V*>(phi + m.offg[s_slot[b]])[q];
-    }
-    __syncthreads();
-    if (pull) {
-      // Ghost values of this level's current state; no block writes this level
-      // during the launch (restriction writes the parents' interiors).
-      for (int e = threadIdx.x; e < nbox * G::NNB * G::NF; e += blockDim.x) {
-        int b = e / (G::NNB * G::NF);
-        int r = e % (G::NNB * G::NF);
-        int f = r / G::NF, lin = r % G::NF;
-        int a = lin % NC + 1, c = lin / NC + 1;
-        if (!s_act[b]) continue;
-        const T* bx = sm + b * G::SG;
-        auto own = [&](int i, int j, int k) { return bx[G::g(i, j, k)]; };
-        T v = ghost_value<D, NC, T>(m, phi, s_slot[b], f, a, c, homog != 0, own);
-        Face<D, NC> F(f, a, c);
-        sm[b * G::SG + G::g(F.gi, F.gj, F.gk)] = v;
-      }
-      __syncthreads();
-    }
+    const int nbox = stage_boxes<D, NC, T, BPC>(m, bs, grp, phi, sm, s_slot, s_act);
+    if (pull && with_res) pull_all_ghosts<D, NC, T>(m, phi, sm, s_slot, s_act, nbox, homog != 0, nullptr);
     int b = threadIdx.x / PER_BOX, q = threadIdx.x % PER_BOX;
     if (b < nbox && s_act[b]) {
       int s = s_slot[b];
+      const SlotDesc& d = m.desc[s];
       const T* bx = sm + b * G::SG;
-      const T* f = rhs + m.offi[s];
-      T inv = (T)1 / (T)(m.dr[s] * m.dr[s]);
-      if constexpr (sizeof(T) == 8) inv = 1 / (m.dr[s] * m.dr[s]);
+      const T* f = rhs + d.offi;
+      const T inv = Sc<T>::inv(d);
       int ic = q % H + 1, jc = (q / H) % H + 1, kc = (D == 3) ? q / (H * H) + 1 : 0;
       int off[3] = {0, 0, 0};
       if (!SUB) {
-        int qd = m.qd[s];
-        for (int d = 0; d < D; ++d) off[d] = ((qd >> d) & 1) * H;
+        const int qd = d.qd;
+        off[0] = (qd & 1) * H;
+        off[1] = ((qd >> 1) & 1) * H;
+        off[2] = ((qd >> 2) & 1) * H;
       }
       T sr = 0, sp = 0;
-      int kk_n = (D == 3) ? 2 : 1;
-      for (int kk = 0; kk < kk_n; ++kk)
+      constexpr int KK = (D == 3) ? 2 : 1;
+#pragma unroll
+      for (int kk = 0; kk < KK; ++kk)
+#pragma unroll
         for (int jj = 0; jj < 2; ++jj)
+#pragma unroll
           for (int ii = 0; ii < 2; ++ii) {
             int i = 2 * ic - 1 + ii, j = 2 * jc - 1 + jj, k = (D == 3) ? 2 * kc - 1 + kk : 0;
             if (with_res) {
-              T r = f[G::in(i, j, D == 3 ? k : 1)] - lpl_at<D, NC, T>(bx, i, j, k, inv);
+              T r = f[G::in(i, j, k)] - lpl_at<D, NC, T>(bx, i, j, k, inv);
               sr = sr + r;
             }
             sp = sp + bx[G::g(i, j, k)];
           }
       const T w = (D == 2) ? (T)0.25 : (T)0.125;
-      int p = m.parent[s];
-      long long po = m.offg[p] + GP::g(off[0] + ic, off[1] + jc, (D == 3) ? off[2] + kc : 0);
+      long long po = m.offg[d.parent] + GP::g(off[0] + ic, off[1] + jc, (D == 3) ? off[2] + kc : 0);
       if (with_res) tmp[po] = w * sr;
       phi[po] = w * sp;
     }
@@ -603,7 +613,9 @@ k_restrict_res(Meta m, BoxSet bs, T* __restrict__ phi, const T* __restrict__ rhs
 // Coarse right-hand side on the parents of a level after restriction
 // (src/m_aX_mg.f90:472-479 and :510-515): rhs = L(phi) + tmp over the interior,
 // then, for update_coarse, tmp = phi over the whole box including its ghosts
-// (a$D_box_copy_cc, src/m_aX_utils.f90:331-339).
+// (a$D_box_copy_cc, src/m_aX_utils.f90:331-339). With pull the parents'
+// ghosts (fill_gc_phi of the parent level, :467) are recomputed here and
+// stored.
 // ---------------------------------------------------------------------------
 template <int D, int NC, class T>
 __global__ void __launch_bounds__(kThreads)
@@ -619,49 +631,17 @@ k_coarse_rhs(Meta m, BoxSet bs, T* __restrict__ phi, T* __restrict__ rhs,
   __shared__ int s_act[BPC];
   const int groups = (bs.n + BPC - 1) / BPC;
   for (int grp = blockIdx.x; grp < groups; grp += gridDim.x) {
-    const int nbox = min(BPC, bs.n - grp * BPC);
-    if (threadIdx.x < BPC) {
-      int s = threadIdx.x < nbox ? box_at(bs, grp * BPC + threadIdx.x) : -1;
-      s_slot[threadIdx.x] = s;
-      s_act[threadIdx.x] = (s >= 0) ? m.active[m.tree[s]] : 0;
-    }
-    __syncthreads();
-    for (int e = threadIdx.x; e < nbox * (G::SG / VW); e += blockDim.x) {
-      int b = e / (G::SG / VW), q = e % (G::SG / VW);
-      reinterpret_cast<V*>(sm + b * G::SG)[q] =
-          reinterpret_cast<const V*>(phi + m.offg[s_slot[b]])[q];
-    }
-    __syncthreads();
-    if (pull) {
-      // The fill_gc_phi of the parent level (src/m_aX_mg.f90:467) for the boxes
-      // that need it here; the values are also stored as the boxes' ghosts.
-      for (int e = threadIdx.x; e < nbox * G::NNB * G::NF; e += blockDim.x) {
-        int b = e / (G::NNB * G::NF);
-        int r = e % (G::NNB * G::NF);
-        int f = r / G::NF, lin = r % G::NF;
-        int a = lin % NC + 1, c = lin / NC + 1;
-        if (!s_act[b]) continue;
-        const T* bx = sm + b * G::SG;
-        auto own = [&](int i, int j, int k) { return bx[G::g(i, j, k)]; };
-        T v = ghost_value<D, NC, T>(m, phi, s_slot[b], f, a, c, homog != 0, own);
-        Face<D, NC> F(f, a, c);
-        int gpos = G::g(F.gi, F.gj, F.gk);
-        sm[b * G::SG + gpos] = v;
-        phi[m.offg[s_slot[b]] + gpos] = v;
-      }
-      __syncthreads();
-    }
+    const int nbox = stage_boxes<D, NC, T, BPC>(m, bs, grp, phi, sm, s_slot, s_act);
+    if (pull) pull_all_ghosts<D, NC, T>(m, phi, sm, s_slot, s_act, nbox, homog != 0, phi);
     int b = threadIdx.x / PER_BOX, q0 = threadIdx.x % PER_BOX;
     if (b < nbox && s_act[b]) {
-      int s = s_slot[b];
+      const SlotDesc& d = m.desc[s_slot[b]];
       const T* bx = sm + b * G::SG;
-      T inv = (T)1 / (T)(m.dr[s] * m.dr[s]);
-      if constexpr (sizeof(T) == 8) inv = 1 / (m.dr[s] * m.dr[s]);
+      const T inv = Sc<T>::inv(d);
       for (int q = q0; q < G::SI; q += PER_BOX) {
         int i = q % NC + 1, j = (q / NC) % NC + 1, k = (D == 3) ? q / (NC * NC) + 1 : 0;
         T l = lpl_at<D, NC, T>(bx, i, j, k, inv);
-        long long gi = m.offg[s] + G::g(i, j, k);
-        rhs[m.offi[s] + q] = l + tmp[gi];
+        rhs[d.offi + q] = l + tmp[d.offg + G::g(i, j, k)];
       }
     }
     __syncthreads();
@@ -669,8 +649,7 @@ k_coarse_rhs(Meta m, BoxSet bs, T* __restrict__ phi, T* __restrict__ rhs,
       for (int e = threadIdx.x; e < nbox * (G::SG / VW); e += blockDim.x) {
         int b2 = e / (G::SG / VW), q = e % (G::SG / VW);
         if (!s_act[b2]) continue;
-        reinterpret_cast<V*>(tmp + m.offg[s_slot[b2]])[q] =
-            reinterpret_cast<const V*>(sm + b2 * G::SG)[q];
+        reinterpret_cast<V*>(tmp + m.offg[s_slot[b2]])[q] = reinterpret_cast<const V*>(sm + b2 * G::SG)[q];
       }
     }
     __syncthreads();
@@ -732,17 +711,18 @@ k_correct(Meta m, BoxSet bs, T* __restrict__ phi, T* __restrict__ tmp) {
       int s = s_slot[b];
       const T* t = sm + b * G::SG;
       constexpr int H = NC / 2;
+      const int fc = m.first_child[s];
       for (int q = q0; q < G::SI; q += PER_BOX) {
         int ic = q % NC + 1, jc = (q / NC) % NC + 1, kc = (D == 3) ? q / (NC * NC) + 1 : 0;
         int child, li, lj, lk;
         if (SUB) {
-          child = m.first_child[s];
+          child = fc;
           li = ic;
           lj = jc;
           lk = kc;
         } else {
           int qx = (ic - 1) / H, qy = (jc - 1) / H, qz = (D == 3) ? (kc - 1) / H : 0;
-          child = m.first_child[s] + qx + 2 * qy + 4 * qz;
+          child = fc + qx + 2 * qy + 4 * qz;
           li = ic - qx * H;
           lj = jc - qy * H;
           lk = (D == 3) ? kc - qz * H : 0;
@@ -788,38 +768,103 @@ k_correct(Meta m, BoxSet bs, T* __restrict__ phi, T* __restrict__ tmp) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// Reductions. Per-tree maxima are accumulated in kStripes slots per tree (box
+// index modulo kStripes) so that the boxes of one tree do not all contend for
+// one address; k_stripe_reduce folds them. The bit pattern of a non-negative
+// double orders like its value, and a NaN orders above every number.
+// ---------------------------------------------------------------------------
+constexpr int kStripes = 64;
+
 // max that keeps a NaN once seen (fmax would drop it and hide a diverged solve)
 __device__ __forceinline__ double nanmax(double a, double b) { return (b > a || b != b) ? b : a; }
-
-// Per-tree maxima are accumulated in kStripes slots per tree (box index
-// modulo kStripes) so that boxes of one tree do not all contend for one
-// address; k_stripe_reduce folds them. The bit pattern of a non-negative
-// double orders like its value, and a NaN orders above every number.
-constexpr int kStripes = 64;
+__device__ __forceinline__ float nanmaxf(float a, float b) { return (b > a || b != b) ? b : a; }
 
 __device__ __forceinline__ unsigned long long dbits(double v) {
   return (unsigned long long)__double_as_longlong(v);
 }
 
+// Exact float -> double conversion with integer instructions (keeps the
+// mixed path's conversions off the FP64 pipe).
+__device__ __forceinline__ double f2d_exact(float x) {
+  const uint32_t b = __float_as_uint(x);
+  const uint64_t s = (uint64_t)(b >> 31) << 63;
+  const uint32_t e = (b >> 23) & 0xffu;
+  const uint32_t m = b & 0x7fffffu;
+  uint64_t out;
+  if (e == 0xffu) {
+    out = s | (0x7ffull << 52) | ((uint64_t)m << 29);
+  } else if (e == 0) {
+    if (m == 0) {
+      out = s;
+    } else {  // subnormal float: normalise
+      const int p = 31 - __clz((int)m);  // position of the leading one, 0..22
+      const uint64_t mant = ((uint64_t)m << (52 - p)) & 0xfffffffffffffull;
+      out = s | ((uint64_t)(p - 149 + 1023) << 52) | mant;
+    }
+  } else {
+    out = s | ((uint64_t)(e - 127 + 1023) << 52) | ((uint64_t)m << 29);
+  }
+  return __longlong_as_double((long long)out);
+}
+
+// double -> float, round to nearest even, with integer instructions.
+// Results below the float range flush to signed zero.
+__device__ __forceinline__ float d2f_rn(double x) {
+  const uint64_t b = (uint64_t)__double_as_longlong(x);
+  const uint32_t s = (uint32_t)(b >> 63) << 31;
+  const int E = (int)((b >> 52) & 0x7ff);
+  const uint64_t M = b & 0xfffffffffffffull;
+  if (E == 0x7ff) return __uint_as_float(s | 0x7f800000u | (M ? 0x400000u : 0u));
+  const int e = E - 1023 + 127;
+  if (e >= 255) return __uint_as_float(s | 0x7f800000u);
+  if (e <= 0) {
+    if (E == 0 || e < -24) return __uint_as_float(s);
+    // subnormal float result
+    const uint64_t full = M | (1ull << 52);
+    const int shift = 29 + (1 - e);
+    const uint64_t q = full >> shift;
+    const uint64_t rem = full & ((1ull << shift) - 1);
+    const uint64_t half = 1ull << (shift - 1);
+    const uint32_t r = (uint32_t)q + ((rem > half || (rem == half && (q & 1))) ? 1u : 0u);
+    return __uint_as_float(s | r);
+  }
+  const uint32_t m23 = (uint32_t)(M >> 29);
+  const uint32_t rem = (uint32_t)(M & ((1u << 29) - 1));
+  const uint32_t half = 1u << 28;
+  uint32_t out = ((uint32_t)e << 23) | m23;
+  out += (rem > half || (rem == half && (m23 & 1))) ? 1u : 0u;
+  return __uint_as_float(s | out);
+}
+
 // Max over the PER_BOX threads of each box (PER_BOX a power of two), then one
 // atomicMax per box into dst (uniform per box, may be null).
-template <int PER_BOX>
-__device__ __forceinline__ void box_max_atomic(double v, unsigned long long* dst, double* red) {
+template <int PER_BOX, class V>
+__device__ __forceinline__ void box_max_atomic(V v, unsigned long long* dst, V* red) {
   constexpr int W = PER_BOX < 32 ? PER_BOX : 32;
+  auto mx = [](V a, V b) { return (b > a || b != b) ? b : a; };
 #pragma unroll
-  for (int o = W / 2; o > 0; o >>= 1) v = nanmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  for (int o = W / 2; o > 0; o >>= 1) v = mx(v, __shfl_xor_sync(0xffffffffu, v, o));
+  auto commit = [&](V x) {
+    double dv;
+    if constexpr (sizeof(V) == 4)
+      dv = f2d_exact(x);
+    else
+      dv = x;
+    atomicMax(dst, dbits(dv));
+  };
   if constexpr (PER_BOX <= 32) {
-    if ((threadIdx.x & (W - 1)) == 0 && dst) atomicMax(dst, dbits(v));
+    if ((threadIdx.x & (W - 1)) == 0 && dst) commit(v);
   } else {
     constexpr int WPB = PER_BOX / 32;
     const int warp = threadIdx.x >> 5;
     if ((threadIdx.x & 31) == 0) red[warp] = v;
     __syncthreads();
     if ((threadIdx.x % PER_BOX) == 0 && dst) {
-      double mm = red[warp];
+      V mm = red[warp];
 #pragma unroll
-      for (int w = 1; w < WPB; ++w) mm = nanmax(mm, red[warp + w]);
-      atomicMax(dst, dbits(mm));
+      for (int w = 1; w < WPB; ++w) mm = mx(mm, red[warp + w]);
+      commit(mm);
     }
     __syncthreads();
   }
@@ -829,12 +874,12 @@ __global__ void k_stripe_reduce(int n_trees, const unsigned long long* __restric
                                 unsigned long long* __restrict__ out) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t < n_trees) {
-    unsigned long long m = 0;
+    unsigned long long mx = 0;
     for (int k = 0; k < kStripes; ++k) {
       unsigned long long v = norm[(size_t)t * kStripes + k];
-      m = v > m ? v : m;
+      mx = v > mx ? v : mx;
     }
-    out[t] = m;
+    out[t] = mx;
   }
 }
 
@@ -860,16 +905,16 @@ k_residual(Meta m, BoxSet bs, const T* __restrict__ phi, const T* __restrict__ r
     bool leaf = false;
     if (bi < bs.n) {
       int s = box_at(bs, bi);
-      tr = m.tree[s];
+      const SlotDesc& d = m.desc[s];
+      tr = d.tree;
       if (m.active[tr]) {
         leaf = m.first_child[s] < 0;
-        const T* bx = phi + m.offg[s];
-        T inv = (T)1 / (T)(m.dr[s] * m.dr[s]);
-        if constexpr (sizeof(T) == 8) inv = 1 / (m.dr[s] * m.dr[s]);
+        const T* bx = phi + d.offg;
+        const T inv = Sc<T>::inv(d);
         for (int q = q0; q < G::SI; q += PER_BOX) {
           int i = q % NC + 1, j = (q / NC) % NC + 1, k = (D == 3) ? q / (NC * NC) + 1 : 0;
-          T r = rhs[m.offi[s] + q] - lpl_at<D, NC, T>(bx, i, j, k, inv);
-          if (store) tmp[m.offg[s] + G::g(i, j, k)] = r;
+          T r = rhs[d.offi + q] - lpl_at<D, NC, T>(bx, i, j, k, inv);
+          if (store) tmp[d.offg + G::g(i, j, k)] = r;
           mx = nanmax(mx, fabs((double)r));
         }
       } else {
@@ -878,7 +923,7 @@ k_residual(Meta m, BoxSet bs, const T* __restrict__ phi, const T* __restrict__ r
     }
     if (norm_per_tree) {
       // all threads of a PER_BOX segment belong to the same box
-      box_max_atomic<PER_BOX>(
+      box_max_atomic<PER_BOX, double>(
           mx, (tr >= 0 && leaf) ? norm_per_tree + (size_t)tr * kStripes + (bi & (kStripes - 1)) : nullptr,
           red);
     }
@@ -913,7 +958,7 @@ k_maxabs(Meta m, BoxSet bs, const T* __restrict__ v, int ghosted,
         }
       }
     }
-    box_max_atomic<PER_BOX>(
+    box_max_atomic<PER_BOX, double>(
         mx, tr >= 0 ? norm_per_tree + (size_t)tr * kStripes + (bi & (kStripes - 1)) : nullptr, red);
   }
 }
@@ -964,29 +1009,39 @@ k_restrict_interior(Meta m, BoxSet bs, T* __restrict__ v) {
        e += (long long)gridDim.x * blockDim.x) {
     int bi = (int)(e / PER_BOX), q = (int)(e % PER_BOX);
     int s = box_at(bs, bi);
-    if (!m.active[m.tree[s]]) continue;
+    const SlotDesc& d = m.desc[s];
+    if (!m.active[d.tree]) continue;
     int ic = q % H + 1, jc = (q / H) % H + 1, kc = (D == 3) ? q / (H * H) + 1 : 1;
     int off[3] = {0, 0, 0};
     if (!SUB) {
-      int qd = m.qd[s];
-      for (int d = 0; d < D; ++d) off[d] = ((qd >> d) & 1) * H;
+      const int qd = d.qd;
+      off[0] = (qd & 1) * H;
+      off[1] = ((qd >> 1) & 1) * H;
+      off[2] = ((qd >> 2) & 1) * H;
     }
-    const T* f = v + m.offi[s];
+    const T* f = v + d.offi;
     T acc = 0;
-    int kk_n = (D == 3) ? 2 : 1;
-    for (int kk = 0; kk < kk_n; ++kk)
+    constexpr int KK = (D == 3) ? 2 : 1;
+#pragma unroll
+    for (int kk = 0; kk < KK; ++kk)
+#pragma unroll
       for (int jj = 0; jj < 2; ++jj)
-        for (int ii = 0; ii < 2; ++ii)
-          acc = acc + f[G::in(2 * ic - 1 + ii, 2 * jc - 1 + jj, D == 3 ? 2 * kc - 1 + kk : 1)];
+#pragma unroll
+        for (int ii = 0; ii < 2; ++ii) acc = acc + f[G::in(2 * ic - 1 + ii, 2 * jc - 1 + jj, 2 * kc - 1 + kk)];
     const T w = (D == 2) ? (T)0.25 : (T)0.125;
-    int p = m.parent[s];
-    v[m.offi[p] + GP::in(off[0] + ic, off[1] + jc, D == 3 ? off[2] + kc : 1)] = w * acc;
+    v[m.offi[d.parent] + GP::in(off[0] + ic, off[1] + jc, off[2] + kc)] = w * acc;
   }
 }
 
 // ---------------------------------------------------------------------------
-// Mixed precision: FP64 defect on the leaves written as the FP32 right-hand
-// side, and the FP64 accumulate of the FP32 correction.
+// Mixed precision: FP64 defect correction around FP32 V-cycles.
+//
+// k_defect: on every leaf, r = f - L(u) in FP64 with fused multiply-adds,
+// stored as the FP32 right-hand side of the correction cycle, and max |r| per
+// tree. The ghost cells of u are recomputed here from the current state:
+// neighbours' cells, physical boundaries, and at refinement boundaries the
+// coarse neighbour's cell that the parent's ghost cell would hold (two hops:
+// the parent's neighbour exists by 2:1 balance and is a leaf).
 // ---------------------------------------------------------------------------
 template <int D, int NC>
 __global__ void __launch_bounds__(kThreads)
@@ -994,34 +1049,72 @@ k_defect(Meta m, BoxSet bs, const double* __restrict__ u, const double* __restri
          float* __restrict__ r32, unsigned long long* __restrict__ norm_per_tree) {
   using G = Geo<D, NC>;
   constexpr int PER_BOX = G::SI < kThreads ? G::SI : kThreads;
-  constexpr int BPC = kThreads / PER_BOX;
-  __shared__ double red[kThreads / 32];
+  constexpr int BPC = boxes_per_cta<G::SG, PER_BOX, double>(1);
+  __shared__ __align__(16) double sm[BPC * G::SG];
+  __shared__ int s_slot[BPC];
+  __shared__ int s_act[BPC];
+  __shared__ float red[kThreads / 32];
   const int groups = (bs.n + BPC - 1) / BPC;
   for (int grp = blockIdx.x; grp < groups; grp += gridDim.x) {
-    int b = threadIdx.x / PER_BOX, q0 = threadIdx.x % PER_BOX;
-    int bi = grp * BPC + b;
-    double mx = 0;
+    const int nbox = stage_boxes<D, NC, double, BPC>(m, bs, grp, u, sm, s_slot, s_act);
+    for (int e = threadIdx.x; e < nbox * G::NNB * G::NF; e += blockDim.x) {
+      const int b = e / (G::NNB * G::NF);
+      const int r = e % (G::NNB * G::NF);
+      const int fc = r / G::NF, lin = r % G::NF;
+      const int a = lin % NC + 1, c = lin / NC + 1;
+      if (!s_act[b]) continue;
+      const int s = s_slot[b];
+      const SlotDesc& d = m.desc[s];
+      const double* bx = sm + b * G::SG;
+      auto own = [&](int i, int j, int k) { return bx[G::g(i, j, k)]; };
+      const Face<D, NC> F(fc, a, c);
+      const int code = d.code[fc];
+      double v;
+      if (code >= 0) {
+        v = u[d.nbo[fc] + G::g(F.ni, F.nj, F.nk)];
+      } else if (code == kFaceRefinement) {
+        const double g0 = u[m.nbo2[s * G::NNB + fc] + parent_cell<D, NC>(F, fc, d.qd, true)];
+        v = rb_value<D, NC, double>(F, fc, g0, own);
+      } else {
+        double bv = 0;
+        if (d.nbo[fc] >= 0) bv = m.bcval[d.nbo[fc] + ((D == 2) ? (a - 1) : (a - 1) + NC * (c - 1))];
+        v = bc_value<double>(code, fc, bv, own(F.ai, F.aj, F.ak), d.dr);
+      }
+      sm[b * G::SG + G::g(F.gi, F.gj, F.gk)] = v;
+    }
+    __syncthreads();
+    const int b = threadIdx.x / PER_BOX, q0 = threadIdx.x % PER_BOX;
+    float mx = 0.f;
     int tr = -1;
-    if (bi < bs.n) {
-      int s = box_at(bs, bi);
-      tr = m.tree[s];
-      if (!m.active[tr]) tr = -1;
-      if (tr >= 0) {
-        const double* bx = u + m.offg[s];
-        double inv = 1 / (m.dr[s] * m.dr[s]);
-        for (int q = q0; q < G::SI; q += PER_BOX) {
-          int i = q % NC + 1, j = (q / NC) % NC + 1, k = (D == 3) ? q / (NC * NC) + 1 : 0;
-          double r = f[m.offi[s] + q] - lpl_at<D, NC, double>(bx, i, j, k, inv);
-          r32[m.offi[s] + q] = (float)r;
-          mx = nanmax(mx, fabs(r));
-        }
+    if (b < nbox && s_act[b]) {
+      const SlotDesc& d = m.desc[s_slot[b]];
+      tr = d.tree;
+      const double* bx = sm + b * G::SG;
+      const double ninv = -d.inv_dx2;
+      for (int q = q0; q < G::SI; q += PER_BOX) {
+        const int i = q % NC + 1, j = (q / NC) % NC + 1, k = (D == 3) ? q / (NC * NC) + 1 : 0;
+        double sum;
+        if constexpr (D == 2)
+          sum = ((bx[G::g(i - 1, j, 0)] + bx[G::g(i + 1, j, 0)]) + bx[G::g(i, j - 1, 0)]) + bx[G::g(i, j + 1, 0)];
+        else
+          sum = ((((bx[G::g(i - 1, j, k)] + bx[G::g(i + 1, j, k)]) + bx[G::g(i, j - 1, k)]) +
+                  bx[G::g(i, j + 1, k)]) + bx[G::g(i, j, k - 1)]) + bx[G::g(i, j, k + 1)];
+        const double t = fma(-(double)(2 * D), bx[G::g(i, j, k)], sum);
+        const double rr = fma(ninv, t, f[d.offi + q]);
+        const float r = d2f_rn(rr);
+        r32[d.offi + q] = r;
+        mx = nanmaxf(mx, fabsf(r));
       }
     }
-    box_max_atomic<PER_BOX>(
-        mx, tr >= 0 ? norm_per_tree + (size_t)tr * kStripes + (bi & (kStripes - 1)) : nullptr, red);
+    box_max_atomic<PER_BOX, float>(
+        mx,
+        (tr >= 0) ? norm_per_tree + (size_t)tr * kStripes + ((grp * BPC + b) & (kStripes - 1)) : nullptr,
+        red);
+    __syncthreads();
   }
 }
 
+// u += e over the interiors of the leaves (FP64 accumulate of the FP32 correction).
 template <int D, int NC>
 __global__ void __launch_bounds__(kThreads)
 k_accumulate(Meta m, BoxSet bs, double* __restrict__ u, const float* __restrict__ e) {
@@ -1034,7 +1127,45 @@ k_accumulate(Meta m, BoxSet bs, double* __restrict__ u, const float* __restrict_
     if (!m.active[m.tree[s]]) continue;
     int i = q % NC + 1, j = (q / NC) % NC + 1, k = (D == 3) ? q / (NC * NC) + 1 : 0;
     long long o = m.offg[s] + G::g(i, j, k);
-    u[o] = u[o] + (double)e[o];
+    u[o] = u[o] + f2d_exact(e[o]);
+  }
+}
+
+// Parents of a level >= 1: the increment of a parent cell is the restriction
+// (2^D-cell average) of its children's increments -- the correction e on leaf
+// children, the increment stored here by the previous call on parent children.
+// The parent's u gets the increment in FP64 and the increment replaces e on the
+// parent, so that after the finest-to-coarsest pass every parent holds the
+// restriction of its children, as at the fixed point of the FAS cycle.
+template <int D, int NC>
+__global__ void __launch_bounds__(kThreads)
+k_restrict_increment(Meta m, BoxSet bs, double* __restrict__ u, float* __restrict__ e) {
+  using G = Geo<D, NC>;
+  constexpr int H = NC / 2;
+  const long long total = (long long)bs.n * G::SI;
+  for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < total;
+       x += (long long)gridDim.x * blockDim.x) {
+    const int bi = (int)(x / G::SI), q = (int)(x % G::SI);
+    const int s = box_at(bs, bi);
+    if (!m.active[m.tree[s]]) continue;
+    const int ic = q % NC + 1, jc = (q / NC) % NC + 1, kc = (D == 3) ? q / (NC * NC) + 1 : 0;
+    const int qx = (ic - 1) / H, qy = (jc - 1) / H, qz = (D == 3) ? (kc - 1) / H : 0;
+    const int child = m.first_child[s] + qx + 2 * qy + 4 * qz;
+    const int li = ic - qx * H, lj = jc - qy * H, lk = (D == 3) ? kc - qz * H : 0;
+    const float* ce = e + m.offg[child];
+    float acc = 0.f;
+    constexpr int KK = (D == 3) ? 2 : 1;
+#pragma unroll
+    for (int kk = 0; kk < KK; ++kk)
+#pragma unroll
+      for (int jj = 0; jj < 2; ++jj)
+#pragma unroll
+        for (int ii = 0; ii < 2; ++ii)
+          acc += ce[G::g(2 * li - 1 + ii, 2 * lj - 1 + jj, (D == 3) ? 2 * lk - 1 + kk : 0)];
+    const float inc = acc * ((D == 2) ? 0.25f : 0.125f);
+    const long long o = m.offg[s] + G::g(ic, jc, kc);
+    e[o] = inc;
+    u[o] = u[o] + f2d_exact(inc);
   }
 }
 
@@ -1076,7 +1207,7 @@ __global__ void k_scatter(Meta m, const int* __restrict__ slots, int n,
     if (dev_ghosted) {
       dst[m.offg[s] + G::g(i, j, k)] = (T)src[x];
     } else if (interior) {
-      dst[m.offi[s] + G::in(i, j, D == 3 ? k : 1)] = (T)src[x];
+      dst[m.offi[s] + G::in(i, j, k)] = (T)src[x];
     }
   }
 }
@@ -1106,13 +1237,13 @@ __global__ void k_gather(Meta m, const int* __restrict__ slots, int n, const T* 
     if (dev_ghosted)
       v = (double)src[m.offg[s] + G::g(i, j, k)];
     else if (interior)
-      v = (double)src[m.offi[s] + G::in(i, j, D == 3 ? k : 1)];
+      v = (double)src[m.offi[s] + G::in(i, j, k)];
     dst[x] = v;
   }
 }
 
 // Per-tree convergence bookkeeping on the device: a tree stays active while
-// max|r| > tol * max|f|; counts the cycles applied to active trees.
+// max|r| > tol * max|f|; a non-finite residual stops it and marks it failed.
 __global__ void k_check(int n_trees, const unsigned long long* __restrict__ rnorm,
                         const double* __restrict__ fmax, double tol, int* __restrict__ active,
                         int* __restrict__ failed, int* __restrict__ n_active_out) {
@@ -1120,7 +1251,7 @@ __global__ void k_check(int n_trees, const unsigned long long* __restrict__ rnor
   if (t < n_trees) {
     double r = __longlong_as_double((long long)rnorm[t]);  // reduced over stripes
     int a = active[t];
-    if (a && !(r <= 1.0e300)) {  // NaN or overflow: stop this tree, report failure
+    if (a && !(r <= 1.0e300)) {
       a = 0;
       failed[t] = 1;
     } else if (a && r <= tol * fmax[t]) {

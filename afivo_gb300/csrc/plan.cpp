@@ -217,72 +217,46 @@ void plan_build_desc(Plan& p) {
     SlotDesc& d = p.desc[s];
     std::memset(&d, 0, sizeof(d));
     for (int f = 0; f < 6; ++f) {
-      d.code[f] = -2;
+      d.code[f] = kFaceDirichlet;
       d.nbo[f] = -1;
     }
     for (int f = 0; f < NNB; ++f) {
       size_t k = (size_t)s * NNB + f;
       int code = p.nb[k];
-      if (code >= -1) {
-        d.code[f] = code;
+      if (code >= 0) {
+        d.code[f] = 0;
+        d.nbo[f] = p.nbo[k];
+      } else if (code == -1) {
+        d.code[f] = kFaceRefinement;
         d.nbo[f] = p.nbo[k];
       } else {
-        d.code[f] = p.bctype[k] ? -3 : -2;
+        d.code[f] = p.bctype[k] ? kFaceNeumann : kFaceDirichlet;
         d.nbo[f] = p.bcoff[k];
       }
     }
     d.qd = p.qd[s];
     d.tree = p.tree[s];
     d.dr = p.dr[s];
+    d.dx2 = p.dr[s] * p.dr[s];
+    d.inv_dx2 = 1 / (p.dr[s] * p.dr[s]);
     d.offg = p.offg[s];
     d.offi = p.offi[s];
+    d.drf = (float)p.dr[s];
+    d.dx2f = (float)(p.dr[s] * p.dr[s]);
+    d.inv_dx2f = 1.0f / (float)(p.dr[s] * p.dr[s]);
     d.first_child = p.first_child[s];
     d.parent = p.parent[s];
   }
-}
-
-void plan_fill_bc(Plan& p, int t) {
-  const int D = p.dim, NNB = 2 * D;
-  const BcSpec& bc = p.bc[t];
-  // Drop the old records of this tree by rebuilding the value table.
-  std::vector<double> vals;
-  std::vector<long long> newoff(p.bcoff.size(), -1);
+  // Two-hop sources for refinement boundaries: the parent's neighbour in the
+  // face direction, whose boundary cells the parent's ghost cells copy.
+  p.nbo2.assign((size_t)p.n_slots * NNB, -1);
   for (int s = 0; s < p.n_slots; ++s)
-    for (int f = 0; f < NNB; ++f) {
-      size_t k = (size_t)s * NNB + f;
-      if (p.nb[k] != -2) continue;
-      if (p.tree[s] != t) {
-        if (p.bcoff[k] >= 0) {  // keep other trees' records
-          int ncl = p.nc_at(p.lvl[s]);
-          long long nfc = D == 2 ? ncl : (long long)ncl * ncl;
-          newoff[k] = (long long)vals.size();
-          vals.insert(vals.end(), p.bcval.begin() + p.bcoff[k], p.bcval.begin() + p.bcoff[k] + nfc);
-        }
-        continue;
+    for (int f = 0; f < NNB; ++f)
+      if (p.nb[(size_t)s * NNB + f] == -1) {
+        int par = p.parent[s];
+        int q = p.nb[(size_t)par * NNB + f];
+        if (q >= 0) p.nbo2[(size_t)s * NNB + f] = p.offg[q];
       }
-      p.bctype[k] = bc.type == AFV_BC_NEUMANN ? 1 : 0;
-      if (bc.gauss.empty()) continue;
-      int ncl = p.nc_at(p.lvl[s]);
-      int dim = f >> 1;
-      bool low = (f & 1) == 0;
-      newoff[k] = (long long)vals.size();
-      int cmax = D == 3 ? ncl : 1;
-      for (int c = 1; c <= cmax; ++c)
-        for (int a = 1; a <= ncl; ++a) {
-          // face centre: a$D_rr_cc(box, [0.5 or nc+0.5, tangential indices])
-          int tang[2] = {a, c};
-          int k2 = 0;
-          double r[3];
-          for (int e = 0; e < D; ++e) {
-            double cix = (e == dim) ? (low ? 0.5 : ncl + 0.5) : (double)tang[k2++];
-            r[e] = p.r_min[(size_t)s * D + e] + (cix - 0.5) * p.dr[s];
-          }
-          vals.push_back(source_eval(D, bc.src_lpl, bc.gauss.data(),
-                                     (int)bc.gauss.size() / (2 + D), r));
-        }
-    }
-  p.bcval.swap(vals);
-  p.bcoff.swap(newoff);
 }
 
 }  // namespace afv

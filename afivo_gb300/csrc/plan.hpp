@@ -51,6 +51,7 @@ struct Plan {
   std::vector<long long> tree_leaf_cells;
   std::vector<BcSpec> bc;
   std::vector<SlotDesc> desc;   // per slot, see desc.hpp
+  std::vector<long long> nbo2;  // [s*2D+f] refinement boundary: offg of the parent's neighbour
 
   int nc_at(int l) const { return l >= 1 ? nc : (nc >> (1 - l)); }
   int L(int l) const { return l - min_lvl; }

@@ -37,20 +37,15 @@ static bool with_nc(int D, int nc, F&& f) {
 
 static Meta meta_of(const DevMeta& d) {
   Meta m;
-  m.nb = d.nb;
+  m.tree = d.tree;
   m.parent = d.parent;
   m.first_child = d.first_child;
-  m.tree = d.tree;
-  m.qd = d.qd;
-  m.dr = d.dr;
   m.offg = d.offg;
   m.offi = d.offi;
-  m.bctype = d.bctype;
-  m.bcoff = d.bcoff;
   m.bcval = d.bcval;
   m.active = d.active;
-  m.nbo = d.nbo;
   m.desc = d.desc;
+  m.nbo2 = d.nbo2;
   m.err = d.err;
   return m;
 }
@@ -80,9 +75,8 @@ static int dupload(T** p, const std::vector<T>& v, long long& bytes) {
 Forest::~Forest() {
   cudaSetDevice(device);
   if (stream) cudaStreamSynchronize(stream);
-  void* ptrs[] = {meta.nb, meta.parent, meta.first_child, meta.tree, meta.qd, meta.dr, meta.offg,
-                  meta.offi, meta.bctype, meta.bcoff, meta.bcval, meta.active, meta.nbo, meta.desc,
-                  meta.err, d64.phi, d64.rhs,
+  void* ptrs[] = {meta.parent, meta.first_child, meta.tree, meta.offg, meta.offi, meta.bcval,
+                  meta.active, meta.desc, meta.nbo2, meta.err, d64.phi, d64.rhs,
                   d64.tmp, d32.phi, d32.rhs, d32.tmp, base_phi64, base_rhs64, d_lists, d_norm, d_red,
                   d_fmax, d_count, d_failed, d_stage, d_stage_slots};
   for (void* p : ptrs)
@@ -196,16 +190,12 @@ int Forest::create(const std::vector<const HostTree*>& trees, const afv_forest_o
   bytes = 0;
 #define UP(field, vec) \
   if ((rc = dupload(&meta.field, p.vec, bytes))) return err = "device allocation failed", rc;
-  UP(nb, nb);
   UP(parent, parent);
   UP(first_child, first_child);
   UP(tree, tree);
-  UP(qd, qd);
-  UP(dr, dr);
   UP(offg, offg);
   UP(offi, offi);
-  UP(bctype, bctype);
-  UP(nbo, nbo);
+  UP(nbo2, nbo2);
 #undef UP
   if (dmalloc(&meta.err, 1, bytes)) return err = "device allocation failed", AFV_ERR_NOMEM;
   cudaMemset(meta.err, 0, sizeof(int));
@@ -269,20 +259,14 @@ void Forest::norm_fold() {
 
 int Forest::upload_bc(std::string& err) {
   long long b = 0;
-  if (meta.bcoff) cudaFree(meta.bcoff);
   if (meta.bcval) cudaFree(meta.bcval);
-  meta.bcoff = nullptr;
   meta.bcval = nullptr;
-  if (dupload(&meta.bcoff, plan.bcoff, b) || dupload(&meta.bcval, plan.bcval, b))
-    return err = "device allocation failed", AFV_ERR_NOMEM;
+  if (dupload(&meta.bcval, plan.bcval, b)) return err = "device allocation failed", AFV_ERR_NOMEM;
   if (!meta.desc && dmalloc(&meta.desc, (long long)plan.desc.size(), bytes))
     return err = "device allocation failed", AFV_ERR_NOMEM;
   if (cudaMemcpy(meta.desc, plan.desc.data(), plan.desc.size() * sizeof(SlotDesc),
                  cudaMemcpyHostToDevice) != cudaSuccess)
     return err = "descriptor upload failed", AFV_ERR_CUDA;
-  if (cudaMemcpy(meta.bctype, plan.bctype.data(), plan.bctype.size() * sizeof(int),
-                 cudaMemcpyHostToDevice) != cudaSuccess)
-    return err = "bc upload failed", AFV_ERR_CUDA;
   return AFV_OK;
 }
 
@@ -405,14 +389,17 @@ void Forest::sweep(const Arrays<T>& a, int lvl, int n, bool pull, bool homog) {
     using C = dev::SweepCfg<D, NC, T>;
     static int occ = 0;
     if (!occ) {
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, dev::k_sweep_tma<D, NC, T>, dev::kThreads, 0);
+      cudaFuncSetAttribute(dev::k_sweep_tma<D, NC, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           C::SMEM_B);
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, dev::k_sweep_tma<D, NC, T>, dev::kThreads,
+                                                    C::SMEM_B);
       if (occ < 1) occ = 1;
     }
     const long long groups = (nbx + C::BPC - 1) / C::BPC;
     const int grid = (int)std::max(1LL, std::min(groups, (long long)n_sm * occ));
     // read phi and f, write phi over the interior
     ProfScope ps(this, kProfSweep, 3.0 * nbx * G::SI * sizeof(T));
-    dev::k_sweep_tma<D, NC, T><<<grid, dev::kThreads, 0, stream>>>(
+    dev::k_sweep_tma<D, NC, T><<<grid, dev::kThreads, C::SMEM_B, stream>>>(
         m, bs.lo, nbx, a.phi, a.rhs, n, pull ? 1 : 0, homog ? 1 : 0);
   });
 }
@@ -808,21 +795,17 @@ int Forest::solve(const MgOpts& mg, int precision, double tol, int max_cycles, S
   auto residual_check = [&](bool mixed_path) -> int {
     norm_reset();
     if (mixed_path) {
-      // Parents hold the restriction of their children, as at the fixed point
-      // of the FAS cycle: coarse leaves next to a refined region see them
-      // through their ghost cells.
-      for (int l = plan.max_lvl; l >= plan.min_lvl + 1; --l) restrict_res(d64, l, false);
-      fill_all64(false);
+      // FP64 defect on the leaves; ghost cells are pulled inside the kernel.
       int nl = (int)plan.all_leaves.size();
       BoxSet bs{d_lists + all_leaves_off, 0, nl};
       with_nc(plan.dim, plan.nc, [&](auto d_, auto nc_) {
         constexpr int D = decltype(d_)::value, NC = decltype(nc_)::value;
         using G = dev::Geo<D, NC>;
         constexpr int PER_BOX = G::SI < dev::kThreads ? G::SI : dev::kThreads;
-        constexpr int BPC = dev::kThreads / PER_BOX;
+        constexpr int BPC = dev::boxes_per_cta<G::SG, PER_BOX, double>(1);
         // read u (8 B), f (8 B); write r (4 B)
         ProfScope ps(this, kProfDefect, 20.0 * nl * G::SI);
-        dev::k_defect<D, NC><<<grid_for((nl + BPC - 1) / BPC, n_sm), dev::kThreads, 0, stream>>>(
+        dev::k_defect<D, NC><<<grid_for((nl + BPC - 1) / BPC, n_sm * 4), dev::kThreads, 0, stream>>>(
             m, bs, d64.phi, d64.rhs, d32.rhs, d_norm);
       });
     } else {
@@ -847,6 +830,11 @@ int Forest::solve(const MgOpts& mg, int precision, double tol, int max_cycles, S
     for (int t = 0; t < nt; ++t)
       if (was_active[t]) final_r[t] = h_norm[t];
   };
+  if (precision == AFV_PREC_MIXED) {
+    // Parents start as the restriction of their children (their values are
+    // only read by coarse leaves next to refined regions).
+    for (int l = plan.max_lvl; l >= plan.min_lvl + 1; --l) restrict_res(d64, l, false);
+  }
   std::vector<int> was(nt, 1);
   int n_active = residual_check(precision == AFV_PREC_MIXED);
   record(was);
@@ -862,10 +850,22 @@ int Forest::solve(const MgOpts& mg, int precision, double tol, int max_cycles, S
         constexpr int D = decltype(d_)::value, NC = decltype(nc_)::value;
         using G = dev::Geo<D, NC>;
         long long items = (long long)nl * G::SI;
-        // read e (4 B), read and write u (16 B)
-        ProfScope ps(this, kProfAccumulate, 20.0 * items);
-        dev::k_accumulate<D, NC><<<grid_for((items + 255) / 256, n_sm), 256, 0, stream>>>(m, bs, d64.phi,
-                                                                                       d32.phi);
+        {
+          // read e (4 B), read and write u (16 B)
+          ProfScope ps(this, kProfAccumulate, 20.0 * items);
+          dev::k_accumulate<D, NC><<<grid_for((items + 255) / 256, n_sm), 256, 0, stream>>>(
+              m, bs, d64.phi, d32.phi);
+        }
+        // parents (finest first) take the restriction of their children's increments
+        for (int l = plan.max_lvl - 1; l >= 1; --l) {
+          int np = n_parents(l);
+          if (!np) continue;
+          BoxSet pb{parents_list(l), 0, np};
+          long long pit = (long long)np * G::SI;
+          ProfScope ps(this, kProfAccumulate, (4.0 * (1 << D) + 4.0 + 16.0) * pit);
+          dev::k_restrict_increment<D, NC><<<grid_for((pit + 255) / 256, n_sm), 256, 0, stream>>>(
+              m, pb, d64.phi, d32.phi);
+        }
       });
     } else {
       vcycle_t(d64, mg, plan.max_lvl, false, false);
@@ -878,10 +878,9 @@ int Forest::solve(const MgOpts& mg, int precision, double tol, int max_cycles, S
     if (int rc = check_device_error(err)) return rc;
   }
   if (precision == AFV_PREC_MIXED) {
+    // Complete state: parents as restrictions, ghost cells filled.
     set_active_all(1);
     restrict_tree_phi64();
-    // residual on every box, as the FP64 path leaves it
-    for (int l = plan.min_lvl; l <= plan.max_lvl; ++l) residual(d64, l, nullptr, true);
   }
   set_active_all(1);
   for (int t = 0; t < nt; ++t) {
