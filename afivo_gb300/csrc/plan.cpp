@@ -210,6 +210,51 @@ int build_plan(const std::vector<const HostTree*>& trees, Plan& p, std::string& 
   return AFV_OK;
 }
 
+void plan_fill_bc(Plan& p, int t) {
+  const int D = p.dim, NNB = 2 * D;
+  const BcSpec& bc = p.bc[t];
+  // Rebuild the value table: other trees' records are kept, this tree's
+  // records are recomputed from its BcSpec.
+  std::vector<double> vals;
+  std::vector<long long> newoff(p.bcoff.size(), -1);
+  for (int s = 0; s < p.n_slots; ++s)
+    for (int f = 0; f < NNB; ++f) {
+      size_t k = (size_t)s * NNB + f;
+      if (p.nb[k] != -2) continue;
+      if (p.tree[s] != t) {
+        if (p.bcoff[k] >= 0) {
+          int ncl = p.nc_at(p.lvl[s]);
+          long long nfc = D == 2 ? ncl : (long long)ncl * ncl;
+          newoff[k] = (long long)vals.size();
+          vals.insert(vals.end(), p.bcval.begin() + p.bcoff[k], p.bcval.begin() + p.bcoff[k] + nfc);
+        }
+        continue;
+      }
+      p.bctype[k] = bc.type == AFV_BC_NEUMANN ? 1 : 0;
+      if (bc.gauss.empty()) continue;
+      int ncl = p.nc_at(p.lvl[s]);
+      int dim = f >> 1;
+      bool low = (f & 1) == 0;
+      newoff[k] = (long long)vals.size();
+      int cmax = D == 3 ? ncl : 1;
+      for (int c = 1; c <= cmax; ++c)
+        for (int a = 1; a <= ncl; ++a) {
+          // face centre: a$D_rr_cc(box, [0.5 or nc+0.5, tangential indices])
+          int tang[2] = {a, c};
+          int k2 = 0;
+          double r[3];
+          for (int e = 0; e < D; ++e) {
+            double cix = (e == dim) ? (low ? 0.5 : ncl + 0.5) : (double)tang[k2++];
+            r[e] = p.r_min[(size_t)s * D + e] + (cix - 0.5) * p.dr[s];
+          }
+          vals.push_back(source_eval(D, bc.src_lpl, bc.gauss.data(),
+                                     (int)bc.gauss.size() / (2 + D), r));
+        }
+    }
+  p.bcval.swap(vals);
+  p.bcoff.swap(newoff);
+}
+
 void plan_build_desc(Plan& p) {
   const int NNB = 2 * p.dim;
   p.desc.assign(p.n_slots, SlotDesc());
