@@ -90,6 +90,16 @@ class Forest {
   int* d_stage_slots = nullptr;
   long long bytes = 0;
   std::vector<int> host_active;
+  int* h_active = nullptr;  // pinned copy of the device activity flags (read back by solves)
+  // CUDA graphs of one solve iteration, per precision, keyed by the options
+  struct GraphCache {
+    cudaGraphExec_t exec = nullptr;
+    long long kernels = 0;
+    int n_down = -1, n_up = -1, n_base = -1;
+    double tol = -1;
+  } graphs[2];
+  bool use_graphs = true;
+  void drop_graphs();
   // event profiler: when enabled, launches of the selected kinds (bit mask)
   // are bracketed by CUDA events on the forest's stream
   int prof_mask = 0;
@@ -140,6 +150,9 @@ class Forest {
   template <class T> void vcycle_t(const Arrays<T>& a, const MgOpts& mg, int highest, bool homog,
                                    bool base64);
   void fill_all64(bool homog);
+  // Enqueue (no host synchronisation) one solve iteration / its residual check.
+  void enqueue_iteration(const MgOpts& mg, int precision, double tol);
+  void enqueue_residual_check(int precision, double tol);
   void restrict_tree_phi64();
 
   int check(std::string& err, const char* where);

@@ -282,7 +282,9 @@ struct SweepCfg {
 // groups ahead), and loads the ghost sources of the next group into registers
 // while the current group is updated. One block barrier per group: the stage
 // refilled at group k was last read at group k-2, which every thread finished
-// before the barrier of group k-1.
+// before the barrier of group k-1. The colour is fixed per launch, so each
+// thread's ghost items and updated cell -- and all their index arithmetic --
+// are the same for every group and are computed once.
 //
 // With pull = 1 the ghost cells this colour reads are the values of the
 // a$D_gc_box fill the reference runs after the previous half-sweep
@@ -311,6 +313,48 @@ k_sweep_tma(Meta m, int lo, int nbx, T* __restrict__ phi, const T* __restrict__ 
     s_abort = 0;
     fence_mbar_init();
   }
+
+  // Per-thread constants of the ghost items (face cells this colour reads).
+  int it_b[C::ITEMS], it_f[C::ITEMS], it_gpos[C::ITEMS], it_npos[C::ITEMS], it_apos[C::ITEMS];
+  int it_lin[C::ITEMS];
+  short it_gi[C::ITEMS], it_gj[C::ITEMS], it_gk[C::ITEMS];
+#pragma unroll
+  for (int j = 0; j < C::ITEMS; ++j) {
+    const int e = threadIdx.x + j * kThreads;
+    it_b[j] = e / C::NEED;  // box within the group (>= BPC: no item)
+    const int r = e % C::NEED;
+    const int f = r / (G::NF / 2), mm = r % (G::NF / 2);
+    int a, c;
+    needed_face_cell<D, NC>(f, mm, n, a, c);
+    const Face<D, NC> F(f, a, c);
+    it_f[j] = f;
+    it_gpos[j] = G::g(F.gi, F.gj, F.gk);
+    it_npos[j] = G::g(F.ni, F.nj, F.nk);
+    it_apos[j] = G::g(F.ai, F.aj, F.ak);
+    it_lin[j] = (D == 2) ? (a - 1) : (a - 1) + NC * (c - 1);
+    it_gi[j] = (short)F.gi;
+    it_gj[j] = (short)F.gj;
+    it_gk[j] = (short)F.gk;
+  }
+  // The cell this thread updates.
+  const int ub = threadIdx.x / C::PER_BOX, uq = threadIdx.x % C::PER_BOX;
+  int upos, rpos;
+  {
+    const int p = uq % (NC / 2);
+    if constexpr (D == 2) {
+      const int j = uq / (NC / 2) + 1;
+      const int i = 2 * p + 1 + ((1 + j + n) & 1);
+      upos = G::g(i, j, 0);
+      rpos = G::in(i, j, 1);
+    } else {
+      const int j = (uq / (NC / 2)) % NC + 1;
+      const int k = uq / ((NC / 2) * NC) + 1;
+      const int i = 2 * p + 1 + ((1 + j + k + n) & 1);
+      upos = G::g(i, j, k);
+      rpos = G::in(i, j, k);
+    }
+  }
+  constexpr int OX = 1, OY = G::NG, OZ = G::NG * G::NG;
   __syncthreads();
 
   auto group_first = [&](int k) { return ((int)blockIdx.x + k * (int)gridDim.x) * C::BPC; };
@@ -333,23 +377,23 @@ k_sweep_tma(Meta m, int lo, int nbx, T* __restrict__ phi, const T* __restrict__ 
     act = ((int)threadIdx.x < nb) ? m.active[dsc[threadIdx.x].tree] : 0;
 #pragma unroll
     for (int j = 0; j < C::ITEMS; ++j) {
-      const int e = threadIdx.x + j * kThreads;
       val[j] = (T)0;
-      if (!pull || e >= nb * C::NEED) continue;
-      const int b = e / C::NEED, r = e % C::NEED;
-      const int f = r / (G::NF / 2), mm = r % (G::NF / 2);
-      int a, c;
-      needed_face_cell<D, NC>(f, mm, n, a, c);
-      const Face<D, NC> F(f, a, c);
-      const SlotDesc& d = dsc[b];
+      if (!pull || it_b[j] >= nb) continue;
+      const SlotDesc& d = dsc[it_b[j]];
+      const int f = it_f[j];
       const int code = d.code[f];
       const long long o = d.nbo[f];
-      if (code >= 0)
-        val[j] = phi[o + G::g(F.ni, F.nj, F.nk)];
-      else if (code == kFaceRefinement)
-        val[j] = phi[o + parent_cell<D, NC>(F, f, d.qd, false)];
-      else if (o >= 0 && !homog)
-        val[j] = (T)m.bcval[o + ((D == 2) ? (a - 1) : (a - 1) + NC * (c - 1))];
+      if (code >= 0) {
+        val[j] = phi[o + it_npos[j]];
+      } else if (code == kFaceRefinement) {
+        const int h = NC >> 1, qd = d.qd;
+        const int pi = (qd & 1) * h + ((it_gi[j] + 1) >> 1);
+        const int pj = ((qd >> 1) & 1) * h + ((it_gj[j] + 1) >> 1);
+        const int pk = (D == 3) ? ((qd >> 2) & 1) * h + ((it_gk[j] + 1) >> 1) : 0;
+        val[j] = phi[o + G::g(pi, pj, pk)];
+      } else if (o >= 0 && !homog) {
+        val[j] = (T)m.bcval[o + it_lin[j]];
+      }
     }
   };
 
@@ -379,52 +423,55 @@ k_sweep_tma(Meta m, int lo, int nbx, T* __restrict__ phi, const T* __restrict__ 
     if (pull) {
 #pragma unroll
       for (int j = 0; j < C::ITEMS; ++j) {
-        const int e = threadIdx.x + j * kThreads;
-        if (e >= nb * C::NEED) continue;
-        const int b = e / C::NEED, r = e % C::NEED;
-        const int f = r / (G::NF / 2), mm = r % (G::NF / 2);
-        int a, c;
-        needed_face_cell<D, NC>(f, mm, n, a, c);
-        const Face<D, NC> F(f, a, c);
-        const SlotDesc& d = dsc[b];
+        if (it_b[j] >= nb) continue;
+        const SlotDesc& d = dsc[it_b[j]];
+        const int f = it_f[j];
         const int code = d.code[f];
-        const T* bx = sphi + b * G::SG;
-        auto own = [&](int i, int jj, int kk) { return bx[G::g(i, jj, kk)]; };
-        T v;
-        if (code >= 0)
-          v = cur[j];
-        else if (code == kFaceRefinement)
-          v = rb_value<D, NC, T>(F, f, cur[j], own);
-        else
-          v = bc_value<T>(code, f, cur[j], own(F.ai, F.aj, F.ak), Sc<T>::dr(d));
-        sphi[b * G::SG + G::g(F.gi, F.gj, F.gk)] = v;
+        T* bx = sphi + it_b[j] * G::SG;
+        T v = cur[j];
+        if (code < 0) {  // boundary: formula from the box's own cells
+          if (code == kFaceRefinement) {  // mg$D_sides_rb, src/m_aX_mg.f90:286-347
+            const int dix = (f & 1) ? -1 : 1;
+            const int ap = it_apos[j];
+            const int dim = f >> 1;
+            if constexpr (D == 2) {
+              // x-direction term first, then the y-direction term; the
+              // tangential step alternates with the tangential index
+              if (dim == 0) {
+                const int dj = -1 + 2 * ((int)it_gj[j] & 1);
+                v = (T)0.5 * cur[j] + bx[ap] - (T)0.25 * (bx[ap + dix * OX] + bx[ap + dj * OY]);
+              } else {
+                const int di = -1 + 2 * ((int)it_gi[j] & 1);
+                v = (T)0.5 * cur[j] + bx[ap] - (T)0.25 * (bx[ap + di * OX] + bx[ap + dix * OY]);
+              }
+            } else {
+              const int ti = (int)it_gi[j], tj = (int)it_gj[j], tk = (int)it_gk[j];
+              const int di = (dim == 0) ? dix : -1 + 2 * (ti & 1);
+              const int dj = (dim == 1) ? dix : -1 + 2 * (tj & 1);
+              const int dk = (dim == 2) ? dix : -1 + 2 * (tk & 1);
+              v = (T)0.5 * cur[j] + (T)0.75 * bx[ap] - (T)0.25 * bx[ap + di * OX + dj * OY + dk * OZ];
+            }
+          } else {
+            v = bc_value<T>(code, f, cur[j], bx[it_apos[j]], Sc<T>::dr(d));
+          }
+        }
+        bx[it_gpos[j]] = v;
       }
     }
     __syncthreads();
     if (s_abort) return false;
-    const int b = threadIdx.x / C::PER_BOX, q = threadIdx.x % C::PER_BOX;
-    if (b < nb && s_act[st][b]) {
-      const T* bx = sphi + b * G::SG;
-      const T* f = srhs + b * G::SI;
-      const SlotDesc& d = dsc[b];
-      const T dx2 = Sc<T>::dx2(d);
-      const int p = q % (NC / 2);
+    if (ub < nb && s_act[st][ub]) {
+      const T* bx = sphi + ub * G::SG + upos;
+      const SlotDesc& d = dsc[ub];
+      const T f = srhs[ub * G::SI + rpos];
+      T v;
       if constexpr (D == 2) {
-        const int j = q / (NC / 2) + 1;
-        const int i = 2 * p + 1 + ((1 + j + n) & 1);
-        const T v = (T)0.25 * (bx[G::g(i + 1, j, 0)] + bx[G::g(i - 1, j, 0)] + bx[G::g(i, j + 1, 0)] +
-                               bx[G::g(i, j - 1, 0)] - dx2 * f[G::in(i, j, 1)]);
-        phi[d.offg + G::g(i, j, 0)] = v;
+        v = (T)0.25 * (bx[OX] + bx[-OX] + bx[OY] + bx[-OY] - Sc<T>::dx2(d) * f);
       } else {
-        const int j = (q / (NC / 2)) % NC + 1;
-        const int kk = q / ((NC / 2) * NC) + 1;
-        const int i = 2 * p + 1 + ((1 + j + kk + n) & 1);
         const T sixth = (T)(1 / 6.0);
-        const T v = sixth * (bx[G::g(i + 1, j, kk)] + bx[G::g(i - 1, j, kk)] + bx[G::g(i, j + 1, kk)] +
-                             bx[G::g(i, j - 1, kk)] + bx[G::g(i, j, kk + 1)] + bx[G::g(i, j, kk - 1)] -
-                             dx2 * f[G::in(i, j, kk)]);
-        phi[d.offg + G::g(i, j, kk)] = v;
+        v = sixth * (bx[OX] + bx[-OX] + bx[OY] + bx[-OY] + bx[OZ] + bx[-OZ] - Sc<T>::dx2(d) * f);
       }
+      phi[d.offg + upos] = v;
     }
     return true;
   };

@@ -86,7 +86,9 @@ Forest::~Forest() {
     cudaEventDestroy(p.stop);
   }
   for (cudaEvent_t e : event_pool) cudaEventDestroy(e);
+  drop_graphs();
   if (h_count) cudaFreeHost(h_count);
+  if (h_active) cudaFreeHost(h_active);
   if (h_norm) cudaFreeHost(h_norm);
   if (stream) cudaStreamDestroy(stream);
 }
@@ -241,11 +243,19 @@ int Forest::create(const std::vector<const HostTree*>& trees, const afv_forest_o
       dmalloc(&d_red, p.n_trees, bytes) || dmalloc(&d_fmax, p.n_trees, bytes) ||
       dmalloc(&d_count, 1, bytes) || dmalloc(&d_failed, p.n_trees, bytes))
     return err = "device allocation failed", AFV_ERR_NOMEM;
-  if (cudaMallocHost((void**)&h_count, sizeof(int)) != cudaSuccess ||
+  if (cudaMallocHost((void**)&h_active, sizeof(int) * p.n_trees) != cudaSuccess ||
+      cudaMallocHost((void**)&h_count, sizeof(int)) != cudaSuccess ||
       cudaMallocHost((void**)&h_norm, sizeof(unsigned long long) * p.n_trees) != cudaSuccess)
     return err = "pinned allocation failed", AFV_ERR_NOMEM;
   if (cudaDeviceSynchronize() != cudaSuccess) return check(err, "forest create");
   return AFV_OK;
+}
+
+void Forest::drop_graphs() {
+  for (auto& g : graphs) {
+    if (g.exec) cudaGraphExecDestroy(g.exec);
+    g = GraphCache();
+  }
 }
 
 void Forest::norm_reset() {
@@ -758,7 +768,82 @@ void Forest::restrict_tree_phi64() {
   fill_all64(false);
 }
 
-// Solve every tree to max|f - L phi| <= tol * max|f| over its leaves.
+// One residual check, enqueued only: per-tree max |r| over the leaves (the FP64
+// residual, or the FP64 defect written as the FP32 right-hand side of the
+// mixed cycle), the convergence flags, and their copies to pinned host memory.
+void Forest::enqueue_residual_check(int precision, double tol) {
+  const int nt = plan.n_trees;
+  Meta m = meta_of(meta);
+  norm_reset();
+  if (precision == AFV_PREC_MIXED) {
+    // FP64 defect on the leaves; ghost cells are pulled inside the kernel.
+    int nl = (int)plan.all_leaves.size();
+    BoxSet bs{d_lists + all_leaves_off, 0, nl};
+    with_nc(plan.dim, plan.nc, [&](auto d_, auto nc_) {
+      constexpr int D = decltype(d_)::value, NC = decltype(nc_)::value;
+      using G = dev::Geo<D, NC>;
+      constexpr int PER_BOX = G::SI < dev::kThreads ? G::SI : dev::kThreads;
+      constexpr int BPC = dev::boxes_per_cta<G::SG, PER_BOX, double>(1);
+      // read u (8 B), f (8 B); write r (4 B)
+      ProfScope ps(this, kProfDefect, 20.0 * nl * G::SI);
+      dev::k_defect<D, NC><<<grid_for((nl + BPC - 1) / BPC, n_sm * 4), dev::kThreads, 0, stream>>>(
+          m, bs, d64.phi, d64.rhs, d32.rhs, d_norm);
+    });
+  } else {
+    for (int l = plan.min_lvl; l <= plan.max_lvl; ++l) residual(d64, l, d_norm, true);
+  }
+  cudaMemsetAsync(d_count, 0, sizeof(int), stream);
+  norm_fold();
+  {
+    ProfScope ps(this, kProfOther, 20.0 * nt);
+    dev::k_check<<<(nt + 255) / 256, 256, 0, stream>>>(nt, d_red, d_fmax, tol, meta.active, d_failed,
+                                                       d_count);
+  }
+  cudaMemcpyAsync(h_count, d_count, sizeof(int), cudaMemcpyDeviceToHost, stream);
+  cudaMemcpyAsync(h_norm, d_red, sizeof(unsigned long long) * nt, cudaMemcpyDeviceToHost, stream);
+  cudaMemcpyAsync(h_active, meta.active, sizeof(int) * nt, cudaMemcpyDeviceToHost, stream);
+}
+
+// One solve iteration, enqueued only: a V-cycle (FP64), or an FP32 V-cycle
+// on the defect with the FP64 accumulate (mixed), then the residual check.
+void Forest::enqueue_iteration(const MgOpts& mg, int precision, double tol) {
+  Meta m = meta_of(meta);
+  if (precision == AFV_PREC_MIXED) {
+    cudaMemsetAsync(d32.phi, 0, sizeof(float) * plan.n_elem_g, stream);
+    vcycle_t(d32, mg, plan.max_lvl, true, true);
+    int nl = (int)plan.all_leaves.size();
+    BoxSet bs{d_lists + all_leaves_off, 0, nl};
+    with_nc(plan.dim, plan.nc, [&](auto d_, auto nc_) {
+      constexpr int D = decltype(d_)::value, NC = decltype(nc_)::value;
+      using G = dev::Geo<D, NC>;
+      long long items = (long long)nl * G::SI;
+      {
+        // read e (4 B), read and write u (16 B)
+        ProfScope ps(this, kProfAccumulate, 20.0 * items);
+        dev::k_accumulate<D, NC><<<grid_for((items + 255) / 256, n_sm), 256, 0, stream>>>(m, bs, d64.phi,
+                                                                                       d32.phi);
+      }
+      // parents (finest first) take the restriction of their children's increments
+      for (int l = plan.max_lvl - 1; l >= 1; --l) {
+        int np = n_parents(l);
+        if (!np) continue;
+        BoxSet pb{parents_list(l), 0, np};
+        long long pit = (long long)np * G::SI;
+        ProfScope ps(this, kProfAccumulate, (4.0 * (1 << D) + 4.0 + 16.0) * pit);
+        dev::k_restrict_increment<D, NC><<<grid_for((pit + 255) / 256, n_sm), 256, 0, stream>>>(
+            m, pb, d64.phi, d32.phi);
+      }
+    });
+  } else {
+    vcycle_t(d64, mg, plan.max_lvl, false, false);
+  }
+  enqueue_residual_check(precision, tol);
+}
+
+// Solve every tree to max|f - L phi| <= tol * max|f| over its leaves. Each
+// iteration is one CUDA-graph launch (captured on first use); trees that have
+// converged are masked out on the device, so the graph does not change while
+// the set of active trees shrinks.
 int Forest::solve(const MgOpts& mg, int precision, double tol, int max_cycles, SolveStats& st,
                   std::string& err) {
   const int nt = plan.n_trees;
@@ -788,92 +873,61 @@ int Forest::solve(const MgOpts& mg, int precision, double tol, int max_cycles, S
   cudaMemcpyAsync(d_fmax, d_red, sizeof(double) * nt, cudaMemcpyDeviceToDevice, stream);
   std::vector<double> fmax(nt);
   cudaMemcpyAsync(fmax.data(), d_red, sizeof(double) * nt, cudaMemcpyDeviceToHost, stream);
+  cudaMemsetAsync(d_failed, 0, sizeof(int) * nt, stream);
   cudaStreamSynchronize(stream);
   std::vector<int> done_cycles(nt, 0);
-  cudaMemsetAsync(d_failed, 0, sizeof(int) * nt, stream);
-
-  auto residual_check = [&](bool mixed_path) -> int {
-    norm_reset();
-    if (mixed_path) {
-      // FP64 defect on the leaves; ghost cells are pulled inside the kernel.
-      int nl = (int)plan.all_leaves.size();
-      BoxSet bs{d_lists + all_leaves_off, 0, nl};
-      with_nc(plan.dim, plan.nc, [&](auto d_, auto nc_) {
-        constexpr int D = decltype(d_)::value, NC = decltype(nc_)::value;
-        using G = dev::Geo<D, NC>;
-        constexpr int PER_BOX = G::SI < dev::kThreads ? G::SI : dev::kThreads;
-        constexpr int BPC = dev::boxes_per_cta<G::SG, PER_BOX, double>(1);
-        // read u (8 B), f (8 B); write r (4 B)
-        ProfScope ps(this, kProfDefect, 20.0 * nl * G::SI);
-        dev::k_defect<D, NC><<<grid_for((nl + BPC - 1) / BPC, n_sm * 4), dev::kThreads, 0, stream>>>(
-            m, bs, d64.phi, d64.rhs, d32.rhs, d_norm);
-      });
-    } else {
-      for (int l = plan.min_lvl; l <= plan.max_lvl; ++l) residual(d64, l, d_norm, true);
-    }
-    cudaMemsetAsync(d_count, 0, sizeof(int), stream);
-    norm_fold();
-    {
-      ProfScope ps(this, kProfOther, 20.0 * nt);
-      dev::k_check<<<(nt + 255) / 256, 256, 0, stream>>>(nt, d_red, d_fmax, tol, meta.active,
-                                                         d_failed, d_count);
-    }
-    cudaMemcpyAsync(h_count, d_count, sizeof(int), cudaMemcpyDeviceToHost, stream);
-    cudaMemcpyAsync(h_norm, d_red, sizeof(unsigned long long) * nt, cudaMemcpyDeviceToHost, stream);
-    cudaMemcpyAsync(host_active.data(), meta.active, sizeof(int) * nt, cudaMemcpyDeviceToHost, stream);
-    cudaStreamSynchronize(stream);
-    return *h_count;
-  };
 
   std::vector<unsigned long long> final_r(nt, 0);
-  auto record = [&](const std::vector<int>& was_active) {
+  std::vector<int> was(nt, 1);
+  auto record = [&]() {
     for (int t = 0; t < nt; ++t)
-      if (was_active[t]) final_r[t] = h_norm[t];
+      if (was[t]) final_r[t] = h_norm[t];
+    for (int t = 0; t < nt; ++t) was[t] = h_active[t];
   };
   if (precision == AFV_PREC_MIXED) {
     // Parents start as the restriction of their children (their values are
     // only read by coarse leaves next to refined regions).
     for (int l = plan.max_lvl; l >= plan.min_lvl + 1; --l) restrict_res(d64, l, false);
   }
-  std::vector<int> was(nt, 1);
-  int n_active = residual_check(precision == AFV_PREC_MIXED);
-  record(was);
+  enqueue_residual_check(precision, tol);
+  if (cudaStreamSynchronize(stream) != cudaSuccess) return check(err, "solve");
+  int n_active = *h_count;
+  record();
+
+  const bool graph = use_graphs && prof_mask == 0;
+  GraphCache& gc = graphs[precision == AFV_PREC_MIXED ? 1 : 0];
+  if (graph && (gc.n_down != mg.n_down || gc.n_up != mg.n_up || gc.n_base != mg.n_base || gc.tol != tol)) {
+    if (gc.exec) cudaGraphExecDestroy(gc.exec);
+    gc = GraphCache();
+    long long before = n_launches;
+    cudaGraph_t g = nullptr;
+    if (cudaStreamBeginCapture(stream, cudaStreamCaptureModeRelaxed) != cudaSuccess)
+      return check(err, "graph capture");
+    enqueue_iteration(mg, precision, tol);
+    if (cudaStreamEndCapture(stream, &g) != cudaSuccess || !g) return check(err, "graph capture");
+    cudaError_t ie = cudaGraphInstantiate(&gc.exec, g, 0);
+    cudaGraphDestroy(g);
+    if (ie != cudaSuccess) return check(err, "graph instantiate");
+    gc.kernels = n_launches - before;
+    n_launches = before;
+    gc.n_down = mg.n_down;
+    gc.n_up = mg.n_up;
+    gc.n_base = mg.n_base;
+    gc.tol = tol;
+  }
   int cyc = 0;
   while (n_active > 0 && cyc < max_cycles) {
-    for (int t = 0; t < nt; ++t) done_cycles[t] += host_active[t] ? 1 : 0;
-    if (precision == AFV_PREC_MIXED) {
-      cudaMemsetAsync(d32.phi, 0, sizeof(float) * plan.n_elem_g, stream);
-      vcycle_t(d32, mg, plan.max_lvl, true, true);
-      int nl = (int)plan.all_leaves.size();
-      BoxSet bs{d_lists + all_leaves_off, 0, nl};
-      with_nc(plan.dim, plan.nc, [&](auto d_, auto nc_) {
-        constexpr int D = decltype(d_)::value, NC = decltype(nc_)::value;
-        using G = dev::Geo<D, NC>;
-        long long items = (long long)nl * G::SI;
-        {
-          // read e (4 B), read and write u (16 B)
-          ProfScope ps(this, kProfAccumulate, 20.0 * items);
-          dev::k_accumulate<D, NC><<<grid_for((items + 255) / 256, n_sm), 256, 0, stream>>>(
-              m, bs, d64.phi, d32.phi);
-        }
-        // parents (finest first) take the restriction of their children's increments
-        for (int l = plan.max_lvl - 1; l >= 1; --l) {
-          int np = n_parents(l);
-          if (!np) continue;
-          BoxSet pb{parents_list(l), 0, np};
-          long long pit = (long long)np * G::SI;
-          ProfScope ps(this, kProfAccumulate, (4.0 * (1 << D) + 4.0 + 16.0) * pit);
-          dev::k_restrict_increment<D, NC><<<grid_for((pit + 255) / 256, n_sm), 256, 0, stream>>>(
-              m, pb, d64.phi, d32.phi);
-        }
-      });
+    for (int t = 0; t < nt; ++t) done_cycles[t] += h_active[t] ? 1 : 0;
+    if (graph) {
+      if (cudaGraphLaunch(gc.exec, stream) != cudaSuccess) return check(err, "graph launch");
+      n_launches += gc.kernels;
     } else {
-      vcycle_t(d64, mg, plan.max_lvl, false, false);
+      enqueue_iteration(mg, precision, tol);
     }
+    if (cudaStreamSynchronize(stream) != cudaSuccess) return check(err, "solve");
+    n_active = *h_count;
+    record();
     ++cyc;
-    was = host_active;
-    n_active = residual_check(precision == AFV_PREC_MIXED);
-    record(was);
     if (int rc = check(err, "solve")) return rc;
     if (int rc = check_device_error(err)) return rc;
   }
