@@ -11,6 +11,11 @@
 
 namespace afv {
 
+namespace dev {
+struct BoxSet;
+}
+using dev_BoxSet = dev::BoxSet;
+
 template <class T>
 struct Arrays {
   T* phi = nullptr;  // ghosted
@@ -148,7 +153,8 @@ class Forest {
   template <class T> void gsrb_boxes(const Arrays<T>& a, int lvl, int n_cycle, bool homog);
   template <class T> void update_coarse_t(const Arrays<T>& a, int lvl, bool homog, bool copy_tmp);
   template <class T> void vcycle_t(const Arrays<T>& a, const MgOpts& mg, int highest, bool homog,
-                                   bool base64);
+                                   bool base64, bool inner = false);
+  template <class T> void fill_set(const Arrays<T>& a, int lvl, dev_BoxSet bs, bool homog);
   void fill_all64(bool homog);
   // Enqueue (no host synchronisation) one solve iteration / its residual check.
   void enqueue_iteration(const MgOpts& mg, int precision, double tol);

@@ -224,12 +224,14 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned by
       "l"(src), "r"(bytes), "r"(smem_addr(bar))
       : "memory");
 }
+// try_wait with a suspend-time hint (ns): the warp sleeps until the phase
+// completes or the hint elapses instead of spinning.
 __device__ __forceinline__ bool mbar_test(unsigned long long* bar, unsigned parity) {
   unsigned ok;
   asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}"
       : "=r"(ok)
-      : "r"(smem_addr(bar)), "r"(parity)
+      : "r"(smem_addr(bar)), "r"(parity), "r"(20000u)
       : "memory");
   return ok != 0;
 }
@@ -255,55 +257,66 @@ __device__ __forceinline__ void needed_face_cell(int f, int m, int n, int& a, in
   }
 }
 
-template <int D, int NC, class T>
-struct SweepCfg {
+enum { kModeSweep = 0, kModeFill = 1 };
+
+template <int D, int NC, class T, int MODE>
+struct LevelCfg {
   using G = Geo<D, NC>;
-  static constexpr int S = 4;                   // pipeline stages
-  static constexpr int PER_BOX = G::SI / 2;     // one thread per updated cell
-  static constexpr int BOX_B = (int)sizeof(SlotDesc) + (G::SG + G::SI) * (int)sizeof(T);
-  static constexpr int BPC_T = kThreads / PER_BOX;
-  static constexpr int BPC_S = 56 * 1024 / (S * BOX_B);
+  static constexpr int S = 6;                   // pipeline stages
+  static constexpr int LA = S - 2;              // groups issued ahead of the one in use
+  static constexpr bool SWEEP = MODE == kModeSweep;
+  static constexpr int PER_BOX = G::SI / 2;     // sweep: one thread per updated cell
+  static constexpr int NEED = SWEEP ? 2 * D * (G::NF / 2) : 2 * D * G::NF;  // ghost items per box
+  static constexpr int BOX_B = (int)sizeof(SlotDesc) + (G::SG + (SWEEP ? G::SI : 0)) * (int)sizeof(T);
+  static constexpr int BPC_T = SWEEP ? kThreads / PER_BOX : (2 * kThreads / NEED > 0 ? 2 * kThreads / NEED : 1);
+  static constexpr int BPC_S = 100 * 1024 / (S * BOX_B);
   static constexpr int BPC = BPC_T < BPC_S ? BPC_T : (BPC_S < 1 ? 1 : BPC_S);
-  static constexpr int NEED = 2 * D * (G::NF / 2);  // ghost cells one colour reads
   static constexpr int ITEMS = (BPC * NEED + kThreads - 1) / kThreads;
   static constexpr int DESC_B = BPC * (int)sizeof(SlotDesc);
   static constexpr int PHI_B = BPC * G::SG * (int)sizeof(T);
-  static constexpr int RHS_B = BPC * G::SI * (int)sizeof(T);
+  static constexpr int RHS_B = SWEEP ? BPC * G::SI * (int)sizeof(T) : 0;
   static constexpr int STAGE_B = DESC_B + PHI_B + RHS_B;
   static constexpr int SMEM_B = S * STAGE_B;  // dynamic shared memory
-  static_assert(PHI_B % 16 == 0 && RHS_B % 16 == 0 && DESC_B % 16 == 0, "bulk copy sizes");
+  static_assert(G::SG * sizeof(T) % 16 == 0 && G::SI * sizeof(T) % 16 == 0, "bulk copy sizes");
 };
 
 // ---------------------------------------------------------------------------
-// GSRB half-sweep on every box of one level (mg$D_box_gsrb_lpl,
-// src/m_aX_mg.f90:718-760), persistent and pipelined. Each block streams its
-// groups of consecutive boxes through an S-stage ring in shared memory (one
-// bulk copy each for the descriptors, phi and rhs of a group, issued two
-// groups ahead), and loads the ghost sources of the next group into registers
-// while the current group is updated. One block barrier per group: the stage
-// refilled at group k was last read at group k-2, which every thread finished
-// before the barrier of group k-1. The colour is fixed per launch, so each
-// thread's ghost items and updated cell -- and all their index arithmetic --
-// are the same for every group and are computed once.
+// Level kernel, persistent and pipelined, in two modes.
 //
-// With pull = 1 the ghost cells this colour reads are the values of the
-// a$D_gc_box fill the reference runs after the previous half-sweep
-// (src/m_aX_mg.f90:412-417): neighbours' cells of the other colour, which no
-// block writes during this sweep, so all blocks update in place. With
+// kModeSweep -- GSRB half-sweep on every box of one level (mg$D_box_gsrb_lpl,
+// src/m_aX_mg.f90:718-760). With pull = 1 the ghost cells this colour reads
+// are the values of the a$D_gc_box fill the reference runs after the previous
+// half-sweep (src/m_aX_mg.f90:412-417): neighbours' cells of the other colour,
+// which no block writes during this sweep, so all blocks update in place. With
 // pull = 0 the stored ghost cells are used (first half-sweep).
+//
+// kModeFill -- ghost fill of every face of every box of a set (a$D_gc_box,
+// src/m_aX_gc.f90:50-69, as called by fill_gc_phi, src/m_aX_mg.f90:352-365):
+// writes only ghost cells, reads only interior cells of the level and the
+// parents' stored cells, so all boxes fill concurrently.
+//
+// Each block streams its groups of boxes through an S-stage ring in shared
+// memory (bulk copies of descriptors, phi and rhs, issued LA groups ahead) and
+// loads the ghost sources of the next group into registers while the current
+// group is processed. One block barrier per group: the stage refilled at
+// group k was last read at group k-2, which every thread finished before the
+// barrier of group k-1. The colour is fixed per launch, so each thread's ghost
+// items and updated cell -- and their index arithmetic -- are computed once.
 // ---------------------------------------------------------------------------
-template <int D, int NC, class T>
+template <int D, int NC, class T, int MODE>
 __global__ void __launch_bounds__(kThreads)
-k_sweep_tma(Meta m, int lo, int nbx, T* __restrict__ phi, const T* __restrict__ rhs, int n, int pull,
-            int homog) {
-  using C = SweepCfg<D, NC, T>;
+k_level_tma(Meta m, BoxSet bs, T* __restrict__ phi, const T* __restrict__ rhs, int n, int pull, int homog) {
+  using C = LevelCfg<D, NC, T, MODE>;
   using G = Geo<D, NC>;
   constexpr int S = C::S;
+  constexpr bool SWEEP = C::SWEEP;
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) unsigned long long bar[S];
   __shared__ int s_act[S][C::BPC];
   __shared__ int s_abort;
+  if (!SWEEP) pull = 1;
 
+  const int nbx = bs.n;
   const int groups = (nbx + C::BPC - 1) / C::BPC;
   if ((int)blockIdx.x >= groups) return;
   const int my_groups = (groups - 1 - (int)blockIdx.x) / (int)gridDim.x + 1;
@@ -314,7 +327,7 @@ k_sweep_tma(Meta m, int lo, int nbx, T* __restrict__ phi, const T* __restrict__ 
     fence_mbar_init();
   }
 
-  // Per-thread constants of the ghost items (face cells this colour reads).
+  // Per-thread constants of the ghost items.
   int it_b[C::ITEMS], it_f[C::ITEMS], it_gpos[C::ITEMS], it_npos[C::ITEMS], it_apos[C::ITEMS];
   int it_lin[C::ITEMS];
   short it_gi[C::ITEMS], it_gj[C::ITEMS], it_gk[C::ITEMS];
@@ -323,9 +336,16 @@ k_sweep_tma(Meta m, int lo, int nbx, T* __restrict__ phi, const T* __restrict__ 
     const int e = threadIdx.x + j * kThreads;
     it_b[j] = e / C::NEED;  // box within the group (>= BPC: no item)
     const int r = e % C::NEED;
-    const int f = r / (G::NF / 2), mm = r % (G::NF / 2);
-    int a, c;
-    needed_face_cell<D, NC>(f, mm, n, a, c);
+    int f, a, c;
+    if constexpr (SWEEP) {
+      f = r / (G::NF / 2);
+      needed_face_cell<D, NC>(f, r % (G::NF / 2), n, a, c);
+    } else {
+      f = r / G::NF;
+      const int lin = r % G::NF;
+      a = lin % NC + 1;
+      c = lin / NC + 1;
+    }
     const Face<D, NC> F(f, a, c);
     it_f[j] = f;
     it_gpos[j] = G::g(F.gi, F.gj, F.gk);
@@ -336,10 +356,10 @@ k_sweep_tma(Meta m, int lo, int nbx, T* __restrict__ phi, const T* __restrict__ 
     it_gj[j] = (short)F.gj;
     it_gk[j] = (short)F.gk;
   }
-  // The cell this thread updates.
+  // Sweep: the cell this thread updates.
   const int ub = threadIdx.x / C::PER_BOX, uq = threadIdx.x % C::PER_BOX;
-  int upos, rpos;
-  {
+  int upos = 0, rpos = 0;
+  if constexpr (SWEEP) {
     const int p = uq % (NC / 2);
     if constexpr (D == 2) {
       const int j = uq / (NC / 2) + 1;
@@ -360,14 +380,27 @@ k_sweep_tma(Meta m, int lo, int nbx, T* __restrict__ phi, const T* __restrict__ 
   auto group_first = [&](int k) { return ((int)blockIdx.x + k * (int)gridDim.x) * C::BPC; };
   auto group_n = [&](int k) { return min(C::BPC, nbx - group_first(k)); };
   auto issue = [&](int k) {  // one thread
-    const int first = group_first(k), nb = group_n(k), s0 = lo + first;
+    const int first = group_first(k), nb = group_n(k);
     unsigned char* sp = smem + (k % S) * C::STAGE_B;
+    unsigned long long* b = &bar[k % S];
     fence_proxy_async();
-    mbar_expect_tx(&bar[k % S], nb * (unsigned)C::BOX_B);
-    bulk_g2s(sp, m.desc + s0, nb * (unsigned)sizeof(SlotDesc), &bar[k % S]);
-    bulk_g2s(sp + C::DESC_B, phi + m.offg[s0], nb * (unsigned)(G::SG * sizeof(T)), &bar[k % S]);
-    bulk_g2s(sp + C::DESC_B + C::PHI_B, rhs + m.offi[s0], nb * (unsigned)(G::SI * sizeof(T)),
-             &bar[k % S]);
+    mbar_expect_tx(b, nb * (unsigned)C::BOX_B);
+    if (!bs.list) {  // consecutive slots: consecutive storage
+      const int s0 = bs.lo + first;
+      bulk_g2s(sp, m.desc + s0, nb * (unsigned)sizeof(SlotDesc), b);
+      bulk_g2s(sp + C::DESC_B, phi + m.offg[s0], nb * (unsigned)(G::SG * sizeof(T)), b);
+      if constexpr (SWEEP)
+        bulk_g2s(sp + C::DESC_B + C::PHI_B, rhs + m.offi[s0], nb * (unsigned)(G::SI * sizeof(T)), b);
+    } else {
+      for (int q = 0; q < nb; ++q) {
+        const int s = bs.list[first + q];
+        bulk_g2s(sp + q * sizeof(SlotDesc), m.desc + s, (unsigned)sizeof(SlotDesc), b);
+        bulk_g2s(sp + C::DESC_B + q * G::SG * sizeof(T), phi + m.offg[s], (unsigned)(G::SG * sizeof(T)), b);
+        if constexpr (SWEEP)
+          bulk_g2s(sp + C::DESC_B + C::PHI_B + q * G::SI * sizeof(T), rhs + m.offi[s],
+                   (unsigned)(G::SI * sizeof(T)), b);
+      }
+    }
   };
   // Ghost sources of group k (its stage has landed): neighbour cells, parent
   // cells at refinement boundaries, or boundary values.
@@ -397,7 +430,7 @@ k_sweep_tma(Meta m, int lo, int nbx, T* __restrict__ phi, const T* __restrict__ 
     }
   };
 
-  int issued = min(2, my_groups);
+  int issued = min(C::LA, my_groups);
   if (threadIdx.x == 0)
     for (int k = 0; k < issued; ++k) issue(k);
 
@@ -407,10 +440,9 @@ k_sweep_tma(Meta m, int lo, int nbx, T* __restrict__ phi, const T* __restrict__ 
     unsigned char* sp = smem + st * C::STAGE_B;
     const SlotDesc* dsc = reinterpret_cast<const SlotDesc*>(sp);
     T* sphi = reinterpret_cast<T*>(sp + C::DESC_B);
-    const T* srhs = reinterpret_cast<const T*>(sp + C::DESC_B + C::PHI_B);
     const int nb = group_n(k);
-    if (k + 2 < my_groups) {
-      if (threadIdx.x == 0) issue(k + 2);
+    if (k + C::LA < my_groups) {
+      if (threadIdx.x == 0) issue(k + C::LA);
       ++issued;
     }
     if (k + 1 < my_groups) {
@@ -425,6 +457,7 @@ k_sweep_tma(Meta m, int lo, int nbx, T* __restrict__ phi, const T* __restrict__ 
       for (int j = 0; j < C::ITEMS; ++j) {
         if (it_b[j] >= nb) continue;
         const SlotDesc& d = dsc[it_b[j]];
+        if (!SWEEP && !m.active[d.tree]) continue;
         const int f = it_f[j];
         const int code = d.code[f];
         T* bx = sphi + it_b[j] * G::SG;
@@ -455,23 +488,29 @@ k_sweep_tma(Meta m, int lo, int nbx, T* __restrict__ phi, const T* __restrict__ 
             v = bc_value<T>(code, f, cur[j], bx[it_apos[j]], Sc<T>::dr(d));
           }
         }
-        bx[it_gpos[j]] = v;
+        if constexpr (SWEEP)
+          bx[it_gpos[j]] = v;
+        else
+          phi[d.offg + it_gpos[j]] = v;
       }
     }
     __syncthreads();
     if (s_abort) return false;
-    if (ub < nb && s_act[st][ub]) {
-      const T* bx = sphi + ub * G::SG + upos;
-      const SlotDesc& d = dsc[ub];
-      const T f = srhs[ub * G::SI + rpos];
-      T v;
-      if constexpr (D == 2) {
-        v = (T)0.25 * (bx[OX] + bx[-OX] + bx[OY] + bx[-OY] - Sc<T>::dx2(d) * f);
-      } else {
-        const T sixth = (T)(1 / 6.0);
-        v = sixth * (bx[OX] + bx[-OX] + bx[OY] + bx[-OY] + bx[OZ] + bx[-OZ] - Sc<T>::dx2(d) * f);
+    if constexpr (SWEEP) {
+      const T* srhs = reinterpret_cast<const T*>(sp + C::DESC_B + C::PHI_B);
+      if (ub < nb && s_act[st][ub]) {
+        const T* bx = sphi + ub * G::SG + upos;
+        const SlotDesc& d = dsc[ub];
+        const T f = srhs[ub * G::SI + rpos];
+        T v;
+        if constexpr (D == 2) {
+          v = (T)0.25 * (bx[OX] + bx[-OX] + bx[OY] + bx[-OY] - Sc<T>::dx2(d) * f);
+        } else {
+          const T sixth = (T)(1 / 6.0);
+          v = sixth * (bx[OX] + bx[-OX] + bx[OY] + bx[-OY] + bx[OZ] + bx[-OZ] - Sc<T>::dx2(d) * f);
+        }
+        phi[d.offg + upos] = v;
       }
-      phi[d.offg + upos] = v;
     }
     return true;
   };
@@ -498,34 +537,6 @@ k_sweep_tma(Meta m, int lo, int nbx, T* __restrict__ phi, const T* __restrict__ 
   if (k < my_groups && threadIdx.x == 0) {  // gave up: drain this block's copies
     atomicExch(m.err, 1);
     for (int j = k + 1; j < issued; ++j) mbar_wait_bounded(&bar[j % S], (j / S) & 1);
-  }
-}
-
-// ---------------------------------------------------------------------------
-// Ghost fill of every face of every box of a level (a$D_gc_box per box,
-// src/m_aX_gc.f90:50-69, as called by fill_gc_phi, src/m_aX_mg.f90:352-365).
-// Writes only ghost cells and reads only interior cells (own, neighbours')
-// and the parent's stored cells, so all boxes fill concurrently.
-// ---------------------------------------------------------------------------
-template <int D, int NC, class T>
-__global__ void __launch_bounds__(kThreads)
-k_fill(Meta m, BoxSet bs, T* __restrict__ phi, int homog) {
-  using G = Geo<D, NC>;
-  const long long total = (long long)bs.n * G::NNB * G::NF;
-  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
-       e += (long long)gridDim.x * blockDim.x) {
-    int bi = (int)(e / (G::NNB * G::NF));
-    int r = (int)(e % (G::NNB * G::NF));
-    int f = r / G::NF, lin = r % G::NF;
-    int a = lin % NC + 1, c = lin / NC + 1;
-    int s = box_at(bs, bi);
-    const SlotDesc& d = m.desc[s];
-    if (!m.active[d.tree]) continue;
-    const T* bx = phi + d.offg;
-    auto own = [&](int i, int j, int k) { return bx[G::g(i, j, k)]; };
-    T v = ghost_value<D, NC, T>(m, d, phi, f, a, c, homog != 0, own);
-    Face<D, NC> F(f, a, c);
-    phi[d.offg + G::g(F.gi, F.gj, F.gk)] = v;
   }
 }
 

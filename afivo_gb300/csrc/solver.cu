@@ -387,6 +387,25 @@ int Forest::set_var(int t, int var, const double* host, int interior_only, std::
 // Level operators
 // ---------------------------------------------------------------------------
 
+// Launches the pipelined level kernel (sweep or ghost fill) on a box set.
+template <int D, int NC, class T, int MODE>
+static void launch_level(Forest& F, const Meta& m, BoxSet bs, T* phi, const T* rhs, int n, bool pull,
+                         bool homog) {
+  using C = dev::LevelCfg<D, NC, T, MODE>;
+  static int occ = 0;
+  if (!occ) {
+    cudaFuncSetAttribute(dev::k_level_tma<D, NC, T, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         C::SMEM_B);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, dev::k_level_tma<D, NC, T, MODE>, dev::kThreads,
+                                                  C::SMEM_B);
+    if (occ < 1) occ = 1;
+  }
+  const long long groups = (bs.n + C::BPC - 1) / C::BPC;
+  const int grid = (int)std::max(1LL, std::min(groups, (long long)F.n_sm * occ));
+  dev::k_level_tma<D, NC, T, MODE><<<grid, dev::kThreads, C::SMEM_B, F.stream>>>(
+      m, bs, phi, rhs, n, pull ? 1 : 0, homog ? 1 : 0);
+}
+
 template <class T>
 void Forest::sweep(const Arrays<T>& a, int lvl, int n, bool pull, bool homog) {
   int nbx = lvl_n(lvl);
@@ -396,21 +415,9 @@ void Forest::sweep(const Arrays<T>& a, int lvl, int n, bool pull, bool homog) {
   with_nc(plan.dim, plan.nc_at(lvl), [&](auto d_, auto nc_) {
     constexpr int D = decltype(d_)::value, NC = decltype(nc_)::value;
     using G = dev::Geo<D, NC>;
-    using C = dev::SweepCfg<D, NC, T>;
-    static int occ = 0;
-    if (!occ) {
-      cudaFuncSetAttribute(dev::k_sweep_tma<D, NC, T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           C::SMEM_B);
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, dev::k_sweep_tma<D, NC, T>, dev::kThreads,
-                                                    C::SMEM_B);
-      if (occ < 1) occ = 1;
-    }
-    const long long groups = (nbx + C::BPC - 1) / C::BPC;
-    const int grid = (int)std::max(1LL, std::min(groups, (long long)n_sm * occ));
     // read phi and f, write phi over the interior
     ProfScope ps(this, kProfSweep, 3.0 * nbx * G::SI * sizeof(T));
-    dev::k_sweep_tma<D, NC, T><<<grid, dev::kThreads, C::SMEM_B, stream>>>(
-        m, bs.lo, nbx, a.phi, a.rhs, n, pull ? 1 : 0, homog ? 1 : 0);
+    launch_level<D, NC, T, dev::kModeSweep>(*this, m, bs, a.phi, a.rhs, n, pull, homog);
   });
 }
 
@@ -418,16 +425,19 @@ template <class T>
 void Forest::fill(const Arrays<T>& a, int lvl, bool homog) {
   int nbx = lvl_n(lvl);
   if (!nbx) return;
-  BoxSet bs{nullptr, plan.lvl_lo[plan.L(lvl)], nbx};
+  fill_set(a, lvl, BoxSet{nullptr, plan.lvl_lo[plan.L(lvl)], nbx}, homog);
+}
+
+template <class T>
+void Forest::fill_set(const Arrays<T>& a, int lvl, BoxSet bs, bool homog) {
+  if (!bs.n) return;
   Meta m = meta_of(meta);
   with_nc(plan.dim, plan.nc_at(lvl), [&](auto d_, auto nc_) {
     constexpr int D = decltype(d_)::value, NC = decltype(nc_)::value;
     using G = dev::Geo<D, NC>;
-    long long items = (long long)nbx * G::NNB * G::NF;
-    int grid = grid_for((items + dev::kThreads - 1) / dev::kThreads, n_sm);
     // read the neighbour face value, write the ghost value
-    ProfScope ps(this, kProfFill, 2.0 * items * sizeof(T));
-    dev::k_fill<D, NC, T><<<grid, dev::kThreads, 0, stream>>>(m, bs, a.phi, homog ? 1 : 0);
+    ProfScope ps(this, kProfFill, 2.0 * bs.n * G::NNB * G::NF * sizeof(T));
+    launch_level<D, NC, T, dev::kModeFill>(*this, m, bs, a.phi, nullptr, 0, true, homog);
   });
 }
 
@@ -547,7 +557,8 @@ void Forest::update_coarse_t(const Arrays<T>& a, int lvl, bool homog, bool copy_
 // every level ends the cycle with a stored ghost fill (valid on output).
 // base64: smooth the coarsest level in FP64 (mixed cycle).
 template <class T>
-void Forest::vcycle_t(const Arrays<T>& a, const MgOpts& mg, int highest, bool homog, bool base64) {
+void Forest::vcycle_t(const Arrays<T>& a, const MgOpts& mg, int highest, bool homog, bool base64,
+                      bool inner) {
   const int l0 = plan.min_lvl;
   auto sweeps = [&](const auto& arr, int l, int n_cycle) {
     for (int n = 1; n <= 2 * n_cycle; ++n) sweep(arr, l, n, n > 1 || l != highest, homog);
@@ -589,7 +600,14 @@ void Forest::vcycle_t(const Arrays<T>& a, const MgOpts& mg, int highest, bool ho
     if (mg.n_up > 0) {
       for (int n = 1; n <= 2 * mg.n_up; ++n) sweep(a, l, n, true, homog);
     }
-    fill(a, l, homog);
+    if (!inner) {
+      fill(a, l, homog);
+    } else if (l < highest && n_parents(l)) {
+      // Inner correction cycle of the mixed path: its result is read only on
+      // interiors, and its ghost cells only by the children of parents at
+      // refinement boundaries during this cycle.
+      fill_set(a, l, BoxSet{parents_list(l), 0, n_parents(l)}, homog);
+    }
   }
 }
 
@@ -810,7 +828,7 @@ void Forest::enqueue_iteration(const MgOpts& mg, int precision, double tol) {
   Meta m = meta_of(meta);
   if (precision == AFV_PREC_MIXED) {
     cudaMemsetAsync(d32.phi, 0, sizeof(float) * plan.n_elem_g, stream);
-    vcycle_t(d32, mg, plan.max_lvl, true, true);
+    vcycle_t(d32, mg, plan.max_lvl, true, true, true);
     int nl = (int)plan.all_leaves.size();
     BoxSet bs{d_lists + all_leaves_off, 0, nl};
     with_nc(plan.dim, plan.nc, [&](auto d_, auto nc_) {
