@@ -100,6 +100,7 @@ def lib():
         ip = ctypes.POINTER(I)
         dp = ctypes.POINTER(Dd)
         llp = ctypes.POINTER(ctypes.c_longlong)
+        LL = ctypes.c_longlong
         sig = {
             "afv_last_error": (ctypes.c_char_p, []),
             "afv_version": (I, []),
@@ -119,6 +120,7 @@ def lib():
             "afv_forest_set_var": (I, [P, I, I, dp, I]),
             "afv_forest_get_var": (I, [P, I, I, dp, I]),
             "afv_forest_set_source": (I, [P, I, I, I, dp]),
+            "afv_forest_set_bc_faces": (I, [P, I, LL, ip, LL, dp]),
             "afv_forest_set_bc": (I, [P, I, I, I, I, dp]),
             "afv_forest_zero": (I, [P, I]),
             "afv_forest_sync": (I, [P]),
@@ -252,6 +254,32 @@ class Tree:
         _check(lib().afv_tree_level(self.h, lvl, _ip(sz), _ip(ids), _ip(lv), _ip(pa)))
         return ids[:sz[0]].copy(), lv[:sz[1]].copy(), pa[:sz[2]].copy()
 
+    def bc_faces(self):
+        """Physical-boundary faces in the order afv_forest_set_bc_faces takes
+        them: list of (id, face, centres), centres an (nc^(D-1), D) array of the
+        face-cell centres (first tangential index fastest)."""
+        b = self.boxes()
+        D = self.dim
+        out = []
+        for lvl in range(self.min_lvl, self.highest_lvl + 1):
+            ids, _, _ = self.level(lvl)
+            for i in ids:
+                k = int(i) - 1
+                nc, dr, rmin = int(b["n_cell"][k]), float(b["dr"][k]), b["r_min"][k]
+                for f in range(2 * D):
+                    if b["neighbors"][k, f] >= 0:
+                        continue
+                    dim, low = f // 2, f % 2 == 0
+                    tang = [e for e in range(D) if e != dim]
+                    idx = np.arange(1, nc + 1, dtype=np.float64)
+                    grids = np.meshgrid(*([idx] * (D - 1)), indexing="xy") if D == 3 else [idx]
+                    cen = np.empty((nc ** (D - 1), D))
+                    cen[:, dim] = rmin[dim] + ((0.5 if low else nc + 0.5) - 0.5) * dr
+                    for e, g in zip(tang, grids):
+                        cen[:, e] = rmin[e] + (g.ravel() - 0.5) * dr
+                    out.append((int(i), f, cen))
+        return out
+
     def n_cell_at(self, lvl):
         nc = self.info()["n_cell"]
         return nc if lvl >= 1 else nc >> (1 - lvl)
@@ -321,6 +349,13 @@ class Forest:
     def set_source(self, tree, gauss, lpl=False):
         g = np.ascontiguousarray(gauss, dtype=np.float64)
         _check(lib().afv_forest_set_source(self.h, tree, int(lpl), g.size // (2 + self.dim), _dp(g)))
+
+    def set_bc_faces(self, tree, bc_types, values):
+        """Sampled sides_bc hook: one AFV_BC_* per physical face and the face
+        values, in the order of Tree.bc_faces()."""
+        t = np.ascontiguousarray(bc_types, dtype=np.int32).ravel()
+        v = np.ascontiguousarray(values, dtype=np.float64).ravel()
+        _check(lib().afv_forest_set_bc_faces(self.h, tree, t.size, _ip(t), v.size, _dp(v)))
 
     def set_bc(self, tree, bc_type=AFV_BC_DIRICHLET, gauss=None, lpl=False):
         if gauss is None:

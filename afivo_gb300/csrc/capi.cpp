@@ -250,9 +250,39 @@ int afv_forest_set_bc(afv_forest* f, int tree, int bc_type, int src_lpl, int n_g
     afv::Plan& p = f->f.plan;
     if (tree < 0 || tree >= p.n_trees) return err = "tree index out of range", AFV_ERR_INVALID;
     afv::BcSpec& bc = p.bc[tree];
+    bc.per_face = false;
+    bc.face_type.clear();
+    bc.face_vals.clear();
     bc.type = bc_type;
     bc.src_lpl = src_lpl;
     bc.gauss.assign(gauss ? gauss : nullptr, gauss ? gauss + (size_t)n_gauss * (2 + p.dim) : nullptr);
+    afv::plan_fill_bc(p, tree);
+    afv::plan_build_desc(p);
+    return f->f.upload_bc(err);
+  });
+}
+
+int afv_forest_set_bc_faces(afv_forest* f, int tree, long long n_faces, const int* bc_type,
+                            long long n_values, const double* values) {
+  if (!f || n_faces < 0 || n_values < 0 || (n_faces > 0 && !bc_type) || (n_values > 0 && !values))
+    return fail(AFV_ERR_INVALID, "bad arguments");
+  return guarded([&](std::string& err) -> int {
+    afv::Plan& p = f->f.plan;
+    if (tree < 0 || tree >= p.n_trees) return err = "tree index out of range", AFV_ERR_INVALID;
+    long long nf = 0, nv = 0;
+    afv::plan_count_bc_faces(p, tree, nf, nv);
+    if (nf != n_faces || nv != n_values)
+      return err = "tree has " + std::to_string(nf) + " physical faces with " + std::to_string(nv) +
+                   " face cells, got " + std::to_string(n_faces) + " and " + std::to_string(n_values),
+             AFV_ERR_INVALID;
+    for (long long i = 0; i < n_faces; ++i)
+      if (bc_type[i] != AFV_BC_DIRICHLET && bc_type[i] != AFV_BC_NEUMANN)
+        return err = "unknown boundary condition at face " + std::to_string(i), AFV_ERR_INVALID;
+    afv::BcSpec& bc = p.bc[tree];
+    bc.per_face = true;
+    bc.gauss.clear();
+    bc.face_type.assign(bc_type, bc_type + n_faces);
+    bc.face_vals.assign(values, values + n_values);
     afv::plan_fill_bc(p, tree);
     afv::plan_build_desc(p);
     return f->f.upload_bc(err);

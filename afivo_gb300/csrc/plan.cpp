@@ -210,9 +210,37 @@ int build_plan(const std::vector<const HostTree*>& trees, Plan& p, std::string& 
   return AFV_OK;
 }
 
+void plan_count_bc_faces(const Plan& p, int t, long long& n_faces, long long& n_values) {
+  const int D = p.dim, NNB = 2 * D;
+  n_faces = n_values = 0;
+  for (int s : p.host_order[t])
+    for (int f = 0; f < NNB; ++f)
+      if (p.nb[(size_t)s * NNB + f] == -2) {
+        int ncl = p.nc_at(p.lvl[s]);
+        ++n_faces;
+        n_values += D == 2 ? ncl : (long long)ncl * ncl;
+      }
+}
+
 void plan_fill_bc(Plan& p, int t) {
   const int D = p.dim, NNB = 2 * D;
   const BcSpec& bc = p.bc[t];
+  // Caller-given records: position of each face in the caller's lists.
+  std::vector<long long> face_pos, val_pos;
+  if (bc.per_face) {
+    face_pos.assign(p.nb.size(), -1);
+    val_pos.assign(p.nb.size(), -1);
+    long long nf = 0, nv = 0;
+    for (int s : p.host_order[t])
+      for (int f = 0; f < NNB; ++f) {
+        size_t k = (size_t)s * NNB + f;
+        if (p.nb[k] != -2) continue;
+        int ncl = p.nc_at(p.lvl[s]);
+        face_pos[k] = nf++;
+        val_pos[k] = nv;
+        nv += D == 2 ? ncl : (long long)ncl * ncl;
+      }
+  }
   // Rebuild the value table: other trees' records are kept, this tree's
   // records are recomputed from its BcSpec.
   std::vector<double> vals;
@@ -228,6 +256,15 @@ void plan_fill_bc(Plan& p, int t) {
           newoff[k] = (long long)vals.size();
           vals.insert(vals.end(), p.bcval.begin() + p.bcoff[k], p.bcval.begin() + p.bcoff[k] + nfc);
         }
+        continue;
+      }
+      if (bc.per_face) {
+        int ncl = p.nc_at(p.lvl[s]);
+        long long nfc = D == 2 ? ncl : (long long)ncl * ncl;
+        p.bctype[k] = bc.face_type[face_pos[k]] == AFV_BC_NEUMANN ? 1 : 0;
+        newoff[k] = (long long)vals.size();
+        vals.insert(vals.end(), bc.face_vals.begin() + val_pos[k],
+                    bc.face_vals.begin() + val_pos[k] + nfc);
         continue;
       }
       p.bctype[k] = bc.type == AFV_BC_NEUMANN ? 1 : 0;

@@ -20,6 +20,12 @@ struct BcSpec {
   int type = AFV_BC_DIRICHLET;  // AFV_BC_DIRICHLET / AFV_BC_NEUMANN
   int src_lpl = 0;
   std::vector<double> gauss;    // empty: boundary value 0
+  // Per-face records given by the caller instead (a sampled sides_bc hook):
+  // one type per physical face and nc^(D-1) values per face, faces in the
+  // host exchange order (boxes of the level lists, faces low x first).
+  bool per_face = false;
+  std::vector<int> face_type;
+  std::vector<double> face_vals;
 };
 
 struct Plan {
@@ -65,5 +71,8 @@ void plan_fill_bc(Plan& p, int tree);
 
 // (Re)build the per-slot descriptors (after the tables or the boundary values change).
 void plan_build_desc(Plan& p);
+
+// Number of physical-boundary faces of one tree and of their face cells.
+void plan_count_bc_faces(const Plan& p, int tree, long long& n_faces, long long& n_values);
 
 }  // namespace afv

@@ -11,7 +11,7 @@ solve time. The same solve with FP64 V-cycles is timed beside it.
 
 --impl reference times the CPU oracle (the C++/OpenMP restatement of the
 reference's solver, oracle/) on all host cores, FP64 V-cycles on the same
-tree, one V-cycle per step. Under torchrun each rank solves its own replica
+tree, one solve to 1e-8 per step. Under torchrun each rank solves its own replica
 (one tree does not shard; there is no data-path collective).
 """
 import argparse
@@ -28,6 +28,13 @@ sys.path.insert(0, ROOT)
 import numpy as np  # noqa: E402
 
 TOL = 1e-8
+METRIC = "V-cycle unknowns/s, solve to 1e-8 relative residual"
+os.environ.setdefault("OMP_PROC_BIND", "close")
+
+
+def config_of(spec, cells, boxes):
+    return {"workload": spec["name"], "leaf_cells": int(cells), "boxes": int(boxes), "tol": TOL,
+            "step": "one solve from phi = 0", "l2": "inputs larger than L2 (no flush)"}
 
 
 def dist_setup(n_gpus):
@@ -143,63 +150,108 @@ def build_workload(spec):
     return tree, time.time() - t0
 
 
-def cpu_baseline_sample(spec, threads, cycles=2):
-    """Oracle FP64 V-cycles on the same tree, timed on the host cores."""
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    sys.path.insert(0, os.path.join(ROOT, "tests"))
-    import oracle as O
-    from helpers import oracle_tree
-    O.build()
-    O.set_threads(threads)
-    ot = oracle_tree(spec)
-    ot.fill_gauss(O.I_RHS, spec["gauss"], lpl=True)
-    ot.mg_init()
-    leaves = sum(len(ot.level(l)[1]) for l in range(ot.min_lvl, ot.highest_lvl + 1))
-    cells = leaves * spec["n_cell"] ** spec["dim"]
-    ot.vcycle(set_residual=False)  # warm-up
-    t0 = time.perf_counter()
-    for _ in range(cycles):
-        ot.vcycle(set_residual=False)
-    dt = time.perf_counter() - t0
-    return cells * cycles / dt, dt, cells
+class OracleSolver:
+    """The CPU oracle (C++/OpenMP restatement of the reference solver) on the
+    same tree and source: FP64 V-cycles from phi = 0 until the leaf residual
+    max |f - L phi| <= TOL * max |f|, the reference's own loop
+    (examples/poisson_basic_2d.f90:84-92)."""
+
+    def __init__(self, spec, threads):
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        import oracle as O
+        from helpers import oracle_tree
+        O.build()
+        O.set_threads(threads)
+        self.O = O
+        self.ot = oracle_tree(spec)
+        self.ot.fill_gauss(O.I_RHS, spec["gauss"], lpl=True)
+        self.ot.mg_init()
+        self.fmax = self.ot.max_abs(O.I_RHS)
+        nc, D = spec["n_cell"], spec["dim"]
+        self.leaves = sum(len(self.ot.level(l)[1]) for l in range(self.ot.min_lvl, self.ot.highest_lvl + 1))
+        self.boxes = sum(len(self.ot.level(l)[0]) for l in range(self.ot.min_lvl, self.ot.highest_lvl + 1))
+        self.cells = self.leaves * nc ** D
+
+    def solve(self, max_cycles=60):
+        """One solve; returns (V-cycles, seconds, relative residual)."""
+        O, ot = self.O, self.ot
+        ot.zero(O.I_PHI)
+        t0 = time.perf_counter()
+        for k in range(1, max_cycles + 1):
+            ot.vcycle(set_residual=True)
+            rel = ot.max_abs_residual() / self.fmax
+            if rel <= TOL:
+                break
+        return k, time.perf_counter() - t0, rel
+
+
+def cpu_baseline_sample(spec, threads, seconds=10.0):
+    """Oracle solves on the host cores for about `seconds`, after one warm-up
+    solve; value = median over solves of leaf cells x V-cycles / solve time."""
+    s = OracleSolver(spec, threads)
+    s.solve()
+    rates, total, n = [], 0.0, 0
+    while total < seconds or n < 5:
+        c, dt, _ = s.solve()
+        rates.append(s.cells * c / dt)
+        total += dt
+        n += 1
+    return statistics.median(rates), total, n, s
 
 
 def run_reference(args, spec):
     rank, world, local = dist_setup(args.gpus)
     if rank != 0:
         return
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    sys.path.insert(0, os.path.join(ROOT, "tests"))
-    import oracle as O
-    from helpers import oracle_tree
-    O.build()
     cores = os.cpu_count() or 1
-    O.set_threads(cores)
-    ot = oracle_tree(spec)
-    ot.fill_gauss(O.I_RHS, spec["gauss"], lpl=True)
-    ot.mg_init()
-    leaves = sum(len(ot.level(l)[1]) for l in range(ot.min_lvl, ot.highest_lvl + 1))
-    cells = leaves * spec["n_cell"] ** spec["dim"]
+    s = OracleSolver(spec, cores)
     for _ in range(args.warmup):
-        ot.vcycle(set_residual=False)
-    t0 = time.perf_counter()
+        s.solve()
+    cycles, secs, rels = [], [], []
     for _ in range(args.steps):
-        ot.vcycle(set_residual=False)
-    dt = time.perf_counter() - t0
-    value = cells * args.steps / dt
+        c, dt, rel = s.solve()
+        cycles.append(c)
+        secs.append(dt)
+        rels.append(rel)
+    total = sum(secs)
+    value = s.cells * sum(cycles) / total
     line = {
-        "impl": "reference", "metric": "V-cycle unknowns/s", "value": value, "unit": "unknowns/s",
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "unknowns/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "ms_per_step": total / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": spec["name"], "leaf_cells": cells, "cycle": "FAS V(2,2), FP64"},
+        "config": config_of(spec, s.cells, s.boxes),
+        "solve": {"cycles": cycles, "rel_res": max(rels),
+                  "ms_p50": float(np.percentile(secs, 50)) * 1e3,
+                  "ms_p99": float(np.percentile(secs, 99)) * 1e3},
         "cpu_baseline": {"value": value, "unit": "unknowns/s", "cores": cores, "kind": "port",
-                         "sample": f"{args.steps} FP64 V-cycles of the full tree (oracle, "
-                                   f"C++/OpenMP restatement of the reference solver)"},
+                         "sample": f"{args.steps} FP64 solves of the full tree to {TOL:g} "
+                                   f"(oracle: C++/OpenMP restatement of the reference solver, "
+                                   f"{cores} threads)"},
         "e2e": {"value": value, "unit": "unknowns/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
+
+
+def profile_solves(spec, n):
+    """n mixed solves of the workload with nothing timed: the command the
+    kernel profiles are taken on (few launches before the first V-cycle)."""
+    from afivo_gb300 import build as B
+    B.build()
+    import afivo_gb300 as afv
+    tree, _ = build_workload(spec)
+    forest = afv.Forest([tree], mixed=True)
+    forest.set_source(0, spec["gauss"], lpl=True)
+    for _ in range(n):
+        forest.zero(afv.AFV_PHI)
+        l0 = forest.launches()
+        cyc, rel, rc = forest.solve(afv.AFV_PREC_MIXED, tol=TOL, max_cycles=60, check=False)
+        print(f"solve: rc {rc}, cycles {int(cyc[0])}, rel {float(rel[0]):.3e}, "
+              f"launches {forest.launches() - l0}", flush=True)
+        if rc != 0:
+            raise SystemExit(1)
 
 
 def main():
@@ -210,11 +262,17 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--small", action="store_true", help="smaller tree (quick checks)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-solves", type=int, default=0,
+                    help="only run this many mixed solves, untimed (a short command to profile)")
     args = ap.parse_args()
     from afivo_gb300 import workloads as W
     spec = W.c2_poisson_3d(thr=3e-3, lvl_max=7) if args.small else W.c2_poisson_3d()
+    if args.small:
+        spec["name"] += "_thr3e-3_lvl7"
     if args.impl == "reference":
         return run_reference(args, spec)
+    if args.profile_solves:
+        return profile_solves(spec, args.profile_solves)
 
     rank, world, local = dist_setup(args.gpus)
     import torch
@@ -238,6 +296,9 @@ def main():
         return int(cyc[0]), float(rel[0])
 
     def timed(prec, steps, mask=0):
+        """`steps` solves between events on the forest's stream; mask != 0
+        turns on per-launch CUDA events of those kernel kinds (and so runs
+        the solve without graphs)."""
         forest.profile(mask)
         cycles, rels, per = [], [], []
         barrier(world)
@@ -262,24 +323,25 @@ def main():
         ms = ev0.elapsed_time(ev1)
         return ms, cycles, rels, per, forest.launches() - l0
 
-    # warm-up
     for _ in range(args.warmup):
         solve(afv.AFV_PREC_MIXED)
         solve(afv.AFV_PREC_FP64)
 
+    # headline: mixed solves, graphs on, nothing profiled
     with Clocks(local) as clk:
-        ms, cyc, rels, per, launches = timed(afv.AFV_PREC_MIXED, args.steps, mask=1 << 0)
-    sweep_n, sweep_ms, sweep_bytes = forest.profile_read(0)
+        ms, cyc, rels, per, launches = timed(afv.AFV_PREC_MIXED, args.steps)
     ms = max_over_ranks(ms, world)
-    total_cycles = sum_over_ranks(float(sum(cyc)), world)
-    value = cells * total_cycles / (ms / 1e3)
+    value = cells * sum_over_ranks(float(sum(cyc)), world) / (ms / 1e3)
 
-    ms64, cyc64, rels64, per64, _ = timed(afv.AFV_PREC_FP64, max(1, args.steps // 2))
+    ms64, cyc64, rels64, per64, _ = timed(afv.AFV_PREC_FP64, args.steps)
     ms64 = max_over_ranks(ms64, world)
     value64 = cells * sum_over_ranks(float(sum(cyc64)), world) / (ms64 / 1e3)
 
-    # per-kernel breakdown of one mixed solve (separate pass, all kinds profiled)
-    _, _, _, _, _ = timed(afv.AFV_PREC_MIXED, 1, mask=0xFF)
+    # roofline: one mixed solve with CUDA events around every sweep launch
+    timed(afv.AFV_PREC_MIXED, 1, mask=1 << 0)
+    sweep_n, sweep_ms, sweep_bytes = forest.profile_read(0)
+    # per-kernel breakdown: one mixed solve, every kind profiled
+    timed(afv.AFV_PREC_MIXED, 1, mask=0xFF)
     breakdown = {}
     for k, name in enumerate(afv.KERNEL_KINDS):
         n, kms, kb = forest.profile_read(k)
@@ -288,13 +350,12 @@ def main():
                                "GB/s": round(kb / (kms / 1e3) / 1e9, 1) if kms > 0 else None}
     forest.profile(0)
 
-    # end to end through the C ABI with host buffers
-    from afivo_gb300 import lib  # noqa: F401
+    # end to end through the C ABI: rhs in from pinned host memory, solution out
     n_in = forest._n_values(0, True)
     host_rhs = torch.empty(n_in, dtype=torch.float64, pin_memory=True)
     host_phi = torch.empty(n_in, dtype=torch.float64, pin_memory=True)
     forest.get_var(0, afv.AFV_RHS, interior_only=True, out=host_rhs.numpy())
-    e2e_ms, e2e_cycles = [], 0
+    e2e_cycles = 0
     barrier(world)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -313,32 +374,34 @@ def main():
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cores = os.cpu_count() or 1
-        v, dt, _ = cpu_baseline_sample(spec, cores, cycles=2)
+        v, dt, n, _s = cpu_baseline_sample(spec, cores)
         cpu = {"value": v, "unit": "unknowns/s", "cores": cores, "kind": "port",
-               "sample": f"2 FP64 V-cycles of the full tree on the oracle ({dt:.1f} s)"}
+               "sample": f"{n} FP64 solves of the full tree to {TOL:g} on the oracle "
+                         f"({dt:.1f} s, {cores} threads; median rate)"}
     if rank != 0:
         return
     line = {
-        "metric": "V-cycle unknowns/s (mixed FP32/FP64, to 1e-8 rel. residual)",
-        "value": value, "unit": "unknowns/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
-        "config": {"workload": spec["name"], "leaf_cells": cells, "boxes": info["n_boxes"],
-                   "levels": [info["min_lvl"], info["max_lvl"]], "tol": TOL,
-                   "cycle": "FAS V(2,2); FP32 cycles in FP64 defect correction",
-                   "l2": "inputs larger than L2 (device state %.0f MB)" % (info["bytes"] / 2 ** 20),
-                   "tree_build_s": round(t_build, 2)},
+        "metric": METRIC, "value": value, "unit": "unknowns/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+        "data": "synthetic",
+        "config": config_of(spec, cells, info["n_boxes"]),
+        "method": "mixed: FP32 FAS V(2,2) cycles inside FP64 defect correction; CUDA graphs",
         "solve": {"cycles": cyc, "rel_res": max(rels), "ms_p50": float(np.percentile(per, 50)),
                   "ms_p99": float(np.percentile(per, 99))},
         "fp64": {"value": value64, "unit": "unknowns/s", "cycles": cyc64, "rel_res": max(rels64),
                  "ms_per_solve": ms64 / len(cyc64)},
         "mixed_vs_fp64_solve_speedup": (ms64 / len(cyc64)) / (ms / args.steps),
-        "roofline": {"bound": "hbm", "kernel": "k_sweep<3,8,float>", "achieved": achieved,
-                     "peak": peak, "unit": "GB/s",
+        "roofline": {"bound": "hbm", "kernel": "k_level_tma<3,8,float,sweep>",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None,
                      "peak_kind": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
+                     "algorithmic_bytes": "12 B per cell of the swept level per half-sweep "
+                                          "(read phi, rhs; write phi; FP32)",
+                     "timed": "CUDA events around each sweep launch, one profiled mixed solve",
                      "launches": sweep_n, "ms": sweep_ms,
-                     "traffic": traffic.get("dram_bytes_per_launch") if traffic else None},
+                     "traffic": traffic.get("dram_bytes_per_launch") if traffic else None,
+                     "traffic_note": traffic.get("note") if traffic else None},
         "kernels": breakdown,
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": "unknowns/s", "h2d_bytes_per_step": n_in * 8,

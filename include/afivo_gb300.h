@@ -4,9 +4,11 @@
  *
  * Every entry point here replaces one routine of the Afivo reference's Fortran
  * API for this path; the citation beside each names it (file:line, paths
- * relative to the reference project). The Fortran module
- * fortran/m_afivo_gb300.f90 binds these functions through iso_c_binding
- * under the reference's own routine names.
+ * relative to the reference project). fortran/m_afivo_gb300.f90 binds these
+ * functions through iso_c_binding, and fortran/m_aX_gb300.f90 (expanded to
+ * modules m_a2_gb300 / m_a3_gb300) provides mg2_fas_vcycle, mg2_fas_fmg,
+ * mg3_fas_vcycle and mg3_fas_fmg with the reference's names and arguments
+ * on the reference's own tree type.
  *
  * Conventions
  *  - Every function returns AFV_OK (0) or a negative AFV_ERR_* code; it never
@@ -161,6 +163,16 @@ int afv_forest_set_source(afv_forest* f, int tree, int src_lpl, int n_gauss, con
  * centres (examples/poisson_basic_2d.f90:167-203). */
 int afv_forest_set_bc(afv_forest* f, int tree, int bc_type, int src_lpl, int n_gauss,
                       const double* gauss);
+/* The sides_bc hook of the reference (src/m_aX_t.f90:276-282), sampled on
+ * the host for every physical-boundary face of one tree: bc_type[i] (AFV_BC_*)
+ * and nc^(D-1) boundary values per face, in the order of the ghost cells
+ * cc(0, 1:nc[, 1:nc]) etc. (first tangential index fastest). Faces are listed
+ * box by box in the host exchange order, faces of a box low x, high x, low y,
+ * ... and only those whose neighbour is < 0. n_faces and n_values must match
+ * the tree. Used by bc_to_gc (src/m_aX_gc.f90:71-132) as the reference uses
+ * the hook's output. */
+int afv_forest_set_bc_faces(afv_forest* f, int tree, long long n_faces, const int* bc_type,
+                            long long n_values, const double* values);
 int afv_forest_zero(afv_forest* f, int var);
 int afv_forest_sync(afv_forest* f);
 /* No counterpart in the reference: the cudaStream_t that orders this

@@ -140,7 +140,8 @@ struct RefCrit {
 
 // Boundary-value kinds standing in for the user's sides_bc hook
 // (src/m_aX_t.f90:276-282).
-enum BcKind { BC_DIRICHLET_ZERO = 0, BC_NEUMANN_ZERO = 1, BC_DIRICHLET_GAUSS = 2 };
+enum BcKind { BC_DIRICHLET_ZERO = 0, BC_NEUMANN_ZERO = 1, BC_DIRICHLET_GAUSS = 2,
+              BC_TABLE = 3 /* per (box, face) type and values, as a hook might return */ };
 
 template <int D> struct Tree {
   static constexpr int NCH = 1 << D, NNB = 2 * D;
@@ -161,6 +162,11 @@ struct MG {
   int n_cycle_down = 2, n_cycle_up = 2, n_cycle_base = 2;
   int bc_kind = BC_DIRICHLET_ZERO;
   std::vector<double> bc_gauss;
+  // BC_TABLE: per (id, face) the bc type and the offset of its face values
+  // (first tangential index fastest); indexed by id * 2D + (nb - 1).
+  std::vector<int> tab_type;
+  std::vector<long long> tab_off;
+  std::vector<double> tab_vals;
   bool initialized = false;
 };
 
@@ -753,16 +759,20 @@ template <int D> double& face_ghost(Box<D>& b, int nb, int a, int c) {
 // The user's sides_bc hook: writes the boundary value b into the ghost face and
 // returns the type (a$D_bc_dirichlet_zero / a$D_bc_neumann_zero, gc:361-378;
 // the position-dependent form of examples/poisson_basic_2d.f90:167-203).
-template <int D> int sides_bc(Box<D>& b, int nb, int iv, const MG& mg) {
+template <int D> int sides_bc(Box<D>& b, int id, int nb, int iv, const MG& mg) {
   using T = Topo<D>;
   int nc = b.n_cell;
   int vol = b.nvol();
   int bc_type = (mg.bc_kind == BC_NEUMANN_ZERO) ? a5_bc_neumann : a5_bc_dirichlet;
+  size_t tk = (size_t)id * T::NNB + (nb - 1);
+  if (mg.bc_kind == BC_TABLE) bc_type = mg.tab_type[tk];
   int cmax = (D == 3) ? nc : 1;
   for (int c = 1; c <= cmax; ++c)
     for (int a = 1; a <= nc; ++a) {
       double val = 0.0;
-      if (mg.bc_kind == BC_DIRICHLET_GAUSS) {
+      if (mg.bc_kind == BC_TABLE) {
+        val = mg.tab_vals[mg.tab_off[tk] + (size_t)(c - 1) * nc + (a - 1)];
+      } else if (mg.bc_kind == BC_DIRICHLET_GAUSS) {
         // Face centre: a$D_rr_cc with 0.5 or nc+0.5 in the normal direction.
         double rr[3];
         int d = T::neighb_dim(nb);
@@ -943,7 +953,7 @@ template <int D> void gc_box(Tree<D>& t, int id, int iv, const MG& mg) {
     } else if (nb_id == a5_no_box) {
       sides_rb(t, id, nb, iv);
     } else {
-      int bc_type = sides_bc(t.boxes[id], nb, iv, mg);
+      int bc_type = sides_bc(t.boxes[id], id, nb, iv, mg);
       bc_to_gc(t.boxes[id], nb, iv, bc_type);
     }
   }
@@ -1496,8 +1506,28 @@ void orc_set_level_cc(OrcHandle* h, int lvl, int iv, double* in) {
     level_cc<3>(TT<3>(h), lvl, iv, in, false);
 }
 
+// cc(..., iv) := 0 on every box of every level, ghosts included
+// (a$D_box_clear_cc, src/m_aX_utils.f90:262-270, on all boxes).
+void orc_zero_var(OrcHandle* h, int iv);
+
 // rhs (or any iv) := sum of Gaussians at the cell centres of every box.
 }  // extern "C"
+template <int D> static void zero_var(Tree<D>& t, int iv) {
+  for (int lvl = t.min_lvl; lvl <= t.highest_lvl; ++lvl) {
+    const std::vector<int>& ids = t.L(lvl).ids;
+#pragma omp parallel for
+    for (int n = 0; n < (int)ids.size(); ++n) {
+      Box<D>& b = t.boxes[ids[n]];
+      std::fill(b.cc.begin() + (size_t)iv * b.nvol(), b.cc.begin() + (size_t)(iv + 1) * b.nvol(), 0.0);
+    }
+  }
+}
+extern "C" void orc_zero_var(OrcHandle* h, int iv) {
+  if (h->dim == 2)
+    zero_var<2>(TT<2>(h), iv);
+  else
+    zero_var<3>(TT<3>(h), iv);
+}
 template <int D> static void fill_gauss(Tree<D>& t, int iv, int lpl, const std::vector<double>& g) {
   for (int lvl = t.min_lvl; lvl <= t.highest_lvl; ++lvl) {
     const std::vector<int>& ids = t.L(lvl).ids;
@@ -1540,6 +1570,29 @@ void orc_mg_init(OrcHandle* h, int n_down, int n_up, int n_base, int bc_kind, in
   mg.bc_kind = bc_kind;
   mg.bc_gauss.assign(gauss ? gauss : nullptr, gauss ? gauss + (size_t)n_gauss * (2 + h->dim) : nullptr);
   mg.initialized = true;
+}
+
+// Per-face boundary records for BC_TABLE: face i is (ids[i], faces[i]
+// 0-based), its type types[i] (a5_bc_dirichlet / a5_bc_neumann) and nc^(D-1)
+// values of that box's n_cell, consecutive in face order.
+void orc_mg_set_bc_table(OrcHandle* h, int n_faces, const int* ids, const int* faces,
+                         const int* types, const double* values) {
+  MG& mg = h->mg;
+  int D = h->dim, NNB = 2 * D;
+  int hid = D == 2 ? TT<2>(h).highest_id : TT<3>(h).highest_id;
+  mg.tab_type.assign((size_t)(hid + 1) * NNB, a5_bc_dirichlet);
+  mg.tab_off.assign((size_t)(hid + 1) * NNB, -1);
+  mg.tab_vals.clear();
+  for (int i = 0; i < n_faces; ++i) {
+    int nc = D == 2 ? TT<2>(h).boxes[ids[i]].n_cell : TT<3>(h).boxes[ids[i]].n_cell;
+    size_t k = (size_t)ids[i] * NNB + faces[i];
+    mg.tab_type[k] = types[i];
+    mg.tab_off[k] = (long long)mg.tab_vals.size();
+    long long nfc = D == 2 ? nc : (long long)nc * nc;
+    mg.tab_vals.insert(mg.tab_vals.end(), values, values + nfc);
+    values += nfc;
+  }
+  mg.bc_kind = BC_TABLE;
 }
 
 void orc_vcycle(OrcHandle* h, int highest_lvl, int set_residual) {

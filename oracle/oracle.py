@@ -21,7 +21,7 @@ _SO = os.path.join(_HERE, "_build", "libafivo_oracle.so")
 
 I_PHI, I_RHS, I_TMP = 0, 1, 2
 REF_UNIFORM, REF_GAUSS, REF_RANDOM, REF_RANDOM_RM = 0, 1, 2, 3
-BC_DIRICHLET_ZERO, BC_NEUMANN_ZERO, BC_DIRICHLET_GAUSS = 0, 1, 2
+BC_DIRICHLET_ZERO, BC_NEUMANN_ZERO, BC_DIRICHLET_GAUSS, BC_TABLE = 0, 1, 2, 3
 
 _lib = None
 
@@ -57,6 +57,8 @@ def lib():
         L.orc_fill_gauss.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, dp]
         L.orc_mg_init.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                   ctypes.c_int, dp]
+        L.orc_zero_var.argtypes = [P, ctypes.c_int]
+        L.orc_mg_set_bc_table.argtypes = [P, ctypes.c_int, ip, ip, ip, dp]
         L.orc_vcycle.argtypes = [P, ctypes.c_int, ctypes.c_int]
         L.orc_fmg.argtypes = [P, ctypes.c_int, ctypes.c_int]
         L.orc_gsrb_level.argtypes = [P, ctypes.c_int, ctypes.c_int]
@@ -189,6 +191,16 @@ class OracleTree:
         n_g = 0 if bc_gauss is None else g.size // (2 + self.dim)
         lib().orc_mg_init(self.h, n_down, n_up, n_base, bc_kind, n_g, _dp(g))
 
+    def set_bc_table(self, ids, faces, types, values):
+        """Per-face boundary records (kind BC_TABLE): face i of box ids[i]
+        (0-based face), type types[i] (-1 Dirichlet, -2 Neumann), values of all
+        faces concatenated (first tangential index fastest)."""
+        ids = np.ascontiguousarray(ids, dtype=np.int32)
+        faces = np.ascontiguousarray(faces, dtype=np.int32)
+        types = np.ascontiguousarray(types, dtype=np.int32)
+        v = np.ascontiguousarray(values, dtype=np.float64)
+        lib().orc_mg_set_bc_table(self.h, ids.size, _ip(ids), _ip(faces), _ip(types), _dp(v))
+
     def vcycle(self, highest_lvl=None, set_residual=True):
         hl = self.highest_lvl if highest_lvl is None else highest_lvl
         lib().orc_vcycle(self.h, hl, int(set_residual))
@@ -213,6 +225,9 @@ class OracleTree:
 
     def residual_all(self):
         lib().orc_residual_all(self.h)
+
+    def zero(self, iv):
+        lib().orc_zero_var(self.h, iv)
 
     def max_abs_residual(self):
         L = lib()

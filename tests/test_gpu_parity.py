@@ -106,6 +106,47 @@ def test_dirichlet_values(gpu):
     assert_state(gpu, f, ot, spec)
 
 
+def _bc_table(tree):
+    """Mixed per-face boundary records: Neumann with a smooth flux on x
+    faces, Dirichlet with smooth values on y (and z) faces."""
+    ids, faces, types, vals = [], [], [], []
+    for i, fc, cen in tree.bc_faces():
+        ids.append(i)
+        faces.append(fc)
+        types.append(-2 if fc // 2 == 0 else -1)
+        vals.append(np.sin(3.0 * cen[:, 0]) + np.cos(2.0 * cen[:, 1]) * (0.5 if fc % 2 else -1.0))
+    return ids, faces, types, np.concatenate(vals)
+
+
+def test_bc_faces_hook(gpu):
+    """A sampled sides_bc hook with a type and values per face
+    (afv_forest_set_bc_faces) against the oracle's hook returning the same."""
+    spec = W.c1_poisson_2d()
+    f, ot, pt = setup_pair(gpu, spec)
+    ids, faces, types, vals = _bc_table(pt)
+    ot.set_bc_table(ids, faces, types, vals)
+    f.set_bc_faces(0, types, vals)
+    for _ in range(3):
+        ot.vcycle()
+        f.vcycle()
+        assert_state(gpu, f, ot, spec)
+    ot.fmg(set_residual=True, have_guess=True)
+    f.fmg(set_residual=True, have_guess=True)
+    assert_state(gpu, f, ot, spec)
+
+
+def test_bc_faces_hook_3d(gpu):
+    spec = W.c2_poisson_3d(thr=3e-3, lvl_max=5)
+    f, ot, pt = setup_pair(gpu, spec)
+    ids, faces, types, vals = _bc_table(pt)
+    ot.set_bc_table(ids, faces, types, vals)
+    f.set_bc_faces(0, types, vals)
+    for _ in range(2):
+        ot.vcycle()
+        f.vcycle()
+        assert_state(gpu, f, ot, spec)
+
+
 def test_neumann(gpu):
     spec = dict(W.c3_uniform_2d(4), nb=[[-1] * 4], n_cell=8, dr=1 / 8, name="neumann")
     ot = oracle_tree(spec)

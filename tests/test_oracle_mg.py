@@ -66,3 +66,24 @@ def test_manufactured_solution_second_order(oracle_lib):
             err = max(err, np.abs(phi[n] - u).max())
         errs.append(err)
     assert errs[0] / errs[1] > 3.5 and errs[1] / errs[2] > 3.5, errs
+
+
+def test_bc_table_matches_builtin_hooks(oracle_lib):
+    """Per-face records that restate a built-in hook give the same bits."""
+    spec = W.c1_poisson_2d()
+    for kind, typ in ((O.BC_DIRICHLET_ZERO, -1), (O.BC_NEUMANN_ZERO, -2)):
+        a = oracle_tree(spec)
+        b = oracle_tree(spec)
+        for t in (a, b):
+            t.fill_gauss(O.I_RHS, spec["gauss"], lpl=True)
+        a.mg_init(bc_kind=kind)
+        b.mg_init()
+        pt = W.build_tree(spec)
+        fl = pt.bc_faces()
+        b.set_bc_table([x[0] for x in fl], [x[1] for x in fl], [typ] * len(fl),
+                       np.zeros(sum(len(x[2]) for x in fl)))
+        for _ in range(2):
+            a.vcycle()
+            b.vcycle()
+        for lvl in range(a.min_lvl, a.highest_lvl + 1):
+            assert np.array_equal(a.get_level(lvl, O.I_PHI, 8), b.get_level(lvl, O.I_PHI, 8))
