@@ -130,6 +130,7 @@ def lib():
             "afv_mg_fas_fmg": (I, [P, ctypes.POINTER(MgOpts), I, I]),
             "afv_gc_tree": (I, [P]),
             "afv_tree_max_abs_cc": (I, [P, I, I, dp]),
+            "afv_tree_max_abs_cc_noalloc": (I, [P, I, I, dp]),
             "afv_mg_solve": (I, [P, ctypes.POINTER(MgOpts), I, Dd, I, ip, dp]),
             "afv_mg_gsrb_level": (I, [P, I, I]),
             "afv_fill_gc_level": (I, [P, I]),
@@ -395,6 +396,12 @@ class Forest:
     def max_abs(self, tree, var):
         out = ctypes.c_double(0)
         _check(lib().afv_tree_max_abs_cc(self.h, tree, var, ctypes.byref(out)))
+        return out.value
+
+    def max_abs_noalloc(self, tree, var):
+        """max_abs with static device scratch: allocates nothing (forests of <= 1024 trees)."""
+        out = ctypes.c_double(0)
+        _check(lib().afv_tree_max_abs_cc_noalloc(self.h, tree, var, ctypes.byref(out)))
         return out.value
 
     def solve(self, precision=AFV_PREC_FP64, tol=1e-8, max_cycles=50, mg=None, check=True):

@@ -342,6 +342,11 @@ int afv_tree_max_abs_cc(afv_forest* f, int tree, int var, double* out) {
   FOREST_CALL(f, return f->f.max_abs(tree, var, out, err));
 }
 
+int afv_tree_max_abs_cc_noalloc(afv_forest* f, int tree, int var, double* out) {
+  if (!out) return fail(AFV_ERR_INVALID, "out is NULL");
+  FOREST_CALL(f, return f->f.max_abs_static(tree, var, out, err));
+}
+
 int afv_mg_solve(afv_forest* f, const afv_mg_opts* mg, int precision, double tol, int max_cycles,
                  int* cycles, double* rel_res) {
   if (precision != AFV_PREC_FP64 && precision != AFV_PREC_MIXED)

@@ -138,6 +138,8 @@ class Forest {
   int fmg(const MgOpts& mg, bool set_residual, bool have_guess, std::string& err);
   int gc_tree(std::string& err);
   int max_abs(int tree, int var, double* out, std::string& err);
+  // max_abs with its scratch in static device memory (noalloc.cuh)
+  int max_abs_static(int tree, int var, double* out, std::string& err);
   int solve(const MgOpts& mg, int precision, double tol, int max_cycles, SolveStats& st,
             std::string& err);
 

@@ -975,3 +975,5 @@ int Forest::solve(const MgOpts& mg, int precision, double tol, int max_cycles, S
 }
 
 }  // namespace afv
+
+#include "noalloc.cuh"  // Forest::max_abs_static

@@ -192,6 +192,19 @@ int afv_gc_tree(afv_forest* f);
 /* max(|a$D_tree_min_cc|, |a$D_tree_max_cc|) over leaf interiors,
  * src/m_aX_utils.f90:468-571. */
 int afv_tree_max_abs_cc(afv_forest* f, int tree, int var, double* out);
+/* afv_tree_max_abs_cc without any allocation (no counterpart in the
+ * reference): the reduction scratch is a static device array of 536,576
+ * bytes per device, which limits it to forests of at most 1024 trees
+ * (larger ones get AFV_ERR_INVALID). The first call on a device takes the
+ * array's address (cudaGetSymbolAddress) and should come before any stream
+ * capture; every call clears the scratch it uses on the forest's stream.
+ * Calls that overlap in time on one device (two host threads, or two forests
+ * on different streams) share the scratch and race: serialise them. For
+ * callers that cannot allocate at the time of the call: a request loop whose
+ * device memory is fully committed to admitted trees, where an allocation
+ * would fail, and loops that poll a norm often, where every cudaMalloc and
+ * cudaFree would synchronise the device. */
+int afv_tree_max_abs_cc_noalloc(afv_forest* f, int tree, int var, double* out);
 /* Solve every tree to max|rhs - L phi| <= tol * max|rhs| over its leaves,
  * from the current phi, with FP64 V-cycles (AFV_PREC_FP64) or FP64 defect
  * correction around FP32 V-cycles (AFV_PREC_MIXED). cycles[t] and rel_res[t]
