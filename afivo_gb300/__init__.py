@@ -40,6 +40,7 @@ AFV_PHI, AFV_RHS, AFV_TMP = 0, 1, 2
 AFV_BC_DIRICHLET, AFV_BC_NEUMANN = -1, -2
 AFV_REF_UNIFORM, AFV_REF_SOURCE, AFV_REF_RANDOM, AFV_REF_RANDOM_RM = 0, 1, 2, 3
 AFV_PREC_FP64, AFV_PREC_MIXED = 0, 1
+AFV_OPT_SWEEP_KERNEL, AFV_OPT_GRAPHS = 0, 1
 KERNEL_KINDS = ("sweep", "fill", "restrict", "coarse_rhs", "correct", "residual", "defect",
                 "accumulate")
 
@@ -130,6 +131,9 @@ def lib():
             "afv_mg_fas_fmg": (I, [P, ctypes.POINTER(MgOpts), I, I]),
             "afv_gc_tree": (I, [P]),
             "afv_tree_max_abs_cc": (I, [P, I, I, dp]),
+            "afv_forest_profile_entries": (I, [P, LL, ip, ip, dp, dp, llp]),
+            "afv_forest_set_option": (I, [P, I, I]),
+            "afv_forest_get_option": (I, [P, I, ip]),
             "afv_tree_max_abs_cc_noalloc": (I, [P, I, I, dp]),
             "afv_mg_solve": (I, [P, ctypes.POINTER(MgOpts), I, Dd, I, ip, dp]),
             "afv_mg_gsrb_level": (I, [P, I, I]),
@@ -434,6 +438,26 @@ class Forest:
     # event profiler
     def profile(self, mask):
         _check(lib().afv_forest_profile(self.h, mask))
+
+    def set_option(self, option, value):
+        _check(lib().afv_forest_set_option(self.h, option, int(value)))
+
+    def get_option(self, option):
+        v = ctypes.c_int(0)
+        _check(lib().afv_forest_get_option(self.h, option, ctypes.byref(v)))
+        return v.value
+
+    def profile_entries(self):
+        """Profiled launches one by one: dict of arrays kind, level, ms, bytes."""
+        n = ctypes.c_longlong(0)
+        _check(lib().afv_forest_profile_entries(self.h, 0, None, None, None, None, ctypes.byref(n)))
+        m = max(int(n.value), 1)
+        kind, level = np.zeros(m, np.int32), np.zeros(m, np.int32)
+        ms, by = np.zeros(m), np.zeros(m)
+        _check(lib().afv_forest_profile_entries(self.h, m, _ip(kind), _ip(level), _dp(ms), _dp(by),
+                                                ctypes.byref(n)))
+        k = int(n.value)
+        return dict(kind=kind[:k], level=level[:k], ms=ms[:k], bytes=by[:k])
 
     def profile_read(self, kind):
         n, ms, b = ctypes.c_longlong(0), ctypes.c_double(0), ctypes.c_double(0)

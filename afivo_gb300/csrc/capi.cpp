@@ -401,4 +401,39 @@ int afv_forest_profile_read(afv_forest* f, int kind, long long* launches, double
   });
 }
 
+int afv_forest_profile_entries(afv_forest* f, long long max, int* kind, int* level, double* ms,
+                               double* algorithmic_bytes, long long* n_total) {
+  if (!n_total || (max > 0 && (!kind || !level || !ms || !algorithmic_bytes)))
+    return fail(AFV_ERR_INVALID, "NULL argument");
+  FOREST_CALL(f, {
+    (void)err;
+    *n_total = f->f.prof_entries(max, kind, level, ms, algorithmic_bytes);
+    return AFV_OK;
+  });
+}
+
+int afv_forest_set_option(afv_forest* f, int option, int value) {
+  if (!f) return fail(AFV_ERR_INVALID, "forest is NULL");
+  switch (option) {
+    case AFV_OPT_SWEEP_KERNEL:
+      if (value < 0 || value > 2) return fail(AFV_ERR_INVALID, "sweep kernel must be 0, 1 or 2");
+      f->f.sweep_kernel = value;
+      return AFV_OK;
+    case AFV_OPT_GRAPHS:
+      f->f.use_graphs = value != 0;
+      f->f.drop_graphs();
+      return AFV_OK;
+  }
+  return fail(AFV_ERR_INVALID, "unknown option");
+}
+
+int afv_forest_get_option(afv_forest* f, int option, int* value) {
+  if (!f || !value) return fail(AFV_ERR_INVALID, "NULL argument");
+  switch (option) {
+    case AFV_OPT_SWEEP_KERNEL: *value = f->f.sweep_kernel; return AFV_OK;
+    case AFV_OPT_GRAPHS: *value = f->f.use_graphs ? 1 : 0; return AFV_OK;
+  }
+  return fail(AFV_ERR_INVALID, "unknown option");
+}
+
 }  // extern "C"

@@ -2,6 +2,7 @@
 // one 128-byte record that a bulk copy brings into shared memory together
 // with the box's cells.
 #pragma once
+#include <cstddef>
 
 namespace afv {
 
@@ -33,5 +34,9 @@ struct alignas(16) SlotDesc {
   int pad1;
 };
 static_assert(sizeof(SlotDesc) == 128, "SlotDesc must be 128 bytes");
+// Kernels read these fields as 32-bit words (word = byte offset / 4).
+static_assert(offsetof(SlotDesc, nbo) == 0 && offsetof(SlotDesc, code) == 48 &&
+                  offsetof(SlotDesc, qd) == 56 && offsetof(SlotDesc, tree) == 60,
+              "SlotDesc field offsets");
 
 }  // namespace afv

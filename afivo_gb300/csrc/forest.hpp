@@ -57,6 +57,7 @@ enum ProfKind {
 struct ProfEntry {
   cudaEvent_t start, stop;
   int kind;
+  int level;     // level the launch works on (parents' level for coarse_rhs / correct)
   double bytes;  // algorithmic bytes of the launch
 };
 
@@ -71,6 +72,7 @@ class Forest {
   Plan plan;
   int device = 0;
   int n_sm = 148;
+  int sweep_kernel = 1;  // 0: block-pipelined k_level_tma, 1: warp-per-box k_sweep_warp
   cudaStream_t stream = nullptr;
   DevMeta meta;
   Arrays<double> d64;
@@ -108,12 +110,14 @@ class Forest {
   // event profiler: when enabled, launches of the selected kinds (bit mask)
   // are bracketed by CUDA events on the forest's stream
   int prof_mask = 0;
+  int prof_level = 0;  // level tag of the next profiled launches
   long long n_launches = 0;  // every kernel launched on the stream
   std::vector<ProfEntry> prof;
   std::vector<cudaEvent_t> event_pool;
   cudaEvent_t prof_begin(int kind);
   void prof_end(cudaEvent_t start, int kind, double bytes);
   int prof_read(int kind, long long* launches, double* ms, double* bytes);
+  long long prof_entries(long long max, int* kind, int* level, double* ms, double* bytes);
   void prof_reset();
 
   ~Forest();
@@ -171,6 +175,7 @@ class Forest {
     return (l < plan.min_lvl || l > plan.max_lvl) ? 0 : plan.lvl_n[plan.L(l)];
   }
   int* leaves_list(int l) { return d_lists + leaves_off[plan.L(l)]; }
+  dev_BoxSet level_set(int l) const;  // all boxes of level l (a slot range)
   int* parents_list(int l) { return d_lists + parents_off[plan.L(l)]; }
   int n_leaves(int l) const { return (int)plan.leaves[plan.L(l)].size(); }
   int n_parents(int l) const {

@@ -28,6 +28,8 @@ struct BoxSet {
   const int* list;  // slot list, or nullptr for the range [lo, lo+n)
   int lo;
   int n;
+  long long g0, i0;  // range: offg and offi of slot lo (a level's boxes are stored
+                     // consecutively, so box i of the range is at g0 + i * SG)
 };
 
 struct Meta {
@@ -44,6 +46,16 @@ struct Meta {
 };
 
 __device__ __forceinline__ int box_at(const BoxSet& s, int i) { return s.list ? s.list[i] : s.lo + i; }
+// Storage offsets of box i (slot s) of a set: arithmetic for ranges, a table
+// load for lists.
+template <int SG>
+__device__ __forceinline__ long long box_offg(const Meta& m, const BoxSet& bs, int i, int s) {
+  return bs.list ? m.offg[s] : bs.g0 + (long long)i * SG;
+}
+template <int SI>
+__device__ __forceinline__ long long box_offi(const Meta& m, const BoxSet& bs, int i, int s) {
+  return bs.list ? m.offi[s] : bs.i0 + (long long)i * SI;
+}
 
 template <int D, int NC>
 struct Geo {
@@ -192,6 +204,13 @@ __device__ __forceinline__ T ghost_value(const Meta& m, const SlotDesc& d, const
   return bc_value<T>(code, f, b, own(F.ai, F.aj, F.ak), Sc<T>::dr(d));
 }
 
+// Programmatic dependent launch: every kernel may be scheduled while the
+// previous kernel on its stream drains; pdl_wait() returns once that kernel
+// has finished and its writes are visible, pdl_trigger() lets the next kernel
+// be scheduled. Both are no-ops for a launch without the attribute.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 // ---------------------------------------------------------------------------
 // Bulk copies (TMA, cp.async.bulk) into shared memory, completed on mbarriers.
 // Every wait is bounded by a clock budget; a kernel that gives up records it in
@@ -223,6 +242,16 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned by
           smem_addr(dst)),
       "l"(src), "r"(bytes), "r"(smem_addr(bar))
       : "memory");
+}
+// Per-thread asynchronous 16-byte copies global -> shared (cp.async), grouped
+// per thread and waited for with cp.async.wait_group.
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 // try_wait with a suspend-time hint (ns): the warp sleeps until the phase
 // completes or the hint elapses instead of spinning.
@@ -306,6 +335,8 @@ struct LevelCfg {
 template <int D, int NC, class T, int MODE>
 __global__ void __launch_bounds__(kThreads)
 k_level_tma(Meta m, BoxSet bs, T* __restrict__ phi, const T* __restrict__ rhs, int n, int pull, int homog) {
+  pdl_wait();
+  pdl_trigger();
   using C = LevelCfg<D, NC, T, MODE>;
   using G = Geo<D, NC>;
   constexpr int S = C::S;
@@ -388,9 +419,10 @@ k_level_tma(Meta m, BoxSet bs, T* __restrict__ phi, const T* __restrict__ rhs, i
     if (!bs.list) {  // consecutive slots: consecutive storage
       const int s0 = bs.lo + first;
       bulk_g2s(sp, m.desc + s0, nb * (unsigned)sizeof(SlotDesc), b);
-      bulk_g2s(sp + C::DESC_B, phi + m.offg[s0], nb * (unsigned)(G::SG * sizeof(T)), b);
+      bulk_g2s(sp + C::DESC_B, phi + bs.g0 + (long long)first * G::SG, nb * (unsigned)(G::SG * sizeof(T)), b);
       if constexpr (SWEEP)
-        bulk_g2s(sp + C::DESC_B + C::PHI_B, rhs + m.offi[s0], nb * (unsigned)(G::SI * sizeof(T)), b);
+        bulk_g2s(sp + C::DESC_B + C::PHI_B, rhs + bs.i0 + (long long)first * G::SI,
+                 nb * (unsigned)(G::SI * sizeof(T)), b);
     } else {
       for (int q = 0; q < nb; ++q) {
         const int s = bs.list[first + q];
@@ -540,6 +572,297 @@ k_level_tma(Meta m, BoxSet bs, T* __restrict__ phi, const T* __restrict__ rhs, i
   }
 }
 
+// ---------------------------------------------------------------------------
+// Warp-per-box GSRB half-sweep (mg$D_box_gsrb_lpl, src/m_aX_mg.f90:718-760).
+//
+// Each warp owns a ring of S shared-memory stages and streams its own boxes
+// (global warp w takes boxes w, w + total warps, ...) through it: lane 0
+// issues the bulk copies of descriptor and phi S-1 boxes ahead, and all lanes
+// wait on the stage's mbarrier. No block barrier: the warp's lanes pull the
+// ghost cells this colour reads into the staged box (the same values as in
+// k_level_tma), __syncwarp, then update the box's cells of the colour (CPL per
+// lane) and store them. The ghost sources and the rhs values of a box are
+// loaded into registers two boxes ahead, from its descriptor read straight
+// from global memory four boxes ahead, so no load latency sits on the path.
+// ---------------------------------------------------------------------------
+template <int D, int NC, class T, int W, int S>
+struct WarpCfg {
+  using G = Geo<D, NC>;
+  static constexpr int UPD = G::SI / 2;             // cells of one colour
+  static constexpr int CPL = (UPD + 31) / 32;       // per lane
+  static constexpr int NEED = 2 * D * (G::NF / 2);  // ghost cells this colour reads
+  static constexpr int GPL = (NEED + 31) / 32;      // per lane
+  static constexpr int PHI_OFF = (int)sizeof(SlotDesc);
+  static constexpr int BOX_B = PHI_OFF + G::SG * (int)sizeof(T);  // rhs goes to registers
+  static constexpr int SMEM_B = W * S * BOX_B;
+  static_assert(BOX_B % 16 == 0, "bulk copy alignment");
+};
+
+// Fields of a SlotDesc held as one 32-bit word per lane (lane q: bytes 4q..4q+3).
+struct DescWords {
+  static __device__ __forceinline__ long long nbo(unsigned w, int f) {
+    const unsigned lo = __shfl_sync(0xffffffffu, w, 2 * f);
+    const unsigned hi = __shfl_sync(0xffffffffu, w, 2 * f + 1);
+    return (long long)(((unsigned long long)hi << 32) | lo);
+  }
+  static __device__ __forceinline__ int code(unsigned w, int f) {
+    const unsigned x = __shfl_sync(0xffffffffu, w, 12 + (f >> 2));
+    return (int)(signed char)((x >> (8 * (f & 3))) & 0xffu);
+  }
+  static __device__ __forceinline__ int qd(unsigned w) { return (int)__shfl_sync(0xffffffffu, w, 14); }
+  static __device__ __forceinline__ int tree(unsigned w) { return (int)__shfl_sync(0xffffffffu, w, 15); }
+};
+
+template <int D, int NC, class T, int W, int S, int ASYNC>
+__global__ void __launch_bounds__(W * 32)
+k_sweep_warp(Meta m, BoxSet bs, T* __restrict__ phi, const T* __restrict__ rhs, int n, int pull,
+             int homog) {
+  pdl_wait();
+  pdl_trigger();
+  using C = WarpCfg<D, NC, T, W, S>;
+  using G = Geo<D, NC>;
+  static_assert(S >= 2, "at least two stages");
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ __align__(8) unsigned long long bar[W][S];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int gw = (int)blockIdx.x * W + wid, nw = (int)gridDim.x * W;
+  const int nbx = bs.n;
+  if (gw >= nbx) return;
+  const int my_boxes = (nbx - 1 - gw) / nw + 1;
+  unsigned char* ring = smem + (size_t)wid * S * C::BOX_B;
+  if (lane == 0) {
+    for (int st = 0; st < S; ++st) mbar_init(&bar[wid][st], 1);
+    fence_mbar_init();
+  }
+  __syncwarp();
+
+  // Per-lane constants: ghost items and updated cells.
+  int it_f[C::GPL], it_gpos[C::GPL], it_npos[C::GPL], it_apos[C::GPL], it_lin[C::GPL];
+  short it_gi[C::GPL], it_gj[C::GPL], it_gk[C::GPL];
+  bool it_on[C::GPL];
+#pragma unroll
+  for (int j = 0; j < C::GPL; ++j) {
+    const int r = lane + 32 * j;
+    it_on[j] = r < C::NEED;
+    const int rr = it_on[j] ? r : 0;
+    const int f = rr / (G::NF / 2);
+    int a, c;
+    needed_face_cell<D, NC>(f, rr % (G::NF / 2), n, a, c);
+    const Face<D, NC> F(f, a, c);
+    it_f[j] = f;
+    it_gpos[j] = G::g(F.gi, F.gj, F.gk);
+    it_npos[j] = G::g(F.ni, F.nj, F.nk);
+    it_apos[j] = G::g(F.ai, F.aj, F.ak);
+    it_lin[j] = (D == 2) ? (a - 1) : (a - 1) + NC * (c - 1);
+    it_gi[j] = (short)F.gi;
+    it_gj[j] = (short)F.gj;
+    it_gk[j] = (short)F.gk;
+  }
+  int upos[C::CPL], rpos[C::CPL];
+  bool uon[C::CPL];
+#pragma unroll
+  for (int c = 0; c < C::CPL; ++c) {
+    const int uq = lane + 32 * c;
+    uon[c] = uq < C::UPD;
+    const int q = uon[c] ? uq : 0;
+    const int p = q % (NC / 2);
+    if constexpr (D == 2) {
+      const int j = q / (NC / 2) + 1;
+      const int i = 2 * p + 1 + ((1 + j + n) & 1);
+      upos[c] = G::g(i, j, 0);
+      rpos[c] = G::in(i, j, 1);
+    } else {
+      const int j = (q / (NC / 2)) % NC + 1;
+      const int k = q / ((NC / 2) * NC) + 1;
+      const int i = 2 * p + 1 + ((1 + j + k + n) & 1);
+      upos[c] = G::g(i, j, k);
+      rpos[c] = G::in(i, j, k);
+    }
+  }
+  constexpr int OX = 1, OY = G::NG, OZ = G::NG * G::NG;
+
+  int issued = 0;  // boxes whose copies lane 0 has issued
+  auto stage = [&](int k) { return ring + (k % S) * C::BOX_B; };
+  auto issue = [&](int k) {  // lane 0 (bulk copies) or all lanes (cp.async)
+    ++issued;
+    const int i = gw + k * nw;
+    const int s = box_at(bs, i);
+    unsigned char* sp = stage(k);
+    if constexpr (ASYNC) {
+      const unsigned char* src = reinterpret_cast<const unsigned char*>(phi + box_offg<G::SG>(m, bs, i, s));
+      for (int q = lane; q < (G::SG * (int)sizeof(T)) / 16; q += 32) cp_async16(sp + C::PHI_OFF + 16 * q, src + 16 * q);
+      if (lane < (int)sizeof(SlotDesc) / 16)
+        cp_async16(sp + 16 * lane, reinterpret_cast<const unsigned char*>(m.desc + s) + 16 * lane);
+    } else {
+      unsigned long long* b = &bar[wid][k % S];
+      fence_proxy_async();
+      mbar_expect_tx(b, (unsigned)C::BOX_B);
+      bulk_g2s(sp, m.desc + s, (unsigned)sizeof(SlotDesc), b);
+      bulk_g2s(sp + C::PHI_OFF, phi + box_offg<G::SG>(m, bs, i, s), (unsigned)(G::SG * sizeof(T)), b);
+    }
+  };
+  // Descriptor words of box k, straight from global memory (the ghost
+  // sources are fetched two boxes ahead, before the box's bulk copy lands).
+  auto desc_words = [&](int k) -> unsigned {
+    if (k >= my_boxes) return 0u;
+    const int s = box_at(bs, gw + k * nw);
+    return reinterpret_cast<const unsigned*>(m.desc + s)[lane];
+  };
+  // Ghost sources and rhs values of box k from its descriptor words.
+  auto fetch = [&](int k, unsigned w, bool live, T (&val)[C::GPL], T (&rv)[C::CPL], int& act) {
+    act = 0;
+#pragma unroll
+    for (int j = 0; j < C::GPL; ++j) val[j] = (T)0;
+#pragma unroll
+    for (int c = 0; c < C::CPL; ++c) rv[c] = (T)0;
+    if (!live) return;
+    act = m.active[DescWords::tree(w)];
+    {
+      const int i = gw + k * nw;
+      const T* rb = rhs + box_offi<G::SI>(m, bs, i, bs.list ? bs.list[i] : 0);
+#pragma unroll
+      for (int c = 0; c < C::CPL; ++c)
+        if (uon[c]) rv[c] = rb[rpos[c]];
+    }
+    const int qd = DescWords::qd(w);
+#pragma unroll
+    for (int j = 0; j < C::GPL; ++j) {
+      const int f = it_f[j];
+      const int code = DescWords::code(w, f);
+      const long long o = DescWords::nbo(w, f);
+      if (!pull || !it_on[j]) continue;
+      if (code >= 0) {
+        val[j] = phi[o + it_npos[j]];
+      } else if (code == kFaceRefinement) {
+        const int h = NC >> 1;
+        const int pi = (qd & 1) * h + ((it_gi[j] + 1) >> 1);
+        const int pj = ((qd >> 1) & 1) * h + ((it_gj[j] + 1) >> 1);
+        const int pk = (D == 3) ? ((qd >> 2) & 1) * h + ((it_gk[j] + 1) >> 1) : 0;
+        val[j] = phi[o + G::g(pi, pj, pk)];
+      } else if (o >= 0 && !homog) {
+        val[j] = (T)m.bcval[o + it_lin[j]];
+      }
+    }
+  };
+  // Box k: issue box k+S-1, read the descriptor of box k+4, fetch the ghost
+  // sources of box k+2, then update box k from its stage with the ghost
+  // sources fetched two boxes ago. False if a bounded wait gave up.
+  auto body = [&](int k, T (&g0)[C::GPL], T (&r0)[C::CPL], int& a0, T (&g2)[C::GPL], T (&r2)[C::CPL],
+                  int& a2, unsigned& w2, unsigned& w4) -> bool {
+    if constexpr (ASYNC) {
+      if (k + S - 1 < my_boxes) issue(k + S - 1);
+      cp_async_commit();  // one group per box (empty past the end)
+    } else {
+      if (lane == 0 && k + S - 1 < my_boxes) issue(k + S - 1);
+    }
+    const unsigned w_new = desc_words(k + 4);
+    fetch(k + 2, w2, k + 2 < my_boxes, g2, r2, a2);
+    if constexpr (ASYNC) {
+      cp_async_wait<S - 1>();  // box k's group has landed
+      __syncwarp();
+    } else {
+      const bool ok = mbar_wait_bounded(&bar[wid][k % S], (k / S) & 1);
+      if (!__all_sync(0xffffffffu, ok)) return false;
+    }
+    unsigned char* sp = stage(k);
+    const SlotDesc& d = *reinterpret_cast<const SlotDesc*>(sp);
+    T* bx = reinterpret_cast<T*>(sp + C::PHI_OFF);
+    if (a0) {
+      if (pull) {
+#pragma unroll
+        for (int j = 0; j < C::GPL; ++j) {
+          if (!it_on[j]) continue;
+          const int f = it_f[j];
+          const int code = d.code[f];
+          T v = g0[j];
+          if (code < 0) {
+            if (code == kFaceRefinement) {  // mg$D_sides_rb, src/m_aX_mg.f90:286-347
+              const int dix = (f & 1) ? -1 : 1;
+              const int ap = it_apos[j];
+              const int dim = f >> 1;
+              if constexpr (D == 2) {
+                if (dim == 0) {
+                  const int dj = -1 + 2 * ((int)it_gj[j] & 1);
+                  v = (T)0.5 * g0[j] + bx[ap] - (T)0.25 * (bx[ap + dix * OX] + bx[ap + dj * OY]);
+                } else {
+                  const int di = -1 + 2 * ((int)it_gi[j] & 1);
+                  v = (T)0.5 * g0[j] + bx[ap] - (T)0.25 * (bx[ap + di * OX] + bx[ap + dix * OY]);
+                }
+              } else {
+                const int ti = (int)it_gi[j], tj = (int)it_gj[j], tk = (int)it_gk[j];
+                const int di = (dim == 0) ? dix : -1 + 2 * (ti & 1);
+                const int dj = (dim == 1) ? dix : -1 + 2 * (tj & 1);
+                const int dk = (dim == 2) ? dix : -1 + 2 * (tk & 1);
+                v = (T)0.5 * g0[j] + (T)0.75 * bx[ap] - (T)0.25 * bx[ap + di * OX + dj * OY + dk * OZ];
+              }
+            } else {
+              v = bc_value<T>(code, f, g0[j], bx[it_apos[j]], Sc<T>::dr(d));
+            }
+          }
+          bx[it_gpos[j]] = v;
+        }
+        __syncwarp();
+      }
+      const T dx2 = Sc<T>::dx2(d);
+      T* out = phi + d.offg;
+#pragma unroll
+      for (int c = 0; c < C::CPL; ++c) {
+        if (!uon[c]) continue;
+        const T* b = bx + upos[c];
+        const T f = r0[c];
+        T v;
+        if constexpr (D == 2) {
+          v = (T)0.25 * (b[OX] + b[-OX] + b[OY] + b[-OY] - dx2 * f);
+        } else {
+          const T sixth = (T)(1 / 6.0);
+          v = sixth * (b[OX] + b[-OX] + b[OY] + b[-OY] + b[OZ] + b[-OZ] - dx2 * f);
+        }
+        out[upos[c]] = v;
+      }
+    }
+    __syncwarp();  // the stage of box k is refilled at box k + 1
+    w2 = w4;       // rotate: the words of box k+3 move up
+    w4 = w_new;
+    return true;
+  };
+
+  if constexpr (ASYNC) {
+    for (int k = 0; k < S - 1; ++k) {
+      if (k < my_boxes) issue(k);
+      cp_async_commit();
+    }
+  } else {
+    if (lane == 0)
+      for (int k = 0; k < S - 1 && k < my_boxes; ++k) issue(k);
+  }
+  T ga[C::GPL], gb[C::GPL], gc[C::GPL];
+  T ra[C::CPL], rb[C::CPL], rc[C::CPL];
+  int aa = 0, ab = 0, ac = 0;
+  {
+    const unsigned w0 = desc_words(0), w1 = desc_words(1);
+    fetch(0, w0, true, ga, ra, aa);
+    fetch(1, w1, 1 < my_boxes, gb, rb, ab);
+  }
+  // Descriptor words of boxes k+2 and k+3 at the start of box k.
+  unsigned wq = desc_words(2), wr = desc_words(3);
+  int k = 0;
+  bool ok = true;
+  for (; k < my_boxes; k += 3) {
+    // body(k) uses set a and fetches box k+2 into set c; words rotate wq <- wr <- new
+    if (!(ok = body(k, ga, ra, aa, gc, rc, ac, wq, wr))) break;
+    if (k + 1 >= my_boxes) break;
+    if (!(ok = body(k + 1, gb, rb, ab, ga, ra, aa, wq, wr))) { k += 1; break; }
+    if (k + 2 >= my_boxes) break;
+    if (!(ok = body(k + 2, gc, rc, ac, gb, rb, ab, wq, wr))) { k += 2; break; }
+  }
+  if constexpr (ASYNC) {
+    cp_async_wait<0>();
+  } else if (!ok && lane == 0) {  // gave up at box k: drain this warp's copies from box k on
+    atomicExch(m.err, 1);
+    for (int j = k; j < issued; ++j) mbar_wait_bounded(&bar[wid][j % S], (j / S) & 1);
+  }
+}
+
 // Laplacian of mg$D_box_lpl (src/m_aX_mg.f90:763-797) at (i,j,k) of a staged box.
 template <int D, int NC, class T>
 __device__ __forceinline__ T lpl_at(const T* bx, int i, int j, int k, T inv_dr_sq) {
@@ -615,6 +938,8 @@ template <int D, int NC, bool SUB, class T>
 __global__ void __launch_bounds__(kThreads)
 k_restrict_res(Meta m, BoxSet bs, T* __restrict__ phi, const T* __restrict__ rhs,
                T* __restrict__ tmp, int with_res, int pull, int homog) {
+  pdl_wait();
+  pdl_trigger();
   using G = Geo<D, NC>;
   constexpr int H = NC / 2;
   constexpr int PNC = SUB ? NC / 2 : NC;
@@ -679,6 +1004,8 @@ template <int D, int NC, class T>
 __global__ void __launch_bounds__(kThreads)
 k_coarse_rhs(Meta m, BoxSet bs, T* __restrict__ phi, T* __restrict__ rhs,
              T* __restrict__ tmp, int copy_tmp, int pull, int homog) {
+  pdl_wait();
+  pdl_trigger();
   using G = Geo<D, NC>;
   constexpr int PER_BOX = G::SI < kThreads ? G::SI : kThreads;
   constexpr int BPC = boxes_per_cta<G::SG, PER_BOX, T>(1);
@@ -725,6 +1052,8 @@ k_coarse_rhs(Meta m, BoxSet bs, T* __restrict__ phi, T* __restrict__ rhs,
 template <int D, int NC, bool SUB, class T>
 __global__ void __launch_bounds__(kThreads)
 k_correct(Meta m, BoxSet bs, T* __restrict__ phi, T* __restrict__ tmp) {
+  pdl_wait();
+  pdl_trigger();
   using G = Geo<D, NC>;  // parent geometry
   constexpr int CNC = SUB ? 2 * NC : NC;
   using GC = Geo<D, CNC>;
@@ -930,6 +1259,8 @@ __device__ __forceinline__ void box_max_atomic(V v, unsigned long long* dst, V* 
 
 __global__ void k_stripe_reduce(int n_trees, const unsigned long long* __restrict__ norm,
                                 unsigned long long* __restrict__ out) {
+  pdl_wait();
+  pdl_trigger();
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t < n_trees) {
     unsigned long long mx = 0;
@@ -950,6 +1281,8 @@ template <int D, int NC, class T>
 __global__ void __launch_bounds__(kThreads)
 k_residual(Meta m, BoxSet bs, const T* __restrict__ phi, const T* __restrict__ rhs,
            T* __restrict__ tmp, unsigned long long* __restrict__ norm_per_tree, int store) {
+  pdl_wait();
+  pdl_trigger();
   using G = Geo<D, NC>;
   constexpr int PER_BOX = G::SI < kThreads ? G::SI : kThreads;
   constexpr int BPC = kThreads / PER_BOX;
@@ -994,6 +1327,8 @@ template <int D, int NC, class T>
 __global__ void __launch_bounds__(kThreads)
 k_maxabs(Meta m, BoxSet bs, const T* __restrict__ v, int ghosted,
          unsigned long long* __restrict__ norm_per_tree) {
+  pdl_wait();
+  pdl_trigger();
   using G = Geo<D, NC>;
   constexpr int PER_BOX = G::SI < kThreads ? G::SI : kThreads;
   constexpr int BPC = kThreads / PER_BOX;
@@ -1027,6 +1362,8 @@ k_maxabs(Meta m, BoxSet bs, const T* __restrict__ v, int ghosted,
 template <int D, int NC, class T>
 __global__ void __launch_bounds__(kThreads)
 k_box_op(Meta m, BoxSet bs, T* __restrict__ dst, const T* __restrict__ src, int op) {
+  pdl_wait();
+  pdl_trigger();
   using G = Geo<D, NC>;
   using V = typename Vec<T>::type;
   constexpr int VW = Vec<T>::w;
@@ -1057,6 +1394,8 @@ k_box_op(Meta m, BoxSet bs, T* __restrict__ dst, const T* __restrict__ src, int 
 template <int D, int NC, bool SUB, class T>
 __global__ void __launch_bounds__(kThreads)
 k_restrict_interior(Meta m, BoxSet bs, T* __restrict__ v) {
+  pdl_wait();
+  pdl_trigger();
   constexpr int H = NC / 2;
   constexpr int PNC = SUB ? NC / 2 : NC;
   constexpr int PER_BOX = D == 2 ? H * H : H * H * H;
@@ -1105,6 +1444,8 @@ template <int D, int NC>
 __global__ void __launch_bounds__(kThreads)
 k_defect(Meta m, BoxSet bs, const double* __restrict__ u, const double* __restrict__ f,
          float* __restrict__ r32, unsigned long long* __restrict__ norm_per_tree) {
+  pdl_wait();
+  pdl_trigger();
   using G = Geo<D, NC>;
   constexpr int PER_BOX = G::SI < kThreads ? G::SI : kThreads;
   constexpr int BPC = boxes_per_cta<G::SG, PER_BOX, double>(1);
@@ -1176,6 +1517,8 @@ k_defect(Meta m, BoxSet bs, const double* __restrict__ u, const double* __restri
 template <int D, int NC>
 __global__ void __launch_bounds__(kThreads)
 k_accumulate(Meta m, BoxSet bs, double* __restrict__ u, const float* __restrict__ e) {
+  pdl_wait();
+  pdl_trigger();
   using G = Geo<D, NC>;
   const long long total = (long long)bs.n * G::SI;
   for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < total;
@@ -1198,6 +1541,8 @@ k_accumulate(Meta m, BoxSet bs, double* __restrict__ u, const float* __restrict_
 template <int D, int NC>
 __global__ void __launch_bounds__(kThreads)
 k_restrict_increment(Meta m, BoxSet bs, double* __restrict__ u, float* __restrict__ e) {
+  pdl_wait();
+  pdl_trigger();
   using G = Geo<D, NC>;
   constexpr int H = NC / 2;
   const long long total = (long long)bs.n * G::SI;
@@ -1231,6 +1576,8 @@ k_restrict_increment(Meta m, BoxSet bs, double* __restrict__ u, float* __restric
 // cycle is smoothed in FP64).
 template <class TD, class TS>
 __global__ void k_convert(TD* __restrict__ dst, const TS* __restrict__ src, long long n) {
+  pdl_wait();
+  pdl_trigger();
   for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < n;
        x += (long long)gridDim.x * blockDim.x)
     dst[x] = (TD)src[x];
@@ -1244,6 +1591,8 @@ template <int D, int NC, class T>
 __global__ void k_scatter(Meta m, const int* __restrict__ slots, int n,
                           const double* __restrict__ src, T* __restrict__ dst, int host_interior,
                           int dev_ghosted) {
+  pdl_wait();
+  pdl_trigger();
   using G = Geo<D, NC>;
   const int per = host_interior ? G::SI : G::SG;
   const long long total = (long long)n * per;
@@ -1273,6 +1622,8 @@ __global__ void k_scatter(Meta m, const int* __restrict__ slots, int n,
 template <int D, int NC, class T>
 __global__ void k_gather(Meta m, const int* __restrict__ slots, int n, const T* __restrict__ src,
                          double* __restrict__ dst, int host_interior, int dev_ghosted) {
+  pdl_wait();
+  pdl_trigger();
   using G = Geo<D, NC>;
   const int per = host_interior ? G::SI : G::SG;
   const long long total = (long long)n * per;
@@ -1305,6 +1656,8 @@ __global__ void k_gather(Meta m, const int* __restrict__ slots, int n, const T* 
 __global__ void k_check(int n_trees, const unsigned long long* __restrict__ rnorm,
                         const double* __restrict__ fmax, double tol, int* __restrict__ active,
                         int* __restrict__ failed, int* __restrict__ n_active_out) {
+  pdl_wait();
+  pdl_trigger();
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t < n_trees) {
     double r = __longlong_as_double((long long)rnorm[t]);  // reduced over stripes

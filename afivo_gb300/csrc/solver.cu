@@ -5,6 +5,7 @@
 #include <cmath>
 #include <cstring>
 #include <type_traits>
+#include <utility>
 
 #include "forest.hpp"
 #include "kernels.cuh"
@@ -48,6 +49,25 @@ static Meta meta_of(const DevMeta& d) {
   m.nbo2 = d.nbo2;
   m.err = d.err;
   return m;
+}
+
+// Kernel launch with programmatic stream serialization: the next kernel on
+// the stream may be scheduled while this one drains, and waits in
+// dev::pdl_wait() for it to finish before touching memory.
+template <class... KArgs, class... Args>
+static void launch_k(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                     Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...);
 }
 
 static int grid_for(long long units, int n_sm) {
@@ -138,7 +158,23 @@ void Forest::prof_end(cudaEvent_t start, int kind, double b) {
     cudaEventCreate(&e);
   }
   cudaEventRecord(e, stream);
-  prof.push_back(ProfEntry{start, e, kind, b});
+  prof.push_back(ProfEntry{start, e, kind, prof_level, b});
+}
+
+long long Forest::prof_entries(long long max, int* kind, int* level, double* ms, double* b) {
+  cudaStreamSynchronize(stream);
+  long long n = 0;
+  for (const ProfEntry& p : prof) {
+    if (n >= max) break;
+    float x = 0;
+    cudaEventElapsedTime(&x, p.start, p.stop);
+    kind[n] = p.kind;
+    level[n] = p.level;
+    ms[n] = x;
+    b[n] = p.bytes;
+    ++n;
+  }
+  return (long long)prof.size();
 }
 
 int Forest::prof_read(int kind, long long* launches, double* ms, double* b) {
@@ -264,7 +300,7 @@ void Forest::norm_reset() {
 
 void Forest::norm_fold() {
   ProfScope ps(this, kProfOther, 8.0 * plan.n_trees * dev::kStripes);
-  dev::k_stripe_reduce<<<(plan.n_trees + 255) / 256, 256, 0, stream>>>(plan.n_trees, d_norm, d_red);
+  launch_k(dev::k_stripe_reduce, (plan.n_trees + 255) / 256, 256, 0, stream, plan.n_trees, d_norm, d_red);
 }
 
 int Forest::upload_bc(std::string& err) {
@@ -351,10 +387,10 @@ static int exchange(Forest& F, int t, int var, double* host, int interior_only, 
       int grid = grid_for((n * per + 255) / 256, F.n_sm);
       ProfScope ps(&F, kProfOther, 16.0 * n * per);
       if (to_dev)
-        dev::k_scatter<DD, NC, double><<<grid, 256, 0, st>>>(m, F.d_stage_slots + i, n, F.d_stage + off,
+        launch_k(dev::k_scatter<DD, NC, double>, grid, 256, 0, st, m, F.d_stage_slots + i, n, F.d_stage + off,
                                                             dvar, interior_only, ghosted);
       else
-        dev::k_gather<DD, NC, double><<<grid, 256, 0, st>>>(m, F.d_stage_slots + i, n, dvar,
+        launch_k(dev::k_gather<DD, NC, double>, grid, 256, 0, st, m, F.d_stage_slots + i, n, dvar,
                                                            F.d_stage + off, interior_only, ghosted);
     });
     off += n * per;
@@ -402,22 +438,59 @@ static void launch_level(Forest& F, const Meta& m, BoxSet bs, T* phi, const T* r
   }
   const long long groups = (bs.n + C::BPC - 1) / C::BPC;
   const int grid = (int)std::max(1LL, std::min(groups, (long long)F.n_sm * occ));
-  dev::k_level_tma<D, NC, T, MODE><<<grid, dev::kThreads, C::SMEM_B, F.stream>>>(
+  launch_k(dev::k_level_tma<D, NC, T, MODE>, grid, dev::kThreads, C::SMEM_B, F.stream, 
       m, bs, phi, rhs, n, pull ? 1 : 0, homog ? 1 : 0);
+}
+
+// Launches the warp-per-box sweep: W warps per block, S stages per warp.
+template <int D, int NC, class T, int W, int S, int ASYNC>
+static void launch_sweep_warp(Forest& F, const Meta& m, BoxSet bs, T* phi, const T* rhs, int n,
+                              bool pull, bool homog) {
+  using C = dev::WarpCfg<D, NC, T, W, S>;
+  static int occ = 0;
+  if (!occ) {
+    cudaFuncSetAttribute(dev::k_sweep_warp<D, NC, T, W, S, ASYNC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         C::SMEM_B);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, dev::k_sweep_warp<D, NC, T, W, S, ASYNC>, W * 32,
+                                                  C::SMEM_B);
+    if (occ < 1) occ = 1;
+  }
+  const long long blocks = (bs.n + W - 1) / W;
+  const int grid = (int)std::max(1LL, std::min(blocks, (long long)F.n_sm * occ));
+  launch_k(dev::k_sweep_warp<D, NC, T, W, S, ASYNC>, grid, W * 32, C::SMEM_B, F.stream, m, bs, phi, rhs, n, pull ? 1 : 0,
+                                                                          homog ? 1 : 0);
+}
+
+dev_BoxSet Forest::level_set(int lvl) const {
+  const int lo = plan.lvl_lo[plan.L(lvl)];
+  return BoxSet{nullptr, lo, plan.lvl_n[plan.L(lvl)], plan.offg[lo], plan.offi[lo]};
 }
 
 template <class T>
 void Forest::sweep(const Arrays<T>& a, int lvl, int n, bool pull, bool homog) {
+  prof_level = lvl;
   int nbx = lvl_n(lvl);
   if (!nbx) return;
-  BoxSet bs{nullptr, plan.lvl_lo[plan.L(lvl)], nbx};
+  BoxSet bs = level_set(lvl);
   Meta m = meta_of(meta);
   with_nc(plan.dim, plan.nc_at(lvl), [&](auto d_, auto nc_) {
     constexpr int D = decltype(d_)::value, NC = decltype(nc_)::value;
     using G = dev::Geo<D, NC>;
     // read phi and f, write phi over the interior
     ProfScope ps(this, kProfSweep, 3.0 * nbx * G::SI * sizeof(T));
-    launch_level<D, NC, T, dev::kModeSweep>(*this, m, bs, a.phi, a.rhs, n, pull, homog);
+    if (sweep_kernel == 0) {
+      launch_level<D, NC, T, dev::kModeSweep>(*this, m, bs, a.phi, a.rhs, n, pull, homog);
+    } else if constexpr (std::is_same<T, float>::value) {
+      if (sweep_kernel == 1)
+        launch_sweep_warp<D, NC, T, 16, 3, 0>(*this, m, bs, a.phi, a.rhs, n, pull, homog);
+      else
+        launch_sweep_warp<D, NC, T, 16, 3, 1>(*this, m, bs, a.phi, a.rhs, n, pull, homog);
+    } else {
+      if (sweep_kernel == 1)
+        launch_sweep_warp<D, NC, T, 8, 3, 0>(*this, m, bs, a.phi, a.rhs, n, pull, homog);
+      else
+        launch_sweep_warp<D, NC, T, 8, 3, 1>(*this, m, bs, a.phi, a.rhs, n, pull, homog);
+    }
   });
 }
 
@@ -425,11 +498,12 @@ template <class T>
 void Forest::fill(const Arrays<T>& a, int lvl, bool homog) {
   int nbx = lvl_n(lvl);
   if (!nbx) return;
-  fill_set(a, lvl, BoxSet{nullptr, plan.lvl_lo[plan.L(lvl)], nbx}, homog);
+  fill_set(a, lvl, level_set(lvl), homog);
 }
 
 template <class T>
 void Forest::fill_set(const Arrays<T>& a, int lvl, BoxSet bs, bool homog) {
+  prof_level = lvl;
   if (!bs.n) return;
   Meta m = meta_of(meta);
   with_nc(plan.dim, plan.nc_at(lvl), [&](auto d_, auto nc_) {
@@ -443,9 +517,10 @@ void Forest::fill_set(const Arrays<T>& a, int lvl, BoxSet bs, bool homog) {
 
 template <class T>
 void Forest::restrict_res(const Arrays<T>& a, int lvl, bool with_res, bool pull, bool homog) {
+  prof_level = lvl;
   int nbx = lvl_n(lvl);
   if (!nbx || lvl <= plan.min_lvl) return;
-  BoxSet bs{nullptr, plan.lvl_lo[plan.L(lvl)], nbx};
+  BoxSet bs = level_set(lvl);
   Meta m = meta_of(meta);
   bool sub = lvl <= 1;
   with_nc(plan.dim, plan.nc_at(lvl), [&](auto d_, auto nc_) {
@@ -459,16 +534,17 @@ void Forest::restrict_res(const Arrays<T>& a, int lvl, bool with_res, bool pull,
     ProfScope ps(this, kProfRestrict,
                  (2.0 + 2.0 / (1 << D)) * nbx * G::SI * sizeof(T));
     if (sub)
-      dev::k_restrict_res<D, NC, true, T><<<grid, dev::kThreads, 0, stream>>>(
+      launch_k(dev::k_restrict_res<D, NC, true, T>, grid, dev::kThreads, 0, stream, 
           m, bs, a.phi, a.rhs, a.tmp, with_res ? 1 : 0, pull ? 1 : 0, homog ? 1 : 0);
     else
-      dev::k_restrict_res<D, NC, false, T><<<grid, dev::kThreads, 0, stream>>>(
+      launch_k(dev::k_restrict_res<D, NC, false, T>, grid, dev::kThreads, 0, stream, 
           m, bs, a.phi, a.rhs, a.tmp, with_res ? 1 : 0, pull ? 1 : 0, homog ? 1 : 0);
   });
 }
 
 template <class T>
 void Forest::coarse_rhs(const Arrays<T>& a, int lp, bool copy_tmp, bool pull, bool homog) {
+  prof_level = lp;
   int np = n_parents(lp);
   if (!np) return;
   BoxSet bs{parents_list(lp), 0, np};
@@ -481,13 +557,14 @@ void Forest::coarse_rhs(const Arrays<T>& a, int lp, bool copy_tmp, bool pull, bo
     int grid = grid_for((np + BPC - 1) / BPC, n_sm);
     // read phi, tmp; write rhs, tmp
     ProfScope ps(this, kProfCoarseRhs, 4.0 * np * G::SI * sizeof(T));
-    dev::k_coarse_rhs<D, NC, T><<<grid, dev::kThreads, 0, stream>>>(
+    launch_k(dev::k_coarse_rhs<D, NC, T>, grid, dev::kThreads, 0, stream, 
         m, bs, a.phi, a.rhs, a.tmp, copy_tmp ? 1 : 0, pull ? 1 : 0, homog ? 1 : 0);
   });
 }
 
 template <class T>
 void Forest::correct(const Arrays<T>& a, int lp) {
+  prof_level = lp;
   int np = n_parents(lp);
   if (!np) return;
   BoxSet bs{parents_list(lp), 0, np};
@@ -503,18 +580,19 @@ void Forest::correct(const Arrays<T>& a, int lp) {
     ProfScope ps(this, kProfCorrect, (3.0 + 2.0 * (1 << D)) * np * G::SI * sizeof(T));
     if (sub) {
       if constexpr (!(D == 2 && NC == 16) && !(D == 3 && NC == 8))
-        dev::k_correct<D, NC, true, T><<<grid, dev::kThreads, 0, stream>>>(m, bs, a.phi, a.tmp);
+        launch_k(dev::k_correct<D, NC, true, T>, grid, dev::kThreads, 0, stream, m, bs, a.phi, a.tmp);
     } else {
-      dev::k_correct<D, NC, false, T><<<grid, dev::kThreads, 0, stream>>>(m, bs, a.phi, a.tmp);
+      launch_k(dev::k_correct<D, NC, false, T>, grid, dev::kThreads, 0, stream, m, bs, a.phi, a.tmp);
     }
   });
 }
 
 template <class T>
 void Forest::residual(const Arrays<T>& a, int lvl, unsigned long long* norm, bool store) {
+  prof_level = lvl;
   int nbx = lvl_n(lvl);
   if (!nbx) return;
-  BoxSet bs{nullptr, plan.lvl_lo[plan.L(lvl)], nbx};
+  BoxSet bs = level_set(lvl);
   Meta m = meta_of(meta);
   with_nc(plan.dim, plan.nc_at(lvl), [&](auto d_, auto nc_) {
     constexpr int D = decltype(d_)::value, NC = decltype(nc_)::value;
@@ -523,7 +601,7 @@ void Forest::residual(const Arrays<T>& a, int lvl, unsigned long long* norm, boo
     constexpr int BPC = dev::kThreads / PER_BOX;
     int grid = grid_for((nbx + BPC - 1) / BPC, n_sm);
     ProfScope ps(this, kProfResidual, (store ? 3.0 : 2.0) * nbx * G::SI * sizeof(T));
-    dev::k_residual<D, NC, T><<<grid, dev::kThreads, 0, stream>>>(m, bs, a.phi, a.rhs, a.tmp, norm,
+    launch_k(dev::k_residual<D, NC, T>, grid, dev::kThreads, 0, stream, m, bs, a.phi, a.rhs, a.tmp, norm,
                                                                  store ? 1 : 0);
   });
 }
@@ -576,11 +654,11 @@ void Forest::vcycle_t(const Arrays<T>& a, const MgOpts& mg, int highest, bool ho
     int g1 = grid_for((ng + 255) / 256, n_sm), g2 = grid_for((ni + 255) / 256, n_sm);
     {
       ProfScope ps(this, kProfOther, (8.0 + sizeof(T)) * ng);
-      dev::k_convert<double, T><<<g1, 256, 0, stream>>>(base_phi64, a.phi, ng);
+      launch_k(dev::k_convert<double, T>, g1, 256, 0, stream, base_phi64, a.phi, ng);
     }
     {
       ProfScope ps(this, kProfOther, (8.0 + sizeof(T)) * ni);
-      dev::k_convert<double, T><<<g2, 256, 0, stream>>>(base_rhs64, a.rhs, ni);
+      launch_k(dev::k_convert<double, T>, g2, 256, 0, stream, base_rhs64, a.rhs, ni);
     }
     Arrays<double> b{base_phi64, base_rhs64, nullptr};
     if (mg.n_base > 0) {
@@ -589,7 +667,7 @@ void Forest::vcycle_t(const Arrays<T>& a, const MgOpts& mg, int highest, bool ho
     }
     {
       ProfScope ps(this, kProfOther, (8.0 + sizeof(T)) * ng);
-      dev::k_convert<T, double><<<g1, 256, 0, stream>>>(a.phi, base_phi64, ng);
+      launch_k(dev::k_convert<T, double>, g1, 256, 0, stream, a.phi, base_phi64, ng);
     }
   } else if (mg.n_base > 0) {
     sweeps(a, l0, mg.n_base);
@@ -681,7 +759,7 @@ int Forest::fmg(const MgOpts& mg, bool set_residual, bool have_guess, std::strin
     for (int l = plan.max_lvl; l >= l0 + 1; --l) {
       int nbx = lvl_n(l);
       if (!nbx) continue;
-      BoxSet bs{nullptr, plan.lvl_lo[plan.L(l)], nbx};
+      BoxSet bs = level_set(l);
       bool sub = l <= 1;
       with_nc(plan.dim, plan.nc_at(l), [&](auto d_, auto nc_) {
         constexpr int D = decltype(d_)::value, NC = decltype(nc_)::value;
@@ -690,18 +768,16 @@ int Forest::fmg(const MgOpts& mg, bool set_residual, bool have_guess, std::strin
         long long items = (long long)nbx * (G::SG / VW);
         {
           ProfScope ps(this, kProfOther, 8.0 * nbx * G::SG);
-          dev::k_box_op<D, NC, double><<<grid_for((items + 255) / 256, n_sm), 256, 0, stream>>>(
+          launch_k(dev::k_box_op<D, NC, double>, grid_for((items + 255) / 256, n_sm), 256, 0, stream, 
               m, bs, d64.phi, nullptr, 0);
         }
         constexpr int H = NC / 2;
         long long it2 = (long long)nbx * (D == 2 ? H * H : H * H * H);
         ProfScope ps(this, kProfOther, 8.0 * nbx * G::SI * (1.0 + 1.0 / (1 << D)));
         if (sub)
-          dev::k_restrict_interior<D, NC, true, double>
-              <<<grid_for((it2 + 255) / 256, n_sm), 256, 0, stream>>>(m, bs, d64.rhs);
+          launch_k(dev::k_restrict_interior<D, NC, true, double>, grid_for((it2 + 255) / 256, n_sm), 256, 0, stream, m, bs, d64.rhs);
         else
-          dev::k_restrict_interior<D, NC, false, double>
-              <<<grid_for((it2 + 255) / 256, n_sm), 256, 0, stream>>>(m, bs, d64.rhs);
+          launch_k(dev::k_restrict_interior<D, NC, false, double>, grid_for((it2 + 255) / 256, n_sm), 256, 0, stream, m, bs, d64.rhs);
       });
     }
   }
@@ -711,14 +787,14 @@ int Forest::fmg(const MgOpts& mg, bool set_residual, bool have_guess, std::strin
     set_active_host(act);
     int nbx = lvl_n(l);
     if (nbx) {
-      BoxSet bs{nullptr, plan.lvl_lo[plan.L(l)], nbx};
+      BoxSet bs = level_set(l);
       with_nc(plan.dim, plan.nc_at(l), [&](auto d_, auto nc_) {
         constexpr int D = decltype(d_)::value, NC = decltype(nc_)::value;
         using G = dev::Geo<D, NC>;
         constexpr int VW = dev::Vec<double>::w;
         long long items = (long long)nbx * (G::SG / VW);
         ProfScope ps(this, kProfOther, 16.0 * nbx * G::SG);
-        dev::k_box_op<D, NC, double><<<grid_for((items + 255) / 256, n_sm), 256, 0, stream>>>(
+        launch_k(dev::k_box_op<D, NC, double>, grid_for((items + 255) / 256, n_sm), 256, 0, stream, 
             m, bs, d64.tmp, d64.phi, 1);
       });
     }
@@ -762,7 +838,7 @@ int Forest::max_abs(int t, int var, double* out, std::string& err) {
       constexpr int PER_BOX = G::SI < dev::kThreads ? G::SI : dev::kThreads;
       constexpr int BPC = dev::kThreads / PER_BOX;
       ProfScope ps(this, kProfOther, 8.0 * nl * G::SI);
-      dev::k_maxabs<D, NC, double><<<grid_for((nl + BPC - 1) / BPC, n_sm), dev::kThreads, 0, stream>>>(
+      launch_k(dev::k_maxabs<D, NC, double>, grid_for((nl + BPC - 1) / BPC, n_sm), dev::kThreads, 0, stream, 
           m, bs, v, var != AFV_RHS, d_norm);
     });
   }
@@ -804,7 +880,7 @@ void Forest::enqueue_residual_check(int precision, double tol) {
       constexpr int BPC = dev::boxes_per_cta<G::SG, PER_BOX, double>(1);
       // read u (8 B), f (8 B); write r (4 B)
       ProfScope ps(this, kProfDefect, 20.0 * nl * G::SI);
-      dev::k_defect<D, NC><<<grid_for((nl + BPC - 1) / BPC, n_sm * 4), dev::kThreads, 0, stream>>>(
+      launch_k(dev::k_defect<D, NC>, grid_for((nl + BPC - 1) / BPC, n_sm * 4), dev::kThreads, 0, stream, 
           m, bs, d64.phi, d64.rhs, d32.rhs, d_norm);
     });
   } else {
@@ -814,7 +890,7 @@ void Forest::enqueue_residual_check(int precision, double tol) {
   norm_fold();
   {
     ProfScope ps(this, kProfOther, 20.0 * nt);
-    dev::k_check<<<(nt + 255) / 256, 256, 0, stream>>>(nt, d_red, d_fmax, tol, meta.active, d_failed,
+    launch_k(dev::k_check, (nt + 255) / 256, 256, 0, stream, nt, d_red, d_fmax, tol, meta.active, d_failed,
                                                        d_count);
   }
   cudaMemcpyAsync(h_count, d_count, sizeof(int), cudaMemcpyDeviceToHost, stream);
@@ -838,7 +914,7 @@ void Forest::enqueue_iteration(const MgOpts& mg, int precision, double tol) {
       {
         // read e (4 B), read and write u (16 B)
         ProfScope ps(this, kProfAccumulate, 20.0 * items);
-        dev::k_accumulate<D, NC><<<grid_for((items + 255) / 256, n_sm), 256, 0, stream>>>(m, bs, d64.phi,
+        launch_k(dev::k_accumulate<D, NC>, grid_for((items + 255) / 256, n_sm), 256, 0, stream, m, bs, d64.phi,
                                                                                        d32.phi);
       }
       // parents (finest first) take the restriction of their children's increments
@@ -848,7 +924,7 @@ void Forest::enqueue_iteration(const MgOpts& mg, int precision, double tol) {
         BoxSet pb{parents_list(l), 0, np};
         long long pit = (long long)np * G::SI;
         ProfScope ps(this, kProfAccumulate, (4.0 * (1 << D) + 4.0 + 16.0) * pit);
-        dev::k_restrict_increment<D, NC><<<grid_for((pit + 255) / 256, n_sm), 256, 0, stream>>>(
+        launch_k(dev::k_restrict_increment<D, NC>, grid_for((pit + 255) / 256, n_sm), 256, 0, stream, 
             m, pb, d64.phi, d32.phi);
       }
     });
@@ -883,7 +959,7 @@ int Forest::solve(const MgOpts& mg, int precision, double tol, int max_cycles, S
       constexpr int PER_BOX = G::SI < dev::kThreads ? G::SI : dev::kThreads;
       constexpr int BPC = dev::kThreads / PER_BOX;
       ProfScope ps(this, kProfOther, 8.0 * nl * G::SI);
-      dev::k_maxabs<D, NC, double><<<grid_for((nl + BPC - 1) / BPC, n_sm), dev::kThreads, 0, stream>>>(
+      launch_k(dev::k_maxabs<D, NC, double>, grid_for((nl + BPC - 1) / BPC, n_sm), dev::kThreads, 0, stream, 
           m, bs, d64.rhs, 0, d_norm);
     });
   }

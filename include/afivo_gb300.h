@@ -248,6 +248,20 @@ int afv_forest_profile(afv_forest* f, int mask);
  * number of kernels launched on the forest's stream since it was created. */
 int afv_forest_profile_read(afv_forest* f, int kind, long long* launches, double* ms,
                             double* algorithmic_bytes);
+/* No counterpart in the reference: tuning switches of a forest (the
+ * autotuner sets them). AFV_OPT_SWEEP_KERNEL: 0 block-pipelined level kernel,
+ * 1 warp-per-box kernel with bulk copies (default), 2 warp-per-box kernel with
+ * per-lane asynchronous copies. AFV_OPT_GRAPHS: 1 (default) replays solve
+ * iterations as CUDA graphs, 0 launches them one by one. */
+enum { AFV_OPT_SWEEP_KERNEL = 0, AFV_OPT_GRAPHS = 1 };
+int afv_forest_set_option(afv_forest* f, int option, int value);
+int afv_forest_get_option(afv_forest* f, int option, int* value);
+
+/* No counterpart in the reference: the profiled launches one by one (up to
+ * max; n_total receives how many were recorded): kernel kind, level, device
+ * time in ms and algorithmic bytes. */
+int afv_forest_profile_entries(afv_forest* f, long long max, int* kind, int* level, double* ms,
+                               double* algorithmic_bytes, long long* n_total);
 
 #ifdef __cplusplus
 }

@@ -253,3 +253,29 @@ def test_mixed_batch_alone_vs_mix(gpu):
         assert np.array_equal(f1.get_var(0, gpu.AFV_PHI), forest.get_var(k, gpu.AFV_PHI))
         outs.append(r1[0])
     assert max(outs) <= 1e-8
+
+
+@pytest.mark.parametrize("which", ["c1", "3d"])
+def test_sweep_kernel_variants_agree(gpu, which):
+    """Every sweep kernel variant (block-pipelined, warp-per-box with bulk
+    copies, warp-per-box with per-lane copies) gives the oracle's bits, FP64
+    and mixed."""
+    spec = W.c1_poisson_2d() if which == "c1" else W.c2_poisson_3d(thr=3e-3, lvl_max=5)
+    f, ot, _ = setup_pair(gpu, spec)
+    for _ in range(2):
+        ot.vcycle()
+    ref = oracle_var(ot, O.I_PHI, spec["n_cell"])
+    rhs = f.get_var(0, gpu.AFV_RHS)
+    mixed = []
+    for sk in (0, 1, 2):
+        g = gpu.Forest([W.build_tree(spec)], mixed=True)
+        g.set_var(0, gpu.AFV_RHS, rhs)
+        g.set_option(gpu.AFV_OPT_SWEEP_KERNEL, sk)
+        for _ in range(2):
+            g.vcycle()
+        assert compare_var(g.get_var(0, gpu.AFV_PHI), ref, ot, spec["n_cell"], spec["dim"], False) == 0.0
+        g.zero(gpu.AFV_PHI)
+        g.solve(gpu.AFV_PREC_MIXED, tol=1e-8, max_cycles=30)
+        mixed.append(g.get_var(0, gpu.AFV_PHI))
+        g.close()
+    assert np.array_equal(mixed[0], mixed[1]) and np.array_equal(mixed[0], mixed[2])
