@@ -133,6 +133,8 @@ def lib():
             "afv_tree_max_abs_cc": (I, [P, I, I, dp]),
             "afv_forest_profile_entries": (I, [P, LL, ip, ip, dp, dp, llp]),
             "afv_forest_set_option": (I, [P, I, I]),
+            "afv_forest_set_source_device": (I, [P, I, I, I, dp]),
+            "afv_forest_autotune": (I, [P, ip, ctypes.POINTER(ctypes.c_float)]),
             "afv_forest_get_option": (I, [P, I, ip]),
             "afv_tree_max_abs_cc_noalloc": (I, [P, I, I, dp]),
             "afv_mg_solve": (I, [P, ctypes.POINTER(MgOpts), I, Dd, I, ip, dp]),
@@ -355,6 +357,12 @@ class Forest:
         g = np.ascontiguousarray(gauss, dtype=np.float64)
         _check(lib().afv_forest_set_source(self.h, tree, int(lpl), g.size // (2 + self.dim), _dp(g)))
 
+    def set_source_device(self, tree, gauss, lpl=False):
+        """set_source evaluated on the device (may differ in the last bit)."""
+        g = np.ascontiguousarray(gauss, dtype=np.float64)
+        _check(lib().afv_forest_set_source_device(self.h, tree, int(lpl), g.size // (2 + self.dim),
+                                                  _dp(g)))
+
     def set_bc_faces(self, tree, bc_types, values):
         """Sampled sides_bc hook: one AFV_BC_* per physical face and the face
         values, in the order of Tree.bc_faces()."""
@@ -438,6 +446,14 @@ class Forest:
     # event profiler
     def profile(self, mask):
         _check(lib().afv_forest_profile(self.h, mask))
+
+    def autotune(self):
+        """Pick the fastest sweep kernel for this forest; returns (choice,
+        {variant: ms per FP32 V-cycle})."""
+        c = ctypes.c_int(0)
+        ms = (ctypes.c_float * 3)()
+        _check(lib().afv_forest_autotune(self.h, ctypes.byref(c), ms))
+        return c.value, {1: ms[0], 2: ms[1], 0: ms[2]}
 
     def set_option(self, option, value):
         _check(lib().afv_forest_set_option(self.h, option, int(value)))

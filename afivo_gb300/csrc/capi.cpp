@@ -436,4 +436,13 @@ int afv_forest_get_option(afv_forest* f, int option, int* value) {
   return fail(AFV_ERR_INVALID, "unknown option");
 }
 
+int afv_forest_autotune(afv_forest* f, int* choice, float* ms3) {
+  FOREST_CALL(f, return f->f.autotune(choice, ms3, err));
+}
+
+int afv_forest_set_source_device(afv_forest* f, int tree, int src_lpl, int n_gauss, const double* gauss) {
+  if (n_gauss < 0 || (n_gauss > 0 && !gauss)) return fail(AFV_ERR_INVALID, "bad arguments");
+  FOREST_CALL(f, return f->f.set_source_device(tree, src_lpl, n_gauss, gauss, err));
+}
+
 }  // extern "C"

@@ -34,6 +34,7 @@ struct DevMeta {
   SlotDesc* desc = nullptr;
   long long* nbo2 = nullptr;
   int* err = nullptr;  // device error word (bounded waits)
+  double* rmin = nullptr;  // [slot*D + d] lower corner of the box
 };
 
 struct MgOpts {
@@ -139,6 +140,8 @@ class Forest {
   int correct_children(int lvl_parent, std::string& err);
   int residual_all(unsigned long long* norm, std::string& err);
   int vcycle(const MgOpts& mg, int highest, bool set_residual, std::string& err);
+  int autotune(int* choice, float* ms3, std::string& err);
+  int set_source_device(int tree, int lpl, int n_gauss, const double* gauss, std::string& err);
   int fmg(const MgOpts& mg, bool set_residual, bool have_guess, std::string& err);
   int gc_tree(std::string& err);
   int max_abs(int tree, int var, double* out, std::string& err);

@@ -1572,6 +1572,48 @@ k_restrict_increment(Meta m, BoxSet bs, double* __restrict__ u, float* __restric
   }
 }
 
+// Right-hand side from a sum of Gaussians a*exp(-|r-c|^2/s^2), or their
+// Laplacian (lpl), at the cell centres of a slot range of one tree
+// (the source of examples/m_gaussians.f90:64-102), evaluated on the device.
+constexpr int kMaxGauss = 16;
+struct GaussSet {
+  int n, lpl;
+  double g[kMaxGauss * 5];  // per Gaussian: a, s, c_1..c_D
+};
+
+template <int D, int NC>
+__global__ void __launch_bounds__(kThreads)
+k_source(Meta m, BoxSet bs, int tree, const double* __restrict__ rmin, GaussSet gs,
+         double* __restrict__ rhs) {
+  pdl_wait();
+  pdl_trigger();
+  using G = Geo<D, NC>;
+  const long long total = (long long)bs.n * G::SI;
+  for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < total;
+       x += (long long)gridDim.x * blockDim.x) {
+    const int bi = (int)(x / G::SI), q = (int)(x % G::SI);
+    const int s = bs.lo + bi;
+    if (m.tree[s] != tree) continue;
+    const int cix[3] = {q % NC + 1, (q / NC) % NC + 1, (D == 3) ? q / (NC * NC) + 1 : 1};
+    const double dr = m.desc[s].dr;
+    double v = 0;
+    for (int k = 0; k < gs.n; ++k) {
+      const double* p = gs.g + k * (2 + D);
+      double xr2 = 0;
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        const double xx = (rmin[(size_t)s * D + d] + (cix[d] - 0.5) * dr - p[2 + d]) / p[1];
+        xr2 = xr2 + xx * xx;
+      }
+      if (gs.lpl)
+        v = v + p[0] * (4 / (p[1] * p[1]) * (xr2 - 0.5 * D) * exp(-xr2));
+      else
+        v = v + p[0] * exp(-xr2);
+    }
+    rhs[bs.i0 + (long long)bi * G::SI + q] = v;
+  }
+}
+
 // Precision conversion over whole boxes (the coarsest level of the mixed
 // cycle is smoothed in FP64).
 template <class TD, class TS>

@@ -75,32 +75,53 @@ static int grid_for(long long units, int n_sm) {
   return (int)std::max(1LL, std::min(units, cap));
 }
 
+// Device allocations are stream-ordered (cudaMallocAsync / cudaFreeAsync on
+// the forest's stream), so creating and destroying a forest does not
+// synchronise the work of other forests on the device.
 template <class T>
-static int dmalloc(T** p, long long n, long long& bytes) {
+static int dmalloc(T** p, long long n, long long& bytes, cudaStream_t st) {
   size_t b = (size_t)std::max(1LL, n) * sizeof(T);
-  if (cudaMalloc((void**)p, b) != cudaSuccess) return AFV_ERR_NOMEM;
+  if (cudaMallocAsync((void**)p, b, st) != cudaSuccess) {
+    *p = nullptr;
+    return AFV_ERR_NOMEM;
+  }
   bytes += (long long)b;
   return AFV_OK;
 }
 
 template <class T>
-static int dupload(T** p, const std::vector<T>& v, long long& bytes) {
-  int rc = dmalloc(p, (long long)v.size(), bytes);
+static int dupload(T** p, const std::vector<T>& v, long long& bytes, cudaStream_t st) {
+  int rc = dmalloc(p, (long long)v.size(), bytes, st);
   if (rc) return rc;
-  if (!v.empty() && cudaMemcpy(*p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice) != cudaSuccess)
+  if (!v.empty() &&
+      cudaMemcpyAsync(*p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, st) != cudaSuccess)
     return AFV_ERR_CUDA;
-  return AFV_OK;
+  return cudaStreamSynchronize(st) == cudaSuccess ? AFV_OK : AFV_ERR_CUDA;  // v may go away
+}
+
+// Freed device memory up to this size stays in the device's pool for the
+// next forest instead of going back to the driver at every synchronisation.
+static void retain_pool(int device) {
+  static bool done[64] = {};
+  if (device < 0 || device >= 64 || done[device]) return;
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+    unsigned long long keep = 8ULL << 30;
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  }
+  done[device] = true;
 }
 
 Forest::~Forest() {
   cudaSetDevice(device);
   if (stream) cudaStreamSynchronize(stream);
   void* ptrs[] = {meta.parent, meta.first_child, meta.tree, meta.offg, meta.offi, meta.bcval,
-                  meta.active, meta.desc, meta.nbo2, meta.err, d64.phi, d64.rhs,
+                  meta.active, meta.desc, meta.nbo2, meta.err, meta.rmin, d64.phi, d64.rhs,
                   d64.tmp, d32.phi, d32.rhs, d32.tmp, base_phi64, base_rhs64, d_lists, d_norm, d_red,
                   d_fmax, d_count, d_failed, d_stage, d_stage_slots};
   for (void* p : ptrs)
-    if (p) cudaFree(p);
+    if (p) cudaFreeAsync(p, stream);
+  if (stream) cudaStreamSynchronize(stream);
   for (const ProfEntry& p : prof) {
     cudaEventDestroy(p.start);
     cudaEventDestroy(p.stop);
@@ -224,41 +245,43 @@ int Forest::create(const std::vector<const HostTree*>& trees, const afv_forest_o
   cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, device);
   if (cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking) != cudaSuccess)
     return err = "cudaStreamCreate failed", AFV_ERR_CUDA;
+  retain_pool(device);
   const Plan& p = plan;
   bytes = 0;
 #define UP(field, vec) \
-  if ((rc = dupload(&meta.field, p.vec, bytes))) return err = "device allocation failed", rc;
+  if ((rc = dupload(&meta.field, p.vec, bytes, stream))) return err = "device allocation failed", rc;
   UP(parent, parent);
   UP(first_child, first_child);
   UP(tree, tree);
   UP(offg, offg);
   UP(offi, offi);
   UP(nbo2, nbo2);
+  UP(rmin, r_min);
 #undef UP
-  if (dmalloc(&meta.err, 1, bytes)) return err = "device allocation failed", AFV_ERR_NOMEM;
-  cudaMemset(meta.err, 0, sizeof(int));
+  if (dmalloc(&meta.err, 1, bytes, stream)) return err = "device allocation failed", AFV_ERR_NOMEM;
+  cudaMemsetAsync(meta.err, 0, sizeof(int), stream);
   if ((rc = upload_bc(err))) return rc;
   std::vector<int> act(p.n_trees, 1);
-  if ((rc = dupload(&meta.active, act, bytes))) return err = "device allocation failed", rc;
+  if ((rc = dupload(&meta.active, act, bytes, stream))) return err = "device allocation failed", rc;
   host_active = act;
 
-  if (dmalloc(&d64.phi, p.n_elem_g, bytes) || dmalloc(&d64.tmp, p.n_elem_g, bytes) ||
-      dmalloc(&d64.rhs, p.n_elem_i, bytes))
+  if (dmalloc(&d64.phi, p.n_elem_g, bytes, stream) || dmalloc(&d64.tmp, p.n_elem_g, bytes, stream) ||
+      dmalloc(&d64.rhs, p.n_elem_i, bytes, stream))
     return err = "device allocation of the FP64 state failed", AFV_ERR_NOMEM;
-  cudaMemset(d64.phi, 0, p.n_elem_g * sizeof(double));
-  cudaMemset(d64.tmp, 0, p.n_elem_g * sizeof(double));
-  cudaMemset(d64.rhs, 0, p.n_elem_i * sizeof(double));
+  cudaMemsetAsync(d64.phi, 0, p.n_elem_g * sizeof(double), stream);
+  cudaMemsetAsync(d64.tmp, 0, p.n_elem_g * sizeof(double), stream);
+  cudaMemsetAsync(d64.rhs, 0, p.n_elem_i * sizeof(double), stream);
   if (mixed) {
-    if (dmalloc(&d32.phi, p.n_elem_g, bytes) || dmalloc(&d32.tmp, p.n_elem_g, bytes) ||
-        dmalloc(&d32.rhs, p.n_elem_i, bytes))
+    if (dmalloc(&d32.phi, p.n_elem_g, bytes, stream) || dmalloc(&d32.tmp, p.n_elem_g, bytes, stream) ||
+        dmalloc(&d32.rhs, p.n_elem_i, bytes, stream))
       return err = "device allocation of the FP32 state failed", AFV_ERR_NOMEM;
-    cudaMemset(d32.phi, 0, p.n_elem_g * sizeof(float));
-    cudaMemset(d32.tmp, 0, p.n_elem_g * sizeof(float));
-    cudaMemset(d32.rhs, 0, p.n_elem_i * sizeof(float));
+    cudaMemsetAsync(d32.phi, 0, p.n_elem_g * sizeof(float), stream);
+    cudaMemsetAsync(d32.tmp, 0, p.n_elem_g * sizeof(float), stream);
+    cudaMemsetAsync(d32.rhs, 0, p.n_elem_i * sizeof(float), stream);
     int l0 = p.min_lvl;
     long long ng = (long long)p.lvl_n[p.L(l0)] * (long long)std::pow(p.nc_at(l0) + 2, p.dim);
     long long ni = (long long)p.lvl_n[p.L(l0)] * (long long)std::pow(p.nc_at(l0), p.dim);
-    if (dmalloc(&base_phi64, ng, bytes) || dmalloc(&base_rhs64, ni, bytes))
+    if (dmalloc(&base_phi64, ng, bytes, stream) || dmalloc(&base_rhs64, ni, bytes, stream))
       return err = "device allocation failed", AFV_ERR_NOMEM;
   }
   // level lists
@@ -274,10 +297,10 @@ int Forest::create(const std::vector<const HostTree*>& trees, const afv_forest_o
   }
   all_leaves_off = (int)lists.size();
   lists.insert(lists.end(), p.all_leaves.begin(), p.all_leaves.end());
-  if ((rc = dupload(&d_lists, lists, bytes))) return err = "device allocation failed", rc;
-  if (dmalloc(&d_norm, (long long)p.n_trees * dev::kStripes, bytes) ||
-      dmalloc(&d_red, p.n_trees, bytes) || dmalloc(&d_fmax, p.n_trees, bytes) ||
-      dmalloc(&d_count, 1, bytes) || dmalloc(&d_failed, p.n_trees, bytes))
+  if ((rc = dupload(&d_lists, lists, bytes, stream))) return err = "device allocation failed", rc;
+  if (dmalloc(&d_norm, (long long)p.n_trees * dev::kStripes, bytes, stream) ||
+      dmalloc(&d_red, p.n_trees, bytes, stream) || dmalloc(&d_fmax, p.n_trees, bytes, stream) ||
+      dmalloc(&d_count, 1, bytes, stream) || dmalloc(&d_failed, p.n_trees, bytes, stream))
     return err = "device allocation failed", AFV_ERR_NOMEM;
   if (cudaMallocHost((void**)&h_active, sizeof(int) * p.n_trees) != cudaSuccess ||
       cudaMallocHost((void**)&h_count, sizeof(int)) != cudaSuccess ||
@@ -305,13 +328,14 @@ void Forest::norm_fold() {
 
 int Forest::upload_bc(std::string& err) {
   long long b = 0;
-  if (meta.bcval) cudaFree(meta.bcval);
+  if (meta.bcval) cudaFreeAsync(meta.bcval, stream);
   meta.bcval = nullptr;
-  if (dupload(&meta.bcval, plan.bcval, b)) return err = "device allocation failed", AFV_ERR_NOMEM;
-  if (!meta.desc && dmalloc(&meta.desc, (long long)plan.desc.size(), bytes))
+  if (dupload(&meta.bcval, plan.bcval, b, stream)) return err = "device allocation failed", AFV_ERR_NOMEM;
+  if (!meta.desc && dmalloc(&meta.desc, (long long)plan.desc.size(), bytes, stream))
     return err = "device allocation failed", AFV_ERR_NOMEM;
-  if (cudaMemcpy(meta.desc, plan.desc.data(), plan.desc.size() * sizeof(SlotDesc),
-                 cudaMemcpyHostToDevice) != cudaSuccess)
+  if (cudaMemcpyAsync(meta.desc, plan.desc.data(), plan.desc.size() * sizeof(SlotDesc),
+                      cudaMemcpyHostToDevice, stream) != cudaSuccess ||
+      cudaStreamSynchronize(stream) != cudaSuccess)
     return err = "descriptor upload failed", AFV_ERR_CUDA;
   return AFV_OK;
 }
@@ -351,18 +375,18 @@ static int exchange(Forest& F, int t, int var, double* host, int interior_only, 
     total += interior_only ? (long long)std::pow(nc, D) : (long long)std::pow(nc + 2, D);
   }
   if (F.stage_elems < total || !F.d_stage) {
-    if (F.d_stage) cudaFree(F.d_stage);
-    if (F.d_stage_slots) cudaFree(F.d_stage_slots);
+    if (F.d_stage) cudaFreeAsync(F.d_stage, F.stream);
+    if (F.d_stage_slots) cudaFreeAsync(F.d_stage_slots, F.stream);
     F.d_stage = nullptr;
     F.d_stage_slots = nullptr;
-    if (cudaMalloc((void**)&F.d_stage, sizeof(double) * std::max(1LL, total)) != cudaSuccess)
+    if (cudaMallocAsync((void**)&F.d_stage, sizeof(double) * std::max(1LL, total), F.stream) != cudaSuccess)
       return err = "staging allocation failed", AFV_ERR_NOMEM;
     F.stage_elems = total;
   }
   if (!F.d_stage_slots) {
     size_t maxn = 0;
     for (const auto& o : p.host_order) maxn = std::max(maxn, o.size());
-    if (cudaMalloc((void**)&F.d_stage_slots, sizeof(int) * std::max<size_t>(1, maxn)) != cudaSuccess)
+    if (cudaMallocAsync((void**)&F.d_stage_slots, sizeof(int) * std::max<size_t>(1, maxn), F.stream) != cudaSuccess)
       return err = "staging allocation failed", AFV_ERR_NOMEM;
   }
   cudaStream_t st = F.stream;
@@ -727,6 +751,81 @@ int Forest::vcycle(const MgOpts& mg, int highest, bool set_residual, std::string
   return check_device_error(err);
 }
 
+// Times the sweep kernel variants on this forest (two FP32 correction
+// V-cycles each, on the mixed scratch state, which every solve
+// re-initialises) and keeps the fastest. Needs the mixed buffers.
+int Forest::autotune(int* choice, float* ms_out, std::string& err) {
+  if (!mixed) return err = "autotune needs a forest created with mixed_buffers", AFV_ERR_STATE;
+  MgOpts mg;
+  mg.n_down = mg.n_up = mg.n_base = 2;
+  const int candidates[3] = {1, 2, 0};
+  const int saved = sweep_kernel, saved_mask = prof_mask;
+  prof_mask = 0;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  int best = saved;
+  float best_ms = 1e30f;
+  for (int c = 0; c < 3; ++c) {
+    sweep_kernel = candidates[c];
+    vcycle_t(d32, mg, plan.max_lvl, true, true, true);  // warm-up (first launches set attributes)
+    cudaEventRecord(e0, stream);
+    for (int r = 0; r < 2; ++r) vcycle_t(d32, mg, plan.max_lvl, true, true, true);
+    cudaEventRecord(e1, stream);
+    cudaEventSynchronize(e1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms_out) ms_out[c] = ms / 2;
+    if (ms < best_ms) {
+      best_ms = ms;
+      best = candidates[c];
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  sweep_kernel = best;
+  prof_mask = saved_mask;
+  drop_graphs();
+  if (choice) *choice = best;
+  if (int rc = check(err, "autotune")) return rc;
+  return check_device_error(err);
+}
+
+// rhs of one tree := sum of Gaussians (or their Laplacian) at the cell
+// centres, evaluated on the device: one launch per level over the tree's
+// slots of that level (a contiguous range, trees being stored tree-major
+// within a level).
+int Forest::set_source_device(int t, int lpl, int n_gauss, const double* gauss, std::string& err) {
+  if (t < 0 || t >= plan.n_trees) return err = "tree index out of range", AFV_ERR_INVALID;
+  if (n_gauss < 0 || n_gauss > dev::kMaxGauss)
+    return err = "at most " + std::to_string(dev::kMaxGauss) + " Gaussians on the device", AFV_ERR_INVALID;
+  dev::GaussSet gs;
+  gs.n = n_gauss;
+  gs.lpl = lpl;
+  for (int k = 0; k < n_gauss * (2 + plan.dim); ++k) gs.g[k] = gauss[k];
+  Meta m = meta_of(meta);
+  for (int l = plan.min_lvl; l <= plan.max_lvl; ++l) {
+    const int lo = plan.lvl_lo[plan.L(l)], n = plan.lvl_n[plan.L(l)];
+    int a = -1, b = -1;
+    for (int k = 0; k < n; ++k)
+      if (plan.tree[lo + k] == t) {
+        if (a < 0) a = lo + k;
+        b = lo + k;
+      }
+    if (a < 0) continue;
+    BoxSet bs{nullptr, a, b - a + 1, plan.offg[a], plan.offi[a]};
+    with_nc(plan.dim, plan.nc_at(l), [&](auto d_, auto nc_) {
+      constexpr int D = decltype(d_)::value, NC = decltype(nc_)::value;
+      using G = dev::Geo<D, NC>;
+      long long items = (long long)bs.n * G::SI;
+      ProfScope ps(this, kProfOther, 8.0 * items);
+      launch_k(dev::k_source<D, NC>, grid_for((items + 255) / 256, n_sm), 256, 0, stream, m, bs, t,
+               (const double*)meta.rmin, gs, d64.rhs);
+    });
+  }
+  return check(err, "set_source_device");
+}
+
 int Forest::gc_tree(std::string& err) {
   for (int l = plan.min_lvl; l <= plan.max_lvl; ++l) fill(d64, l, false);
   return check(err, "gc_tree");
@@ -1039,7 +1138,8 @@ int Forest::solve(const MgOpts& mg, int precision, double tol, int max_cycles, S
   }
   if (int rc = check(err, "solve")) return rc;
   std::vector<int> failed(nt, 0);
-  cudaMemcpy(failed.data(), d_failed, sizeof(int) * nt, cudaMemcpyDeviceToHost);
+  cudaMemcpyAsync(failed.data(), d_failed, sizeof(int) * nt, cudaMemcpyDeviceToHost, stream);
+  cudaStreamSynchronize(stream);
   int n_failed = 0;
   for (int t = 0; t < nt; ++t) n_failed += failed[t] != 0;
   st.status = n_failed ? AFV_ERR_DIVERGED : n_active > 0 ? AFV_ERR_TIMEOUT : AFV_OK;

@@ -55,24 +55,25 @@ def barrier(world):
         dist.barrier()
 
 
-def max_over_ranks(x, world):
+def _reduce(x, world, op):
     if world == 1:
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=op)
     return float(t.item())
+
+
+def max_over_ranks(x, world):
+    import torch.distributed as dist
+    return _reduce(x, world, dist.ReduceOp.MAX) if world > 1 else x
 
 
 def sum_over_ranks(x, world):
-    if world == 1:
-        return x
-    import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.SUM)
-    return float(t.item())
+    return _reduce(x, world, dist.ReduceOp.SUM) if world > 1 else x
 
 
 class Clocks:
@@ -235,6 +236,95 @@ def run_reference(args, spec):
     print(json.dumps(line))
 
 
+def run_batched(afv, W, local, rank, world, n_trees=256):
+    """Batched 2-D solves: 256 independent random quadtrees in one forest per
+    GPU (trees placed over the ranks), one launch per level and operator for
+    all of them, autotuned sweep kernel, mixed-precision solve to 1e-8."""
+    import torch
+    from afivo_gb300 import placement
+    specs = W.c4_random_2d(n_trees)
+    t0 = time.time()
+    trees = [W.build_tree(s) for s in specs]
+    t_build = time.time() - t0
+    work = [float(t.leaf_cells()) for t in trees]
+    mine = placement.shard(list(range(n_trees)), work, rank, world)
+    forest = afv.Forest([trees[i] for i in mine], device=local, mixed=True)
+    for k, i in enumerate(mine):
+        forest.set_source(k, specs[i]["gauss"], lpl=True)
+    choice, tune_ms = forest.autotune()
+    ext = torch.cuda.ExternalStream(forest.stream())
+
+    def solve():
+        forest.zero(afv.AFV_PHI)
+        cyc, rel, rc = forest.solve(afv.AFV_PREC_MIXED, tol=TOL, max_cycles=60, check=False)
+        if rc != 0:
+            raise RuntimeError(f"batched solve failed: rc={rc}")
+        return cyc, rel
+
+    solve()
+    barrier(world)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(ext)
+    cyc, rel = solve()
+    e1.record(ext)
+    e1.synchronize()
+    ms = max_over_ranks(e0.elapsed_time(e1), world)
+    cells = forest.info()["leaf_cells"]
+    unknowns = sum(float(t.leaf_cells()) * c for t, c in zip([trees[i] for i in mine], cyc))
+    unknowns = sum_over_ranks(unknowns, world)
+    total_cells = sum_over_ranks(float(cells), world)
+    out = {"workload": "random2d_256trees_seed4", "trees": n_trees, "leaf_cells": int(total_cells),
+           "boxes": int(sum_over_ranks(float(forest.info()["n_boxes"]), world)),
+           "ms_per_solve": ms, "unknowns_per_s": unknowns / (ms / 1e3),
+           "cycles_min": int(min(cyc)), "cycles_max": int(max(cyc)), "rel_res_max": float(max(rel)),
+           "sweep_kernel": choice, "autotune_ms_per_vcycle": {str(k): round(v, 3) for k, v in tune_ms.items()},
+           "tree_build_s": round(t_build, 2)}
+    forest.close()
+    return out
+
+
+def run_serving(afv, W, local, rank, world, n_requests=64):
+    """Served 3-D requests (Poisson arrivals, mean 200/s; uniform octrees of
+    8^3 boxes from 32^3 to 256^3 cells): continuous batching under an HBM
+    budget, mixed and FP64, p50/p99 latency and solves/s."""
+    from afivo_gb300 import placement, serving
+    reqs = W.c5_requests(n=n_requests)
+    t0 = time.time()
+    trees = [W.build_tree(r) for r in reqs]
+    t_build = time.time() - t0
+    work = [float(t.leaf_cells()) for t in trees]
+    mine = placement.shard(list(range(len(reqs))), work, rank, world)
+    out = {"workload": "poisson3d_requests_seed5", "requests": len(reqs), "tree_build_s": round(t_build, 2)}
+    for name, prec in (("mixed", afv.AFV_PREC_MIXED), ("fp64", afv.AFV_PREC_FP64)):
+        srv = serving.Server(device=local, budget_bytes=32 << 30, slots=4, max_batch=8, precision=prec)
+        srv.serve([reqs[i] for i in mine[:4]], [trees[i] for i in mine[:4]], realtime=False)  # warm-up
+        res = srv.serve([reqs[i] for i in mine], [trees[i] for i in mine], realtime=True)
+        summ = serving.summary(res)
+        summ["p99_ms"] = max_over_ranks(summ["p99_ms"], world)
+        summ["solves_per_s"] = sum_over_ranks(summ["solves_per_s"], world)
+        summ["unknowns_per_s"] = sum_over_ranks(summ["unknowns_per_s"], world)
+        summ["peak_device_bytes"] = srv.last_peak_bytes
+        out[name] = {k: (float("%.6g" % v) if isinstance(v, float) else v) for k, v in summ.items()}
+    return out, reqs
+
+
+def cpu_serving_sample(reqs, threads, n=4):
+    """The oracle's solve time per request on the host cores for a sample of
+    the requests (solved one after another, as a CPU server would)."""
+    picks = list(range(0, len(reqs), max(1, len(reqs) // n)))[:n]
+    times, cells = [], []
+    for i in picks:
+        s = OracleSolver(reqs[i], threads)
+        c, dt, _ = s.solve()
+        times.append(dt * 1e3)
+        cells.append(s.cells * c)
+    return {"sample": f"requests {picks}, solved one at a time on {threads} threads",
+            "ms_p50": float(np.percentile(times, 50)), "ms_max": float(max(times)),
+            "solves_per_s": len(times) / (sum(times) / 1e3),
+            "unknowns_per_s": sum(cells) / (sum(times) / 1e3)}
+
+
 def profile_solves(spec, n):
     """n mixed solves of the workload with nothing timed: the command the
     kernel profiles are taken on (few launches before the first V-cycle)."""
@@ -262,6 +352,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--small", action="store_true", help="smaller tree (quick checks)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batched", action="store_true", help="skip the 256-tree batched solve")
+    ap.add_argument("--no-serving", action="store_true", help="skip the served request stream")
     ap.add_argument("--profile-solves", type=int, default=0,
                     help="only run this many mixed solves, untimed (a short command to profile)")
     args = ap.parse_args()
@@ -368,6 +460,9 @@ def main():
     e2e_s = max_over_ranks(time.perf_counter() - t0, world)
     e2e_value = cells * sum_over_ranks(float(e2e_cycles), world) / e2e_s
 
+    batched = None if args.no_batched else run_batched(afv, W, local, rank, world)
+    served, reqs = (None, None) if args.no_serving else run_serving(afv, W, local, rank, world)
+
     peak, peak_kind = load_peaks()
     achieved = sweep_bytes / (sweep_ms / 1e3) / 1e9 if sweep_ms > 0 else None
     traffic = load_traffic()
@@ -378,6 +473,8 @@ def main():
         cpu = {"value": v, "unit": "unknowns/s", "cores": cores, "kind": "port",
                "sample": f"{n} FP64 solves of the full tree to {TOL:g} on the oracle "
                          f"({dt:.1f} s, {cores} threads; median rate)"}
+        if served is not None:
+            served["cpu_oracle"] = cpu_serving_sample(reqs, cores)
     if rank != 0:
         return
     line = {
@@ -403,6 +500,8 @@ def main():
                      "traffic": traffic.get("dram_bytes_per_launch") if traffic else None,
                      "traffic_note": traffic.get("note") if traffic else None},
         "kernels": breakdown,
+        "batched": batched,
+        "serving": served,
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": "unknowns/s", "h2d_bytes_per_step": n_in * 8,
                 "d2h_bytes_per_step": n_in * 8},

@@ -157,6 +157,12 @@ int afv_forest_set_var(afv_forest* f, int tree, int var, const double* host, int
 int afv_forest_get_var(afv_forest* f, int tree, int var, double* host, int interior_only);
 /* Fill rhs of one tree with a Gaussian source at the cell centres. */
 int afv_forest_set_source(afv_forest* f, int tree, int src_lpl, int n_gauss, const double* gauss);
+/* afv_forest_set_source evaluated on the device (at most 16 Gaussians), for
+ * callers that stream many trees (a request loop): microseconds instead of
+ * the host evaluation's seconds for a 256^3 tree. Uses the device's exp, so
+ * values may differ from the host evaluation in the last bit. */
+int afv_forest_set_source_device(afv_forest* f, int tree, int src_lpl, int n_gauss,
+                                 const double* gauss);
 /* Boundary values on physical faces of one tree: the sides_bc hook of the
  * reference (src/m_aX_t.f90:276-282) sampled once. bc_type is AFV_BC_*; the
  * boundary value is 0 when n_gauss == 0, else the Gaussian source at the face
@@ -256,6 +262,12 @@ int afv_forest_profile_read(afv_forest* f, int kind, long long* launches, double
 enum { AFV_OPT_SWEEP_KERNEL = 0, AFV_OPT_GRAPHS = 1 };
 int afv_forest_set_option(afv_forest* f, int option, int value);
 int afv_forest_get_option(afv_forest* f, int option, int* value);
+/* No counterpart in the reference: times the sweep kernel variants on this
+ * forest (two FP32 correction V-cycles each on the mixed-precision scratch
+ * state; needs mixed_buffers) and sets AFV_OPT_SWEEP_KERNEL to the fastest.
+ * choice receives it; ms3 (may be NULL) the ms per V-cycle of variants 1, 2
+ * and 0 in that order. */
+int afv_forest_autotune(afv_forest* f, int* choice, float* ms3);
 
 /* No counterpart in the reference: the profiled launches one by one (up to
  * max; n_total receives how many were recorded): kernel kind, level, device
