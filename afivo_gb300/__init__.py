@@ -131,7 +131,7 @@ def lib():
             "afv_mg_fas_fmg": (I, [P, ctypes.POINTER(MgOpts), I, I]),
             "afv_gc_tree": (I, [P]),
             "afv_tree_max_abs_cc": (I, [P, I, I, dp]),
-            "afv_forest_profile_entries": (I, [P, LL, ip, ip, dp, dp, llp]),
+            "afv_forest_profile_entries": (I, [P, LL, ip, ip, dp, dp, ip, llp]),
             "afv_forest_set_option": (I, [P, I, I]),
             "afv_forest_set_source_device": (I, [P, I, I, I, dp]),
             "afv_forest_autotune": (I, [P, ip, ctypes.POINTER(ctypes.c_float)]),
@@ -464,16 +464,16 @@ class Forest:
         return v.value
 
     def profile_entries(self):
-        """Profiled launches one by one: dict of arrays kind, level, ms, bytes."""
+        """Profiled event pairs: dict of arrays kind, level, ms, bytes, launches."""
         n = ctypes.c_longlong(0)
-        _check(lib().afv_forest_profile_entries(self.h, 0, None, None, None, None, ctypes.byref(n)))
+        _check(lib().afv_forest_profile_entries(self.h, 0, None, None, None, None, None, ctypes.byref(n)))
         m = max(int(n.value), 1)
-        kind, level = np.zeros(m, np.int32), np.zeros(m, np.int32)
+        kind, level, cnt = np.zeros(m, np.int32), np.zeros(m, np.int32), np.zeros(m, np.int32)
         ms, by = np.zeros(m), np.zeros(m)
         _check(lib().afv_forest_profile_entries(self.h, m, _ip(kind), _ip(level), _dp(ms), _dp(by),
-                                                ctypes.byref(n)))
+                                                _ip(cnt), ctypes.byref(n)))
         k = int(n.value)
-        return dict(kind=kind[:k], level=level[:k], ms=ms[:k], bytes=by[:k])
+        return dict(kind=kind[:k], level=level[:k], ms=ms[:k], bytes=by[:k], launches=cnt[:k])
 
     def profile_read(self, kind):
         n, ms, b = ctypes.c_longlong(0), ctypes.c_double(0), ctypes.c_double(0)

@@ -402,12 +402,12 @@ int afv_forest_profile_read(afv_forest* f, int kind, long long* launches, double
 }
 
 int afv_forest_profile_entries(afv_forest* f, long long max, int* kind, int* level, double* ms,
-                               double* algorithmic_bytes, long long* n_total) {
-  if (!n_total || (max > 0 && (!kind || !level || !ms || !algorithmic_bytes)))
+                               double* algorithmic_bytes, int* launches, long long* n_total) {
+  if (!n_total || (max > 0 && (!kind || !level || !ms || !algorithmic_bytes || !launches)))
     return fail(AFV_ERR_INVALID, "NULL argument");
   FOREST_CALL(f, {
     (void)err;
-    *n_total = f->f.prof_entries(max, kind, level, ms, algorithmic_bytes);
+    *n_total = f->f.prof_entries(max, kind, level, ms, algorithmic_bytes, launches);
     return AFV_OK;
   });
 }

@@ -59,7 +59,8 @@ struct ProfEntry {
   cudaEvent_t start, stop;
   int kind;
   int level;     // level the launch works on (parents' level for coarse_rhs / correct)
-  double bytes;  // algorithmic bytes of the launch
+  double bytes;  // algorithmic bytes of the launches
+  int count;     // launches between the two events (consecutive half-sweeps share a pair)
 };
 
 struct SolveStats {
@@ -112,13 +113,18 @@ class Forest {
   // are bracketed by CUDA events on the forest's stream
   int prof_mask = 0;
   int prof_level = 0;  // level tag of the next profiled launches
+  // Consecutive half-sweeps of one level are timed by one pair of events
+  // (a group), so the events' own cost is not charged to every launch.
+  bool group_on = false;
+  double group_bytes = 0;
+  int group_count = 0;
   long long n_launches = 0;  // every kernel launched on the stream
   std::vector<ProfEntry> prof;
   std::vector<cudaEvent_t> event_pool;
   cudaEvent_t prof_begin(int kind);
-  void prof_end(cudaEvent_t start, int kind, double bytes);
+  void prof_end(cudaEvent_t start, int kind, double bytes, int count = 1);
   int prof_read(int kind, long long* launches, double* ms, double* bytes);
-  long long prof_entries(long long max, int* kind, int* level, double* ms, double* bytes);
+  long long prof_entries(long long max, int* kind, int* level, double* ms, double* bytes, int* count);
   void prof_reset();
 
   ~Forest();

@@ -158,6 +158,7 @@ int Forest::check(std::string& err, const char* where) {
 cudaEvent_t Forest::prof_begin(int kind) {
   ++n_launches;
   if (!(prof_mask & (1 << kind))) return nullptr;
+  if (group_on && kind == kProfSweep) return nullptr;  // timed by the group
   cudaEvent_t e;
   if (!event_pool.empty()) {
     e = event_pool.back();
@@ -169,7 +170,12 @@ cudaEvent_t Forest::prof_begin(int kind) {
   return e;
 }
 
-void Forest::prof_end(cudaEvent_t start, int kind, double b) {
+void Forest::prof_end(cudaEvent_t start, int kind, double b, int count) {
+  if (group_on && kind == kProfSweep && count == 1) {
+    group_bytes += b;
+    ++group_count;
+    return;
+  }
   if (!start) return;
   cudaEvent_t e;
   if (!event_pool.empty()) {
@@ -179,10 +185,10 @@ void Forest::prof_end(cudaEvent_t start, int kind, double b) {
     cudaEventCreate(&e);
   }
   cudaEventRecord(e, stream);
-  prof.push_back(ProfEntry{start, e, kind, prof_level, b});
+  prof.push_back(ProfEntry{start, e, kind, prof_level, b, count});
 }
 
-long long Forest::prof_entries(long long max, int* kind, int* level, double* ms, double* b) {
+long long Forest::prof_entries(long long max, int* kind, int* level, double* ms, double* b, int* count) {
   cudaStreamSynchronize(stream);
   long long n = 0;
   for (const ProfEntry& p : prof) {
@@ -193,6 +199,7 @@ long long Forest::prof_entries(long long max, int* kind, int* level, double* ms,
     level[n] = p.level;
     ms[n] = x;
     b[n] = p.bytes;
+    count[n] = p.count;
     ++n;
   }
   return (long long)prof.size();
@@ -208,7 +215,7 @@ int Forest::prof_read(int kind, long long* launches, double* ms, double* b) {
     cudaEventElapsedTime(&x, p.start, p.stop);
     t += x;
     by += p.bytes;
-    ++n;
+    n += p.count;
   }
   *launches = n;
   *ms = t;
@@ -226,6 +233,30 @@ void Forest::prof_reset() {
 }
 
 // Brackets one launch with profiler events.
+// One pair of events around consecutive half-sweeps of a level.
+struct SweepGroup {
+  Forest* f;
+  cudaEvent_t e = nullptr;
+  explicit SweepGroup(Forest* f_) : f(f_) {
+    if (f->prof_mask & (1 << kProfSweep)) {
+      e = f->prof_begin(kProfSweep);
+      --f->n_launches;  // the group is not a launch
+      f->group_on = true;
+      f->group_bytes = 0;
+      f->group_count = 0;
+    }
+  }
+  ~SweepGroup() {
+    if (e) {
+      f->group_on = false;
+      if (f->group_count)
+        f->prof_end(e, kProfSweep, f->group_bytes, f->group_count);
+      else
+        f->prof_end(e, kProfSweep, 0.0, 0);
+    }
+  }
+};
+
 struct ProfScope {
   Forest* f;
   int kind;
@@ -663,6 +694,7 @@ void Forest::vcycle_t(const Arrays<T>& a, const MgOpts& mg, int highest, bool ho
                       bool inner) {
   const int l0 = plan.min_lvl;
   auto sweeps = [&](const auto& arr, int l, int n_cycle) {
+    SweepGroup sg(this);
     for (int n = 1; n <= 2 * n_cycle; ++n) sweep(arr, l, n, n > 1 || l != highest, homog);
   };
   for (int l = highest; l >= l0 + 1; --l) {
@@ -700,6 +732,7 @@ void Forest::vcycle_t(const Arrays<T>& a, const MgOpts& mg, int highest, bool ho
   for (int l = l0 + 1; l <= highest; ++l) {
     correct(a, l - 1);
     if (mg.n_up > 0) {
+      SweepGroup sg(this);
       for (int n = 1; n <= 2 * mg.n_up; ++n) sweep(a, l, n, true, homog);
     }
     if (!inner) {

@@ -429,9 +429,22 @@ def main():
     ms64 = max_over_ranks(ms64, world)
     value64 = cells * sum_over_ranks(float(sum(cyc64)), world) / (ms64 / 1e3)
 
-    # roofline: one mixed solve with CUDA events around every sweep launch
+    # roofline: one mixed solve with CUDA events around the sweeps (one pair
+    # per run of consecutive half-sweeps of a level)
     timed(afv.AFV_PREC_MIXED, 1, mask=1 << 0)
     sweep_n, sweep_ms, sweep_bytes = forest.profile_read(0)
+    pe = forest.profile_entries()
+    by_level = {}
+    for k, lv, t_ms, b, c in zip(pe["kind"], pe["level"], pe["ms"], pe["bytes"], pe["launches"]):
+        if k != 0 or c == 0:
+            continue
+        a = by_level.setdefault(int(lv), [0, 0.0, 0.0])
+        a[0] += int(c)
+        a[1] += float(t_ms)
+        a[2] += float(b)
+    sweep_levels = {str(lv): {"launches": a[0], "us_per_launch": round(1e3 * a[1] / a[0], 2),
+                              "GB/s": round(a[2] / (a[1] / 1e3) / 1e9, 1)}
+                    for lv, a in sorted(by_level.items())}
     # per-kernel breakdown: one mixed solve, every kind profiled
     timed(afv.AFV_PREC_MIXED, 1, mask=0xFF)
     breakdown = {}
@@ -495,7 +508,9 @@ def main():
                      "peak_kind": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
                      "algorithmic_bytes": "12 B per cell of the swept level per half-sweep "
                                           "(read phi, rhs; write phi; FP32)",
-                     "timed": "CUDA events around each sweep launch, one profiled mixed solve",
+                     "timed": "CUDA events around each run of consecutive half-sweeps of a level "
+                              "(4 launches), one profiled mixed solve",
+                     "per_level": sweep_levels,
                      "launches": sweep_n, "ms": sweep_ms,
                      "traffic": traffic.get("dram_bytes_per_launch") if traffic else None,
                      "traffic_note": traffic.get("note") if traffic else None},

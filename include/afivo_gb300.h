@@ -269,11 +269,12 @@ int afv_forest_get_option(afv_forest* f, int option, int* value);
  * and 0 in that order. */
 int afv_forest_autotune(afv_forest* f, int* choice, float* ms3);
 
-/* No counterpart in the reference: the profiled launches one by one (up to
- * max; n_total receives how many were recorded): kernel kind, level, device
- * time in ms and algorithmic bytes. */
+/* No counterpart in the reference: the profiled event pairs one by one (up
+ * to max; n_total receives how many were recorded): kernel kind, level,
+ * device time in ms, algorithmic bytes and the launches the pair covers
+ * (the consecutive half-sweeps of a level share one pair). */
 int afv_forest_profile_entries(afv_forest* f, long long max, int* kind, int* level, double* ms,
-                               double* algorithmic_bytes, long long* n_total);
+                               double* algorithmic_bytes, int* launches, long long* n_total);
 
 #ifdef __cplusplus
 }
