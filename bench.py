@@ -309,6 +309,58 @@ def run_serving(afv, W, local, rank, world, n_requests=64):
     return out, reqs
 
 
+def run_uniform(afv, W, local, rank, world):
+    """2-D uniform periodic case: 16x16 boxes, 4096^2 cells, white-noise
+    source with zero mean (seed 3); FMG followed by V-cycles to 1e-8, FP64
+    and mixed, with the per-kernel bandwidth of one mixed solve. The
+    periodic problem is singular; its source has zero mean, so the residual
+    converges without subtracting the mean of phi."""
+    import torch
+    spec = W.c3_uniform_2d()
+    tree = W.build_tree(spec)
+    forest = afv.Forest([tree], device=local, mixed=True)
+    info = forest.info()
+    nc = spec["n_cell"]
+    rng = np.random.default_rng(3)
+    parts = []
+    for lvl in range(tree.min_lvl, tree.highest_lvl + 1):
+        n = len(tree.level(lvl)[0]) * tree.n_cell_at(lvl) ** 2
+        parts.append(rng.standard_normal(n) if lvl == tree.highest_lvl else np.zeros(n))
+    top = parts[-1]
+    top -= top.mean()
+    forest.set_var(0, afv.AFV_RHS, np.concatenate(parts), interior_only=True)
+    ext = torch.cuda.ExternalStream(forest.stream())
+    out = {"workload": spec["name"], "leaf_cells": info["leaf_cells"], "boxes": info["n_boxes"]}
+    for name, prec in (("mixed", afv.AFV_PREC_MIXED), ("fp64", afv.AFV_PREC_FP64)):
+        def run():
+            forest.zero(afv.AFV_PHI)
+            forest.fmg(set_residual=False, have_guess=False)
+            cyc, rel, rc = forest.solve(prec, tol=TOL, max_cycles=60, check=False)
+            return int(cyc[0]), float(rel[0]), rc
+        run()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(ext)
+        cyc, rel, rc = run()
+        e1.record(ext)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        out[name] = {"fmg_then_cycles": cyc, "rel_res": rel, "status": rc, "ms": round(ms, 3),
+                     "unknowns_per_s": info["leaf_cells"] * (cyc + 1) / (ms / 1e3)}
+    forest.profile(0xFF)
+    forest.zero(afv.AFV_PHI)
+    forest.solve(afv.AFV_PREC_MIXED, tol=TOL, max_cycles=60, check=False)
+    kern = {}
+    for k, kname in enumerate(afv.KERNEL_KINDS):
+        n, kms, kb = forest.profile_read(k)
+        if n and kms > 0:
+            kern[kname] = {"launches": int(n), "ms": round(kms, 4), "GB/s": round(kb / (kms / 1e3) / 1e9, 1)}
+    forest.profile(0)
+    out["kernels_mixed_solve"] = kern
+    forest.close()
+    return out
+
+
 def cpu_serving_sample(reqs, threads, n=4):
     """The oracle's solve time per request on the host cores for a sample of
     the requests (solved one after another, as a CPU server would)."""
@@ -354,6 +406,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true", help="skip the 256-tree batched solve")
     ap.add_argument("--no-serving", action="store_true", help="skip the served request stream")
+    ap.add_argument("--no-uniform", action="store_true", help="skip the 4096^2 periodic case")
     ap.add_argument("--profile-solves", type=int, default=0,
                     help="only run this many mixed solves, untimed (a short command to profile)")
     args = ap.parse_args()
@@ -475,6 +528,7 @@ def main():
 
     batched = None if args.no_batched else run_batched(afv, W, local, rank, world)
     served, reqs = (None, None) if args.no_serving else run_serving(afv, W, local, rank, world)
+    uniform = None if args.no_uniform else run_uniform(afv, W, local, rank, world)
 
     peak, peak_kind = load_peaks()
     achieved = sweep_bytes / (sweep_ms / 1e3) / 1e9 if sweep_ms > 0 else None
@@ -517,6 +571,7 @@ def main():
         "kernels": breakdown,
         "batched": batched,
         "serving": served,
+        "uniform_periodic": uniform,
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": "unknowns/s", "h2d_bytes_per_step": n_in * 8,
                 "d2h_bytes_per_step": n_in * 8},
