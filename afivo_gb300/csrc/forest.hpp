@@ -163,7 +163,7 @@ class Forest {
                                        bool homog = false);
   template <class T> void coarse_rhs(const Arrays<T>& a, int lvl_parent, bool copy_tmp,
                                      bool pull = false, bool homog = false);
-  template <class T> void correct(const Arrays<T>& a, int lvl_parent);
+  template <class T> void correct(const Arrays<T>& a, int lvl_parent, bool pull = false, bool homog = false);
   template <class T> void residual(const Arrays<T>& a, int lvl, unsigned long long* norm, bool store);
   template <class T> void gsrb_boxes(const Arrays<T>& a, int lvl, int n_cycle, bool homog);
   template <class T> void update_coarse_t(const Arrays<T>& a, int lvl, bool homog, bool copy_tmp);

@@ -1051,7 +1051,7 @@ k_coarse_rhs(Meta m, BoxSet bs, T* __restrict__ phi, T* __restrict__ rhs,
 // ---------------------------------------------------------------------------
 template <int D, int NC, bool SUB, class T>
 __global__ void __launch_bounds__(kThreads)
-k_correct(Meta m, BoxSet bs, T* __restrict__ phi, T* __restrict__ tmp) {
+k_correct(Meta m, BoxSet bs, T* __restrict__ phi, T* __restrict__ tmp, int pull, int homog) {
   pdl_wait();
   pdl_trigger();
   using G = Geo<D, NC>;  // parent geometry
@@ -1066,18 +1066,26 @@ k_correct(Meta m, BoxSet bs, T* __restrict__ phi, T* __restrict__ tmp) {
   __shared__ int s_act[BPC];
   const int groups = (bs.n + BPC - 1) / BPC;
   for (int grp = blockIdx.x; grp < groups; grp += gridDim.x) {
-    const int nbox = min(BPC, bs.n - grp * BPC);
-    if (threadIdx.x < BPC) {
-      int s = threadIdx.x < nbox ? box_at(bs, grp * BPC + threadIdx.x) : -1;
-      s_slot[threadIdx.x] = s;
-      s_act[threadIdx.x] = (s >= 0) ? m.active[m.tree[s]] : 0;
+    int nbox;
+    if (pull) {
+      // The ghost fill of the parents (a$D_gc_box after their up sweeps),
+      // stored as the fill stores it, then tmp = phi - tmp from the staged box.
+      nbox = stage_boxes<D, NC, T, BPC>(m, bs, grp, phi, sm, s_slot, s_act);
+      pull_all_ghosts<D, NC, T>(m, phi, sm, s_slot, s_act, nbox, homog != 0, phi);
+    } else {
+      nbox = min(BPC, bs.n - grp * BPC);
+      if (threadIdx.x < BPC) {
+        int s = threadIdx.x < nbox ? box_at(bs, grp * BPC + threadIdx.x) : -1;
+        s_slot[threadIdx.x] = s;
+        s_act[threadIdx.x] = (s >= 0) ? m.active[m.tree[s]] : 0;
+      }
+      __syncthreads();
     }
-    __syncthreads();
     for (int e = threadIdx.x; e < nbox * (G::SG / VW); e += blockDim.x) {
       int b = e / (G::SG / VW), q = e % (G::SG / VW);
       if (!s_act[b]) continue;
       long long o = m.offg[s_slot[b]];
-      V p = reinterpret_cast<const V*>(phi + o)[q];
+      V p = pull ? reinterpret_cast<const V*>(sm + b * G::SG)[q] : reinterpret_cast<const V*>(phi + o)[q];
       V t = reinterpret_cast<const V*>(tmp + o)[q];
       V r;
       if constexpr (VW == 2) {

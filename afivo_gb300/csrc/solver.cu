@@ -618,7 +618,7 @@ void Forest::coarse_rhs(const Arrays<T>& a, int lp, bool copy_tmp, bool pull, bo
 }
 
 template <class T>
-void Forest::correct(const Arrays<T>& a, int lp) {
+void Forest::correct(const Arrays<T>& a, int lp, bool pull, bool homog) {
   prof_level = lp;
   int np = n_parents(lp);
   if (!np) return;
@@ -633,11 +633,12 @@ void Forest::correct(const Arrays<T>& a, int lp) {
     int grid = grid_for((np + BPC - 1) / BPC, n_sm);
     // parent: read phi, tmp, write tmp; children: read and write phi
     ProfScope ps(this, kProfCorrect, (3.0 + 2.0 * (1 << D)) * np * G::SI * sizeof(T));
+    const int pl = pull ? 1 : 0, hg = homog ? 1 : 0;
     if (sub) {
       if constexpr (!(D == 2 && NC == 16) && !(D == 3 && NC == 8))
-        launch_k(dev::k_correct<D, NC, true, T>, grid, dev::kThreads, 0, stream, m, bs, a.phi, a.tmp);
+        launch_k(dev::k_correct<D, NC, true, T>, grid, dev::kThreads, 0, stream, m, bs, a.phi, a.tmp, pl, hg);
     } else {
-      launch_k(dev::k_correct<D, NC, false, T>, grid, dev::kThreads, 0, stream, m, bs, a.phi, a.tmp);
+      launch_k(dev::k_correct<D, NC, false, T>, grid, dev::kThreads, 0, stream, m, bs, a.phi, a.tmp, pl, hg);
     }
   });
 }
@@ -730,19 +731,17 @@ void Forest::vcycle_t(const Arrays<T>& a, const MgOpts& mg, int highest, bool ho
     fill(a, l0, homog);
   }
   for (int l = l0 + 1; l <= highest; ++l) {
-    correct(a, l - 1);
+    // Inner correction cycle of the mixed path: its result is read only on
+    // interiors, and its ghost cells only on parents (by the correction of
+    // their children and by the children's refinement-boundary ghosts), so
+    // the ghost fill of level l-1 is done by the correction itself, on the
+    // parents only. The FP64 cycle fills every box, as the reference does.
+    correct(a, l - 1, inner && l - 1 > l0, homog);
     if (mg.n_up > 0) {
       SweepGroup sg(this);
       for (int n = 1; n <= 2 * mg.n_up; ++n) sweep(a, l, n, true, homog);
     }
-    if (!inner) {
-      fill(a, l, homog);
-    } else if (l < highest && n_parents(l)) {
-      // Inner correction cycle of the mixed path: its result is read only on
-      // interiors, and its ghost cells only by the children of parents at
-      // refinement boundaries during this cycle.
-      fill_set(a, l, BoxSet{parents_list(l), 0, n_parents(l)}, homog);
-    }
+    if (!inner) fill(a, l, homog);
   }
 }
 
