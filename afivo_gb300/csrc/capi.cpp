@@ -423,6 +423,11 @@ int afv_forest_set_option(afv_forest* f, int option, int value) {
       f->f.use_graphs = value != 0;
       f->f.drop_graphs();
       return AFV_OK;
+    case AFV_OPT_RESTRICT_KERNEL:
+      if (value != 0 && value != 1) return fail(AFV_ERR_INVALID, "restrict kernel must be 0 or 1");
+      f->f.use_restrict_warp = value != 0;
+      f->f.drop_graphs();
+      return AFV_OK;
   }
   return fail(AFV_ERR_INVALID, "unknown option");
 }
@@ -432,6 +437,7 @@ int afv_forest_get_option(afv_forest* f, int option, int* value) {
   switch (option) {
     case AFV_OPT_SWEEP_KERNEL: *value = f->f.sweep_kernel; return AFV_OK;
     case AFV_OPT_GRAPHS: *value = f->f.use_graphs ? 1 : 0; return AFV_OK;
+    case AFV_OPT_RESTRICT_KERNEL: *value = f->f.use_restrict_warp ? 1 : 0; return AFV_OK;
   }
   return fail(AFV_ERR_INVALID, "unknown option");
 }

@@ -74,7 +74,8 @@ class Forest {
   Plan plan;
   int device = 0;
   int n_sm = 148;
-  int sweep_kernel = 1;  // 0: block-pipelined k_level_tma, 1: warp-per-box k_sweep_warp
+  int sweep_kernel = 1;
+  bool use_restrict_warp = true;  // warp-per-box restriction on levels >= 2  // 0: block-pipelined k_level_tma, 1: warp-per-box k_sweep_warp
   cudaStream_t stream = nullptr;
   DevMeta meta;
   Arrays<double> d64;

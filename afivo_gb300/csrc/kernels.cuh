@@ -877,6 +877,204 @@ __device__ __forceinline__ T lpl_at(const T* bx, int i, int j, int k, T inv_dr_s
   }
 }
 
+// ---------------------------------------------------------------------------
+// Warp-per-box residual and restriction (the fine side of update_coarse,
+// src/m_aX_mg.f90:424-451) on a level >= 2, with the ghost cells pulled: the
+// pipeline of k_sweep_warp (bulk-copied box in an S-stage ring per warp),
+// with every face ghost, the rhs of the lane's fine cells and the parent's
+// offset fetched one box ahead. Each lane owns PPL parent cells and the 2^D
+// fine cells of each; the residual and the restriction are summed in the
+// order of k_restrict_res.
+// ---------------------------------------------------------------------------
+template <int D, int NC, class T, int W, int S>
+struct RestrictCfg {
+  using G = Geo<D, NC>;
+  static constexpr int H = NC / 2;
+  static constexpr int PAR = D == 2 ? H * H : H * H * H;  // parent cells per fine box
+  static constexpr int PPL = (PAR + 31) / 32;             // per lane
+  static constexpr int FINE = 1 << D;
+  static constexpr int NEED = 2 * D * G::NF;              // every face ghost
+  static constexpr int GPL = (NEED + 31) / 32;
+  static constexpr int PHI_OFF = (int)sizeof(SlotDesc);
+  static constexpr int BOX_B = PHI_OFF + G::SG * (int)sizeof(T);
+  static constexpr int SMEM_B = W * S * BOX_B;
+  static_assert(BOX_B % 16 == 0, "bulk copy alignment");
+};
+
+template <int D, int NC, class T, int W, int S>
+__global__ void __launch_bounds__(W * 32)
+k_restrict_warp(Meta m, BoxSet bs, T* __restrict__ phi, const T* __restrict__ rhs, T* __restrict__ tmp,
+                int homog) {
+  pdl_wait();
+  pdl_trigger();
+  using C = RestrictCfg<D, NC, T, W, S>;
+  using G = Geo<D, NC>;
+  constexpr int H = C::H;
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ __align__(8) unsigned long long bar[W][S];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int gw = (int)blockIdx.x * W + wid, nw = (int)gridDim.x * W;
+  const int nbx = bs.n;
+  if (gw >= nbx) return;
+  const int my_boxes = (nbx - 1 - gw) / nw + 1;
+  unsigned char* ring = smem + (size_t)wid * S * C::BOX_B;
+  if (lane == 0) {
+    for (int st = 0; st < S; ++st) mbar_init(&bar[wid][st], 1);
+    fence_mbar_init();
+  }
+  __syncwarp();
+  constexpr int OX = 1, OY = G::NG, OZ = G::NG * G::NG;
+
+  int issued = 0;
+  auto stage = [&](int k) { return ring + (k % S) * C::BOX_B; };
+  auto issue = [&](int k) {  // lane 0
+    ++issued;
+    const int i = gw + k * nw;
+    const int s = box_at(bs, i);
+    unsigned char* sp = stage(k);
+    unsigned long long* b = &bar[wid][k % S];
+    fence_proxy_async();
+    mbar_expect_tx(b, (unsigned)C::BOX_B);
+    bulk_g2s(sp, m.desc + s, (unsigned)sizeof(SlotDesc), b);
+    bulk_g2s(sp + C::PHI_OFF, phi + box_offg<G::SG>(m, bs, i, s), (unsigned)(G::SG * sizeof(T)), b);
+  };
+  // Item j of this lane: face f and face cell (a, c).
+  auto item = [&](int j, int& f, int& a, int& c) {
+    const int r = lane + 32 * j;
+    f = r / G::NF;
+    const int lin = r % G::NF;
+    a = lin % NC + 1;
+    c = lin / NC + 1;
+  };
+  // Ghost sources, rhs values and the parent's offset of box k (its
+  // descriptor has landed).
+  auto fetch = [&](int k, T (&gv)[C::GPL], T (&rv)[C::PPL][C::FINE], long long& po, int& act) {
+    const SlotDesc& d = *reinterpret_cast<const SlotDesc*>(stage(k));
+    act = m.active[d.tree];
+    po = m.offg[d.parent];
+#pragma unroll
+    for (int j = 0; j < C::GPL; ++j) {
+      gv[j] = (T)0;
+      if (lane + 32 * j >= C::NEED) continue;
+      int f, a, c;
+      item(j, f, a, c);
+      const Face<D, NC> F(f, a, c);
+      const int code = d.code[f];
+      const long long o = d.nbo[f];
+      if (code >= 0) {
+        gv[j] = phi[o + G::g(F.ni, F.nj, F.nk)];
+      } else if (code == kFaceRefinement) {
+        gv[j] = phi[o + parent_cell<D, NC>(F, f, d.qd, false)];
+      } else if (o >= 0 && !homog) {
+        gv[j] = (T)m.bcval[o + ((D == 2) ? (a - 1) : (a - 1) + NC * (c - 1))];
+      }
+    }
+    const T* f = rhs + d.offi;
+#pragma unroll
+    for (int p = 0; p < C::PPL; ++p) {
+      const int q = lane + 32 * p;
+      const int qq = q < C::PAR ? q : 0;
+      const int ic = qq % H + 1, jc = (qq / H) % H + 1, kc = (D == 3) ? qq / (H * H) + 1 : 0;
+      constexpr int KK = (D == 3) ? 2 : 1;
+#pragma unroll
+      for (int kk = 0; kk < KK; ++kk)
+#pragma unroll
+        for (int jj = 0; jj < 2; ++jj)
+#pragma unroll
+          for (int ii = 0; ii < 2; ++ii)
+            rv[p][(kk * 2 + jj) * 2 + ii] =
+                f[G::in(2 * ic - 1 + ii, 2 * jc - 1 + jj, (D == 3) ? 2 * kc - 1 + kk : 1)];
+    }
+  };
+  auto body = [&](int k, T (&g0)[C::GPL], T (&r0)[C::PPL][C::FINE], long long po0, int a0, T (&g1)[C::GPL],
+                  T (&r1)[C::PPL][C::FINE], long long& po1, int& a1) -> bool {
+    if (lane == 0 && k + S - 1 < my_boxes) issue(k + S - 1);
+    bool ok = true;
+    if (k + 1 < my_boxes) {
+      ok = mbar_wait_bounded(&bar[wid][(k + 1) % S], ((k + 1) / S) & 1);
+      if (ok) fetch(k + 1, g1, r1, po1, a1);
+    }
+    if (!__all_sync(0xffffffffu, ok)) return false;
+    unsigned char* sp = stage(k);
+    const SlotDesc& d = *reinterpret_cast<const SlotDesc*>(sp);
+    T* bx = reinterpret_cast<T*>(sp + C::PHI_OFF);
+    if (a0) {
+#pragma unroll
+      for (int j = 0; j < C::GPL; ++j) {
+        if (lane + 32 * j >= C::NEED) continue;
+        int f, a, c;
+        item(j, f, a, c);
+        const Face<D, NC> F(f, a, c);
+        const int code = d.code[f];
+        T v = g0[j];
+        if (code < 0) {
+          auto own = [&](int i, int jj, int kk) { return bx[G::g(i, jj, kk)]; };
+          if (code == kFaceRefinement)
+            v = rb_value<D, NC, T>(F, f, g0[j], own);
+          else
+            v = bc_value<T>(code, f, g0[j], own(F.ai, F.aj, F.ak), Sc<T>::dr(d));
+        }
+        bx[G::g(F.gi, F.gj, F.gk)] = v;
+      }
+      __syncwarp();
+      const T inv = Sc<T>::inv(d);
+      const int qd = d.qd;
+      const int off0 = (qd & 1) * H, off1 = ((qd >> 1) & 1) * H, off2 = ((qd >> 2) & 1) * H;
+      using GP = Geo<D, NC>;
+#pragma unroll
+      for (int p = 0; p < C::PPL; ++p) {
+        const int q = lane + 32 * p;
+        if (q >= C::PAR) continue;
+        const int ic = q % H + 1, jc = (q / H) % H + 1, kc = (D == 3) ? q / (H * H) + 1 : 0;
+        T sr = 0, sp2 = 0;
+        constexpr int KK = (D == 3) ? 2 : 1;
+#pragma unroll
+        for (int kk = 0; kk < KK; ++kk)
+#pragma unroll
+          for (int jj = 0; jj < 2; ++jj)
+#pragma unroll
+            for (int ii = 0; ii < 2; ++ii) {
+              const int i = 2 * ic - 1 + ii, j = 2 * jc - 1 + jj, kz = (D == 3) ? 2 * kc - 1 + kk : 0;
+              const T r = r0[p][(kk * 2 + jj) * 2 + ii] - lpl_at<D, NC, T>(bx, i, j, kz, inv);
+              sr = sr + r;
+              sp2 = sp2 + bx[G::g(i, j, kz)];
+            }
+        const T w = (D == 2) ? (T)0.25 : (T)0.125;
+        const long long o = po0 + GP::g(off0 + ic, off1 + jc, (D == 3) ? off2 + kc : 0);
+        tmp[o] = w * sr;
+        phi[o] = w * sp2;
+      }
+    }
+    __syncwarp();  // the stage of box k is refilled at box k + 1
+    return true;
+  };
+
+  const int ahead = min(S - 1, my_boxes);
+  if (lane == 0)
+    for (int k = 0; k < ahead; ++k) issue(k);
+  T ga[C::GPL], gb[C::GPL];
+  T ra[C::PPL][C::FINE], rb[C::PPL][C::FINE];
+  long long pa = 0, pb = 0;
+  int aa = 0, ab = 0;
+  bool ok = mbar_wait_bounded(&bar[wid][0], 0);
+  if (ok) fetch(0, ga, ra, pa, aa);
+  int k = 0, pending = 0;
+  if (__all_sync(0xffffffffu, ok)) {
+    for (; k < my_boxes; k += 2) {
+      if (!body(k, ga, ra, pa, aa, gb, rb, pb, ab)) break;
+      if (k + 1 < my_boxes && !body(k + 1, gb, rb, pb, ab, ga, ra, pa, aa)) {
+        k += 1;
+        break;
+      }
+    }
+    pending = k + 1;
+  }
+  if (k < my_boxes && lane == 0) {  // gave up: drain this warp's copies
+    atomicExch(m.err, 1);
+    for (int j = pending; j < issued; ++j) mbar_wait_bounded(&bar[wid][j % S], (j / S) & 1);
+  }
+}
+
 // Loads a group of BPC boxes of a set into shared memory (whole ghosted
 // boxes, vectorised) and their slots into s_slot; returns the count.
 template <int D, int NC, class T, int BPC>

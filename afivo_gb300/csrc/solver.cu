@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <type_traits>
 #include <utility>
 
@@ -11,6 +12,12 @@
 #include "kernels.cuh"
 
 namespace afv {
+
+// Forests of one process may live on several host threads (the request
+// loop). Graph capture must not overlap calls that synchronise with the
+// device or allocate pinned memory (forest creation and destruction), so
+// those sections share one lock.
+static std::mutex g_capture_mutex;
 
 using dev::BoxSet;
 using dev::Meta;
@@ -113,6 +120,7 @@ static void retain_pool(int device) {
 }
 
 Forest::~Forest() {
+  std::lock_guard<std::mutex> lock(g_capture_mutex);
   cudaSetDevice(device);
   if (stream) cudaStreamSynchronize(stream);
   void* ptrs[] = {meta.parent, meta.first_child, meta.tree, meta.offg, meta.offi, meta.bcval,
@@ -268,6 +276,7 @@ struct ProfScope {
 
 int Forest::create(const std::vector<const HostTree*>& trees, const afv_forest_opts* opts,
                    std::string& err) {
+  std::lock_guard<std::mutex> lock(g_capture_mutex);
   int rc = build_plan(trees, plan, err);
   if (rc) return rc;
   device = opts ? opts->device : 0;
@@ -337,7 +346,7 @@ int Forest::create(const std::vector<const HostTree*>& trees, const afv_forest_o
       cudaMallocHost((void**)&h_count, sizeof(int)) != cudaSuccess ||
       cudaMallocHost((void**)&h_norm, sizeof(unsigned long long) * p.n_trees) != cudaSuccess)
     return err = "pinned allocation failed", AFV_ERR_NOMEM;
-  if (cudaDeviceSynchronize() != cudaSuccess) return check(err, "forest create");
+  if (cudaStreamSynchronize(stream) != cudaSuccess) return check(err, "forest create");
   return AFV_OK;
 }
 
@@ -521,6 +530,27 @@ dev_BoxSet Forest::level_set(int lvl) const {
   return BoxSet{nullptr, lo, plan.lvl_n[plan.L(lvl)], plan.offg[lo], plan.offi[lo]};
 }
 
+// Launches the warp-per-box restriction (16 warps x 3 stages in FP32,
+// 8 x 3 in FP64: about 200 KB of shared memory, one block per SM).
+template <int D, int NC, class T>
+static void launch_restrict_warp(Forest& F, const Meta& m, BoxSet bs, T* phi, const T* rhs, T* tmp,
+                                 bool homog) {
+  constexpr int W = std::is_same<T, float>::value ? 16 : 8, S = 3;
+  using C = dev::RestrictCfg<D, NC, T, W, S>;
+  static int occ = 0;
+  if (!occ) {
+    cudaFuncSetAttribute(dev::k_restrict_warp<D, NC, T, W, S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         C::SMEM_B);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, dev::k_restrict_warp<D, NC, T, W, S>, W * 32,
+                                                  C::SMEM_B);
+    if (occ < 1) occ = 1;
+  }
+  const long long blocks = (bs.n + W - 1) / W;
+  const int grid = (int)std::max(1LL, std::min(blocks, (long long)F.n_sm * occ));
+  launch_k(dev::k_restrict_warp<D, NC, T, W, S>, grid, W * 32, (size_t)C::SMEM_B, F.stream, m, bs, phi, rhs,
+           tmp, homog ? 1 : 0);
+}
+
 template <class T>
 void Forest::sweep(const Arrays<T>& a, int lvl, int n, bool pull, bool homog) {
   prof_level = lvl;
@@ -591,6 +621,8 @@ void Forest::restrict_res(const Arrays<T>& a, int lvl, bool with_res, bool pull,
     if (sub)
       launch_k(dev::k_restrict_res<D, NC, true, T>, grid, dev::kThreads, 0, stream, 
           m, bs, a.phi, a.rhs, a.tmp, with_res ? 1 : 0, pull ? 1 : 0, homog ? 1 : 0);
+    else if (with_res && pull && use_restrict_warp)
+      launch_restrict_warp<D, NC, T>(*this, m, bs, a.phi, a.rhs, a.tmp, homog);
     else
       launch_k(dev::k_restrict_res<D, NC, false, T>, grid, dev::kThreads, 0, stream, 
           m, bs, a.phi, a.rhs, a.tmp, with_res ? 1 : 0, pull ? 1 : 0, homog ? 1 : 0);
@@ -1078,20 +1110,20 @@ int Forest::solve(const MgOpts& mg, int precision, double tol, int max_cycles, S
   st.rel_res.assign(nt, 0.0);
   Meta m = meta_of(meta);
   set_active_all(1);
-  // max |f| over the leaves of every tree
+  // max |f| over the leaves of every tree (all leaves are on levels >= 1,
+  // with nc cells per side: one launch)
   norm_reset();
-  for (int l = plan.min_lvl; l <= plan.max_lvl; ++l) {
-    int nl = n_leaves(l);
-    if (!nl) continue;
-    BoxSet bs{leaves_list(l), 0, nl};
-    with_nc(plan.dim, plan.nc_at(l), [&](auto d_, auto nc_) {
+  {
+    const int nl = (int)plan.all_leaves.size();
+    BoxSet bs{d_lists + all_leaves_off, 0, nl};
+    with_nc(plan.dim, plan.nc, [&](auto d_, auto nc_) {
       constexpr int D = decltype(d_)::value, NC = decltype(nc_)::value;
       using G = dev::Geo<D, NC>;
       constexpr int PER_BOX = G::SI < dev::kThreads ? G::SI : dev::kThreads;
       constexpr int BPC = dev::kThreads / PER_BOX;
       ProfScope ps(this, kProfOther, 8.0 * nl * G::SI);
-      launch_k(dev::k_maxabs<D, NC, double>, grid_for((nl + BPC - 1) / BPC, n_sm), dev::kThreads, 0, stream, 
-          m, bs, d64.rhs, 0, d_norm);
+      launch_k(dev::k_maxabs<D, NC, double>, grid_for((nl + BPC - 1) / BPC, n_sm * 4), dev::kThreads, 0,
+               stream, m, bs, d64.rhs, 0, d_norm);
     });
   }
   norm_fold();
@@ -1126,6 +1158,7 @@ int Forest::solve(const MgOpts& mg, int precision, double tol, int max_cycles, S
     gc = GraphCache();
     long long before = n_launches;
     cudaGraph_t g = nullptr;
+    std::lock_guard<std::mutex> lock(g_capture_mutex);
     if (cudaStreamBeginCapture(stream, cudaStreamCaptureModeRelaxed) != cudaSuccess)
       return check(err, "graph capture");
     enqueue_iteration(mg, precision, tol);

@@ -21,7 +21,7 @@ import time
 
 import numpy as np
 
-from . import AFV_PHI, AFV_PREC_MIXED, Forest, MgOpts
+from . import AFV_PHI, AFV_PREC_MIXED, Forest, MgOpts, lib
 from . import workloads as W
 
 
@@ -145,7 +145,8 @@ class Server:
                         cyc, rel, rc = f.solve(self.precision, tol=self.tol,
                                                max_cycles=self.max_cycles, mg=mg, check=False)
                         if rc != 0:
-                            raise RuntimeError(f"solve failed with status {rc}")
+                            raise RuntimeError(f"solve failed with status {rc}: "
+                                               f"{lib().afv_last_error().decode()}")
                         phis = [f.get_var(i, AFV_PHI, interior_only=True) if self.keep_phi else None
                                 for i in range(len(batch))]
                         done = now()
