@@ -1075,6 +1075,171 @@ k_restrict_warp(Meta m, BoxSet bs, T* __restrict__ phi, const T* __restrict__ rh
   }
 }
 
+// ---------------------------------------------------------------------------
+// Warp-per-box coarse right-hand side (the coarse side of update_coarse,
+// src/m_aX_mg.f90:452-480) on a list of parents: the pipeline of
+// k_restrict_warp; the pulled ghosts are stored (the reference's ghost fill
+// of the coarse level), rhs = L phi + tmp on the interior, tmp = phi on the
+// whole box. Each lane owns CPL interior cells; their tmp values are fetched
+// one box ahead.
+// ---------------------------------------------------------------------------
+template <int D, int NC, class T, int W, int S>
+struct CoarseCfg {
+  using G = Geo<D, NC>;
+  static constexpr int CPL = (G::SI + 31) / 32;
+  static constexpr int NEED = 2 * D * G::NF;
+  static constexpr int GPL = (NEED + 31) / 32;
+  static constexpr int PHI_OFF = (int)sizeof(SlotDesc);
+  static constexpr int BOX_B = PHI_OFF + G::SG * (int)sizeof(T);
+  static constexpr int SMEM_B = W * S * BOX_B;
+  static_assert(BOX_B % 16 == 0, "bulk copy alignment");
+};
+
+template <int D, int NC, class T, int W, int S>
+__global__ void __launch_bounds__(W * 32)
+k_coarse_warp(Meta m, BoxSet bs, T* __restrict__ phi, T* __restrict__ rhs, T* __restrict__ tmp, int homog) {
+  pdl_wait();
+  pdl_trigger();
+  using C = CoarseCfg<D, NC, T, W, S>;
+  using G = Geo<D, NC>;
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ __align__(8) unsigned long long bar[W][S];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int gw = (int)blockIdx.x * W + wid, nw = (int)gridDim.x * W;
+  const int nbx = bs.n;
+  if (gw >= nbx) return;
+  const int my_boxes = (nbx - 1 - gw) / nw + 1;
+  unsigned char* ring = smem + (size_t)wid * S * C::BOX_B;
+  if (lane == 0) {
+    for (int st = 0; st < S; ++st) mbar_init(&bar[wid][st], 1);
+    fence_mbar_init();
+  }
+  __syncwarp();
+
+  int issued = 0;
+  auto stage = [&](int k) { return ring + (k % S) * C::BOX_B; };
+  auto issue = [&](int k) {  // lane 0
+    ++issued;
+    const int i = gw + k * nw;
+    const int s = box_at(bs, i);
+    unsigned char* sp = stage(k);
+    unsigned long long* b = &bar[wid][k % S];
+    fence_proxy_async();
+    mbar_expect_tx(b, (unsigned)C::BOX_B);
+    bulk_g2s(sp, m.desc + s, (unsigned)sizeof(SlotDesc), b);
+    bulk_g2s(sp + C::PHI_OFF, phi + box_offg<G::SG>(m, bs, i, s), (unsigned)(G::SG * sizeof(T)), b);
+  };
+  auto item = [&](int j, int& f, int& a, int& c) {
+    const int r = lane + 32 * j;
+    f = r / G::NF;
+    const int lin = r % G::NF;
+    a = lin % NC + 1;
+    c = lin / NC + 1;
+  };
+  auto fetch = [&](int k, T (&gv)[C::GPL], T (&tv)[C::CPL], int& act) {
+    const SlotDesc& d = *reinterpret_cast<const SlotDesc*>(stage(k));
+    act = m.active[d.tree];
+#pragma unroll
+    for (int j = 0; j < C::GPL; ++j) {
+      gv[j] = (T)0;
+      if (lane + 32 * j >= C::NEED) continue;
+      int f, a, c;
+      item(j, f, a, c);
+      const Face<D, NC> F(f, a, c);
+      const int code = d.code[f];
+      const long long o = d.nbo[f];
+      if (code >= 0) {
+        gv[j] = phi[o + G::g(F.ni, F.nj, F.nk)];
+      } else if (code == kFaceRefinement) {
+        gv[j] = phi[o + parent_cell<D, NC>(F, f, d.qd, false)];
+      } else if (o >= 0 && !homog) {
+        gv[j] = (T)m.bcval[o + ((D == 2) ? (a - 1) : (a - 1) + NC * (c - 1))];
+      }
+    }
+    const T* t = tmp + d.offg;
+#pragma unroll
+    for (int c = 0; c < C::CPL; ++c) {
+      const int q = lane + 32 * c;
+      const int qq = q < G::SI ? q : 0;
+      const int i = qq % NC + 1, j = (qq / NC) % NC + 1, kz = (D == 3) ? qq / (NC * NC) + 1 : 0;
+      tv[c] = t[G::g(i, j, kz)];
+    }
+  };
+  auto body = [&](int k, T (&g0)[C::GPL], T (&t0)[C::CPL], int a0, T (&g1)[C::GPL], T (&t1)[C::CPL],
+                  int& a1) -> bool {
+    if (lane == 0 && k + S - 1 < my_boxes) issue(k + S - 1);
+    bool ok = true;
+    if (k + 1 < my_boxes) {
+      ok = mbar_wait_bounded(&bar[wid][(k + 1) % S], ((k + 1) / S) & 1);
+      if (ok) fetch(k + 1, g1, t1, a1);
+    }
+    if (!__all_sync(0xffffffffu, ok)) return false;
+    unsigned char* sp = stage(k);
+    const SlotDesc& d = *reinterpret_cast<const SlotDesc*>(sp);
+    T* bx = reinterpret_cast<T*>(sp + C::PHI_OFF);
+    if (a0) {
+      T* gphi = phi + d.offg;
+#pragma unroll
+      for (int j = 0; j < C::GPL; ++j) {
+        if (lane + 32 * j >= C::NEED) continue;
+        int f, a, c;
+        item(j, f, a, c);
+        const Face<D, NC> F(f, a, c);
+        const int code = d.code[f];
+        T v = g0[j];
+        if (code < 0) {
+          auto own = [&](int i, int jj, int kk) { return bx[G::g(i, jj, kk)]; };
+          if (code == kFaceRefinement)
+            v = rb_value<D, NC, T>(F, f, g0[j], own);
+          else
+            v = bc_value<T>(code, f, g0[j], own(F.ai, F.aj, F.ak), Sc<T>::dr(d));
+        }
+        const int gp = G::g(F.gi, F.gj, F.gk);
+        bx[gp] = v;
+        gphi[gp] = v;
+      }
+      __syncwarp();
+      const T inv = Sc<T>::inv(d);
+      T* r = rhs + d.offi;
+#pragma unroll
+      for (int c = 0; c < C::CPL; ++c) {
+        const int q = lane + 32 * c;
+        if (q >= G::SI) continue;
+        const int i = q % NC + 1, j = (q / NC) % NC + 1, kz = (D == 3) ? q / (NC * NC) + 1 : 0;
+        const T l = lpl_at<D, NC, T>(bx, i, j, kz, inv);
+        r[q] = l + t0[c];
+      }
+      T* gt = tmp + d.offg;
+      for (int e = lane; e < G::SG; e += 32) gt[e] = bx[e];
+    }
+    __syncwarp();  // the stage of box k is refilled at box k + 1
+    return true;
+  };
+
+  const int ahead = min(S - 1, my_boxes);
+  if (lane == 0)
+    for (int k = 0; k < ahead; ++k) issue(k);
+  T ga[C::GPL], gb[C::GPL], ta[C::CPL], tb[C::CPL];
+  int aa = 0, ab = 0;
+  bool ok = mbar_wait_bounded(&bar[wid][0], 0);
+  if (ok) fetch(0, ga, ta, aa);
+  int k = 0, pending = 0;
+  if (__all_sync(0xffffffffu, ok)) {
+    for (; k < my_boxes; k += 2) {
+      if (!body(k, ga, ta, aa, gb, tb, ab)) break;
+      if (k + 1 < my_boxes && !body(k + 1, gb, tb, ab, ga, ta, aa)) {
+        k += 1;
+        break;
+      }
+    }
+    pending = k + 1;
+  }
+  if (k < my_boxes && lane == 0) {  // gave up: drain this warp's copies
+    atomicExch(m.err, 1);
+    for (int j = pending; j < issued; ++j) mbar_wait_bounded(&bar[wid][j % S], (j / S) & 1);
+  }
+}
+
 // Loads a group of BPC boxes of a set into shared memory (whole ghosted
 // boxes, vectorised) and their slots into s_slot; returns the count.
 template <int D, int NC, class T, int BPC>

@@ -551,6 +551,25 @@ static void launch_restrict_warp(Forest& F, const Meta& m, BoxSet bs, T* phi, co
            tmp, homog ? 1 : 0);
 }
 
+// Launches the warp-per-box coarse right-hand side (same shape as the
+// restriction).
+template <int D, int NC, class T>
+static void launch_coarse_warp(Forest& F, const Meta& m, BoxSet bs, T* phi, T* rhs, T* tmp, bool homog) {
+  constexpr int W = std::is_same<T, float>::value ? 16 : 8, S = 3;
+  using C = dev::CoarseCfg<D, NC, T, W, S>;
+  static int occ = 0;
+  if (!occ) {
+    cudaFuncSetAttribute(dev::k_coarse_warp<D, NC, T, W, S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         C::SMEM_B);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, dev::k_coarse_warp<D, NC, T, W, S>, W * 32, C::SMEM_B);
+    if (occ < 1) occ = 1;
+  }
+  const long long blocks = (bs.n + W - 1) / W;
+  const int grid = (int)std::max(1LL, std::min(blocks, (long long)F.n_sm * occ));
+  launch_k(dev::k_coarse_warp<D, NC, T, W, S>, grid, W * 32, (size_t)C::SMEM_B, F.stream, m, bs, phi, rhs, tmp,
+           homog ? 1 : 0);
+}
+
 template <class T>
 void Forest::sweep(const Arrays<T>& a, int lvl, int n, bool pull, bool homog) {
   prof_level = lvl;
@@ -644,8 +663,11 @@ void Forest::coarse_rhs(const Arrays<T>& a, int lp, bool copy_tmp, bool pull, bo
     int grid = grid_for((np + BPC - 1) / BPC, n_sm);
     // read phi, tmp; write rhs, tmp
     ProfScope ps(this, kProfCoarseRhs, 4.0 * np * G::SI * sizeof(T));
-    launch_k(dev::k_coarse_rhs<D, NC, T>, grid, dev::kThreads, 0, stream, 
-        m, bs, a.phi, a.rhs, a.tmp, copy_tmp ? 1 : 0, pull ? 1 : 0, homog ? 1 : 0);
+    if (copy_tmp && pull && use_restrict_warp && lp >= 1)
+      launch_coarse_warp<D, NC, T>(*this, m, bs, a.phi, a.rhs, a.tmp, homog);
+    else
+      launch_k(dev::k_coarse_rhs<D, NC, T>, grid, dev::kThreads, 0, stream, 
+          m, bs, a.phi, a.rhs, a.tmp, copy_tmp ? 1 : 0, pull ? 1 : 0, homog ? 1 : 0);
   });
 }
 

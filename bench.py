@@ -472,8 +472,11 @@ def main():
         solve(afv.AFV_PREC_MIXED)
         solve(afv.AFV_PREC_FP64)
 
-    # headline: mixed solves, graphs on, nothing profiled
+    # headline: mixed solves, graphs on, nothing profiled (the clock sampler
+    # starts first, so that its start-up does not fall into the timed region)
     with Clocks(local) as clk:
+        time.sleep(0.5)
+        solve(afv.AFV_PREC_MIXED)
         ms, cyc, rels, per, launches = timed(afv.AFV_PREC_MIXED, args.steps)
     ms = max_over_ranks(ms, world)
     value = cells * sum_over_ranks(float(sum(cyc)), world) / (ms / 1e3)
@@ -552,7 +555,7 @@ def main():
         "config": config_of(spec, cells, info["n_boxes"]),
         "method": "mixed: FP32 FAS V(2,2) cycles inside FP64 defect correction; CUDA graphs",
         "solve": {"cycles": cyc, "rel_res": max(rels), "ms_p50": float(np.percentile(per, 50)),
-                  "ms_p99": float(np.percentile(per, 99))},
+                  "ms_p99": float(np.percentile(per, 99)), "ms_each": [round(x, 3) for x in per]},
         "fp64": {"value": value64, "unit": "unknowns/s", "cycles": cyc64, "rel_res": max(rels64),
                  "ms_per_solve": ms64 / len(cyc64)},
         "mixed_vs_fp64_solve_speedup": (ms64 / len(cyc64)) / (ms / args.steps),

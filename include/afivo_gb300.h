@@ -259,8 +259,9 @@ int afv_forest_profile_read(afv_forest* f, int kind, long long* launches, double
  * 1 warp-per-box kernel with bulk copies (default), 2 warp-per-box kernel with
  * per-lane asynchronous copies. AFV_OPT_GRAPHS: 1 (default) replays solve
  * iterations as CUDA graphs, 0 launches them one by one.
- * AFV_OPT_RESTRICT_KERNEL: 1 (default) warp-per-box residual restriction on
- * levels >= 2, 0 the block-staged kernel. */
+ * AFV_OPT_RESTRICT_KERNEL: 1 (default) warp-per-box kernels for the residual
+ * restriction (levels >= 2) and the coarse right-hand side (levels >= 1),
+ * 0 the block-staged kernels. */
 enum { AFV_OPT_SWEEP_KERNEL = 0, AFV_OPT_GRAPHS = 1, AFV_OPT_RESTRICT_KERNEL = 2 };
 int afv_forest_set_option(afv_forest* f, int option, int value);
 int afv_forest_get_option(afv_forest* f, int option, int* value);
