@@ -1884,22 +1884,33 @@ k_defect(Meta m, BoxSet bs, const double* __restrict__ u, const double* __restri
   }
 }
 
-// u += e over the interiors of the leaves (FP64 accumulate of the FP32 correction).
+// u += e over the interiors of the leaves (FP64 accumulate of the FP32
+// correction). One thread per row of NC cells: the slot lookups are made once
+// per row and the row's loads are issued together.
 template <int D, int NC>
 __global__ void __launch_bounds__(kThreads)
 k_accumulate(Meta m, BoxSet bs, double* __restrict__ u, const float* __restrict__ e) {
   pdl_wait();
   pdl_trigger();
   using G = Geo<D, NC>;
-  const long long total = (long long)bs.n * G::SI;
+  constexpr int ROWS = G::SI / NC;  // rows of a box
+  const long long total = (long long)bs.n * ROWS;
   for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < total;
        x += (long long)gridDim.x * blockDim.x) {
-    int bi = (int)(x / G::SI), q = (int)(x % G::SI);
-    int s = box_at(bs, bi);
+    const int bi = (int)(x / ROWS), row = (int)(x % ROWS);
+    const int s = box_at(bs, bi);
     if (!m.active[m.tree[s]]) continue;
-    int i = q % NC + 1, j = (q / NC) % NC + 1, k = (D == 3) ? q / (NC * NC) + 1 : 0;
-    long long o = m.offg[s] + G::g(i, j, k);
-    u[o] = u[o] + f2d_exact(e[o]);
+    const int j = row % NC + 1, k = (D == 3) ? row / NC + 1 : 0;
+    const long long o = m.offg[s] + G::g(1, j, k);
+    double uv[NC];
+    float ev[NC];
+#pragma unroll
+    for (int i = 0; i < NC; ++i) {
+      uv[i] = u[o + i];
+      ev[i] = e[o + i];
+    }
+#pragma unroll
+    for (int i = 0; i < NC; ++i) u[o + i] = uv[i] + f2d_exact(ev[i]);
   }
 }
 

@@ -1099,8 +1099,8 @@ void Forest::enqueue_iteration(const MgOpts& mg, int precision, double tol) {
       {
         // read e (4 B), read and write u (16 B)
         ProfScope ps(this, kProfAccumulate, 20.0 * items);
-        launch_k(dev::k_accumulate<D, NC>, grid_for((items + 255) / 256, n_sm), 256, 0, stream, m, bs, d64.phi,
-                                                                                       d32.phi);
+        launch_k(dev::k_accumulate<D, NC>, grid_for((items / NC + 255) / 256, n_sm), 256, 0, stream, m, bs,
+                 d64.phi, d32.phi);
       }
       // parents (finest first) take the restriction of their children's increments
       for (int l = plan.max_lvl - 1; l >= 1; --l) {
