@@ -1701,7 +1701,7 @@ k_maxabs(Meta m, BoxSet bs, const T* __restrict__ v, int ghosted,
   pdl_wait();
   pdl_trigger();
   using G = Geo<D, NC>;
-  constexpr int PER_BOX = G::SI < kThreads ? G::SI : kThreads;
+  constexpr int PER_BOX = G::SI < 32 ? G::SI : 32;  // one warp per box
   constexpr int BPC = kThreads / PER_BOX;
   __shared__ double red[kThreads / 32];
   const int groups = (bs.n + BPC - 1) / BPC;
