@@ -428,6 +428,10 @@ int afv_forest_set_option(afv_forest* f, int option, int value) {
       f->f.use_restrict_warp = value != 0;
       f->f.drop_graphs();
       return AFV_OK;
+    case AFV_OPT_SMALL_SWEEPS:
+      f->f.use_small_sweeps = value != 0;
+      f->f.drop_graphs();
+      return AFV_OK;
   }
   return fail(AFV_ERR_INVALID, "unknown option");
 }
@@ -438,6 +442,7 @@ int afv_forest_get_option(afv_forest* f, int option, int* value) {
     case AFV_OPT_SWEEP_KERNEL: *value = f->f.sweep_kernel; return AFV_OK;
     case AFV_OPT_GRAPHS: *value = f->f.use_graphs ? 1 : 0; return AFV_OK;
     case AFV_OPT_RESTRICT_KERNEL: *value = f->f.use_restrict_warp ? 1 : 0; return AFV_OK;
+    case AFV_OPT_SMALL_SWEEPS: *value = f->f.use_small_sweeps ? 1 : 0; return AFV_OK;
   }
   return fail(AFV_ERR_INVALID, "unknown option");
 }

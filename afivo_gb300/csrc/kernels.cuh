@@ -1240,6 +1240,130 @@ k_coarse_warp(Meta m, BoxSet bs, T* __restrict__ phi, T* __restrict__ rhs, T* __
   }
 }
 
+// ---------------------------------------------------------------------------
+// Consecutive half-sweeps of a small level in one block (levels of at most a
+// few boxes, where every half-sweep launched alone costs its launch and an L2
+// round trip for little work). All boxes of the level and their rhs are
+// loaded into shared memory once; each half-sweep first fills the ghost cells
+// its colour reads from the current state (same-level neighbours from shared
+// memory, coarse neighbours from the parent level, which does not change
+// while the level is smoothed, and boundary values), then updates its colour
+// in place; after the last one the interiors are written back. The values
+// are those of the half-sweeps launched one by one (with pulled ghosts).
+// ---------------------------------------------------------------------------
+constexpr int kSmallThreads = 512;
+
+template <int D, int NC, class T>
+__global__ void __launch_bounds__(kSmallThreads)
+k_sweep_small(Meta m, BoxSet bs, T* __restrict__ phi, const T* __restrict__ rhs, int n_first, int n_count,
+              int pull_first, int homog) {
+  pdl_wait();
+  pdl_trigger();
+  using G = Geo<D, NC>;
+  constexpr int ITEMS = G::NNB * G::NF;  // face cells of a box
+  extern __shared__ __align__(128) unsigned char smem[];
+  const int nb = bs.n;
+  SlotDesc* sd = reinterpret_cast<SlotDesc*>(smem);                   // nb descriptors
+  T* sb = reinterpret_cast<T*>(smem + (size_t)nb * sizeof(SlotDesc));  // nb ghosted boxes
+  T* sr = sb + (size_t)nb * G::SG;                                     // nb rhs interiors
+  T* sc = sr + (size_t)nb * G::SI;                                     // per face cell: coarse value or boundary value
+  int* sa = reinterpret_cast<int*>(sc + (size_t)nb * ITEMS);           // nb activity flags
+  constexpr int OX = 1, OY = G::NG, OZ = G::NG * G::NG;
+  {
+    const unsigned* src = reinterpret_cast<const unsigned*>(m.desc + bs.lo);
+    unsigned* dst = reinterpret_cast<unsigned*>(sd);
+    for (int e = threadIdx.x; e < nb * (int)(sizeof(SlotDesc) / 4); e += blockDim.x) dst[e] = src[e];
+  }
+  for (int e = threadIdx.x; e < nb * G::SG; e += blockDim.x) sb[e] = phi[bs.g0 + e];
+  for (int e = threadIdx.x; e < nb * G::SI; e += blockDim.x) sr[e] = rhs[bs.i0 + e];
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) sa[b] = m.active[m.tree[bs.lo + b]];
+  __syncthreads();
+  // The sources of the ghost cells that do not change while the level is
+  // smoothed: the parent's injected cell at refinement boundaries, the
+  // boundary value at physical faces.
+  for (int e = threadIdx.x; e < nb * ITEMS; e += blockDim.x) {
+    const int b = e / ITEMS, r = e % ITEMS;
+    const int f = r / G::NF, lin = r % G::NF;
+    const int a = lin % NC + 1, c = lin / NC + 1;
+    const SlotDesc& d = sd[b];
+    const int code = d.code[f];
+    const long long o = d.nbo[f];
+    T v = 0;
+    if (code == kFaceRefinement) {
+      v = phi[o + parent_cell<D, NC>(Face<D, NC>(f, a, c), f, d.qd, false)];
+    } else if (code < 0 && !homog && o >= 0) {
+      v = (T)m.bcval[o + ((D == 2) ? (a - 1) : (a - 1) + NC * (c - 1))];
+    }
+    sc[e] = v;
+  }
+  __syncthreads();
+  for (int h = 0; h < n_count; ++h) {
+    const int nsw = n_first + h;
+    if (h > 0 || pull_first) {
+      for (int e = threadIdx.x; e < nb * ITEMS; e += blockDim.x) {
+        const int b = e / ITEMS, r = e % ITEMS;
+        if (!sa[b]) continue;
+        const int f = r / G::NF, lin = r % G::NF;
+        const int a = lin % NC + 1, c = lin / NC + 1;
+        const SlotDesc& d = sd[b];
+        T* bx = sb + (size_t)b * G::SG;
+        const Face<D, NC> F(f, a, c);
+        const int code = d.code[f];
+        T v;
+        if (code >= 0) {
+          const long long nbi = (d.nbo[f] - bs.g0) / G::SG;  // the neighbour is on this level
+          v = sb[nbi * G::SG + G::g(F.ni, F.nj, F.nk)];
+        } else {
+          auto own = [&](int i, int j, int k) { return bx[G::g(i, j, k)]; };
+          if (code == kFaceRefinement)
+            v = rb_value<D, NC, T>(F, f, sc[e], own);
+          else
+            v = bc_value<T>(code, f, sc[e], own(F.ai, F.aj, F.ak), Sc<T>::dr(d));
+        }
+        bx[G::g(F.gi, F.gj, F.gk)] = v;
+      }
+      __syncthreads();
+    }
+    constexpr int HALF = G::SI / 2;
+    for (int e = threadIdx.x; e < nb * HALF; e += blockDim.x) {
+      const int b = e / HALF, q = e % HALF;
+      if (!sa[b]) continue;
+      const int p = q % (NC / 2);
+      int upos, rpos;
+      if constexpr (D == 2) {
+        const int j = q / (NC / 2) + 1;
+        const int i = 2 * p + 1 + ((1 + j + nsw) & 1);
+        upos = G::g(i, j, 0);
+        rpos = G::in(i, j, 1);
+      } else {
+        const int j = (q / (NC / 2)) % NC + 1;
+        const int k = q / ((NC / 2) * NC) + 1;
+        const int i = 2 * p + 1 + ((1 + j + k + nsw) & 1);
+        upos = G::g(i, j, k);
+        rpos = G::in(i, j, k);
+      }
+      T* bx = sb + (size_t)b * G::SG + upos;
+      const T f = sr[(size_t)b * G::SI + rpos];
+      const T dx2 = Sc<T>::dx2(sd[b]);
+      T v;
+      if constexpr (D == 2) {
+        v = (T)0.25 * (bx[OX] + bx[-OX] + bx[OY] + bx[-OY] - dx2 * f);
+      } else {
+        const T sixth = (T)(1 / 6.0);
+        v = sixth * (bx[OX] + bx[-OX] + bx[OY] + bx[-OY] + bx[OZ] + bx[-OZ] - dx2 * f);
+      }
+      *bx = v;
+    }
+    __syncthreads();
+  }
+  for (int e = threadIdx.x; e < nb * G::SI; e += blockDim.x) {
+    const int b = e / G::SI, q = e % G::SI;
+    const int i = q % NC + 1, j = (q / NC) % NC + 1, k = (D == 3) ? q / (NC * NC) + 1 : 0;
+    const int gp = G::g(i, j, k);
+    phi[bs.g0 + (long long)b * G::SG + gp] = sb[(size_t)b * G::SG + gp];
+  }
+}
+
 // Loads a group of BPC boxes of a set into shared memory (whole ghosted
 // boxes, vectorised) and their slots into s_slot; returns the count.
 template <int D, int NC, class T, int BPC>

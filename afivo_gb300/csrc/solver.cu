@@ -487,19 +487,32 @@ int Forest::set_var(int t, int var, const double* host, int interior_only, std::
 // Level operators
 // ---------------------------------------------------------------------------
 
+// Raises a kernel's dynamic shared-memory limit to smem on the current device
+// and returns its resident blocks per SM (at least 1). The attribute is per
+// device and the forests of a process may run on several devices and host
+// threads, so the result is kept per (kernel, device) under a lock.
+static int kernel_occupancy(const void* kern, int threads, int smem) {
+  static std::mutex mu;
+  static std::vector<std::pair<std::pair<const void*, int>, int>> known;
+  int device = 0;
+  cudaGetDevice(&device);
+  std::lock_guard<std::mutex> lock(mu);
+  for (const auto& e : known)
+    if (e.first.first == kern && e.first.second == device) return e.second;
+  if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  int occ = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, threads, smem);
+  if (occ < 1) occ = 1;
+  known.push_back({{kern, device}, occ});
+  return occ;
+}
+
 // Launches the pipelined level kernel (sweep or ghost fill) on a box set.
 template <int D, int NC, class T, int MODE>
 static void launch_level(Forest& F, const Meta& m, BoxSet bs, T* phi, const T* rhs, int n, bool pull,
                          bool homog) {
   using C = dev::LevelCfg<D, NC, T, MODE>;
-  static int occ = 0;
-  if (!occ) {
-    cudaFuncSetAttribute(dev::k_level_tma<D, NC, T, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         C::SMEM_B);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, dev::k_level_tma<D, NC, T, MODE>, dev::kThreads,
-                                                  C::SMEM_B);
-    if (occ < 1) occ = 1;
-  }
+  const int occ = kernel_occupancy((const void*)dev::k_level_tma<D, NC, T, MODE>, dev::kThreads, (int)C::SMEM_B);
   const long long groups = (bs.n + C::BPC - 1) / C::BPC;
   const int grid = (int)std::max(1LL, std::min(groups, (long long)F.n_sm * occ));
   launch_k(dev::k_level_tma<D, NC, T, MODE>, grid, dev::kThreads, C::SMEM_B, F.stream, 
@@ -511,14 +524,7 @@ template <int D, int NC, class T, int W, int S, int ASYNC>
 static void launch_sweep_warp(Forest& F, const Meta& m, BoxSet bs, T* phi, const T* rhs, int n,
                               bool pull, bool homog) {
   using C = dev::WarpCfg<D, NC, T, W, S>;
-  static int occ = 0;
-  if (!occ) {
-    cudaFuncSetAttribute(dev::k_sweep_warp<D, NC, T, W, S, ASYNC>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         C::SMEM_B);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, dev::k_sweep_warp<D, NC, T, W, S, ASYNC>, W * 32,
-                                                  C::SMEM_B);
-    if (occ < 1) occ = 1;
-  }
+  const int occ = kernel_occupancy((const void*)dev::k_sweep_warp<D, NC, T, W, S, ASYNC>, W * 32, (int)C::SMEM_B);
   const long long blocks = (bs.n + W - 1) / W;
   const int grid = (int)std::max(1LL, std::min(blocks, (long long)F.n_sm * occ));
   launch_k(dev::k_sweep_warp<D, NC, T, W, S, ASYNC>, grid, W * 32, C::SMEM_B, F.stream, m, bs, phi, rhs, n, pull ? 1 : 0,
@@ -537,14 +543,7 @@ static void launch_restrict_warp(Forest& F, const Meta& m, BoxSet bs, T* phi, co
                                  bool homog) {
   constexpr int W = std::is_same<T, float>::value ? 16 : 8, S = 3;
   using C = dev::RestrictCfg<D, NC, T, W, S>;
-  static int occ = 0;
-  if (!occ) {
-    cudaFuncSetAttribute(dev::k_restrict_warp<D, NC, T, W, S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         C::SMEM_B);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, dev::k_restrict_warp<D, NC, T, W, S>, W * 32,
-                                                  C::SMEM_B);
-    if (occ < 1) occ = 1;
-  }
+  const int occ = kernel_occupancy((const void*)dev::k_restrict_warp<D, NC, T, W, S>, W * 32, (int)C::SMEM_B);
   const long long blocks = (bs.n + W - 1) / W;
   const int grid = (int)std::max(1LL, std::min(blocks, (long long)F.n_sm * occ));
   launch_k(dev::k_restrict_warp<D, NC, T, W, S>, grid, W * 32, (size_t)C::SMEM_B, F.stream, m, bs, phi, rhs,
@@ -557,17 +556,33 @@ template <int D, int NC, class T>
 static void launch_coarse_warp(Forest& F, const Meta& m, BoxSet bs, T* phi, T* rhs, T* tmp, bool homog) {
   constexpr int W = std::is_same<T, float>::value ? 16 : 8, S = 3;
   using C = dev::CoarseCfg<D, NC, T, W, S>;
-  static int occ = 0;
-  if (!occ) {
-    cudaFuncSetAttribute(dev::k_coarse_warp<D, NC, T, W, S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         C::SMEM_B);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, dev::k_coarse_warp<D, NC, T, W, S>, W * 32, C::SMEM_B);
-    if (occ < 1) occ = 1;
-  }
+  const int occ = kernel_occupancy((const void*)dev::k_coarse_warp<D, NC, T, W, S>, W * 32, (int)C::SMEM_B);
   const long long blocks = (bs.n + W - 1) / W;
   const int grid = (int)std::max(1LL, std::min(blocks, (long long)F.n_sm * occ));
   launch_k(dev::k_coarse_warp<D, NC, T, W, S>, grid, W * 32, (size_t)C::SMEM_B, F.stream, m, bs, phi, rhs, tmp,
            homog ? 1 : 0);
+}
+
+// Half-sweeps n_first .. n_first + n_count - 1 of a small level in one block
+// (k_sweep_small); false if the level is too large for it.
+template <class T>
+bool Forest::sweeps_small(const Arrays<T>& a, int lvl, int n_first, int n_count, bool pull_first, bool homog) {
+  const int nbx = lvl_n(lvl);
+  if (!use_small_sweeps || nbx == 0) return false;
+  bool done = false;
+  with_nc(plan.dim, plan.nc_at(lvl), [&](auto d_, auto nc_) {
+    constexpr int D = decltype(d_)::value, NC = decltype(nc_)::value;
+    using G = dev::Geo<D, NC>;
+    const size_t smem = (size_t)nbx * (sizeof(SlotDesc) + (G::SG + G::SI + G::NNB * G::NF) * sizeof(T) + 4);
+    if (smem > (size_t)kSmallSmemBytes || (long long)nbx * G::SI > kSmallCells) return;
+    kernel_occupancy((const void*)dev::k_sweep_small<D, NC, T>, dev::kSmallThreads, (int)kSmallSmemBytes);
+    prof_level = lvl;
+    ProfScope ps(this, kProfSweep, 3.0 * n_count * nbx * G::SI * sizeof(T));
+    launch_k(dev::k_sweep_small<D, NC, T>, 1, dev::kSmallThreads, smem, stream, meta_of(meta), level_set(lvl), a.phi,
+             (const T*)a.rhs, n_first, n_count, pull_first ? 1 : 0, homog ? 1 : 0);
+    done = true;
+  });
+  return done;
 }
 
 template <class T>
@@ -749,7 +764,9 @@ void Forest::vcycle_t(const Arrays<T>& a, const MgOpts& mg, int highest, bool ho
                       bool inner) {
   const int l0 = plan.min_lvl;
   auto sweeps = [&](const auto& arr, int l, int n_cycle) {
+    if (n_cycle <= 0) return;
     SweepGroup sg(this);
+    if (sweeps_small(arr, l, 1, 2 * n_cycle, l != highest, homog)) return;
     for (int n = 1; n <= 2 * n_cycle; ++n) sweep(arr, l, n, n > 1 || l != highest, homog);
   };
   for (int l = highest; l >= l0 + 1; --l) {
@@ -793,7 +810,8 @@ void Forest::vcycle_t(const Arrays<T>& a, const MgOpts& mg, int highest, bool ho
     correct(a, l - 1, inner && l - 1 > l0, homog);
     if (mg.n_up > 0) {
       SweepGroup sg(this);
-      for (int n = 1; n <= 2 * mg.n_up; ++n) sweep(a, l, n, true, homog);
+      if (!sweeps_small(a, l, 1, 2 * mg.n_up, true, homog))
+        for (int n = 1; n <= 2 * mg.n_up; ++n) sweep(a, l, n, true, homog);
     }
     if (!inner) fill(a, l, homog);
   }

@@ -504,11 +504,17 @@ def main():
     # per-kernel breakdown: one mixed solve, every kind profiled
     timed(afv.AFV_PREC_MIXED, 1, mask=0xFF)
     breakdown = {}
+    pe = forest.profile_entries()
     for k, name in enumerate(afv.KERNEL_KINDS):
         n, kms, kb = forest.profile_read(k)
         if n:
+            lv_ms = {}
+            for kk, lv, t_ms in zip(pe["kind"], pe["level"], pe["ms"]):
+                if kk == k:
+                    lv_ms[str(int(lv))] = lv_ms.get(str(int(lv)), 0.0) + float(t_ms)
             breakdown[name] = {"launches": n, "ms": round(kms, 4),
-                               "GB/s": round(kb / (kms / 1e3) / 1e9, 1) if kms > 0 else None}
+                               "GB/s": round(kb / (kms / 1e3) / 1e9, 1) if kms > 0 else None,
+                               "us_by_level": {lv: round(1e3 * t, 1) for lv, t in lv_ms.items()}}
     forest.profile(0)
 
     # end to end through the C ABI: rhs in from pinned host memory, solution out
@@ -559,7 +565,7 @@ def main():
         "fp64": {"value": value64, "unit": "unknowns/s", "cycles": cyc64, "rel_res": max(rels64),
                  "ms_per_solve": ms64 / len(cyc64)},
         "mixed_vs_fp64_solve_speedup": (ms64 / len(cyc64)) / (ms / args.steps),
-        "roofline": {"bound": "hbm", "kernel": "k_level_tma<3,8,float,sweep>",
+        "roofline": {"bound": "hbm", "kernel": "k_sweep_warp<3,8,float>",
                      "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None,
                      "peak_kind": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",

@@ -261,8 +261,10 @@ int afv_forest_profile_read(afv_forest* f, int kind, long long* launches, double
  * iterations as CUDA graphs, 0 launches them one by one.
  * AFV_OPT_RESTRICT_KERNEL: 1 (default) warp-per-box kernels for the residual
  * restriction (levels >= 2) and the coarse right-hand side (levels >= 1),
- * 0 the block-staged kernels. */
-enum { AFV_OPT_SWEEP_KERNEL = 0, AFV_OPT_GRAPHS = 1, AFV_OPT_RESTRICT_KERNEL = 2 };
+ * 0 the block-staged kernels. AFV_OPT_SMALL_SWEEPS: 1 (default) runs all
+ * half-sweeps of a level of at most 2048 interior cells in one block, 0
+ * launches them one by one. */
+enum { AFV_OPT_SWEEP_KERNEL = 0, AFV_OPT_GRAPHS = 1, AFV_OPT_RESTRICT_KERNEL = 2, AFV_OPT_SMALL_SWEEPS = 3 };
 int afv_forest_set_option(afv_forest* f, int option, int value);
 int afv_forest_get_option(afv_forest* f, int option, int* value);
 /* No counterpart in the reference: times the sweep kernel variants on this

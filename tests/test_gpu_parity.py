@@ -303,3 +303,27 @@ def test_restrict_kernel_variants_agree(gpu, which):
         g.close()
     for a, b in zip(out[0], out[1]):
         assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("which", ["c1", "3d"])
+def test_small_level_sweeps_agree(gpu, which):
+    """All half-sweeps of a small level in one block (the default) and launched
+    one by one give the same bits (FP64 V-cycles and mixed solves)."""
+    spec = W.c1_poisson_2d() if which == "c1" else W.c2_poisson_3d(thr=3e-3, lvl_max=5)
+    f, ot, _ = setup_pair(gpu, spec)
+    rhs = f.get_var(0, gpu.AFV_RHS)
+    out = []
+    for opt in (1, 0):
+        g = gpu.Forest([W.build_tree(spec)], mixed=True)
+        g.set_var(0, gpu.AFV_RHS, rhs)
+        g.set_option(gpu.AFV_OPT_SMALL_SWEEPS, opt)
+        for _ in range(2):
+            g.vcycle(set_residual=True)
+        v = [g.get_var(0, x) for x in (gpu.AFV_PHI, gpu.AFV_TMP, gpu.AFV_RHS)]
+        g.zero(gpu.AFV_PHI)
+        g.solve(gpu.AFV_PREC_MIXED, tol=1e-8, max_cycles=30)
+        v.append(g.get_var(0, gpu.AFV_PHI))
+        out.append(v)
+        g.close()
+    for a, b in zip(out[0], out[1]):
+        assert np.array_equal(a, b)
