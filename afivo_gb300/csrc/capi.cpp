@@ -416,8 +416,9 @@ int afv_forest_set_option(afv_forest* f, int option, int value) {
   if (!f) return fail(AFV_ERR_INVALID, "forest is NULL");
   switch (option) {
     case AFV_OPT_SWEEP_KERNEL:
-      if (value < 0 || value > 2) return fail(AFV_ERR_INVALID, "sweep kernel must be 0, 1 or 2");
+      if (value < 0 || value > 5) return fail(AFV_ERR_INVALID, "sweep kernel must be 0 .. 5");
       f->f.sweep_kernel = value;
+      f->f.drop_graphs();
       return AFV_OK;
     case AFV_OPT_GRAPHS:
       f->f.use_graphs = value != 0;
@@ -432,6 +433,15 @@ int afv_forest_set_option(afv_forest* f, int option, int value) {
       f->f.use_small_sweeps = value != 0;
       f->f.drop_graphs();
       return AFV_OK;
+    case AFV_OPT_PROFILE_LEAD_US:
+      if (value < 0 || value > 1000000) return fail(AFV_ERR_INVALID, "profile lead must be 0 .. 1e6 us");
+      f->f.prof_lead_us = value;
+      return AFV_OK;
+    case AFV_OPT_DEFECT_KERNEL:
+      if (value != 0 && value != 1) return fail(AFV_ERR_INVALID, "defect kernel must be 0 or 1");
+      f->f.defect_fx = value != 0;
+      f->f.drop_graphs();
+      return AFV_OK;
   }
   return fail(AFV_ERR_INVALID, "unknown option");
 }
@@ -443,6 +453,8 @@ int afv_forest_get_option(afv_forest* f, int option, int* value) {
     case AFV_OPT_GRAPHS: *value = f->f.use_graphs ? 1 : 0; return AFV_OK;
     case AFV_OPT_RESTRICT_KERNEL: *value = f->f.use_restrict_warp ? 1 : 0; return AFV_OK;
     case AFV_OPT_SMALL_SWEEPS: *value = f->f.use_small_sweeps ? 1 : 0; return AFV_OK;
+    case AFV_OPT_PROFILE_LEAD_US: *value = f->f.prof_lead_us; return AFV_OK;
+    case AFV_OPT_DEFECT_KERNEL: *value = f->f.defect_fx ? 1 : 0; return AFV_OK;
   }
   return fail(AFV_ERR_INVALID, "unknown option");
 }

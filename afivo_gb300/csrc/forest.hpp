@@ -76,6 +76,7 @@ class Forest {
   int n_sm = 148;
   int sweep_kernel = 1;  // 0: block-pipelined k_level_tma, 1: warp-per-box k_sweep_warp, 2: its async variant
   bool use_restrict_warp = true;  // warp-per-box restriction on levels >= 2
+  bool defect_fx = true;          // mixed defect: fixed-point Laplacian (false: FP64 sum)
   // All half-sweeps of a level in one block (k_sweep_small) when the level has
   // at most kSmallCells interior cells: measured faster than one launch per
   // half-sweep for 512 cells (8.4 us for four half-sweeps against 14 us),
@@ -121,6 +122,7 @@ class Forest {
   // are bracketed by CUDA events on the forest's stream
   int prof_mask = 0;
   int prof_level = 0;  // level tag of the next profiled launches
+  int prof_lead_us = 0;  // > 0: each profiled solve iteration starts behind a k_hold of this length
   // Consecutive half-sweeps of one level are timed by one pair of events
   // (a group), so the events' own cost is not charged to every launch.
   bool group_on = false;

@@ -58,6 +58,33 @@ static Meta meta_of(const DevMeta& d) {
   return m;
 }
 
+// Raises a kernel's dynamic shared-memory limit to smem on the current device
+// and returns its resident blocks per SM (at least 1). The attribute is per
+// device and the forests of a process may run on several devices and host
+// threads, so the result is kept per (kernel, device) under a lock. (The
+// shared-memory carve-out stays the driver's choice: forcing the largest one
+// on every kernel shrinks L1 under the sweeps, whose neighbour loads use it,
+// and made the C2 mixed solve 10% slower.)
+struct KernelAttrs {
+  const void* kern;
+  int device, threads, smem, occ;
+};
+static int kernel_occupancy(const void* kern, int threads, int smem) {
+  static std::mutex mu;
+  static std::vector<KernelAttrs> known;
+  int device = 0;
+  cudaGetDevice(&device);
+  std::lock_guard<std::mutex> lock(mu);
+  for (const auto& k : known)
+    if (k.kern == kern && k.device == device && k.threads == threads && k.smem >= smem) return k.occ;
+  if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  int occ = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, threads, smem);
+  occ = occ < 1 ? 1 : occ;
+  known.push_back({kern, device, threads, smem, occ});
+  return occ;
+}
+
 // Kernel launch with programmatic stream serialization: the next kernel on
 // the stream may be scheduled while this one drains, and waits in
 // dev::pdl_wait() for it to finish before touching memory.
@@ -487,25 +514,6 @@ int Forest::set_var(int t, int var, const double* host, int interior_only, std::
 // Level operators
 // ---------------------------------------------------------------------------
 
-// Raises a kernel's dynamic shared-memory limit to smem on the current device
-// and returns its resident blocks per SM (at least 1). The attribute is per
-// device and the forests of a process may run on several devices and host
-// threads, so the result is kept per (kernel, device) under a lock.
-static int kernel_occupancy(const void* kern, int threads, int smem) {
-  static std::mutex mu;
-  static std::vector<std::pair<std::pair<const void*, int>, int>> known;
-  int device = 0;
-  cudaGetDevice(&device);
-  std::lock_guard<std::mutex> lock(mu);
-  for (const auto& e : known)
-    if (e.first.first == kern && e.first.second == device) return e.second;
-  if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  int occ = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, threads, smem);
-  if (occ < 1) occ = 1;
-  known.push_back({{kern, device}, occ});
-  return occ;
-}
 
 // Launches the pipelined level kernel (sweep or ghost fill) on a box set.
 template <int D, int NC, class T, int MODE>
@@ -529,6 +537,19 @@ static void launch_sweep_warp(Forest& F, const Meta& m, BoxSet bs, T* phi, const
   const int grid = (int)std::max(1LL, std::min(blocks, (long long)F.n_sm * occ));
   launch_k(dev::k_sweep_warp<D, NC, T, W, S, ASYNC>, grid, W * 32, C::SMEM_B, F.stream, m, bs, phi, rhs, n, pull ? 1 : 0,
                                                                           homog ? 1 : 0);
+}
+
+// Launches the warp-per-parent correction (8 warps x 3 stages in FP32,
+// 4 x 3 in FP64: about 195 KB of shared memory for 8^3 boxes).
+template <int D, int NC, class T>
+static void launch_correct_warp(Forest& F, const Meta& m, BoxSet bs, T* phi, T* tmp, bool pull, bool homog) {
+  constexpr int W = std::is_same<T, float>::value ? 8 : 4, S = 3;
+  using C = dev::CorrectCfg<D, NC, T, W, S>;
+  const int occ = kernel_occupancy((const void*)dev::k_correct_warp<D, NC, T, W, S>, W * 32, (int)C::SMEM_B);
+  const long long blocks = (bs.n + W - 1) / W;
+  const int grid = (int)std::max(1LL, std::min(blocks, (long long)F.n_sm * occ));
+  launch_k(dev::k_correct_warp<D, NC, T, W, S>, grid, W * 32, (size_t)C::SMEM_B, F.stream, m, bs, phi, tmp,
+           pull ? 1 : 0, homog ? 1 : 0);
 }
 
 dev_BoxSet Forest::level_set(int lvl) const {
@@ -600,15 +621,21 @@ void Forest::sweep(const Arrays<T>& a, int lvl, int n, bool pull, bool homog) {
     if (sweep_kernel == 0) {
       launch_level<D, NC, T, dev::kModeSweep>(*this, m, bs, a.phi, a.rhs, n, pull, homog);
     } else if constexpr (std::is_same<T, float>::value) {
-      if (sweep_kernel == 1)
-        launch_sweep_warp<D, NC, T, 16, 3, 0>(*this, m, bs, a.phi, a.rhs, n, pull, homog);
-      else
-        launch_sweep_warp<D, NC, T, 16, 3, 1>(*this, m, bs, a.phi, a.rhs, n, pull, homog);
+      switch (sweep_kernel) {
+        case 1: launch_sweep_warp<D, NC, T, 16, 3, 0>(*this, m, bs, a.phi, a.rhs, n, pull, homog); break;
+        case 2: launch_sweep_warp<D, NC, T, 16, 3, 1>(*this, m, bs, a.phi, a.rhs, n, pull, homog); break;
+        case 3: launch_sweep_warp<D, NC, T, 16, 2, 0>(*this, m, bs, a.phi, a.rhs, n, pull, homog); break;
+        case 4: launch_sweep_warp<D, NC, T, 12, 3, 0>(*this, m, bs, a.phi, a.rhs, n, pull, homog); break;
+        default: launch_sweep_warp<D, NC, T, 24, 2, 0>(*this, m, bs, a.phi, a.rhs, n, pull, homog); break;
+      }
     } else {
-      if (sweep_kernel == 1)
-        launch_sweep_warp<D, NC, T, 8, 3, 0>(*this, m, bs, a.phi, a.rhs, n, pull, homog);
-      else
-        launch_sweep_warp<D, NC, T, 8, 3, 1>(*this, m, bs, a.phi, a.rhs, n, pull, homog);
+      switch (sweep_kernel) {
+        case 1: launch_sweep_warp<D, NC, T, 8, 3, 0>(*this, m, bs, a.phi, a.rhs, n, pull, homog); break;
+        case 2: launch_sweep_warp<D, NC, T, 8, 3, 1>(*this, m, bs, a.phi, a.rhs, n, pull, homog); break;
+        case 3: launch_sweep_warp<D, NC, T, 8, 2, 0>(*this, m, bs, a.phi, a.rhs, n, pull, homog); break;
+        case 4: launch_sweep_warp<D, NC, T, 6, 3, 0>(*this, m, bs, a.phi, a.rhs, n, pull, homog); break;
+        default: launch_sweep_warp<D, NC, T, 12, 2, 0>(*this, m, bs, a.phi, a.rhs, n, pull, homog); break;
+      }
     }
   });
 }
@@ -706,6 +733,8 @@ void Forest::correct(const Arrays<T>& a, int lp, bool pull, bool homog) {
     if (sub) {
       if constexpr (!(D == 2 && NC == 16) && !(D == 3 && NC == 8))
         launch_k(dev::k_correct<D, NC, true, T>, grid, dev::kThreads, 0, stream, m, bs, a.phi, a.tmp, pl, hg);
+    } else if (use_restrict_warp) {
+      launch_correct_warp<D, NC, T>(*this, m, bs, a.phi, a.tmp, pull, homog);
     } else {
       launch_k(dev::k_correct<D, NC, false, T>, grid, dev::kThreads, 0, stream, m, bs, a.phi, a.tmp, pl, hg);
     }
@@ -1083,8 +1112,20 @@ void Forest::enqueue_residual_check(int precision, double tol) {
       constexpr int BPC = dev::boxes_per_cta<G::SG, PER_BOX, double>(1);
       // read u (8 B), f (8 B); write r (4 B)
       ProfScope ps(this, kProfDefect, 20.0 * nl * G::SI);
-      launch_k(dev::k_defect<D, NC>, grid_for((nl + BPC - 1) / BPC, n_sm * 4), dev::kThreads, 0, stream, 
-          m, bs, d64.phi, d64.rhs, d32.rhs, d_norm);
+      if constexpr (dev::DefectFxCfg<D, NC>::OK) {
+        if (defect_fx) {
+          constexpr int T = dev::DefectFxCfg<D, NC>::T;
+          const int occ = kernel_occupancy((const void*)dev::k_defect_fx<D, NC>, T, 0);
+          const int grid = (int)std::max(1LL, std::min((long long)nl, (long long)n_sm * occ));
+          launch_k(dev::k_defect_fx<D, NC>, grid, T, 0, stream, m, bs, (const double*)d64.phi,
+                   (const double*)d64.rhs, d32.rhs, d_norm);
+          return;
+        }
+      }
+      {
+        launch_k(dev::k_defect<D, NC>, grid_for((nl + BPC - 1) / BPC, n_sm * 4), dev::kThreads, 0, stream, m, bs,
+                 d64.phi, d64.rhs, d32.rhs, d_norm);
+      }
     });
   } else {
     for (int l = plan.min_lvl; l <= plan.max_lvl; ++l) residual(d64, l, d_norm, true);
@@ -1220,6 +1261,7 @@ int Forest::solve(const MgOpts& mg, int precision, double tol, int max_cycles, S
       if (cudaGraphLaunch(gc.exec, stream) != cudaSuccess) return check(err, "graph launch");
       n_launches += gc.kernels;
     } else {
+      if (prof_mask && prof_lead_us > 0) dev::k_hold<<<1, 1, 0, stream>>>(1000LL * prof_lead_us);
       enqueue_iteration(mg, precision, tol);
     }
     if (cudaStreamSynchronize(stream) != cudaSuccess) return check(err, "solve");

@@ -260,11 +260,24 @@ int afv_forest_profile_read(afv_forest* f, int kind, long long* launches, double
  * per-lane asynchronous copies. AFV_OPT_GRAPHS: 1 (default) replays solve
  * iterations as CUDA graphs, 0 launches them one by one.
  * AFV_OPT_RESTRICT_KERNEL: 1 (default) warp-per-box kernels for the residual
- * restriction (levels >= 2) and the coarse right-hand side (levels >= 1),
- * 0 the block-staged kernels. AFV_OPT_SMALL_SWEEPS: 1 (default) runs all
+ * restriction (levels >= 2), the coarse right-hand side (levels >= 1) and the
+ * correction of children on levels >= 2, 0 the block-staged kernels. AFV_OPT_SMALL_SWEEPS: 1 (default) runs all
  * half-sweeps of a level of at most 2048 interior cells in one block, 0
- * launches them one by one. */
-enum { AFV_OPT_SWEEP_KERNEL = 0, AFV_OPT_GRAPHS = 1, AFV_OPT_RESTRICT_KERNEL = 2, AFV_OPT_SMALL_SWEEPS = 3 };
+ * launches them one by one. AFV_OPT_PROFILE_LEAD_US: with the event profiler
+ * on, each solve iteration is queued behind a device-side wait of this many
+ * microseconds (default 0), so that the events time the kernels rather than
+ * the host's launch rate. AFV_OPT_DEFECT_KERNEL: the mixed solve's FP64
+ * defect r = f - L u computes the Laplacian in 64-bit fixed point per box
+ * (1, default; exact sums, one FP64 multiply-add per cell) or as an FP64 sum
+ * (0). AFV_OPT_SWEEP_KERNEL 3..5 are other warp and stage counts of 1. */
+enum {
+  AFV_OPT_SWEEP_KERNEL = 0,
+  AFV_OPT_GRAPHS = 1,
+  AFV_OPT_RESTRICT_KERNEL = 2,
+  AFV_OPT_SMALL_SWEEPS = 3,
+  AFV_OPT_PROFILE_LEAD_US = 4,
+  AFV_OPT_DEFECT_KERNEL = 5
+};
 int afv_forest_set_option(afv_forest* f, int option, int value);
 int afv_forest_get_option(afv_forest* f, int option, int* value);
 /* No counterpart in the reference: times the sweep kernel variants on this

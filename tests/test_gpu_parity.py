@@ -327,3 +327,71 @@ def test_small_level_sweeps_agree(gpu, which):
         g.close()
     for a, b in zip(out[0], out[1]):
         assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("which", ["c1", "3d"])
+def test_defect_kernels_agree(gpu, which):
+    """The mixed solve's defect with the fixed-point Laplacian (default) and
+    with the FP64 sum: same cycle counts, residuals within float rounding,
+    solutions within the solve tolerance of each other and of the oracle."""
+    spec = W.c1_poisson_2d() if which == "c1" else W.c2_poisson_3d(thr=3e-3, lvl_max=5)
+    f, ot, _ = setup_pair(gpu, spec)
+    rhs = f.get_var(0, gpu.AFV_RHS)
+    out = []
+    for opt in (1, 0):
+        g = gpu.Forest([W.build_tree(spec)], mixed=True)
+        g.set_var(0, gpu.AFV_RHS, rhs)
+        g.set_option(gpu.AFV_OPT_DEFECT_KERNEL, opt)
+        assert g.get_option(gpu.AFV_OPT_DEFECT_KERNEL) == opt
+        cyc, rel, rc = g.solve(gpu.AFV_PREC_MIXED, tol=1e-8, max_cycles=60)
+        assert rc == 0 and rel[0] <= 1e-8
+        out.append((int(cyc[0]), float(rel[0]), g.get_var(0, gpu.AFV_PHI)))
+        g.close()
+    (c1, r1, p1), (c0, r0, p0) = out
+    assert c1 == c0
+    assert abs(r1 - r0) <= 1e-3 * r0
+    scale = np.abs(p0).max()
+    assert np.abs(p1 - p0).max() <= 1e-7 * scale
+    for _ in range(40):
+        ot.vcycle()
+    ref = oracle_var(ot, O.I_PHI, spec["n_cell"])
+    assert compare_var(p1, ref, ot, spec["n_cell"], spec["dim"], True) < 1e-6
+
+
+def test_mixed_solve_scale_invariant(gpu):
+    """Scaling the right-hand side by 2^k scales every value of the mixed
+    solve exactly (the fixed-point defect shifts its scale with the box's
+    largest exponent), so the solution is the unscaled one times 2^k, bit for
+    bit, and the cycle count is the same."""
+    spec = W.c1_poisson_2d()
+    f, ot, _ = setup_pair(gpu, spec)
+    rhs = f.get_var(0, gpu.AFV_RHS)
+    out = {}
+    for k in (0, -40, 40):
+        g = gpu.Forest([W.build_tree(spec)], mixed=True)
+        g.set_var(0, gpu.AFV_RHS, np.ldexp(rhs, k))
+        cyc, rel, rc = g.solve(gpu.AFV_PREC_MIXED, tol=1e-8, max_cycles=60)
+        assert rc == 0 and rel[0] <= 1e-8
+        out[k] = (int(cyc[0]), float(rel[0]), g.get_var(0, gpu.AFV_PHI))
+        g.close()
+    for k in (-40, 40):
+        assert out[k][0] == out[0][0] and out[k][1] == out[0][1]
+        assert np.array_equal(out[k][2], np.ldexp(out[0][2], k))
+
+
+def test_defect_nonfinite_reports_divergence(gpu):
+    """A box holding a NaN takes the FP64 sum, which carries the NaN into the
+    residual: both defect kernels report the solve as diverged."""
+    spec = W.c1_poisson_2d()
+    f, ot, _ = setup_pair(gpu, spec)
+    rhs = f.get_var(0, gpu.AFV_RHS)
+    phi = np.zeros_like(f.get_var(0, gpu.AFV_PHI, interior_only=True))
+    phi[-1] = np.nan  # a cell of the last box, a leaf on the finest level
+    for opt in (1, 0):
+        g = gpu.Forest([W.build_tree(spec)], mixed=True)
+        g.set_var(0, gpu.AFV_RHS, rhs)
+        g.set_var(0, gpu.AFV_PHI, phi, interior_only=True)
+        g.set_option(gpu.AFV_OPT_DEFECT_KERNEL, opt)
+        cyc, rel, rc = g.solve(gpu.AFV_PREC_MIXED, tol=1e-8, max_cycles=5, check=False)
+        assert rc == gpu.AFV_ERR_DIVERGED
+        g.close()
