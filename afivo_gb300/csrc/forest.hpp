@@ -85,6 +85,10 @@ class Forest {
   static constexpr long long kSmallCells = 2048;
   static constexpr long long kSmallSmemBytes = 200 * 1024;
   cudaStream_t stream = nullptr;
+  cudaStream_t side = nullptr;  // second branch of an iteration (fork / join)
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  void fork();
+  void join();
   DevMeta meta;
   Arrays<double> d64;
   Arrays<float> d32;

@@ -149,6 +149,7 @@ static void retain_pool(int device) {
 Forest::~Forest() {
   std::lock_guard<std::mutex> lock(g_capture_mutex);
   cudaSetDevice(device);
+  if (side) cudaStreamSynchronize(side);
   if (stream) cudaStreamSynchronize(stream);
   void* ptrs[] = {meta.parent, meta.first_child, meta.tree, meta.offg, meta.offi, meta.bcval,
                   meta.active, meta.desc, meta.nbo2, meta.err, meta.rmin, d64.phi, d64.rhs,
@@ -166,6 +167,9 @@ Forest::~Forest() {
   if (h_count) cudaFreeHost(h_count);
   if (h_active) cudaFreeHost(h_active);
   if (h_norm) cudaFreeHost(h_norm);
+  if (ev_fork) cudaEventDestroy(ev_fork);
+  if (ev_join) cudaEventDestroy(ev_join);
+  if (side) cudaStreamDestroy(side);
   if (stream) cudaStreamDestroy(stream);
 }
 
@@ -310,7 +314,10 @@ int Forest::create(const std::vector<const HostTree*>& trees, const afv_forest_o
   mixed = opts ? opts->mixed_buffers != 0 : false;
   if (cudaSetDevice(device) != cudaSuccess) return err = "cudaSetDevice failed", AFV_ERR_CUDA;
   cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, device);
-  if (cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking) != cudaSuccess)
+  if (cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming) != cudaSuccess)
     return err = "cudaStreamCreate failed", AFV_ERR_CUDA;
   retain_pool(device);
   const Plan& p = plan;
@@ -1144,10 +1151,24 @@ void Forest::enqueue_residual_check(int precision, double tol) {
 
 // One solve iteration, enqueued only: a V-cycle (FP64), or an FP32 V-cycle
 // on the defect with the FP64 accumulate (mixed), then the residual check.
+// Work on the side stream between fork() and join() runs beside the main
+// stream's (both are captured into the iteration's graph as parallel
+// branches). Launch helpers take the forest's current stream, so a branch is
+// enqueued with the two streams swapped.
+void Forest::fork() {
+  cudaEventRecord(ev_fork, stream);
+  cudaStreamWaitEvent(side, ev_fork, 0);
+}
+void Forest::join() {
+  cudaEventRecord(ev_join, side);
+  cudaStreamWaitEvent(stream, ev_join, 0);
+}
+
+// One mixed iteration expects the correction array zeroed (solve() zeroes it
+// before the first; each iteration zeroes it for the next beside its defect).
 void Forest::enqueue_iteration(const MgOpts& mg, int precision, double tol) {
   Meta m = meta_of(meta);
   if (precision == AFV_PREC_MIXED) {
-    cudaMemsetAsync(d32.phi, 0, sizeof(float) * plan.n_elem_g, stream);
     vcycle_t(d32, mg, plan.max_lvl, true, true, true);
     int nl = (int)plan.all_leaves.size();
     BoxSet bs{d_lists + all_leaves_off, 0, nl};
@@ -1155,12 +1176,10 @@ void Forest::enqueue_iteration(const MgOpts& mg, int precision, double tol) {
       constexpr int D = decltype(d_)::value, NC = decltype(nc_)::value;
       using G = dev::Geo<D, NC>;
       long long items = (long long)nl * G::SI;
-      {
-        // read e (4 B), read and write u (16 B)
-        ProfScope ps(this, kProfAccumulate, 20.0 * items);
-        launch_k(dev::k_accumulate<D, NC>, grid_for((items / NC + 255) / 256, n_sm), 256, 0, stream, m, bs,
-                 d64.phi, d32.phi);
-      }
+      // The leaves' accumulate and the parents' increments touch disjoint
+      // cells (leaves' u; parents' u and e, from the leaves' e): two branches.
+      fork();
+      std::swap(stream, side);
       // parents (finest first) take the restriction of their children's increments
       for (int l = plan.max_lvl - 1; l >= 1; --l) {
         int np = n_parents(l);
@@ -1168,14 +1187,27 @@ void Forest::enqueue_iteration(const MgOpts& mg, int precision, double tol) {
         BoxSet pb{parents_list(l), 0, np};
         long long pit = (long long)np * G::SI;
         ProfScope ps(this, kProfAccumulate, (4.0 * (1 << D) + 4.0 + 16.0) * pit);
-        launch_k(dev::k_restrict_increment<D, NC>, grid_for((pit + 255) / 256, n_sm), 256, 0, stream, 
-            m, pb, d64.phi, d32.phi);
+        launch_k(dev::k_restrict_increment<D, NC>, grid_for((pit + 255) / 256, n_sm), 256, 0, stream,
+                 m, pb, d64.phi, d32.phi);
       }
+      std::swap(stream, side);
+      {
+        // read e (4 B), read and write u (16 B)
+        ProfScope ps(this, kProfAccumulate, 20.0 * items);
+        launch_k(dev::k_accumulate<D, NC>, grid_for((items / NC + 255) / 256, n_sm), 256, 0, stream, m, bs,
+                 d64.phi, d32.phi);
+      }
+      join();
     });
+    // the next iteration's zero correction, beside this one's defect
+    fork();
+    cudaMemsetAsync(d32.phi, 0, sizeof(float) * plan.n_elem_g, side);
+    enqueue_residual_check(precision, tol);
+    join();
   } else {
     vcycle_t(d64, mg, plan.max_lvl, false, false);
+    enqueue_residual_check(precision, tol);
   }
-  enqueue_residual_check(precision, tol);
 }
 
 // Solve every tree to max|f - L phi| <= tol * max|f| over its leaves. Each
@@ -1226,6 +1258,7 @@ int Forest::solve(const MgOpts& mg, int precision, double tol, int max_cycles, S
     // Parents start as the restriction of their children (their values are
     // only read by coarse leaves next to refined regions).
     for (int l = plan.max_lvl; l >= plan.min_lvl + 1; --l) restrict_res(d64, l, false);
+    cudaMemsetAsync(d32.phi, 0, sizeof(float) * plan.n_elem_g, stream);  // the first correction
   }
   enqueue_residual_check(precision, tol);
   if (cudaStreamSynchronize(stream) != cudaSuccess) return check(err, "solve");
