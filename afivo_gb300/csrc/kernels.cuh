@@ -2531,14 +2531,19 @@ k_defect_fx(Meta m, BoxSet bs, const double* __restrict__ u, const double* __res
 
 // u += e over the interiors of the leaves (FP64 accumulate of the FP32
 // correction). One thread per row of NC cells: the slot lookups are made once
-// per row and the row's loads are issued together.
+// per row. The whole ghosted row (NC + 2 cells, an even count from an even
+// offset: 16-byte aligned doubles, 8-byte aligned floats) moves in vector
+// loads and stores, with its two ghost cells written back unchanged; the
+// sectors touched are those of the interior row alone.
 template <int D, int NC>
 __global__ void __launch_bounds__(kThreads)
 k_accumulate(Meta m, BoxSet bs, double* __restrict__ u, const float* __restrict__ e) {
   pdl_wait();
   pdl_trigger();
   using G = Geo<D, NC>;
+  static_assert(G::NG % 2 == 0, "rows of an even number of cells");
   constexpr int ROWS = G::SI / NC;  // rows of a box
+  constexpr int H = G::NG / 2;      // vector pairs of a ghosted row
   const long long total = (long long)bs.n * ROWS;
   for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < total;
        x += (long long)gridDim.x * blockDim.x) {
@@ -2546,16 +2551,24 @@ k_accumulate(Meta m, BoxSet bs, double* __restrict__ u, const float* __restrict_
     const int s = box_at(bs, bi);
     if (!m.active[m.tree[s]]) continue;
     const int j = row % NC + 1, k = (D == 3) ? row / NC + 1 : 0;
-    const long long o = m.offg[s] + G::g(1, j, k);
-    double uv[NC];
-    float ev[NC];
+    const long long o = m.offg[s] + G::g(0, j, k);
+    double2* ur = reinterpret_cast<double2*>(u + o);
+    const float2* er = reinterpret_cast<const float2*>(e + o);
+    double2 uv[H];
+    float2 ev[H];
 #pragma unroll
-    for (int i = 0; i < NC; ++i) {
-      uv[i] = u[o + i];
-      ev[i] = e[o + i];
+    for (int i = 0; i < H; ++i) {
+      uv[i] = ur[i];
+      ev[i] = er[i];
+    }
+    // cell 0 and cell NG - 1 are ghosts
+#pragma unroll
+    for (int i = 0; i < H; ++i) {
+      if (i > 0) uv[i].x = uv[i].x + f2d_exact(ev[i].x);
+      if (i < H - 1) uv[i].y = uv[i].y + f2d_exact(ev[i].y);
     }
 #pragma unroll
-    for (int i = 0; i < NC; ++i) u[o + i] = uv[i] + f2d_exact(ev[i]);
+    for (int i = 0; i < H; ++i) ur[i] = uv[i];
   }
 }
 
