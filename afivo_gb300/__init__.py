@@ -334,13 +334,19 @@ class Forest:
         return dict(zip(keys, (int(x) for x in out)))
 
     def _n_values(self, tree, interior):
-        t = self.trees[tree]
-        n = 0
-        for lvl in range(t.min_lvl, t.highest_lvl + 1):
-            ids, _, _ = t.level(lvl)
-            nc = t.n_cell_at(lvl)
-            n += len(ids) * ((nc if interior else nc + 2) ** self.dim)
-        return n
+        """Values of a tree's variable in the host layout (the forest's boxes
+        are fixed when it is created, so the count is kept)."""
+        key = (tree, bool(interior))
+        cache = self.__dict__.setdefault("_n_values_cache", {})
+        if key not in cache:
+            t = self.trees[tree]
+            n = 0
+            for lvl in range(t.min_lvl, t.highest_lvl + 1):
+                ids, _, _ = t.level(lvl)
+                nc = t.n_cell_at(lvl)
+                n += len(ids) * ((nc if interior else nc + 2) ** self.dim)
+            cache[key] = n
+        return cache[key]
 
     def set_var(self, tree, var, values, interior_only=False):
         a = np.ascontiguousarray(values, dtype=np.float64).ravel()

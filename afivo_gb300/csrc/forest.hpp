@@ -4,6 +4,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <array>
 #include <string>
 #include <vector>
 
@@ -109,7 +110,17 @@ class Forest {
   unsigned long long* h_norm = nullptr;  // pinned [n_trees]
   double* d_stage = nullptr;             // staging for host exchange
   long long stage_elems = 0;
-  int* d_stage_slots = nullptr;
+  int* d_stage_slots = nullptr;          // every tree's host-order slots, concatenated
+  // host exchange plan, made on the first exchange: per tree the interior
+  // and ghosted value counts, the runs of boxes of one level, and where its
+  // slots start in d_stage_slots
+  struct XferRun {
+    int first, n, lvl;
+  };
+  bool xfer_ready = false;
+  std::vector<std::array<long long, 2>> xfer_total;
+  std::vector<std::vector<XferRun>> xfer_runs;
+  std::vector<long long> xfer_order_off;
   long long bytes = 0;
   std::vector<int> host_active;
   int* h_active = nullptr;  // pinned copy of the device activity flags (read back by solves)

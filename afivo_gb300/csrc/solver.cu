@@ -434,65 +434,86 @@ int Forest::set_active_host(const std::vector<int>& a) {
 
 // Copies between the host layout and slot storage go level by level: the
 // host buffer is the concatenation, over the tree's levels, of its boxes in
-// level-list order.
+// level-list order. The per-tree sizes, the runs of boxes of one level and
+// the slot orders on the device are made on the first exchange of a forest.
+static int exchange_plan(Forest& F, std::string& err) {
+  if (F.xfer_ready) return AFV_OK;
+  const Plan& p = F.plan;
+  const int D = p.dim;
+  F.xfer_total.assign(p.n_trees, {0, 0});
+  F.xfer_runs.assign(p.n_trees, {});
+  F.xfer_order_off.assign(p.n_trees + 1, 0);
+  std::vector<int> all;
+  for (int t = 0; t < p.n_trees; ++t) {
+    const std::vector<int>& order = p.host_order[t];
+    F.xfer_order_off[t] = (long long)all.size();
+    all.insert(all.end(), order.begin(), order.end());
+    size_t i = 0;
+    while (i < order.size()) {
+      const int l = p.lvl[order[i]];
+      size_t j = i;
+      while (j < order.size() && p.lvl[order[j]] == l) ++j;
+      long long si = 1, sg = 1;
+      for (int d = 0; d < D; ++d) {
+        si *= p.nc_at(l);
+        sg *= p.nc_at(l) + 2;
+      }
+      F.xfer_runs[t].push_back({(int)i, (int)(j - i), l});
+      F.xfer_total[t][0] += (long long)(j - i) * si;
+      F.xfer_total[t][1] += (long long)(j - i) * sg;
+      i = j;
+    }
+  }
+  F.xfer_order_off[p.n_trees] = (long long)all.size();
+  if (cudaMallocAsync((void**)&F.d_stage_slots, sizeof(int) * std::max<size_t>(1, all.size()), F.stream) !=
+      cudaSuccess)
+    return err = "staging allocation failed", AFV_ERR_NOMEM;
+  cudaMemcpyAsync(F.d_stage_slots, all.data(), sizeof(int) * all.size(), cudaMemcpyHostToDevice, F.stream);
+  if (cudaStreamSynchronize(F.stream) != cudaSuccess) return F.check(err, "host exchange");
+  F.xfer_ready = true;
+  return AFV_OK;
+}
+
 static int exchange(Forest& F, int t, int var, double* host, int interior_only, bool to_dev,
                     std::string& err) {
   const Plan& p = F.plan;
   if (t < 0 || t >= p.n_trees) return err = "tree index out of range", AFV_ERR_INVALID;
   if (var < AFV_PHI || var > AFV_TMP) return err = "unknown variable", AFV_ERR_INVALID;
-  const std::vector<int>& order = p.host_order[t];
+  if (int rc = exchange_plan(F, err)) return rc;
   const int D = p.dim;
-  // sizes per box follow the level of each slot
-  long long total = 0;
-  for (int s : order) {
-    int nc = p.nc_at(p.lvl[s]);
-    total += interior_only ? (long long)std::pow(nc, D) : (long long)std::pow(nc + 2, D);
-  }
+  const long long total = F.xfer_total[t][interior_only ? 0 : 1];
   if (F.stage_elems < total || !F.d_stage) {
     if (F.d_stage) cudaFreeAsync(F.d_stage, F.stream);
-    if (F.d_stage_slots) cudaFreeAsync(F.d_stage_slots, F.stream);
     F.d_stage = nullptr;
-    F.d_stage_slots = nullptr;
     if (cudaMallocAsync((void**)&F.d_stage, sizeof(double) * std::max(1LL, total), F.stream) != cudaSuccess)
       return err = "staging allocation failed", AFV_ERR_NOMEM;
     F.stage_elems = total;
   }
-  if (!F.d_stage_slots) {
-    size_t maxn = 0;
-    for (const auto& o : p.host_order) maxn = std::max(maxn, o.size());
-    if (cudaMallocAsync((void**)&F.d_stage_slots, sizeof(int) * std::max<size_t>(1, maxn), F.stream) != cudaSuccess)
-      return err = "staging allocation failed", AFV_ERR_NOMEM;
-  }
   cudaStream_t st = F.stream;
-  cudaMemcpyAsync(F.d_stage_slots, order.data(), sizeof(int) * order.size(), cudaMemcpyHostToDevice, st);
+  const int* slots = F.d_stage_slots + F.xfer_order_off[t];
   if (to_dev)
     cudaMemcpyAsync(F.d_stage, host, sizeof(double) * total, cudaMemcpyHostToDevice, st);
   Meta m = meta_of(F.meta);
   bool ghosted = var != AFV_RHS;
   double* dvar = var == AFV_PHI ? F.d64.phi : var == AFV_RHS ? F.d64.rhs : F.d64.tmp;
-  // runs of consecutive boxes with the same level
-  size_t i = 0;
   long long off = 0;
-  while (i < order.size()) {
-    int l = p.lvl[order[i]];
-    size_t j = i;
-    while (j < order.size() && p.lvl[order[j]] == l) ++j;
-    int n = (int)(j - i);
-    int nc = p.nc_at(l);
-    long long per = interior_only ? (long long)std::pow(nc, D) : (long long)std::pow(nc + 2, D);
+  for (const Forest::XferRun& r : F.xfer_runs[t]) {
+    const int nc = p.nc_at(r.lvl);
+    long long per = 1;
+    for (int d = 0; d < D; ++d) per *= interior_only ? nc : nc + 2;
+    const int n = r.n;
     with_nc(D, nc, [&](auto d_, auto nc_) {
       constexpr int DD = decltype(d_)::value, NC = decltype(nc_)::value;
       int grid = grid_for((n * per + 255) / 256, F.n_sm);
       ProfScope ps(&F, kProfOther, 16.0 * n * per);
       if (to_dev)
-        launch_k(dev::k_scatter<DD, NC, double>, grid, 256, 0, st, m, F.d_stage_slots + i, n, F.d_stage + off,
-                                                            dvar, interior_only, ghosted);
+        launch_k(dev::k_scatter<DD, NC, double>, grid, 256, 0, st, m, slots + r.first, n, F.d_stage + off, dvar,
+                 interior_only, ghosted);
       else
-        launch_k(dev::k_gather<DD, NC, double>, grid, 256, 0, st, m, F.d_stage_slots + i, n, dvar,
-                                                           F.d_stage + off, interior_only, ghosted);
+        launch_k(dev::k_gather<DD, NC, double>, grid, 256, 0, st, m, slots + r.first, n, dvar, F.d_stage + off,
+                 interior_only, ghosted);
     });
     off += n * per;
-    i = j;
   }
   if (!to_dev) cudaMemcpyAsync(host, F.d_stage, sizeof(double) * total, cudaMemcpyDeviceToHost, st);
   if (cudaStreamSynchronize(st) != cudaSuccess) return F.check(err, "host exchange");
