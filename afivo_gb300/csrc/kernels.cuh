@@ -618,7 +618,9 @@ template <int D, int NC, class T, int W, int S, int ASYNC>
 __global__ void __launch_bounds__(W * 32)
 k_sweep_warp(Meta m, BoxSet bs, T* __restrict__ phi, const T* __restrict__ rhs, int n, int pull,
              int homog) {
-  pdl_wait();
+  // Everything up to the first data-dependent load runs before pdl_wait():
+  // barrier set-up, per-lane constants and the first descriptors (the slot
+  // tables and descriptors never change after the forest is created).
   pdl_trigger();
   using C = WarpCfg<D, NC, T, W, S>;
   using G = Geo<D, NC>;
@@ -628,7 +630,10 @@ k_sweep_warp(Meta m, BoxSet bs, T* __restrict__ phi, const T* __restrict__ rhs, 
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int gw = (int)blockIdx.x * W + wid, nw = (int)gridDim.x * W;
   const int nbx = bs.n;
-  if (gw >= nbx) return;
+  if (gw >= nbx) {
+    pdl_wait();
+    return;
+  }
   const int my_boxes = (nbx - 1 - gw) / nw + 1;
   unsigned char* ring = smem + (size_t)wid * S * C::BOX_B;
   if (lane == 0) {
@@ -827,6 +832,10 @@ k_sweep_warp(Meta m, BoxSet bs, T* __restrict__ phi, const T* __restrict__ rhs, 
     return true;
   };
 
+  const unsigned w0 = desc_words(0), w1 = desc_words(1);
+  // Descriptor words of boxes k+2 and k+3 at the start of box k.
+  unsigned wq = desc_words(2), wr = desc_words(3);
+  pdl_wait();  // the previous kernel's writes to phi are visible from here on
   if constexpr (ASYNC) {
     for (int k = 0; k < S - 1; ++k) {
       if (k < my_boxes) issue(k);
@@ -839,13 +848,8 @@ k_sweep_warp(Meta m, BoxSet bs, T* __restrict__ phi, const T* __restrict__ rhs, 
   T ga[C::GPL], gb[C::GPL], gc[C::GPL];
   T ra[C::CPL], rb[C::CPL], rc[C::CPL];
   int aa = 0, ab = 0, ac = 0;
-  {
-    const unsigned w0 = desc_words(0), w1 = desc_words(1);
-    fetch(0, w0, true, ga, ra, aa);
-    fetch(1, w1, 1 < my_boxes, gb, rb, ab);
-  }
-  // Descriptor words of boxes k+2 and k+3 at the start of box k.
-  unsigned wq = desc_words(2), wr = desc_words(3);
+  fetch(0, w0, true, ga, ra, aa);
+  fetch(1, w1, 1 < my_boxes, gb, rb, ab);
   int k = 0;
   bool ok = true;
   for (; k < my_boxes; k += 3) {
@@ -906,7 +910,8 @@ template <int D, int NC, class T, int W, int S>
 __global__ void __launch_bounds__(W * 32)
 k_restrict_warp(Meta m, BoxSet bs, T* __restrict__ phi, const T* __restrict__ rhs, T* __restrict__ tmp,
                 int homog) {
-  pdl_wait();
+  // Descriptors never change after the forest is created: those of the
+  // first boxes are loaded before pdl_wait(), the cells after it.
   pdl_trigger();
   using C = RestrictCfg<D, NC, T, W, S>;
   using G = Geo<D, NC>;
@@ -916,7 +921,10 @@ k_restrict_warp(Meta m, BoxSet bs, T* __restrict__ phi, const T* __restrict__ rh
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int gw = (int)blockIdx.x * W + wid, nw = (int)gridDim.x * W;
   const int nbx = bs.n;
-  if (gw >= nbx) return;
+  if (gw >= nbx) {
+    pdl_wait();
+    return;
+  }
   const int my_boxes = (nbx - 1 - gw) / nw + 1;
   unsigned char* ring = smem + (size_t)wid * S * C::BOX_B;
   if (lane == 0) {
@@ -936,6 +944,16 @@ k_restrict_warp(Meta m, BoxSet bs, T* __restrict__ phi, const T* __restrict__ rh
     fence_proxy_async();
     mbar_expect_tx(b, (unsigned)C::BOX_B);
     bulk_g2s(sp, m.desc + s, (unsigned)sizeof(SlotDesc), b);
+    bulk_g2s(sp + C::PHI_OFF, phi + box_offg<G::SG>(m, bs, i, s), (unsigned)(G::SG * sizeof(T)), b);
+  };
+  auto issue_data = [&](int k) {  // lane 0: the cells only (descriptor staged)
+    ++issued;
+    const int i = gw + k * nw;
+    const int s = box_at(bs, i);
+    unsigned char* sp = stage(k);
+    unsigned long long* b = &bar[wid][k % S];
+    fence_proxy_async();
+    mbar_expect_tx(b, (unsigned)(C::BOX_B - (int)sizeof(SlotDesc)));
     bulk_g2s(sp + C::PHI_OFF, phi + box_offg<G::SG>(m, bs, i, s), (unsigned)(G::SG * sizeof(T)), b);
   };
   // Item j of this lane: face f and face cell (a, c).
@@ -1050,14 +1068,19 @@ k_restrict_warp(Meta m, BoxSet bs, T* __restrict__ phi, const T* __restrict__ rh
   };
 
   const int ahead = min(S - 1, my_boxes);
+  for (int k = 0; k < ahead; ++k)
+    reinterpret_cast<unsigned*>(stage(k))[lane] =
+        reinterpret_cast<const unsigned*>(m.desc + box_at(bs, gw + k * nw))[lane];
+  __syncwarp();
+  pdl_wait();  // the previous kernel's writes are visible from here on
   if (lane == 0)
-    for (int k = 0; k < ahead; ++k) issue(k);
+    for (int k = 0; k < ahead; ++k) issue_data(k);
   T ga[C::GPL], gb[C::GPL];
   T ra[C::PPL][C::FINE], rb[C::PPL][C::FINE];
   long long pa = 0, pb = 0;
   int aa = 0, ab = 0;
+  fetch(0, ga, ra, pa, aa);  // from the staged descriptor, beside the cells' copy
   bool ok = mbar_wait_bounded(&bar[wid][0], 0);
-  if (ok) fetch(0, ga, ra, pa, aa);
   int k = 0, pending = 0;
   if (__all_sync(0xffffffffu, ok)) {
     for (; k < my_boxes; k += 2) {
@@ -1098,7 +1121,8 @@ struct CoarseCfg {
 template <int D, int NC, class T, int W, int S>
 __global__ void __launch_bounds__(W * 32)
 k_coarse_warp(Meta m, BoxSet bs, T* __restrict__ phi, T* __restrict__ rhs, T* __restrict__ tmp, int homog) {
-  pdl_wait();
+  // Descriptors never change after the forest is created: those of the
+  // first boxes are loaded before pdl_wait(), the cells after it.
   pdl_trigger();
   using C = CoarseCfg<D, NC, T, W, S>;
   using G = Geo<D, NC>;
@@ -1107,7 +1131,10 @@ k_coarse_warp(Meta m, BoxSet bs, T* __restrict__ phi, T* __restrict__ rhs, T* __
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int gw = (int)blockIdx.x * W + wid, nw = (int)gridDim.x * W;
   const int nbx = bs.n;
-  if (gw >= nbx) return;
+  if (gw >= nbx) {
+    pdl_wait();
+    return;
+  }
   const int my_boxes = (nbx - 1 - gw) / nw + 1;
   unsigned char* ring = smem + (size_t)wid * S * C::BOX_B;
   if (lane == 0) {
@@ -1127,6 +1154,16 @@ k_coarse_warp(Meta m, BoxSet bs, T* __restrict__ phi, T* __restrict__ rhs, T* __
     fence_proxy_async();
     mbar_expect_tx(b, (unsigned)C::BOX_B);
     bulk_g2s(sp, m.desc + s, (unsigned)sizeof(SlotDesc), b);
+    bulk_g2s(sp + C::PHI_OFF, phi + box_offg<G::SG>(m, bs, i, s), (unsigned)(G::SG * sizeof(T)), b);
+  };
+  auto issue_data = [&](int k) {  // lane 0: the cells only (descriptor staged)
+    ++issued;
+    const int i = gw + k * nw;
+    const int s = box_at(bs, i);
+    unsigned char* sp = stage(k);
+    unsigned long long* b = &bar[wid][k % S];
+    fence_proxy_async();
+    mbar_expect_tx(b, (unsigned)(C::BOX_B - (int)sizeof(SlotDesc)));
     bulk_g2s(sp + C::PHI_OFF, phi + box_offg<G::SG>(m, bs, i, s), (unsigned)(G::SG * sizeof(T)), b);
   };
   auto item = [&](int j, int& f, int& a, int& c) {
@@ -1217,12 +1254,17 @@ k_coarse_warp(Meta m, BoxSet bs, T* __restrict__ phi, T* __restrict__ rhs, T* __
   };
 
   const int ahead = min(S - 1, my_boxes);
+  for (int k = 0; k < ahead; ++k)
+    reinterpret_cast<unsigned*>(stage(k))[lane] =
+        reinterpret_cast<const unsigned*>(m.desc + box_at(bs, gw + k * nw))[lane];
+  __syncwarp();
+  pdl_wait();  // the previous kernel's writes are visible from here on
   if (lane == 0)
-    for (int k = 0; k < ahead; ++k) issue(k);
+    for (int k = 0; k < ahead; ++k) issue_data(k);
   T ga[C::GPL], gb[C::GPL], ta[C::CPL], tb[C::CPL];
   int aa = 0, ab = 0;
+  fetch(0, ga, ta, aa);  // from the staged descriptor, beside the cells' copy
   bool ok = mbar_wait_bounded(&bar[wid][0], 0);
-  if (ok) fetch(0, ga, ta, aa);
   int k = 0, pending = 0;
   if (__all_sync(0xffffffffu, ok)) {
     for (; k < my_boxes; k += 2) {
@@ -1275,7 +1317,8 @@ struct CorrectCfg {
 template <int D, int NC, class T, int W, int S>
 __global__ void __launch_bounds__(W * 32)
 k_correct_warp(Meta m, BoxSet bs, T* __restrict__ phi, T* __restrict__ tmp, int pull, int homog) {
-  pdl_wait();
+  // Descriptors never change after the forest is created: those of the
+  // first boxes are loaded before pdl_wait(), the cells after it.
   pdl_trigger();
   using C = CorrectCfg<D, NC, T, W, S>;
   using G = Geo<D, NC>;
@@ -1287,7 +1330,10 @@ k_correct_warp(Meta m, BoxSet bs, T* __restrict__ phi, T* __restrict__ tmp, int 
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int gw = (int)blockIdx.x * W + wid, nw = (int)gridDim.x * W;
   const int nbx = bs.n;
-  if (gw >= nbx) return;
+  if (gw >= nbx) {
+    pdl_wait();
+    return;
+  }
   const int my_boxes = (nbx - 1 - gw) / nw + 1;
   unsigned char* ring = smem + (size_t)wid * S * C::BOX_B;
   if (lane == 0) {
@@ -1308,6 +1354,18 @@ k_correct_warp(Meta m, BoxSet bs, T* __restrict__ phi, T* __restrict__ tmp, int 
     fence_proxy_async();
     mbar_expect_tx(b, (unsigned)C::BOX_B);
     bulk_g2s(sp, m.desc + s, (unsigned)sizeof(SlotDesc), b);
+    bulk_g2s(sp + C::PHI_OFF, phi + o, (unsigned)(G::SG * sizeof(T)), b);
+    bulk_g2s(sp + C::TMP_OFF, tmp + o, (unsigned)(G::SG * sizeof(T)), b);
+  };
+  auto issue_data = [&](int k) {  // lane 0: the cells only (descriptor staged)
+    ++issued;
+    const int i = gw + k * nw;
+    const int s = box_at(bs, i);
+    const long long o = box_offg<G::SG>(m, bs, i, s);
+    unsigned char* sp = stage(k);
+    unsigned long long* b = &bar[wid][k % S];
+    fence_proxy_async();
+    mbar_expect_tx(b, (unsigned)(C::BOX_B - (int)sizeof(SlotDesc)));
     bulk_g2s(sp + C::PHI_OFF, phi + o, (unsigned)(G::SG * sizeof(T)), b);
     bulk_g2s(sp + C::TMP_OFF, tmp + o, (unsigned)(G::SG * sizeof(T)), b);
   };
@@ -1465,13 +1523,18 @@ k_correct_warp(Meta m, BoxSet bs, T* __restrict__ phi, T* __restrict__ tmp, int 
   };
 
   const int ahead = min(S - 1, my_boxes);
+  for (int k = 0; k < ahead; ++k)
+    reinterpret_cast<unsigned*>(stage(k))[lane] =
+        reinterpret_cast<const unsigned*>(m.desc + box_at(bs, gw + k * nw))[lane];
+  __syncwarp();
+  pdl_wait();  // the previous kernel's writes are visible from here on
   if (lane == 0)
-    for (int k = 0; k < ahead; ++k) issue(k);
+    for (int k = 0; k < ahead; ++k) issue_data(k);
   T ga[C::GPL], gb[C::GPL];
   long long oa = 0, ob = 0;
   int aa = 0, ab = 0;
+  fetch(0, ga, oa, aa);  // from the staged descriptor, beside the cells' copy
   bool ok = mbar_wait_bounded(&bar[wid][0], 0);
-  if (ok) fetch(0, ga, oa, aa);
   int k = 0, pending = 0;
   if (__all_sync(0xffffffffu, ok)) {
     for (; k < my_boxes; k += 2) {
@@ -1506,7 +1569,6 @@ template <int D, int NC, class T>
 __global__ void __launch_bounds__(kSmallThreads)
 k_sweep_small(Meta m, BoxSet bs, T* __restrict__ phi, const T* __restrict__ rhs, int n_first, int n_count,
               int pull_first, int homog) {
-  pdl_wait();
   pdl_trigger();
   using G = Geo<D, NC>;
   constexpr int ITEMS = G::NNB * G::NF;  // face cells of a box
@@ -1523,6 +1585,7 @@ k_sweep_small(Meta m, BoxSet bs, T* __restrict__ phi, const T* __restrict__ rhs,
     unsigned* dst = reinterpret_cast<unsigned*>(sd);
     for (int e = threadIdx.x; e < nb * (int)(sizeof(SlotDesc) / 4); e += blockDim.x) dst[e] = src[e];
   }
+  pdl_wait();  // descriptors never change; phi, rhs and the flags may have been written by the previous kernel
   for (int e = threadIdx.x; e < nb * G::SG; e += blockDim.x) sb[e] = phi[bs.g0 + e];
   for (int e = threadIdx.x; e < nb * G::SI; e += blockDim.x) sr[e] = rhs[bs.i0 + e];
   for (int b = threadIdx.x; b < nb; b += blockDim.x) sa[b] = m.active[m.tree[bs.lo + b]];
@@ -2339,8 +2402,7 @@ template <int D, int NC>
 __global__ void __launch_bounds__(256)
 k_defect_fx(Meta m, BoxSet bs, const double* __restrict__ u, const double* __restrict__ f,
             float* __restrict__ r32, unsigned long long* __restrict__ norm_per_tree) {
-  pdl_wait();
-  pdl_trigger();
+  pdl_trigger();  // the first descriptors are copied before pdl_wait() (they never change)
   using C = DefectFxCfg<D, NC>;
   using G = Geo<D, NC>;
   static_assert(C::OK, "k_defect_fx block shape");
@@ -2351,7 +2413,10 @@ k_defect_fx(Meta m, BoxSet bs, const double* __restrict__ u, const double* __res
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int first = blockIdx.x, step = gridDim.x;
   const int my = first < bs.n ? (bs.n - 1 - first) / step + 1 : 0;
-  if (my == 0) return;
+  if (my == 0) {
+    pdl_wait();
+    return;
+  }
   unsigned rmask = 0;  // ghosted cells tid + T j that the stencil reads
 #pragma unroll
   for (int j = 0; j < C::SPT; ++j) {
@@ -2413,14 +2478,15 @@ k_defect_fx(Meta m, BoxSet bs, const double* __restrict__ u, const double* __res
   // prologue: descriptor of leaf 0, then its u and the descriptor of leaf 1
   int s_cur = slot_of(0);
   copy_desc(0, s_cur);
-  cp_async_commit();
-  cp_async_wait<0>();
-  __syncthreads();
-  copy_box(0);
   int s_next = my > 1 ? slot_of(1) : -1;
   if (my > 1) copy_desc(1, s_next);
   cp_async_commit();
   int s_after = my > 2 ? slot_of(2) : -1;
+  cp_async_wait<0>();
+  __syncthreads();
+  pdl_wait();  // u and the flags may have been written by the previous kernel
+  copy_box(0);
+  cp_async_commit();
   double gc[C::IPT], gn[C::IPT], fcv[C::CPT], fnv[C::CPT];
   fetch(0, s_cur, gc, fcv);
   int tree_prev = -1;  // tree of the previous leaf if it was active (thread 0)
