@@ -41,9 +41,9 @@ AFV_BC_DIRICHLET, AFV_BC_NEUMANN = -1, -2
 AFV_REF_UNIFORM, AFV_REF_SOURCE, AFV_REF_RANDOM, AFV_REF_RANDOM_RM = 0, 1, 2, 3
 AFV_PREC_FP64, AFV_PREC_MIXED = 0, 1
 AFV_OPT_SWEEP_KERNEL, AFV_OPT_GRAPHS, AFV_OPT_RESTRICT_KERNEL, AFV_OPT_SMALL_SWEEPS = 0, 1, 2, 3
-AFV_OPT_PROFILE_LEAD_US, AFV_OPT_DEFECT_KERNEL = 4, 5
+AFV_OPT_PROFILE_LEAD_US, AFV_OPT_DEFECT_KERNEL, AFV_OPT_COARSE_END = 4, 5, 6
 KERNEL_KINDS = ("sweep", "fill", "restrict", "coarse_rhs", "correct", "residual", "defect",
-                "accumulate")
+                "accumulate", "coarse_end")
 
 # Refinement flags under the reference's names (src/m_aX_t.f90:17-24)
 a5_rm_ref, a5_keep_ref, a5_do_ref = AFV_RM_REF, AFV_KEEP_REF, AFV_DO_REF

@@ -442,6 +442,10 @@ int afv_forest_set_option(afv_forest* f, int option, int value) {
       f->f.defect_fx = value != 0;
       f->f.drop_graphs();
       return AFV_OK;
+    case AFV_OPT_COARSE_END:
+      f->f.use_coarse_end = value != 0;
+      f->f.drop_graphs();
+      return AFV_OK;
   }
   return fail(AFV_ERR_INVALID, "unknown option");
 }
@@ -455,6 +459,7 @@ int afv_forest_get_option(afv_forest* f, int option, int* value) {
     case AFV_OPT_SMALL_SWEEPS: *value = f->f.use_small_sweeps ? 1 : 0; return AFV_OK;
     case AFV_OPT_PROFILE_LEAD_US: *value = f->f.prof_lead_us; return AFV_OK;
     case AFV_OPT_DEFECT_KERNEL: *value = f->f.defect_fx ? 1 : 0; return AFV_OK;
+    case AFV_OPT_COARSE_END: *value = f->f.use_coarse_end ? 1 : 0; return AFV_OK;
   }
   return fail(AFV_ERR_INVALID, "unknown option");
 }

@@ -52,6 +52,7 @@ enum ProfKind {
   kProfResidual,
   kProfDefect,
   kProfAccumulate,
+  kProfCoarseEnd,
   kProfOther,
   kProfKinds
 };
@@ -78,10 +79,14 @@ class Forest {
   int sweep_kernel = 1;  // 0: block-pipelined k_level_tma, 1: warp-per-box k_sweep_warp, 2: its async variant
   bool use_restrict_warp = true;  // warp-per-box restriction on levels >= 2
   bool defect_fx = true;          // mixed defect: fixed-point Laplacian (false: FP64 sum)
+  bool use_coarse_end = true;     // correction cycle's levels l0..1 in one launch (k_coarse_end)
+  int coarse_end_levels = -1;     // levels k_coarse_end covers (0: not eligible; -1: not yet known)
+  int coarse_end_depth(int highest);
+  void coarse_end(const Arrays<float>& a, const MgOpts& mg, int nl);
   // All half-sweeps of a level in one block (k_sweep_small) when the level has
   // at most kSmallCells interior cells: measured faster than one launch per
-  // half-sweep for 512 cells (8.4 us for four half-sweeps against 14 us),
-  // slower for 4096 (22.7 us against 17.6 us).
+  // half-sweep for 512 cells (8.5 us for four half-sweeps against 14 us),
+  // slower for 4096 (19.8 us against 16.3 us).
   bool use_small_sweeps = true;
   static constexpr long long kSmallCells = 2048;
   static constexpr long long kSmallSmemBytes = 200 * 1024;

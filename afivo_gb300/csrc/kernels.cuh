@@ -1579,6 +1579,7 @@ k_sweep_small(Meta m, BoxSet bs, T* __restrict__ phi, const T* __restrict__ rhs,
   T* sr = sb + (size_t)nb * G::SG;                                     // nb rhs interiors
   T* sc = sr + (size_t)nb * G::SI;                                     // per face cell: coarse value or boundary value
   int* sa = reinterpret_cast<int*>(sc + (size_t)nb * ITEMS);           // nb activity flags
+  int* snb = sa + nb;  // per box and face: the same-level neighbour's index in the level, or -1
   constexpr int OX = 1, OY = G::NG, OZ = G::NG * G::NG;
   {
     const unsigned* src = reinterpret_cast<const unsigned*>(m.desc + bs.lo);
@@ -1590,6 +1591,11 @@ k_sweep_small(Meta m, BoxSet bs, T* __restrict__ phi, const T* __restrict__ rhs,
   for (int e = threadIdx.x; e < nb * G::SI; e += blockDim.x) sr[e] = rhs[bs.i0 + e];
   for (int b = threadIdx.x; b < nb; b += blockDim.x) sa[b] = m.active[m.tree[bs.lo + b]];
   __syncthreads();
+  for (int e = threadIdx.x; e < nb * G::NNB; e += blockDim.x) {
+    const SlotDesc& d = sd[e / G::NNB];
+    const int f = e % G::NNB;
+    snb[e] = d.code[f] >= 0 ? (int)((d.nbo[f] - bs.g0) / G::SG) : -1;  // the neighbour is on this level
+  }
   // The sources of the ghost cells that do not change while the level is
   // smoothed: the parent's injected cell at refinement boundaries, the
   // boundary value at physical faces.
@@ -1612,25 +1618,28 @@ k_sweep_small(Meta m, BoxSet bs, T* __restrict__ phi, const T* __restrict__ rhs,
   for (int h = 0; h < n_count; ++h) {
     const int nsw = n_first + h;
     if (h > 0 || pull_first) {
-      for (int e = threadIdx.x; e < nb * ITEMS; e += blockDim.x) {
-        const int b = e / ITEMS, r = e % ITEMS;
+      // only the ghost cells this colour reads: NF / 2 per face
+      constexpr int HF = G::NF / 2;
+      for (int e = threadIdx.x; e < nb * G::NNB * HF; e += blockDim.x) {
+        const int pair = e / HF, mcell = e % HF;
+        const int b = pair / G::NNB, f = pair % G::NNB;
         if (!sa[b]) continue;
-        const int f = r / G::NF, lin = r % G::NF;
-        const int a = lin % NC + 1, c = lin / NC + 1;
+        int a, c;
+        needed_face_cell<D, NC>(f, mcell, nsw, a, c);
+        const Face<D, NC> F(f, a, c);
         const SlotDesc& d = sd[b];
         T* bx = sb + (size_t)b * G::SG;
-        const Face<D, NC> F(f, a, c);
         const int code = d.code[f];
         T v;
         if (code >= 0) {
-          const long long nbi = (d.nbo[f] - bs.g0) / G::SG;  // the neighbour is on this level
-          v = sb[nbi * G::SG + G::g(F.ni, F.nj, F.nk)];
+          v = sb[(size_t)snb[pair] * G::SG + G::g(F.ni, F.nj, F.nk)];
         } else {
-          auto own = [&](int i, int j, int k) { return bx[G::g(i, j, k)]; };
+          const T src = sc[(size_t)b * ITEMS + f * G::NF + ((D == 2) ? (a - 1) : (a - 1) + NC * (c - 1))];
+          auto own = [&](int i, int j, int kk) { return bx[G::g(i, j, kk)]; };
           if (code == kFaceRefinement)
-            v = rb_value<D, NC, T>(F, f, sc[e], own);
+            v = rb_value<D, NC, T>(F, f, src, own);
           else
-            v = bc_value<T>(code, f, sc[e], own(F.ai, F.aj, F.ak), Sc<T>::dr(d));
+            v = bc_value<T>(code, f, src, own(F.ai, F.aj, F.ak), Sc<T>::dr(d));
         }
         bx[G::g(F.gi, F.gj, F.gk)] = v;
       }

@@ -10,6 +10,7 @@
 
 #include "forest.hpp"
 #include "kernels.cuh"
+#include "coarse_end.cuh"
 
 namespace afv {
 
@@ -622,7 +623,8 @@ bool Forest::sweeps_small(const Arrays<T>& a, int lvl, int n_first, int n_count,
   with_nc(plan.dim, plan.nc_at(lvl), [&](auto d_, auto nc_) {
     constexpr int D = decltype(d_)::value, NC = decltype(nc_)::value;
     using G = dev::Geo<D, NC>;
-    const size_t smem = (size_t)nbx * (sizeof(SlotDesc) + (G::SG + G::SI + G::NNB * G::NF) * sizeof(T) + 4);
+    const size_t smem = (size_t)nbx * (sizeof(SlotDesc) + (G::SG + G::SI + G::NNB * G::NF) * sizeof(T) + 4 +
+                                       4 * G::NNB);
     if (smem > (size_t)kSmallSmemBytes || (long long)nbx * G::SI > kSmallCells) return;
     kernel_occupancy((const void*)dev::k_sweep_small<D, NC, T>, dev::kSmallThreads, (int)kSmallSmemBytes);
     prof_level = lvl;
@@ -816,6 +818,57 @@ void Forest::update_coarse_t(const Arrays<T>& a, int lvl, bool homog, bool copy_
 // first half-sweep on the top level reads stored ghosts (valid on input), and
 // every level ends the cycle with a stored ghost fill (valid on output).
 // base64: smooth the coarsest level in FP64 (mixed cycle).
+// Launches k_coarse_end: one block per tree over the nl levels 1 .. 2 - nl.
+void Forest::coarse_end(const Arrays<float>& a, const MgOpts& mg, int nl) {
+  prof_level = 1;
+  dev::CeSlots sl{};
+  for (int L = 0; L < nl; ++L) sl.lo[L] = plan.lvl_lo[plan.L(1 - L)];
+  Meta m = meta_of(meta);
+  with_nc(plan.dim, plan.nc, [&](auto d_, auto nc_) {
+    constexpr int D = decltype(d_)::value, NC = decltype(nc_)::value;
+    using G = dev::Geo<D, NC>;
+    ProfScope ps(this, kProfCoarseEnd, 4.0 * (G::SG + 2 * G::SI) * plan.n_trees);
+    auto go = [&](auto nl_) {
+      constexpr int NL = decltype(nl_)::value;
+      if constexpr ((NC >> (NL - 1)) >= 2)
+        launch_k(dev::k_coarse_end<D, NC, NL>, plan.n_trees, dev::kCoarseEndThreads, 0, stream, m, sl, a.phi,
+                 (const float*)a.rhs, mg.n_down, mg.n_up, mg.n_base);
+    };
+    switch (nl) {
+      case 1: go(IC<1>{}); break;
+      case 2: go(IC<2>{}); break;
+      case 3: go(IC<3>{}); break;
+      default: go(IC<4>{}); break;
+    }
+  });
+}
+
+// Levels l0..1 run by k_coarse_end (0: not eligible): every tree has one box
+// on each of them, in tree order, with no refinement boundary and periodic
+// faces only onto the box itself; at most four levels, each with at least 2
+// cells per side.
+int Forest::coarse_end_depth(int highest) {
+  if (!use_coarse_end || highest < 2 || plan.min_lvl > 1) return 0;
+  if (coarse_end_levels >= 0) return coarse_end_levels;
+  const Plan& p = plan;
+  const int nl = 2 - p.min_lvl;
+  int ok = nl <= dev::kCoarseEndMaxLevels && (p.nc >> (nl - 1)) >= 2;
+  const int NNB = 2 * p.dim;
+  for (int l = p.min_lvl; ok && l <= 1; ++l) {
+    if (p.lvl_n[p.L(l)] != p.n_trees || p.nc_at(l) != (p.nc >> (1 - l))) ok = 0;
+    for (int t = 0; ok && t < p.n_trees; ++t) {
+      const int sl = p.lvl_lo[p.L(l)] + t;
+      if (p.tree[sl] != t) ok = 0;
+      for (int f = 0; ok && f < NNB; ++f) {
+        const SlotDesc& d = p.desc[sl];
+        if (d.code[f] == kFaceRefinement || (d.code[f] >= 0 && d.nbo[f] != p.offg[sl])) ok = 0;
+      }
+    }
+  }
+  coarse_end_levels = ok ? nl : 0;
+  return coarse_end_levels;
+}
+
 template <class T>
 void Forest::vcycle_t(const Arrays<T>& a, const MgOpts& mg, int highest, bool homog, bool base64,
                       bool inner) {
@@ -826,12 +879,17 @@ void Forest::vcycle_t(const Arrays<T>& a, const MgOpts& mg, int highest, bool ho
     if (sweeps_small(arr, l, 1, 2 * n_cycle, l != highest, homog)) return;
     for (int n = 1; n <= 2 * n_cycle; ++n) sweep(arr, l, n, n > 1 || l != highest, homog);
   };
-  for (int l = highest; l >= l0 + 1; --l) {
+  // The correction cycle's coarse end (levels l0..1) in one launch.
+  const int ce = (std::is_same<T, float>::value && inner && homog && base64) ? coarse_end_depth(highest) : 0;
+  const int l_low = ce ? 2 : l0 + 1;
+  for (int l = highest; l >= l_low; --l) {
     sweeps(a, l, mg.n_down);
     restrict_res(a, l, true, true, homog);
     coarse_rhs(a, l - 1, true, true, homog);
   }
-  if (base64 && !std::is_same<T, double>::value) {
+  if (ce) {
+    if constexpr (std::is_same<T, float>::value) coarse_end(a, mg, ce);
+  } else if (base64 && !std::is_same<T, double>::value) {
     long long ng = 0, ni = 0;
     int nb0 = lvl_n(l0);
     ng = (long long)nb0 * (long long)std::pow(plan.nc_at(l0) + 2, plan.dim);
@@ -858,7 +916,7 @@ void Forest::vcycle_t(const Arrays<T>& a, const MgOpts& mg, int highest, bool ho
     sweeps(a, l0, mg.n_base);
     fill(a, l0, homog);
   }
-  for (int l = l0 + 1; l <= highest; ++l) {
+  for (int l = l_low; l <= highest; ++l) {
     // Inner correction cycle of the mixed path: its result is read only on
     // interiors, and its ghost cells only on parents (by the correction of
     // their children and by the children's refinement-boundary ghosts), so

@@ -347,7 +347,7 @@ def run_uniform(afv, W, local, rank, world):
         ms = e0.elapsed_time(e1)
         out[name] = {"fmg_then_cycles": cyc, "rel_res": rel, "status": rc, "ms": round(ms, 3),
                      "unknowns_per_s": info["leaf_cells"] * (cyc + 1) / (ms / 1e3)}
-    forest.profile(0xFF)
+    forest.profile((1 << len(afv.KERNEL_KINDS)) - 1)
     forest.zero(afv.AFV_PHI)
     forest.solve(afv.AFV_PREC_MIXED, tol=TOL, max_cycles=60, check=False)
     kern = {}
@@ -505,7 +505,7 @@ def main():
                               "GB/s": round(a[2] / (a[1] / 1e3) / 1e9, 1)}
                     for lv, a in sorted(by_level.items())}
     # per-kernel breakdown: one mixed solve, every kind profiled
-    timed(afv.AFV_PREC_MIXED, 1, mask=0xFF)
+    timed(afv.AFV_PREC_MIXED, 1, mask=(1 << len(afv.KERNEL_KINDS)) - 1)
     breakdown = {}
     pe = forest.profile_entries()
     for k, name in enumerate(afv.KERNEL_KINDS):

@@ -243,7 +243,8 @@ enum {
   AFV_KERNEL_CORRECT = 4,   /* coarse correction with prolong2               */
   AFV_KERNEL_RESIDUAL = 5,
   AFV_KERNEL_DEFECT = 6,    /* FP64 defect of the mixed path                 */
-  AFV_KERNEL_ACCUMULATE = 7 /* FP64 accumulate of the FP32 correction        */
+  AFV_KERNEL_ACCUMULATE = 7, /* FP64 accumulate of the FP32 correction       */
+  AFV_KERNEL_COARSE_END = 8  /* correction cycle's levels <= 1, one launch    */
 };
 /* No counterpart in the reference (it has no GPU path): bracket every launch
  * of the kinds in mask (bit k = kind k) with CUDA events on the forest's
@@ -269,14 +270,18 @@ int afv_forest_profile_read(afv_forest* f, int kind, long long* launches, double
  * the host's launch rate. AFV_OPT_DEFECT_KERNEL: the mixed solve's FP64
  * defect r = f - L u computes the Laplacian in 64-bit fixed point per box
  * (1, default; exact sums, one FP64 multiply-add per cell) or as an FP64 sum
- * (0). AFV_OPT_SWEEP_KERNEL 3..5 are other warp and stage counts of 1. */
+ * (0). AFV_OPT_SWEEP_KERNEL 3..5 are other warp and stage counts of 1.
+ * AFV_OPT_COARSE_END: 1 (default) runs the mixed solve's correction cycle on
+ * levels <= 1 (one box per tree each) in one launch, one block per tree;
+ * 0 launches its operators one by one. */
 enum {
   AFV_OPT_SWEEP_KERNEL = 0,
   AFV_OPT_GRAPHS = 1,
   AFV_OPT_RESTRICT_KERNEL = 2,
   AFV_OPT_SMALL_SWEEPS = 3,
   AFV_OPT_PROFILE_LEAD_US = 4,
-  AFV_OPT_DEFECT_KERNEL = 5
+  AFV_OPT_DEFECT_KERNEL = 5,
+  AFV_OPT_COARSE_END = 6
 };
 int afv_forest_set_option(afv_forest* f, int option, int value);
 int afv_forest_get_option(afv_forest* f, int option, int* value);

@@ -395,3 +395,28 @@ def test_defect_nonfinite_reports_divergence(gpu):
         cyc, rel, rc = g.solve(gpu.AFV_PREC_MIXED, tol=1e-8, max_cycles=5, check=False)
         assert rc == gpu.AFV_ERR_DIVERGED
         g.close()
+
+
+@pytest.mark.parametrize("which", ["c1", "3d", "batch"])
+def test_coarse_end_agrees(gpu, which):
+    """The correction cycle's levels <= 1 in one launch (k_coarse_end, the
+    default) and as one launch per operator give the same bits: mixed solves
+    of a 2-D and a 3-D tree with coarsened levels, and of a forest of trees."""
+    if which == "batch":
+        specs = W.c4_random_2d(3, small=True)
+    else:
+        specs = [W.c1_poisson_2d() if which == "c1" else W.c2_poisson_3d(thr=3e-3, lvl_max=5)]
+    out = []
+    for opt in (1, 0):
+        g = gpu.Forest([W.build_tree(s) for s in specs], mixed=True)
+        for k, s in enumerate(specs):
+            g.set_source(k, s["gauss"], lpl=True)
+        g.set_option(gpu.AFV_OPT_COARSE_END, opt)
+        assert g.get_option(gpu.AFV_OPT_COARSE_END) == opt
+        cyc, rel, rc = g.solve(gpu.AFV_PREC_MIXED, tol=1e-8, max_cycles=60)
+        assert rc == 0 and max(rel) <= 1e-8
+        out.append((list(cyc), [g.get_var(k, gpu.AFV_PHI) for k in range(len(specs))]))
+        g.close()
+    assert out[0][0] == out[1][0]
+    for a, b in zip(out[0][1], out[1][1]):
+        assert np.array_equal(a, b)
