@@ -2271,9 +2271,9 @@ __device__ __forceinline__ long long to_fx(double v, int emax) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(v);
   const int E = (int)((b >> 52) & 0x7ff);
   if (E == 0) return 0;  // zero or subnormal (below 2^-1022)
-  const unsigned long long M = (b & 0xfffffffffffffull) | (1ull << 52);
-  const int sh = E - emax + 6;  // <= 6, so |X| < 2^59
-  const unsigned long long X = sh >= 0 ? (M << sh) : (sh > -64 ? (M >> -sh) : 0ull);
+  const unsigned long long M6 = ((b & 0xfffffffffffffull) | (1ull << 52)) << 6;  // < 2^59
+  const int dsh = emax - E;  // >= 0
+  const unsigned long long X = dsh < 64 ? (M6 >> dsh) : 0ull;
   return (b >> 63) ? -(long long)X : (long long)X;
 }
 // S * 2^(emax - 1081) as a double (|S| < 2^63; mantissa truncated).
@@ -2408,7 +2408,7 @@ struct DefectFxCfg {
 };
 
 template <int D, int NC>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 5)
 k_defect_fx(Meta m, BoxSet bs, const double* __restrict__ u, const double* __restrict__ f,
             float* __restrict__ r32, unsigned long long* __restrict__ norm_per_tree) {
   pdl_trigger();  // the first descriptors are copied before pdl_wait() (they never change)
@@ -2443,30 +2443,43 @@ k_defect_fx(Meta m, BoxSet bs, const double* __restrict__ u, const double* __res
     char* dst = reinterpret_cast<char*>(sb[k & 1]);
     for (int c = tid; c < C::CH; c += C::T) cp_async16(dst + 16 * c, src + 16 * c);
   };
-  auto item = [&](int j, int& fc, int& a, int& c) {
+  // This thread's face ghosts (fixed for every leaf): face (-1: none), ghost,
+  // neighbour's and adjacent cell positions, index in the face; and its cells.
+  int it_f[C::IPT], it_g[C::IPT], it_n[C::IPT], it_a[C::IPT], it_lin[C::IPT];
+#pragma unroll
+  for (int j = 0; j < C::IPT; ++j) {
     const int r = tid + C::T * j;
-    fc = r / G::NF;
-    const int lin = r % G::NF;
-    a = lin % NC + 1;
-    c = lin / NC + 1;
-  };
+    const int rr = r < C::NEED ? r : 0;
+    const int fc = rr / G::NF, lin = rr % G::NF;
+    const Face<D, NC> F(fc, lin % NC + 1, lin / NC + 1);
+    it_f[j] = r < C::NEED ? fc : -1;
+    it_g[j] = G::g(F.gi, F.gj, F.gk);
+    it_n[j] = G::g(F.ni, F.nj, F.nk);
+    it_a[j] = G::g(F.ai, F.aj, F.ak);
+    it_lin[j] = lin;
+  }
+  int cpos[C::CPT];
+#pragma unroll
+  for (int c = 0; c < C::CPT; ++c) {
+    const int q = tid + C::T * c;
+    cpos[c] = G::g(q % NC + 1, (q / NC) % NC + 1, (D == 3) ? q / (NC * NC) + 1 : 0);
+  }
   // Ghost sources and f of leaf k (its descriptor has landed) and its slot.
   auto fetch = [&](int k, int s, double (&gv)[C::IPT], double (&fv)[C::CPT]) {
     const SlotDesc& d = sd[k % 3];
 #pragma unroll
     for (int j = 0; j < C::IPT; ++j) {
       gv[j] = 0.0;
-      if (tid + C::T * j >= C::NEED) continue;
-      int fc, a, c;
-      item(j, fc, a, c);
-      const Face<D, NC> F(fc, a, c);
+      const int fc = it_f[j];
+      if (fc < 0) continue;
       const int code = d.code[fc];
       if (code >= 0) {
-        gv[j] = u[d.nbo[fc] + G::g(F.ni, F.nj, F.nk)];
+        gv[j] = u[d.nbo[fc] + it_n[j]];
       } else if (code == kFaceRefinement) {
+        const Face<D, NC> F(fc, it_lin[j] % NC + 1, it_lin[j] / NC + 1);
         gv[j] = u[m.nbo2[(size_t)s * G::NNB + fc] + parent_cell<D, NC>(F, fc, d.qd, true)];
       } else if (d.nbo[fc] >= 0) {
-        gv[j] = m.bcval[d.nbo[fc] + ((D == 2) ? (a - 1) : (a - 1) + NC * (c - 1))];
+        gv[j] = m.bcval[d.nbo[fc] + it_lin[j]];
       }
     }
 #pragma unroll
@@ -2517,20 +2530,18 @@ k_defect_fx(Meta m, BoxSet bs, const double* __restrict__ u, const double* __res
     if (act) {
 #pragma unroll
       for (int j = 0; j < C::IPT; ++j) {
-        if (tid + C::T * j >= C::NEED) continue;
-        int fc, a, c;
-        item(j, fc, a, c);
-        const Face<D, NC> F(fc, a, c);
+        const int fc = it_f[j];
+        if (fc < 0) continue;
         const int code = d.code[fc];
         double v = gc[j];
-        if (code < 0) {
+        if (code == kFaceRefinement) {
+          const Face<D, NC> F(fc, it_lin[j] % NC + 1, it_lin[j] / NC + 1);
           auto own = [&](int i, int jj, int kk) { return bx[G::g(i, jj, kk)]; };
-          if (code == kFaceRefinement)
-            v = rb_value<D, NC, double>(F, fc, gc[j], own);
-          else
-            v = bc_value<double>(code, fc, gc[j], own(F.ai, F.aj, F.ak), d.dr);
+          v = rb_value<D, NC, double>(F, fc, gc[j], own);
+        } else if (code < 0) {
+          v = bc_value<double>(code, fc, gc[j], bx[it_a[j]], d.dr);
         }
-        bx[G::g(F.gi, F.gj, F.gk)] = v;
+        bx[it_g[j]] = v;
       }
     }
     __syncthreads();
@@ -2558,15 +2569,14 @@ k_defect_fx(Meta m, BoxSet bs, const double* __restrict__ u, const double* __res
 #pragma unroll
         for (int c = 0; c < C::CPT; ++c) {
           const int q = tid + C::T * c;
-          const int i = q % NC + 1, j = (q / NC) % NC + 1, kz = (D == 3) ? q / (NC * NC) + 1 : 0;
-          const long long xc = X[G::g(i, j, kz)];
+          const long long* x = X + cpos[c];
+          constexpr int OY = G::NG, OZ = G::NG * G::NG;
+          const long long xc = x[0];
           long long Sx;
           if constexpr (D == 2)
-            Sx = X[G::g(i - 1, j, 0)] + X[G::g(i + 1, j, 0)] + X[G::g(i, j - 1, 0)] + X[G::g(i, j + 1, 0)] -
-                 4 * xc;
+            Sx = x[-1] + x[1] + x[-OY] + x[OY] - 4 * xc;
           else
-            Sx = X[G::g(i - 1, j, kz)] + X[G::g(i + 1, j, kz)] + X[G::g(i, j - 1, kz)] +
-                 X[G::g(i, j + 1, kz)] + X[G::g(i, j, kz - 1)] + X[G::g(i, j, kz + 1)] - 6 * xc;
+            Sx = x[-1] + x[1] + x[-OY] + x[OY] + x[-OZ] + x[OZ] - 6 * xc;
           const float r = __double2float_rn(fma(ninv, from_fx(Sx, emax), fcv[c]));
           rb[q] = r;
           mx = nanmaxf(mx, fabsf(r));
