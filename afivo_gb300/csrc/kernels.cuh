@@ -2045,7 +2045,14 @@ __device__ __forceinline__ float d2f_rn(double x) {
 template <int PER_BOX, class V>
 __device__ __forceinline__ void box_max_atomic(V v, unsigned long long* dst, V* red) {
   constexpr int W = PER_BOX < 32 ? PER_BOX : 32;
-  auto mx = [](V a, V b) { return (b > a || b != b) ? b : a; };
+  // v >= 0 or NaN: doubles compare by their bit patterns (integer
+  // instructions, off the FP64 pipe); floats directly
+  auto mx = [](V a, V b) {
+    if constexpr (sizeof(V) == 8)
+      return dbits(b) > dbits(a) ? b : a;
+    else
+      return (b > a || b != b) ? b : a;
+  };
 #pragma unroll
   for (int o = W / 2; o > 0; o >>= 1) v = mx(v, __shfl_xor_sync(0xffffffffu, v, o));
   auto commit = [&](V x) {
@@ -2107,7 +2114,10 @@ k_residual(Meta m, BoxSet bs, const T* __restrict__ phi, const T* __restrict__ r
   for (int grp = blockIdx.x; grp < groups; grp += gridDim.x) {
     int b = threadIdx.x / PER_BOX, q0 = threadIdx.x % PER_BOX;
     int bi = grp * BPC + b;
-    double mx = 0;
+    // max |r| kept as the bit pattern of |r|: a non-negative double orders
+    // like its bits (a NaN above every number), so the maximum takes integer
+    // instructions instead of FP64 compares on GB300's slow FP64 pipe
+    unsigned long long mbits = 0;
     int tr = -1;
     bool leaf = false;
     if (bi < bs.n) {
@@ -2122,12 +2132,14 @@ k_residual(Meta m, BoxSet bs, const T* __restrict__ phi, const T* __restrict__ r
           int i = q % NC + 1, j = (q / NC) % NC + 1, k = (D == 3) ? q / (NC * NC) + 1 : 0;
           T r = rhs[d.offi + q] - lpl_at<D, NC, T>(bx, i, j, k, inv);
           if (store) tmp[d.offg + G::g(i, j, k)] = r;
-          mx = nanmax(mx, fabs((double)r));
+          const unsigned long long rb = dbits((double)r) & 0x7fffffffffffffffull;
+          mbits = rb > mbits ? rb : mbits;
         }
       } else {
         tr = -1;
       }
     }
+    const double mx = __longlong_as_double((long long)mbits);
     if (norm_per_tree) {
       // all threads of a PER_BOX segment belong to the same box
       box_max_atomic<PER_BOX, double>(
@@ -2163,7 +2175,8 @@ k_maxabs(Meta m, BoxSet bs, const T* __restrict__ v, int ghosted,
         for (int q = q0; q < G::SI; q += PER_BOX) {
           int i = q % NC + 1, j = (q / NC) % NC + 1, k = (D == 3) ? q / (NC * NC) + 1 : 0;
           T x = ghosted ? v[m.offg[s] + G::g(i, j, k)] : v[m.offi[s] + q];
-          mx = nanmax(mx, fabs((double)x));
+          const double ax = __longlong_as_double((long long)(dbits((double)x) & 0x7fffffffffffffffull));
+          mx = dbits(ax) > dbits(mx) ? ax : mx;  // |x| >= 0 or NaN: compare the bits
         }
       }
     }

