@@ -78,7 +78,8 @@ static int kernel_occupancy(const void* kern, int threads, int smem) {
   std::lock_guard<std::mutex> lock(mu);
   for (const auto& k : known)
     if (k.kern == kern && k.device == device && k.threads == threads && k.smem >= smem) return k.occ;
-  if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  // always: the 48 KB default counts the kernel's static shared memory too
+  if (smem > 0) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   int occ = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, threads, smem);
   occ = occ < 1 ? 1 : occ;
