@@ -484,7 +484,19 @@ static int exchange(Forest& F, int t, int var, double* host, int interior_only, 
   if (int rc = exchange_plan(F, err)) return rc;
   const int D = p.dim;
   const long long total = F.xfer_total[t][interior_only ? 0 : 1];
-  if (F.stage_elems < total || !F.d_stage) {
+  // Page-locked host memory is mapped into the device's address space: the
+  // scatter / gather kernels then read or write it directly over the host
+  // link, with no staging copy. Other host memory goes through the staging
+  // buffer and cudaMemcpyAsync.
+  double* mapped = nullptr;
+  {
+    cudaPointerAttributes pa;
+    if (cudaPointerGetAttributes(&pa, host) == cudaSuccess && pa.type == cudaMemoryTypeHost &&
+        pa.devicePointer && pa.device == F.device)
+      mapped = static_cast<double*>(pa.devicePointer);
+    cudaGetLastError();  // an unregistered pointer is not an error here
+  }
+  if (!mapped && (F.stage_elems < total || !F.d_stage)) {
     if (F.d_stage) cudaFreeAsync(F.d_stage, F.stream);
     F.d_stage = nullptr;
     if (cudaMallocAsync((void**)&F.d_stage, sizeof(double) * std::max(1LL, total), F.stream) != cudaSuccess)
@@ -493,7 +505,8 @@ static int exchange(Forest& F, int t, int var, double* host, int interior_only, 
   }
   cudaStream_t st = F.stream;
   const int* slots = F.d_stage_slots + F.xfer_order_off[t];
-  if (to_dev)
+  double* buf = mapped ? mapped : F.d_stage;
+  if (to_dev && !mapped)
     cudaMemcpyAsync(F.d_stage, host, sizeof(double) * total, cudaMemcpyHostToDevice, st);
   Meta m = meta_of(F.meta);
   bool ghosted = var != AFV_RHS;
@@ -509,15 +522,15 @@ static int exchange(Forest& F, int t, int var, double* host, int interior_only, 
       int grid = grid_for((n * per + 255) / 256, F.n_sm);
       ProfScope ps(&F, kProfOther, 16.0 * n * per);
       if (to_dev)
-        launch_k(dev::k_scatter<DD, NC, double>, grid, 256, 0, st, m, slots + r.first, n, F.d_stage + off, dvar,
+        launch_k(dev::k_scatter<DD, NC, double>, grid, 256, 0, st, m, slots + r.first, n, buf + off, dvar,
                  interior_only, ghosted);
       else
-        launch_k(dev::k_gather<DD, NC, double>, grid, 256, 0, st, m, slots + r.first, n, dvar, F.d_stage + off,
+        launch_k(dev::k_gather<DD, NC, double>, grid, 256, 0, st, m, slots + r.first, n, dvar, buf + off,
                  interior_only, ghosted);
     });
     off += n * per;
   }
-  if (!to_dev) cudaMemcpyAsync(host, F.d_stage, sizeof(double) * total, cudaMemcpyDeviceToHost, st);
+  if (!to_dev && !mapped) cudaMemcpyAsync(host, F.d_stage, sizeof(double) * total, cudaMemcpyDeviceToHost, st);
   if (cudaStreamSynchronize(st) != cudaSuccess) return F.check(err, "host exchange");
   return F.check(err, "host exchange");
 }
