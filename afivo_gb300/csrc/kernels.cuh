@@ -1801,6 +1801,52 @@ k_restrict_res(Meta m, BoxSet bs, T* __restrict__ phi, const T* __restrict__ rhs
 }
 
 // ---------------------------------------------------------------------------
+// Restriction of phi alone into the parents (a$D_restrict_box,
+// src/m_aX_restrict.f90:67-132, as k_restrict_res without the residual): one
+// thread per parent cell, its 2^D fine cells read straight from global
+// memory in k_restrict_res's order. No ghost cell is read, so nothing is
+// staged.
+// ---------------------------------------------------------------------------
+template <int D, int NC, bool SUB, class T>
+__global__ void __launch_bounds__(kThreads)
+k_restrict_phi(Meta m, BoxSet bs, T* __restrict__ phi) {
+  pdl_trigger();
+  using G = Geo<D, NC>;
+  constexpr int H = NC / 2;
+  constexpr int PNC = SUB ? NC / 2 : NC;
+  using GP = Geo<D, PNC>;
+  constexpr int PAR = D == 2 ? H * H : H * H * H;
+  pdl_wait();
+  const long long total = (long long)bs.n * PAR;
+  for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < total;
+       x += (long long)gridDim.x * blockDim.x) {
+    const int bi = (int)(x / PAR), q = (int)(x % PAR);
+    const int s = box_at(bs, bi);
+    if (!m.active[m.tree[s]]) continue;
+    const T* bx = phi + box_offg<G::SG>(m, bs, bi, s);
+    const int ic = q % H + 1, jc = (q / H) % H + 1, kc = (D == 3) ? q / (H * H) + 1 : 0;
+    int off0 = 0, off1 = 0, off2 = 0;
+    if (!SUB) {
+      const int qd = m.desc[s].qd;
+      off0 = (qd & 1) * H;
+      off1 = ((qd >> 1) & 1) * H;
+      off2 = ((qd >> 2) & 1) * H;
+    }
+    T sp = 0;
+    constexpr int KK = (D == 3) ? 2 : 1;
+#pragma unroll
+    for (int kk = 0; kk < KK; ++kk)
+#pragma unroll
+      for (int jj = 0; jj < 2; ++jj)
+#pragma unroll
+        for (int ii = 0; ii < 2; ++ii)
+          sp = sp + bx[G::g(2 * ic - 1 + ii, 2 * jc - 1 + jj, (D == 3) ? 2 * kc - 1 + kk : 0)];
+    const T w = (D == 2) ? (T)0.25 : (T)0.125;
+    phi[m.offg[m.parent[s]] + GP::g(off0 + ic, off1 + jc, (D == 3) ? off2 + kc : 0)] = w * sp;
+  }
+}
+
+// ---------------------------------------------------------------------------
 // Coarse right-hand side on the parents of a level after restriction
 // (src/m_aX_mg.f90:472-479 and :510-515): rhs = L(phi) + tmp over the interior,
 // then, for update_coarse, tmp = phi over the whole box including its ghosts

@@ -724,7 +724,15 @@ void Forest::restrict_res(const Arrays<T>& a, int lvl, bool with_res, bool pull,
     // read phi, f; write the parent's phi and tmp (2 values per 2^D fine cells)
     ProfScope ps(this, kProfRestrict,
                  (2.0 + 2.0 / (1 << D)) * nbx * G::SI * sizeof(T));
-    if (sub)
+    if (!with_res) {
+      // phi alone: one thread per parent cell, no staging
+      constexpr int PAR = D == 2 ? H * H : H * H * H;
+      const int g2 = grid_for(((long long)nbx * PAR + dev::kThreads - 1) / dev::kThreads, n_sm);
+      if (sub)
+        launch_k(dev::k_restrict_phi<D, NC, true, T>, g2, dev::kThreads, 0, stream, m, bs, a.phi);
+      else
+        launch_k(dev::k_restrict_phi<D, NC, false, T>, g2, dev::kThreads, 0, stream, m, bs, a.phi);
+    } else if (sub)
       launch_k(dev::k_restrict_res<D, NC, true, T>, grid, dev::kThreads, 0, stream, 
           m, bs, a.phi, a.rhs, a.tmp, with_res ? 1 : 0, pull ? 1 : 0, homog ? 1 : 0);
     else if (with_res && pull && use_restrict_warp)
