@@ -628,8 +628,10 @@ k_sweep_warp(Meta m, BoxSet bs, T* __restrict__ phi, const T* __restrict__ rhs, 
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) unsigned long long bar[W][S];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const int gw = (int)blockIdx.x * W + wid, nw = (int)gridDim.x * W;
+  const int nw = (int)gridDim.x * W;
   const int nbx = bs.n;
+  // few boxes (grid sized one block per box): spread them over the SMs
+  const int gw = nbx <= nw ? wid * (int)gridDim.x + (int)blockIdx.x : (int)blockIdx.x * W + wid;
   if (gw >= nbx) {
     pdl_wait();
     return;
@@ -919,8 +921,10 @@ k_restrict_warp(Meta m, BoxSet bs, T* __restrict__ phi, const T* __restrict__ rh
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) unsigned long long bar[W][S];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const int gw = (int)blockIdx.x * W + wid, nw = (int)gridDim.x * W;
+  const int nw = (int)gridDim.x * W;
   const int nbx = bs.n;
+  // few boxes (grid sized one block per box): spread them over the SMs
+  const int gw = nbx <= nw ? wid * (int)gridDim.x + (int)blockIdx.x : (int)blockIdx.x * W + wid;
   if (gw >= nbx) {
     pdl_wait();
     return;
@@ -1129,8 +1133,10 @@ k_coarse_warp(Meta m, BoxSet bs, T* __restrict__ phi, T* __restrict__ rhs, T* __
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) unsigned long long bar[W][S];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const int gw = (int)blockIdx.x * W + wid, nw = (int)gridDim.x * W;
+  const int nw = (int)gridDim.x * W;
   const int nbx = bs.n;
+  // few boxes (grid sized one block per box): spread them over the SMs
+  const int gw = nbx <= nw ? wid * (int)gridDim.x + (int)blockIdx.x : (int)blockIdx.x * W + wid;
   if (gw >= nbx) {
     pdl_wait();
     return;
@@ -1302,8 +1308,8 @@ struct CorrectCfg {
   static constexpr int CPL = (G::SI + 31) / 32;  // parent interior cells per lane
   static constexpr int NEED = 2 * D * G::NF;
   static constexpr int GPL = (NEED + 31) / 32;
-  // parent cells per batch: 16 fine-cell loads (FP32) or 8 (FP64)
-  static constexpr int PW = (std::is_same<T, float>::value ? 16 : 8) / FINE;
+  // parent cells per batch: 16 fine-cell loads in either precision
+  static constexpr int PW = 16 / FINE;
   static constexpr int P = PW < CPL ? PW : CPL;
   static constexpr int NB = (CPL + P - 1) / P;
   static constexpr int PHI_OFF = (int)sizeof(SlotDesc);
@@ -1314,9 +1320,10 @@ struct CorrectCfg {
   static_assert(S >= 3, "sources are fetched one parent ahead of the one in use");
 };
 
-template <int D, int NC, class T, int W, int S>
+template <int D, int NC, class T, int W, int S, int SPLIT>
 __global__ void __launch_bounds__(W * 32)
 k_correct_warp(Meta m, BoxSet bs, T* __restrict__ phi, T* __restrict__ tmp, int pull, int homog) {
+  constexpr int split = SPLIT;
   // Descriptors never change after the forest is created: those of the
   // first boxes are loaded before pdl_wait(), the cells after it.
   pdl_trigger();
@@ -1328,13 +1335,24 @@ k_correct_warp(Meta m, BoxSet bs, T* __restrict__ phi, T* __restrict__ tmp, int 
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) unsigned long long bar[W][S];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const int gw = (int)blockIdx.x * W + wid, nw = (int)gridDim.x * W;
-  const int nbx = bs.n;
+  const int nw = (int)gridDim.x * W;
+  // split 0: one warp per parent does it all. For levels with few parents,
+  // whose per-parent work would otherwise sit on one SM, two launches:
+  // split 1, a warp per parent makes the ghosts and tmp = phi - tmp and
+  // stores them; split 2, a warp per (parent, child) stages the stored tmp
+  // and adds the prolongation of that child's quadrant.
+  const int per = split == 2 ? C::FINE : 1;
+  const int nbx = bs.n * per;
+  // at most one item per block: spread over the SMs (with more, neighbouring
+  // parents stay in one block, whose children's cells share L1 lines)
+  const int gw = nbx <= (int)gridDim.x ? wid * (int)gridDim.x + (int)blockIdx.x : (int)blockIdx.x * W + wid;
   if (gw >= nbx) {
     pdl_wait();
     return;
   }
   const int my_boxes = (nbx - 1 - gw) / nw + 1;
+  auto parent_of = [&](int k) { return (gw + k * nw) / per; };
+  auto child_of = [&](int k) { return split == 2 ? (gw + k * nw) % per : -1; };
   unsigned char* ring = smem + (size_t)wid * S * C::BOX_B;
   if (lane == 0) {
     for (int st = 0; st < S; ++st) mbar_init(&bar[wid][st], 1);
@@ -1346,7 +1364,7 @@ k_correct_warp(Meta m, BoxSet bs, T* __restrict__ phi, T* __restrict__ tmp, int 
   auto stage = [&](int k) { return ring + (k % S) * C::BOX_B; };
   auto issue = [&](int k) {  // lane 0
     ++issued;
-    const int i = gw + k * nw;
+    const int i = parent_of(k);
     const int s = box_at(bs, i);
     const long long o = box_offg<G::SG>(m, bs, i, s);
     unsigned char* sp = stage(k);
@@ -1359,7 +1377,7 @@ k_correct_warp(Meta m, BoxSet bs, T* __restrict__ phi, T* __restrict__ tmp, int 
   };
   auto issue_data = [&](int k) {  // lane 0: the cells only (descriptor staged)
     ++issued;
-    const int i = gw + k * nw;
+    const int i = parent_of(k);
     const int s = box_at(bs, i);
     const long long o = box_offg<G::SG>(m, bs, i, s);
     unsigned char* sp = stage(k);
@@ -1385,7 +1403,7 @@ k_correct_warp(Meta m, BoxSet bs, T* __restrict__ phi, T* __restrict__ tmp, int 
 #pragma unroll
     for (int j = 0; j < C::GPL; ++j) {
       gv[j] = (T)0;
-      if (!pull || lane + 32 * j >= C::NEED) continue;
+      if (!pull || split == 2 || lane + 32 * j >= C::NEED) continue;
       int f, a, c;
       item(j, f, a, c);
       const Face<D, NC> F(f, a, c);
@@ -1409,22 +1427,37 @@ k_correct_warp(Meta m, BoxSet bs, T* __restrict__ phi, T* __restrict__ tmp, int 
     return (qx + 2 * qy + 4 * qz) * G::SG + G::g(2 * li - 1, 2 * lj - 1, (D == 3) ? 2 * lk - 1 : 0);
   };
   auto foff = [](int f) { return (f & 1) + ((f >> 1) & 1) * G::NG + ((f >> 2) & 1) * G::NG * G::NG; };
-  auto load_batch = [&](int nb, const T* cp, T (&buf)[P][FINE]) {
+  // Parent cell (interior index) of this lane's item idx: all cells, or the
+  // quadrant of child ch; false past the end.
+  auto pcell = [&](int idx, int ch, int& q) -> bool {
+    if (ch < 0) {
+      q = lane + 32 * idx;
+      return idx < C::CPL && q < G::SI;
+    }
+    const int lq = lane + 32 * idx;
+    constexpr int QN = D == 2 ? H * H : H * H * H;
+    if (lq >= QN) return false;
+    const int li = lq % H, lj = (lq / H) % H, lk = (D == 3) ? lq / (H * H) : 0;
+    q = ((ch & 1) * H + li) + NC * (((ch >> 1) & 1) * H + lj) +
+        ((D == 3) ? NC * NC * (((ch >> 2) & 1) * H + lk) : 0);
+    return true;
+  };
+  auto load_batch = [&](int nb, int ch, const T* cp, T (&buf)[P][FINE]) {
 #pragma unroll
     for (int pp = 0; pp < P; ++pp) {
-      const int q = lane + 32 * (nb * P + pp);
-      if (nb * P + pp >= C::CPL || q >= G::SI) continue;
+      int q;
+      if (!pcell(nb * P + pp, ch, q)) continue;
       const T* c = cp + fine_base(q);
 #pragma unroll
       for (int f = 0; f < FINE; ++f) buf[pp][f] = c[foff(f)];
     }
   };
   // phi(fine) = prolongation + old value, in the order of k_correct.
-  auto store_batch = [&](int nb, T* cp, const T* t, const T (&buf)[P][FINE]) {
+  auto store_batch = [&](int nb, int ch, T* cp, const T* t, const T (&buf)[P][FINE]) {
 #pragma unroll
     for (int pp = 0; pp < P; ++pp) {
-      const int q = lane + 32 * (nb * P + pp);
-      if (nb * P + pp >= C::CPL || q >= G::SI) continue;
+      int q;
+      if (!pcell(nb * P + pp, ch, q)) continue;
       const int ic = q % NC + 1, jc = (q / NC) % NC + 1, kc = (D == 3) ? q / (NC * NC) + 1 : 0;
       const T f0 = t[G::g(ic, jc, kc)];
       const T fx = (T)0.125 * (t[G::g(ic + 1, jc, kc)] - t[G::g(ic - 1, jc, kc)]);
@@ -1464,10 +1497,11 @@ k_correct_warp(Meta m, BoxSet bs, T* __restrict__ phi, T* __restrict__ tmp, int 
     T* bx = reinterpret_cast<T*>(sp + C::PHI_OFF);
     T* tx = reinterpret_cast<T*>(sp + C::TMP_OFF);
     if (a0) {
+      const int ch = child_of(k);
       T ca[P][FINE], cb[P][FINE];
       T* cp = phi + co0;
-      load_batch(0, cp, ca);  // the children's cells are not written before the stores below
-      if (pull) {
+      if (split != 1) load_batch(0, ch, cp, ca);  // the children's cells are not written before the stores below
+      if (pull && split != 2) {
         T* gphi = phi + d.offg;
 #pragma unroll
         for (int j = 0; j < C::GPL; ++j) {
@@ -1491,7 +1525,7 @@ k_correct_warp(Meta m, BoxSet bs, T* __restrict__ phi, T* __restrict__ tmp, int 
         __syncwarp();
       }
       V* gt = reinterpret_cast<V*>(tmp + d.offg);
-      for (int e = lane; e < G::SG / VW; e += 32) {
+      for (int e = lane; split != 2 && e < G::SG / VW; e += 32) {
         const V p = reinterpret_cast<const V*>(bx)[e];
         const V t = reinterpret_cast<const V*>(tx)[e];
         V r;
@@ -1509,12 +1543,12 @@ k_correct_warp(Meta m, BoxSet bs, T* __restrict__ phi, T* __restrict__ tmp, int 
       }
       __syncwarp();
 #pragma unroll
-      for (int nb = 0; nb < C::NB; nb += 2) {
-        if (nb + 1 < C::NB) load_batch(nb + 1, cp, cb);
-        store_batch(nb, cp, tx, ca);
+      for (int nb = 0; split != 1 && nb < C::NB; nb += 2) {
+        if (nb + 1 < C::NB) load_batch(nb + 1, ch, cp, cb);
+        store_batch(nb, ch, cp, tx, ca);
         if (nb + 1 < C::NB) {
-          if (nb + 2 < C::NB) load_batch(nb + 2, cp, ca);
-          store_batch(nb + 1, cp, tx, cb);
+          if (nb + 2 < C::NB) load_batch(nb + 2, ch, cp, ca);
+          store_batch(nb + 1, ch, cp, tx, cb);
         }
       }
     }
@@ -1525,7 +1559,7 @@ k_correct_warp(Meta m, BoxSet bs, T* __restrict__ phi, T* __restrict__ tmp, int 
   const int ahead = min(S - 1, my_boxes);
   for (int k = 0; k < ahead; ++k)
     reinterpret_cast<unsigned*>(stage(k))[lane] =
-        reinterpret_cast<const unsigned*>(m.desc + box_at(bs, gw + k * nw))[lane];
+        reinterpret_cast<const unsigned*>(m.desc + box_at(bs, parent_of(k)))[lane];
   __syncwarp();
   pdl_wait();  // the previous kernel's writes are visible from here on
   if (lane == 0)

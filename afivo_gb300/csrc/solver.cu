@@ -576,7 +576,8 @@ static void launch_sweep_warp(Forest& F, const Meta& m, BoxSet bs, T* phi, const
                               bool pull, bool homog) {
   using C = dev::WarpCfg<D, NC, T, W, S>;
   const int occ = kernel_occupancy((const void*)dev::k_sweep_warp<D, NC, T, W, S, ASYNC>, W * 32, (int)C::SMEM_B);
-  const long long blocks = (bs.n + W - 1) / W;
+  // a level with fewer boxes than resident blocks gets one block per box
+  const long long blocks = bs.n;
   const int grid = (int)std::max(1LL, std::min(blocks, (long long)F.n_sm * occ));
   launch_k(dev::k_sweep_warp<D, NC, T, W, S, ASYNC>, grid, W * 32, C::SMEM_B, F.stream, m, bs, phi, rhs, n, pull ? 1 : 0,
                                                                           homog ? 1 : 0);
@@ -588,11 +589,25 @@ template <int D, int NC, class T>
 static void launch_correct_warp(Forest& F, const Meta& m, BoxSet bs, T* phi, T* tmp, bool pull, bool homog) {
   constexpr int W = std::is_same<T, float>::value ? 8 : 4, S = 3;
   using C = dev::CorrectCfg<D, NC, T, W, S>;
-  const int occ = kernel_occupancy((const void*)dev::k_correct_warp<D, NC, T, W, S>, W * 32, (int)C::SMEM_B);
-  const long long blocks = (bs.n + W - 1) / W;
-  const int grid = (int)std::max(1LL, std::min(blocks, (long long)F.n_sm * occ));
-  launch_k(dev::k_correct_warp<D, NC, T, W, S>, grid, W * 32, (size_t)C::SMEM_B, F.stream, m, bs, phi, tmp,
-           pull ? 1 : 0, homog ? 1 : 0);
+  auto go = [&](auto split_) {
+    constexpr int SPLIT = decltype(split_)::value;
+    auto kern = dev::k_correct_warp<D, NC, T, W, S, SPLIT>;
+    const int occ = kernel_occupancy((const void*)kern, W * 32, (int)C::SMEM_B);
+    const long long items = (long long)bs.n * (SPLIT == 2 ? C::FINE : 1);
+    const long long blocks = items;  // one block per item when they are few
+    const int grid = (int)std::max(1LL, std::min(blocks, (long long)F.n_sm * occ));
+    launch_k(kern, grid, W * 32, (size_t)C::SMEM_B, F.stream, m, bs, phi, tmp, pull ? 1 : 0, homog ? 1 : 0);
+  };
+  // FP64 with fewer parents than a quarter of the resident warps (one block
+  // per SM): the prolongation (about 55 FP64 operations per parent cell)
+  // spread over a warp per child, at the cost of a second launch
+  if (std::is_same<T, double>::value && 4LL * bs.n < (long long)F.n_sm * W) {
+    go(IC<1>{});
+    go(IC<2>{});
+    ++F.n_launches;  // the profiler scope around this call counts one
+  } else {
+    go(IC<0>{});
+  }
 }
 
 dev_BoxSet Forest::level_set(int lvl) const {
@@ -608,7 +623,8 @@ static void launch_restrict_warp(Forest& F, const Meta& m, BoxSet bs, T* phi, co
   constexpr int W = std::is_same<T, float>::value ? 16 : 8, S = 3;
   using C = dev::RestrictCfg<D, NC, T, W, S>;
   const int occ = kernel_occupancy((const void*)dev::k_restrict_warp<D, NC, T, W, S>, W * 32, (int)C::SMEM_B);
-  const long long blocks = (bs.n + W - 1) / W;
+  // a level with fewer boxes than resident blocks gets one block per box
+  const long long blocks = bs.n;
   const int grid = (int)std::max(1LL, std::min(blocks, (long long)F.n_sm * occ));
   launch_k(dev::k_restrict_warp<D, NC, T, W, S>, grid, W * 32, (size_t)C::SMEM_B, F.stream, m, bs, phi, rhs,
            tmp, homog ? 1 : 0);
@@ -621,7 +637,8 @@ static void launch_coarse_warp(Forest& F, const Meta& m, BoxSet bs, T* phi, T* r
   constexpr int W = std::is_same<T, float>::value ? 16 : 8, S = 3;
   using C = dev::CoarseCfg<D, NC, T, W, S>;
   const int occ = kernel_occupancy((const void*)dev::k_coarse_warp<D, NC, T, W, S>, W * 32, (int)C::SMEM_B);
-  const long long blocks = (bs.n + W - 1) / W;
+  // a level with fewer boxes than resident blocks gets one block per box
+  const long long blocks = bs.n;
   const int grid = (int)std::max(1LL, std::min(blocks, (long long)F.n_sm * occ));
   launch_k(dev::k_coarse_warp<D, NC, T, W, S>, grid, W * 32, (size_t)C::SMEM_B, F.stream, m, bs, phi, rhs, tmp,
            homog ? 1 : 0);
