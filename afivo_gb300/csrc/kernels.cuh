@@ -1343,9 +1343,8 @@ k_correct_warp(Meta m, BoxSet bs, T* __restrict__ phi, T* __restrict__ tmp, int 
   // and adds the prolongation of that child's quadrant.
   const int per = split == 2 ? C::FINE : 1;
   const int nbx = bs.n * per;
-  // at most one item per block: spread over the SMs (with more, neighbouring
-  // parents stay in one block, whose children's cells share L1 lines)
-  const int gw = nbx <= (int)gridDim.x ? wid * (int)gridDim.x + (int)blockIdx.x : (int)blockIdx.x * W + wid;
+  // few items (grid sized one block per item): spread them over the SMs
+  const int gw = nbx <= nw ? wid * (int)gridDim.x + (int)blockIdx.x : (int)blockIdx.x * W + wid;
   if (gw >= nbx) {
     pdl_wait();
     return;
