@@ -598,10 +598,12 @@ static void launch_correct_warp(Forest& F, const Meta& m, BoxSet bs, T* phi, T* 
     const int grid = (int)std::max(1LL, std::min(blocks, (long long)F.n_sm * occ));
     launch_k(kern, grid, W * 32, (size_t)C::SMEM_B, F.stream, m, bs, phi, tmp, pull ? 1 : 0, homog ? 1 : 0);
   };
-  // FP64 with fewer parents than a quarter of the resident warps (one block
-  // per SM): the prolongation (about 55 FP64 operations per parent cell)
-  // spread over a warp per child, at the cost of a second launch
-  if (std::is_same<T, double>::value && 4LL * bs.n < (long long)F.n_sm * W) {
+  // FP64: the prolongation (about 55 FP64 operations per parent cell) spread
+  // over a warp per child, at the cost of a second launch (C2 FP64 solve
+  // 28.73 ms against 28.86 ms with a warp per parent on levels of at least a
+  // quarter as many parents as resident warps). FP32 keeps one launch (9.01
+  // against 9.11 ms split).
+  if constexpr (std::is_same<T, double>::value) {
     go(IC<1>{});
     go(IC<2>{});
     ++F.n_launches;  // the profiler scope around this call counts one
