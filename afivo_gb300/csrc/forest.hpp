@@ -109,10 +109,20 @@ class Forest {
   unsigned long long* d_norm = nullptr;  // [n_trees * kStripes] striped per-tree maxima
   unsigned long long* d_red = nullptr;   // [n_trees] reduced maxima
   double* d_fmax = nullptr;              // [n_trees]
-  int* d_count = nullptr;                // [1]
+  // [4]: active trees after the last check, the error word at that check,
+  // iterations of the current solve (graph loop), unused
+  int* d_count = nullptr;
   int* d_failed = nullptr;               // [n_trees] nonzero: residual not finite
-  int* h_count = nullptr;                // pinned
+  int* d_cycles = nullptr;               // [n_trees] V-cycles of the current solve
+  unsigned long long* d_final = nullptr; // [n_trees] residual norm at the tree's last check (double bits)
+  int* h_count = nullptr;                // pinned [4]: copy of d_count
   unsigned long long* h_norm = nullptr;  // pinned [n_trees]
+  // pinned results of a solve, copied once at its end
+  int* h_cycles = nullptr;               // [n_trees]
+  unsigned long long* h_final = nullptr; // [n_trees]
+  int* h_failed = nullptr;               // [n_trees]
+  double* h_fmax = nullptr;              // [n_trees]
+  bool readback = true;  // each residual check copies d_count to h_count (host-driven solve loop)
   double* d_stage = nullptr;             // staging for host exchange
   long long stage_elems = 0;
   int* d_stage_slots = nullptr;          // every tree's host-order slots, concatenated
@@ -128,14 +138,16 @@ class Forest {
   std::vector<long long> xfer_order_off;
   long long bytes = 0;
   std::vector<int> host_active;
-  int* h_active = nullptr;  // pinned copy of the device activity flags (read back by solves)
-  // CUDA graphs of one solve iteration, per precision, keyed by the options
+  // CUDA graph of a whole solve, per precision, keyed by the options: set-up,
+  // a conditional while node over the iterations (body captured on
+  // loop_stream), finish; the kernels each part launches
   struct GraphCache {
     cudaGraphExec_t exec = nullptr;
-    long long kernels = 0;
-    int n_down = -1, n_up = -1, n_base = -1;
+    long long k_pre = 0, k_body = 0, k_post = 0;
+    int n_down = -1, n_up = -1, n_base = -1, max_cycles = -1;
     double tol = -1;
   } graphs[2];
+  cudaStream_t loop_stream = nullptr;
   bool use_graphs = true;
   void drop_graphs();
   // event profiler: when enabled, launches of the selected kinds (bit mask)
@@ -203,9 +215,15 @@ class Forest {
                                    bool base64, bool inner = false);
   template <class T> void fill_set(const Arrays<T>& a, int lvl, dev_BoxSet bs, bool homog);
   void fill_all64(bool homog);
-  // Enqueue (no host synchronisation) one solve iteration / its residual check.
+  // Enqueue (no host synchronisation) one solve iteration / its residual
+  // check (count_cycle: the check follows a cycle), the solve's set-up (with
+  // a loop handle: the loop-entry decision) and its finish.
   void enqueue_iteration(const MgOpts& mg, int precision, double tol);
-  void enqueue_residual_check(int precision, double tol);
+  void enqueue_residual_check(int precision, double tol, int count_cycle = 1);
+  void enqueue_solve_begin(int precision, double tol, int max_cycles, const cudaGraphConditionalHandle* h);
+  void enqueue_solve_end(int precision);
+  int build_solve_graph(GraphCache& gc, const MgOpts& mg, int precision, double tol, int max_cycles,
+                        std::string& err);
   void restrict_tree_phi64();
 
   int check(std::string& err, const char* where);

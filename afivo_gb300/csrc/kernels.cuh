@@ -2929,13 +2929,19 @@ __global__ void k_hold(long long ns) {
 // max|r| > tol * max|f|; a non-finite residual stops it and marks it failed.
 __global__ void k_check(int n_trees, const unsigned long long* __restrict__ rnorm,
                         const double* __restrict__ fmax, double tol, int* __restrict__ active,
-                        int* __restrict__ failed, int* __restrict__ n_active_out) {
+                        int* __restrict__ failed, int* __restrict__ n_active_out, const int* __restrict__ err,
+                        int* __restrict__ cycles, unsigned long long* __restrict__ final_r, int count_cycle) {
   pdl_wait();
   pdl_trigger();
   int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t == 0) n_active_out[1] = *err;  // read back with the count
   if (t < n_trees) {
     double r = __longlong_as_double((long long)rnorm[t]);  // reduced over stripes
     int a = active[t];
+    if (a) {  // the tree was cycled (unless this is the check before the first cycle)
+      final_r[t] = rnorm[t];
+      cycles[t] += count_cycle;
+    }
     if (a && !(r <= 1.0e300)) {
       a = 0;
       failed[t] = 1;
@@ -2945,6 +2951,27 @@ __global__ void k_check(int n_trees, const unsigned long long* __restrict__ rnor
     active[t] = a;
     if (a) atomicAdd(n_active_out, 1);
   }
+}
+
+// Sets n ints to v (activity flags).
+__global__ void k_set_int(int* __restrict__ a, int n, int v) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) a[i] = v;
+}
+
+// Loop control of a solve graph (a conditional while node around the
+// iterations; one thread each). Words of count: [0] trees still active after
+// the last check, [1] the device error word at that check, [2] iterations
+// run. k_loop_start enters the loop if a tree is active; k_loop_step, at the
+// end of every iteration, repeats it while one is, below max_cycles
+// iterations and without a device error.
+__global__ void k_loop_start(cudaGraphConditionalHandle h, int* __restrict__ count, int max_cycles) {
+  count[2] = 0;
+  cudaGraphSetConditional(h, (count[0] > 0 && max_cycles > 0) ? 1u : 0u);
+}
+__global__ void k_loop_step(cudaGraphConditionalHandle h, int* __restrict__ count, int max_cycles) {
+  const int c = count[2] + 1;
+  count[2] = c;
+  cudaGraphSetConditional(h, (count[0] > 0 && c < max_cycles && count[1] == 0) ? 1u : 0u);
 }
 
 }  // namespace dev

@@ -156,7 +156,7 @@ Forest::~Forest() {
   void* ptrs[] = {meta.parent, meta.first_child, meta.tree, meta.offg, meta.offi, meta.bcval,
                   meta.active, meta.desc, meta.nbo2, meta.err, meta.rmin, d64.phi, d64.rhs,
                   d64.tmp, d32.phi, d32.rhs, d32.tmp, base_phi64, base_rhs64, d_lists, d_norm, d_red,
-                  d_fmax, d_count, d_failed, d_stage, d_stage_slots};
+                  d_fmax, d_count, d_failed, d_cycles, d_final, d_stage, d_stage_slots};
   for (void* p : ptrs)
     if (p) cudaFreeAsync(p, stream);
   if (stream) cudaStreamSynchronize(stream);
@@ -166,12 +166,12 @@ Forest::~Forest() {
   }
   for (cudaEvent_t e : event_pool) cudaEventDestroy(e);
   drop_graphs();
-  if (h_count) cudaFreeHost(h_count);
-  if (h_active) cudaFreeHost(h_active);
-  if (h_norm) cudaFreeHost(h_norm);
+  for (void* p : {(void*)h_count, (void*)h_norm, (void*)h_cycles, (void*)h_final, (void*)h_failed, (void*)h_fmax})
+    if (p) cudaFreeHost(p);
   if (ev_fork) cudaEventDestroy(ev_fork);
   if (ev_join) cudaEventDestroy(ev_join);
   if (side) cudaStreamDestroy(side);
+  if (loop_stream) cudaStreamDestroy(loop_stream);
   if (stream) cudaStreamDestroy(stream);
 }
 
@@ -318,6 +318,7 @@ int Forest::create(const std::vector<const HostTree*>& trees, const afv_forest_o
   cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, device);
   if (cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&loop_stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming) != cudaSuccess)
     return err = "cudaStreamCreate failed", AFV_ERR_CUDA;
@@ -376,11 +377,16 @@ int Forest::create(const std::vector<const HostTree*>& trees, const afv_forest_o
   if ((rc = dupload(&d_lists, lists, bytes, stream))) return err = "device allocation failed", rc;
   if (dmalloc(&d_norm, (long long)p.n_trees * dev::kStripes, bytes, stream) ||
       dmalloc(&d_red, p.n_trees, bytes, stream) || dmalloc(&d_fmax, p.n_trees, bytes, stream) ||
-      dmalloc(&d_count, 1, bytes, stream) || dmalloc(&d_failed, p.n_trees, bytes, stream))
+      dmalloc(&d_count, 4, bytes, stream) || dmalloc(&d_failed, p.n_trees, bytes, stream) ||
+      dmalloc(&d_cycles, p.n_trees, bytes, stream) || dmalloc(&d_final, p.n_trees, bytes, stream))
     return err = "device allocation failed", AFV_ERR_NOMEM;
-  if (cudaMallocHost((void**)&h_active, sizeof(int) * p.n_trees) != cudaSuccess ||
-      cudaMallocHost((void**)&h_count, sizeof(int)) != cudaSuccess ||
-      cudaMallocHost((void**)&h_norm, sizeof(unsigned long long) * p.n_trees) != cudaSuccess)
+  cudaMemsetAsync(d_count, 0, 4 * sizeof(int), stream);
+  if (cudaMallocHost((void**)&h_count, 4 * sizeof(int)) != cudaSuccess ||
+      cudaMallocHost((void**)&h_norm, sizeof(unsigned long long) * p.n_trees) != cudaSuccess ||
+      cudaMallocHost((void**)&h_cycles, sizeof(int) * p.n_trees) != cudaSuccess ||
+      cudaMallocHost((void**)&h_final, sizeof(unsigned long long) * p.n_trees) != cudaSuccess ||
+      cudaMallocHost((void**)&h_failed, sizeof(int) * p.n_trees) != cudaSuccess ||
+      cudaMallocHost((void**)&h_fmax, sizeof(double) * p.n_trees) != cudaSuccess)
     return err = "pinned allocation failed", AFV_ERR_NOMEM;
   if (cudaStreamSynchronize(stream) != cudaSuccess) return check(err, "forest create");
   return AFV_OK;
@@ -1224,8 +1230,9 @@ void Forest::restrict_tree_phi64() {
 
 // One residual check, enqueued only: per-tree max |r| over the leaves (the FP64
 // residual, or the FP64 defect written as the FP32 right-hand side of the
-// mixed cycle), the convergence flags, and their copies to pinned host memory.
-void Forest::enqueue_residual_check(int precision, double tol) {
+// mixed cycle), the convergence flags, each active tree's cycle count and
+// last norm, and (readback) the active count copied to pinned host memory.
+void Forest::enqueue_residual_check(int precision, double tol, int count_cycle) {
   const int nt = plan.n_trees;
   Meta m = meta_of(meta);
   norm_reset();
@@ -1258,16 +1265,15 @@ void Forest::enqueue_residual_check(int precision, double tol) {
   } else {
     for (int l = plan.min_lvl; l <= plan.max_lvl; ++l) residual(d64, l, d_norm, true);
   }
-  cudaMemsetAsync(d_count, 0, sizeof(int), stream);
+  cudaMemsetAsync(d_count, 0, 2 * sizeof(int), stream);
   norm_fold();
   {
     ProfScope ps(this, kProfOther, 20.0 * nt);
     launch_k(dev::k_check, (nt + 255) / 256, 256, 0, stream, nt, d_red, d_fmax, tol, meta.active, d_failed,
-                                                       d_count);
+             d_count, (const int*)meta.err, d_cycles, d_final, count_cycle);
   }
-  cudaMemcpyAsync(h_count, d_count, sizeof(int), cudaMemcpyDeviceToHost, stream);
-  cudaMemcpyAsync(h_norm, d_red, sizeof(unsigned long long) * nt, cudaMemcpyDeviceToHost, stream);
-  cudaMemcpyAsync(h_active, meta.active, sizeof(int) * nt, cudaMemcpyDeviceToHost, stream);
+  // the active count and the device error word, for a host-driven loop
+  if (readback) cudaMemcpyAsync(h_count, d_count, 4 * sizeof(int), cudaMemcpyDeviceToHost, stream);
 }
 
 // One solve iteration, enqueued only: a V-cycle (FP64), or an FP32 V-cycle
@@ -1331,23 +1337,21 @@ void Forest::enqueue_iteration(const MgOpts& mg, int precision, double tol) {
   }
 }
 
-// Solve every tree to max|f - L phi| <= tol * max|f| over its leaves. Each
-// iteration is one CUDA-graph launch (captured on first use); trees that have
-// converged are masked out on the device, so the graph does not change while
-// the set of active trees shrinks.
-int Forest::solve(const MgOpts& mg, int precision, double tol, int max_cycles, SolveStats& st,
-                  std::string& err) {
+// Set-up of a solve, enqueued only: every tree active, cycle counts zeroed,
+// max |f| over each tree's leaves, parents of the mixed solve's u as the
+// restriction of their children (their values are only read by coarse leaves
+// next to refined regions) and the first correction zeroed, then the residual
+// check before the first cycle. With a loop handle, the loop-entry decision.
+void Forest::enqueue_solve_begin(int precision, double tol, int max_cycles, const cudaGraphConditionalHandle* h) {
   const int nt = plan.n_trees;
-  if (precision == AFV_PREC_MIXED && !mixed)
-    return err = "forest created without mixed_buffers", AFV_ERR_STATE;
-  st.cycles.assign(nt, 0);
-  st.rel_res.assign(nt, 0.0);
   Meta m = meta_of(meta);
-  set_active_all(1);
-  // max |f| over the leaves of every tree (all leaves are on levels >= 1,
-  // with nc cells per side: one launch)
+  dev::k_set_int<<<(nt + 255) / 256, 256, 0, stream>>>(meta.active, nt, 1);
+  ++n_launches;
+  cudaMemsetAsync(d_cycles, 0, sizeof(int) * nt, stream);
+  cudaMemsetAsync(d_failed, 0, sizeof(int) * nt, stream);
   norm_reset();
   {
+    // all leaves are on levels >= 1, with nc cells per side: one launch
     const int nl = (int)plan.all_leaves.size();
     BoxSet bs{d_lists + all_leaves_off, 0, nl};
     with_nc(plan.dim, plan.nc, [&](auto d_, auto nc_) {
@@ -1362,87 +1366,163 @@ int Forest::solve(const MgOpts& mg, int precision, double tol, int max_cycles, S
   }
   norm_fold();
   cudaMemcpyAsync(d_fmax, d_red, sizeof(double) * nt, cudaMemcpyDeviceToDevice, stream);
-  std::vector<double> fmax(nt);
-  cudaMemcpyAsync(fmax.data(), d_red, sizeof(double) * nt, cudaMemcpyDeviceToHost, stream);
-  cudaMemsetAsync(d_failed, 0, sizeof(int) * nt, stream);
-  cudaStreamSynchronize(stream);
-  std::vector<int> done_cycles(nt, 0);
-
-  std::vector<unsigned long long> final_r(nt, 0);
-  std::vector<int> was(nt, 1);
-  auto record = [&]() {
-    for (int t = 0; t < nt; ++t)
-      if (was[t]) final_r[t] = h_norm[t];
-    for (int t = 0; t < nt; ++t) was[t] = h_active[t];
-  };
   if (precision == AFV_PREC_MIXED) {
-    // Parents start as the restriction of their children (their values are
-    // only read by coarse leaves next to refined regions).
     for (int l = plan.max_lvl; l >= plan.min_lvl + 1; --l) restrict_res(d64, l, false);
     cudaMemsetAsync(d32.phi, 0, sizeof(float) * plan.n_elem_g, stream);  // the first correction
   }
-  enqueue_residual_check(precision, tol);
-  if (cudaStreamSynchronize(stream) != cudaSuccess) return check(err, "solve");
-  int n_active = *h_count;
-  record();
+  enqueue_residual_check(precision, tol, 0);
+  if (h) {
+    dev::k_loop_start<<<1, 1, 0, stream>>>(*h, d_count, max_cycles);
+    ++n_launches;
+  }
+}
 
-  const bool graph = use_graphs && prof_mask == 0;
-  GraphCache& gc = graphs[precision == AFV_PREC_MIXED ? 1 : 0];
-  if (graph && (gc.n_down != mg.n_down || gc.n_up != mg.n_up || gc.n_base != mg.n_base || gc.tol != tol)) {
+// Finish of a solve, enqueued only: the mixed solve's state completed
+// (parents as restrictions, ghost cells filled), every tree active again, and
+// the results copied to pinned host memory.
+void Forest::enqueue_solve_end(int precision) {
+  const int nt = plan.n_trees;
+  dev::k_set_int<<<(nt + 255) / 256, 256, 0, stream>>>(meta.active, nt, 1);
+  ++n_launches;
+  if (precision == AFV_PREC_MIXED) restrict_tree_phi64();
+  cudaMemcpyAsync(h_count, d_count, 4 * sizeof(int), cudaMemcpyDeviceToHost, stream);
+  cudaMemcpyAsync(h_cycles, d_cycles, sizeof(int) * nt, cudaMemcpyDeviceToHost, stream);
+  cudaMemcpyAsync(h_final, d_final, sizeof(unsigned long long) * nt, cudaMemcpyDeviceToHost, stream);
+  cudaMemcpyAsync(h_failed, d_failed, sizeof(int) * nt, cudaMemcpyDeviceToHost, stream);
+  cudaMemcpyAsync(h_fmax, d_fmax, sizeof(double) * nt, cudaMemcpyDeviceToHost, stream);
+}
+
+// Captures a whole solve into one graph: the set-up, a conditional while node
+// whose body is one iteration followed by k_loop_step (captured on
+// loop_stream, with side for its parallel branches), and the finish. The
+// device decides every repetition, so a solve is one launch and one host
+// synchronisation.
+int Forest::build_solve_graph(GraphCache& gc, const MgOpts& mg, int precision, double tol, int max_cycles,
+                              std::string& err) {
+  if (gc.exec) cudaGraphExecDestroy(gc.exec);
+  gc = GraphCache();
+  std::lock_guard<std::mutex> lock(g_capture_mutex);
+  cudaGraph_t top = nullptr;
+  cudaGraphConditionalHandle h = 0;
+  cudaGraphNode_t loop = nullptr;
+  cudaGraph_t body = nullptr;
+  readback = false;
+  const long long n0 = n_launches;
+  bool ok = cudaGraphCreate(&top, 0) == cudaSuccess &&
+            cudaGraphConditionalHandleCreate(&h, top, 0, cudaGraphCondAssignDefault) == cudaSuccess &&
+            cudaStreamBeginCaptureToGraph(stream, top, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed) ==
+                cudaSuccess;
+  if (ok) {
+    enqueue_solve_begin(precision, tol, max_cycles, &h);
+    gc.k_pre = n_launches - n0;
+    // the loop node after what has been captured so far
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t cg = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    const cudaGraphEdgeData* edges = nullptr;
+    size_t nd = 0;
+    ok = cudaStreamGetCaptureInfo(stream, &cs, nullptr, &cg, &deps, &edges, &nd) == cudaSuccess &&
+         cs == cudaStreamCaptureStatusActive;
+    if (ok) {
+      cudaGraphNodeParams np = {};
+      np.type = cudaGraphNodeTypeConditional;
+      np.conditional.handle = h;
+      np.conditional.type = cudaGraphCondTypeWhile;
+      np.conditional.size = 1;
+      ok = cudaGraphAddNode(&loop, cg, deps, nullptr, nd, &np) == cudaSuccess &&
+           cudaStreamUpdateCaptureDependencies(stream, &loop, nullptr, 1, cudaStreamSetCaptureDependencies) ==
+               cudaSuccess;
+      if (ok) body = np.conditional.phGraph_out[0];
+    }
+    if (ok) {
+      std::swap(stream, loop_stream);
+      ok = cudaStreamBeginCaptureToGraph(stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed) ==
+           cudaSuccess;
+      if (ok) {
+        const long long n1 = n_launches;
+        enqueue_iteration(mg, precision, tol);
+        dev::k_loop_step<<<1, 1, 0, stream>>>(h, d_count, max_cycles);
+        ++n_launches;
+        gc.k_body = n_launches - n1;
+        cudaGraph_t b = nullptr;
+        ok = cudaStreamEndCapture(stream, &b) == cudaSuccess;
+      }
+      std::swap(stream, loop_stream);
+    }
+    const long long n2 = n_launches;
+    enqueue_solve_end(precision);
+    gc.k_post = n_launches - n2;
+    cudaGraph_t t = nullptr;
+    const bool ended = cudaStreamEndCapture(stream, &t) == cudaSuccess;
+    ok = ok && ended;
+  }
+  n_launches = n0;
+  readback = true;
+  if (ok) ok = cudaGraphInstantiate(&gc.exec, top, 0) == cudaSuccess;
+  if (top) cudaGraphDestroy(top);
+  if (!ok) {
     if (gc.exec) cudaGraphExecDestroy(gc.exec);
     gc = GraphCache();
-    long long before = n_launches;
-    cudaGraph_t g = nullptr;
-    std::lock_guard<std::mutex> lock(g_capture_mutex);
-    if (cudaStreamBeginCapture(stream, cudaStreamCaptureModeRelaxed) != cudaSuccess)
-      return check(err, "graph capture");
-    enqueue_iteration(mg, precision, tol);
-    if (cudaStreamEndCapture(stream, &g) != cudaSuccess || !g) return check(err, "graph capture");
-    cudaError_t ie = cudaGraphInstantiate(&gc.exec, g, 0);
-    cudaGraphDestroy(g);
-    if (ie != cudaSuccess) return check(err, "graph instantiate");
-    gc.kernels = n_launches - before;
-    n_launches = before;
-    gc.n_down = mg.n_down;
-    gc.n_up = mg.n_up;
-    gc.n_base = mg.n_base;
-    gc.tol = tol;
+    if (int rc = check(err, "solve graph")) return rc;
+    return err = "solve graph: capture failed", AFV_ERR_CUDA;
   }
-  int cyc = 0;
-  while (n_active > 0 && cyc < max_cycles) {
-    for (int t = 0; t < nt; ++t) done_cycles[t] += h_active[t] ? 1 : 0;
-    if (graph) {
-      if (cudaGraphLaunch(gc.exec, stream) != cudaSuccess) return check(err, "graph launch");
-      n_launches += gc.kernels;
-    } else {
+  gc.n_down = mg.n_down;
+  gc.n_up = mg.n_up;
+  gc.n_base = mg.n_base;
+  gc.tol = tol;
+  gc.max_cycles = max_cycles;
+  return AFV_OK;
+}
+
+// Solve every tree to max|f - L phi| <= tol * max|f| over its leaves. With
+// graphs on (and the profiler off) the whole solve is one CUDA-graph launch,
+// captured on first use: the iterations repeat on the device (a conditional
+// while node) until no tree is active, max_cycles is reached or a bounded
+// wait gave up. Trees that have converged are masked out on the device, so the
+// graph does not change while the set of active trees shrinks. Otherwise the
+// host drives the loop, one iteration at a time.
+int Forest::solve(const MgOpts& mg, int precision, double tol, int max_cycles, SolveStats& st,
+                  std::string& err) {
+  const int nt = plan.n_trees;
+  if (precision == AFV_PREC_MIXED && !mixed)
+    return err = "forest created without mixed_buffers", AFV_ERR_STATE;
+  st.cycles.assign(nt, 0);
+  st.rel_res.assign(nt, 0.0);
+  const bool graph = use_graphs && prof_mask == 0;
+  if (graph) {
+    GraphCache& gc = graphs[precision == AFV_PREC_MIXED ? 1 : 0];
+    if (!gc.exec || gc.n_down != mg.n_down || gc.n_up != mg.n_up || gc.n_base != mg.n_base || gc.tol != tol ||
+        gc.max_cycles != max_cycles)
+      if (int rc = build_solve_graph(gc, mg, precision, tol, max_cycles, err)) return rc;
+    if (cudaGraphLaunch(gc.exec, stream) != cudaSuccess) return check(err, "graph launch");
+    if (cudaStreamSynchronize(stream) != cudaSuccess) return check(err, "solve");
+    n_launches += gc.k_pre + gc.k_post + gc.k_body * h_count[2];
+  } else {
+    enqueue_solve_begin(precision, tol, max_cycles, nullptr);
+    if (cudaStreamSynchronize(stream) != cudaSuccess) return check(err, "solve");
+    int cyc = 0;
+    while (h_count[0] > 0 && cyc < max_cycles && !h_count[1]) {
       if (prof_mask && prof_lead_us > 0) dev::k_hold<<<1, 1, 0, stream>>>(1000LL * prof_lead_us);
       enqueue_iteration(mg, precision, tol);
+      if (cudaStreamSynchronize(stream) != cudaSuccess) return check(err, "solve");
+      ++cyc;
+      if (int rc = check(err, "solve")) return rc;
     }
+    enqueue_solve_end(precision);
     if (cudaStreamSynchronize(stream) != cudaSuccess) return check(err, "solve");
-    n_active = *h_count;
-    record();
-    ++cyc;
-    if (int rc = check(err, "solve")) return rc;
-    if (int rc = check_device_error(err)) return rc;
   }
-  if (precision == AFV_PREC_MIXED) {
-    // Complete state: parents as restrictions, ghost cells filled.
-    set_active_all(1);
-    restrict_tree_phi64();
-  }
-  set_active_all(1);
+  host_active.assign(nt, 1);
+  if (int rc = check(err, "solve")) return rc;
+  if (h_count[1]) return check_device_error(err);  // a bounded wait gave up
+  int n_failed = 0;
   for (int t = 0; t < nt; ++t) {
     double r;
-    std::memcpy(&r, &final_r[t], sizeof(double));
-    st.cycles[t] = done_cycles[t];
-    st.rel_res[t] = fmax[t] > 0 ? r / fmax[t] : r;
+    std::memcpy(&r, &h_final[t], sizeof(double));
+    st.cycles[t] = h_cycles[t];
+    st.rel_res[t] = h_fmax[t] > 0 ? r / h_fmax[t] : r;
+    n_failed += h_failed[t] != 0;
   }
-  if (int rc = check(err, "solve")) return rc;
-  std::vector<int> failed(nt, 0);
-  cudaMemcpyAsync(failed.data(), d_failed, sizeof(int) * nt, cudaMemcpyDeviceToHost, stream);
-  cudaStreamSynchronize(stream);
-  int n_failed = 0;
-  for (int t = 0; t < nt; ++t) n_failed += failed[t] != 0;
+  const int n_active = h_count[0];
   st.status = n_failed ? AFV_ERR_DIVERGED : n_active > 0 ? AFV_ERR_TIMEOUT : AFV_OK;
   if (n_failed)
     err = std::to_string(n_failed) + " tree(s) diverged (non-finite residual)";
