@@ -58,3 +58,20 @@ def test_mg_init_defaults(afv):
     mg = afv.MgOpts()
     afv._check(afv.lib().afv_mg_init(ctypes.byref(mg)))
     assert (mg.n_cycle_down, mg.n_cycle_up, mg.n_cycle_base) == (2, 2, 2)
+
+
+def test_python_constants_match_the_header(afv):
+    """Every enumerator the header gives a value has the same value in the
+    Python module, and the profiler's kernel kinds are in the header's order."""
+    text = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
+    values = {n: int(v) for n, v in re.findall(r"\b(AFV_[A-Z0-9_]+)\s*=\s*(-?\d+)", text)}
+    assert len(values) >= 30
+    kinds = {n: v for n, v in values.items() if n.startswith("AFV_KERNEL_")}
+    for n, v in values.items():
+        if n in kinds:
+            continue
+        assert hasattr(afv, n), n
+        assert getattr(afv, n) == v, (n, getattr(afv, n), v)
+    assert len(afv.KERNEL_KINDS) == len(kinds)
+    for n, v in kinds.items():
+        assert afv.KERNEL_KINDS[v] == n[len("AFV_KERNEL_"):].lower(), (n, v)
