@@ -1,7 +1,7 @@
 // ORACLE — test infrastructure only. Nothing in the afivo_gb300 product links,
 // loads or calls this file; only tests/, __graft_entry__.smoke() and the
-// cpu_baseline / --impl reference legs of bench.py use it, as the checker and
-// as the timed CPU baseline.
+// cpu_baseline / --impl reference legs of bench.py use it, to check the GPU
+// results and as the timed CPU baseline.
 //
 // A C++17 + OpenMP restatement of the Afivo reference's quadtree/octree build
 // and its FAS multigrid hot path. Both dimensions come from one template, the

@@ -1,7 +1,7 @@
 """ctypes wrapper of the CPU oracle (oracle/afivo_oracle.cpp).
 
 Test infrastructure only: tests/, __graft_entry__.smoke() and the CPU legs of
-bench.py import this module, as the checker and the timed CPU baseline. The
+bench.py import this module, to check the GPU results and as the timed CPU baseline. The
 afivo_gb300 product never imports it.
 
 The oracle restates the Afivo reference's tree build (src/m_aX_core.f90,
