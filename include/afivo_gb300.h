@@ -258,8 +258,9 @@ int afv_forest_profile_read(afv_forest* f, int kind, long long* launches, double
 /* No counterpart in the reference: tuning switches of a forest (the
  * autotuner sets them). AFV_OPT_SWEEP_KERNEL: 0 block-pipelined level kernel,
  * 1 warp-per-box kernel with bulk copies (default), 2 warp-per-box kernel with
- * per-lane asynchronous copies. AFV_OPT_GRAPHS: 1 (default) replays solve
- * iterations as CUDA graphs, 0 launches them one by one.
+ * per-lane asynchronous copies. AFV_OPT_GRAPHS: 1 (default) runs each solve as
+ * one CUDA graph (its iterations repeated on the device), 0 launches the
+ * kernels one by one with the host deciding every iteration.
  * AFV_OPT_RESTRICT_KERNEL: 1 (default) warp-per-box kernels for the residual
  * restriction (levels >= 2), the coarse right-hand side (levels >= 1) and the
  * correction of children on levels >= 2, 0 the block-staged kernels. AFV_OPT_SMALL_SWEEPS: 1 (default) runs all
