@@ -175,6 +175,41 @@ def test_periodic_uniform_2d(gpu):
         assert_state(gpu, f, ot, spec)
 
 
+def _uniform_3d(lvl, periodic):
+    return dict(name="uniform3d_nc8_lvl%d" % lvl, dim=3, n_cell=8, coarsen_to=2, dr=1 / 8,
+                ix=[[1, 1, 1]], nb=[[1] * 6] if periodic else [[-1] * 6], gauss=None, lpl=False,
+                crit=W.AFV_REF_UNIFORM, thr=0.0, lvl_max=lvl, bc=W.AFV_BC_DIRICHLET)
+
+
+def test_periodic_uniform_3d(gpu):
+    """3-D, the base box its own neighbour on all six faces."""
+    spec = _uniform_3d(4, periodic=True)
+    f, ot, _ = setup_pair(gpu, spec)
+    for _ in range(3):
+        ot.vcycle()
+        f.vcycle()
+        assert_state(gpu, f, ot, spec)
+
+
+def test_neumann_3d(gpu):
+    spec = _uniform_3d(4, periodic=False)
+    ot = oracle_tree(spec)
+    pt = W.build_tree(spec)
+    rng = np.random.default_rng(11)
+    for l in range(ot.min_lvl, ot.highest_lvl + 1):
+        a = ot.get_level(l, O.I_RHS, 8).copy()
+        a[...] = rng.standard_normal(a.shape)
+        ot.set_level(l, O.I_RHS, a)
+    ot.mg_init(bc_kind=O.BC_NEUMANN_ZERO)
+    f = gpu.Forest([pt])
+    f.set_var(0, gpu.AFV_RHS, oracle_var(ot, O.I_RHS, 8))
+    f.set_bc(0, gpu.AFV_BC_NEUMANN)
+    for _ in range(3):
+        ot.vcycle()
+        f.vcycle()
+        assert_state(gpu, f, ot, spec)
+
+
 def test_forest_matches_single_trees(gpu):
     """Several trees of different depth in one forest give, per tree, the same
     bits as the tree alone and the oracle's values."""
