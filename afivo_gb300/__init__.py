@@ -34,7 +34,7 @@ LIB_PATH = os.path.join(_HERE, "_lib", "libafivo_gb300.so")
 AFV_OK = 0
 AFV_ERR_INVALID, AFV_ERR_CUDA, AFV_ERR_NOMEM = -1, -2, -3
 AFV_ERR_UNSUPPORTED, AFV_ERR_TIMEOUT, AFV_ERR_STATE, AFV_ERR_BUDGET = -4, -5, -6, -7
-AFV_ERR_DIVERGED = -8
+AFV_ERR_DIVERGED, AFV_ERR_NOT_CONVERGED = -8, -9
 AFV_RM_REF, AFV_KEEP_REF, AFV_DO_REF = -1, 0, 1
 AFV_PHI, AFV_RHS, AFV_TMP = 0, 1, 2
 AFV_BC_DIRICHLET, AFV_BC_NEUMANN = -1, -2
@@ -42,6 +42,7 @@ AFV_REF_UNIFORM, AFV_REF_SOURCE, AFV_REF_RANDOM, AFV_REF_RANDOM_RM = 0, 1, 2, 3
 AFV_PREC_FP64, AFV_PREC_MIXED = 0, 1
 AFV_OPT_SWEEP_KERNEL, AFV_OPT_GRAPHS, AFV_OPT_RESTRICT_KERNEL, AFV_OPT_SMALL_SWEEPS = 0, 1, 2, 3
 AFV_OPT_PROFILE_LEAD_US, AFV_OPT_DEFECT_KERNEL, AFV_OPT_COARSE_END = 4, 5, 6
+AFV_OPT_WAIT_LIMIT_US = 7
 KERNEL_KINDS = ("sweep", "fill", "restrict", "coarse_rhs", "correct", "residual", "defect",
                 "accumulate", "coarse_end")
 

@@ -36,6 +36,9 @@ struct DevMeta {
   long long* nbo2 = nullptr;
   int* err = nullptr;  // device error word (bounded waits)
   double* rmin = nullptr;  // [slot*D + d] lower corner of the box
+  // clock cycles a kernel's wait for one of its copies may take before it
+  // gives up (AFV_OPT_WAIT_LIMIT_US; about two seconds by default)
+  long long wait_limit = 4000000000LL;
 };
 
 struct MgOpts {

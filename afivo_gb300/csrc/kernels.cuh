@@ -44,6 +44,8 @@ struct Meta {
   const SlotDesc* desc;    // [slot]
   const long long* nbo2;   // [slot*2D + face] refinement boundary: offg of the parent's neighbour
   int* err;                // device error word: nonzero after a bounded wait gave up
+  long long wait_limit;    // clock cycles a wait for a copy may take before it gives up;
+                           // <= 0: give up at once (exercises the error path)
 };
 
 __device__ __forceinline__ int box_at(const BoxSet& s, int i) { return s.list ? s.list[i] : s.lo + i; }
@@ -214,10 +216,14 @@ __device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.lau
 
 // ---------------------------------------------------------------------------
 // Bulk copies (TMA, cp.async.bulk) into shared memory, completed on mbarriers.
-// Every wait is bounded by a clock budget; a kernel that gives up records it in
-// the error word and drains its own copies before it returns.
+// Every wait is bounded by a clock budget (Meta::wait_limit, set per forest);
+// a kernel that gives up records it in the error word and drains its own
+// copies before it returns. The drain waits with the fixed kDrainLimitCycles,
+// so that a short (or zero) wait limit still lets every copy in flight land
+// before the block's shared memory is released.
 // ---------------------------------------------------------------------------
-constexpr long long kWaitLimitCycles = 4000000000LL;  // about two seconds
+constexpr long long kWaitLimitCycles = 4000000000LL;   // default limit, about two seconds
+constexpr long long kDrainLimitCycles = 4000000000LL;  // drain after giving up
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -265,10 +271,12 @@ __device__ __forceinline__ bool mbar_test(unsigned long long* bar, unsigned pari
       : "memory");
   return ok != 0;
 }
-__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned parity) {
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned parity,
+                                                  long long limit) {
+  if (limit <= 0) return false;
   const long long t0 = clock64();
   while (!mbar_test(bar, parity)) {
-    if (clock64() - t0 > kWaitLimitCycles) return false;
+    if (clock64() - t0 > limit) return false;
   }
   return true;
 }
@@ -479,7 +487,7 @@ k_level_tma(Meta m, BoxSet bs, T* __restrict__ phi, const T* __restrict__ rhs, i
       ++issued;
     }
     if (k + 1 < my_groups) {
-      if (mbar_wait_bounded(&bar[(k + 1) % S], ((k + 1) / S) & 1))
+      if (mbar_wait_bounded(&bar[(k + 1) % S], ((k + 1) / S) & 1, m.wait_limit))
         prefetch(k + 1, nxt, nxt_act);
       else
         s_abort = 1;
@@ -550,12 +558,12 @@ k_level_tma(Meta m, BoxSet bs, T* __restrict__ phi, const T* __restrict__ rhs, i
 
   T ra[C::ITEMS], rb[C::ITEMS];
   int act_a = 0, act_b = 0;
-  bool ok = mbar_wait_bounded(&bar[0], 0);
+  bool ok = mbar_wait_bounded(&bar[0], 0, m.wait_limit);
   if (ok) prefetch(0, ra, act_a);
   if (__syncthreads_or(!ok)) {
     if (threadIdx.x == 0) {
       atomicExch(m.err, 1);
-      for (int k = 0; k < issued; ++k) mbar_wait_bounded(&bar[k % S], (k / S) & 1);
+      for (int k = 0; k < issued; ++k) mbar_wait_bounded(&bar[k % S], (k / S) & 1, kDrainLimitCycles);
     }
     return;
   }
@@ -569,7 +577,7 @@ k_level_tma(Meta m, BoxSet bs, T* __restrict__ phi, const T* __restrict__ rhs, i
   }
   if (k < my_groups && threadIdx.x == 0) {  // gave up: drain this block's copies
     atomicExch(m.err, 1);
-    for (int j = k + 1; j < issued; ++j) mbar_wait_bounded(&bar[j % S], (j / S) & 1);
+    for (int j = k + 1; j < issued; ++j) mbar_wait_bounded(&bar[j % S], (j / S) & 1, kDrainLimitCycles);
   }
 }
 
@@ -769,7 +777,7 @@ k_sweep_warp(Meta m, BoxSet bs, T* __restrict__ phi, const T* __restrict__ rhs, 
       cp_async_wait<S - 1>();  // box k's group has landed
       __syncwarp();
     } else {
-      const bool ok = mbar_wait_bounded(&bar[wid][k % S], (k / S) & 1);
+      const bool ok = mbar_wait_bounded(&bar[wid][k % S], (k / S) & 1, m.wait_limit);
       if (!__all_sync(0xffffffffu, ok)) return false;
     }
     unsigned char* sp = stage(k);
@@ -866,7 +874,7 @@ k_sweep_warp(Meta m, BoxSet bs, T* __restrict__ phi, const T* __restrict__ rhs, 
     cp_async_wait<0>();
   } else if (!ok && lane == 0) {  // gave up at box k: drain this warp's copies from box k on
     atomicExch(m.err, 1);
-    for (int j = k; j < issued; ++j) mbar_wait_bounded(&bar[wid][j % S], (j / S) & 1);
+    for (int j = k; j < issued; ++j) mbar_wait_bounded(&bar[wid][j % S], (j / S) & 1, kDrainLimitCycles);
   }
 }
 
@@ -1013,7 +1021,7 @@ k_restrict_warp(Meta m, BoxSet bs, T* __restrict__ phi, const T* __restrict__ rh
     if (lane == 0 && k + S - 1 < my_boxes) issue(k + S - 1);
     bool ok = true;
     if (k + 1 < my_boxes) {
-      ok = mbar_wait_bounded(&bar[wid][(k + 1) % S], ((k + 1) / S) & 1);
+      ok = mbar_wait_bounded(&bar[wid][(k + 1) % S], ((k + 1) / S) & 1, m.wait_limit);
       if (ok) fetch(k + 1, g1, r1, po1, a1);
     }
     if (!__all_sync(0xffffffffu, ok)) return false;
@@ -1084,7 +1092,7 @@ k_restrict_warp(Meta m, BoxSet bs, T* __restrict__ phi, const T* __restrict__ rh
   long long pa = 0, pb = 0;
   int aa = 0, ab = 0;
   fetch(0, ga, ra, pa, aa);  // from the staged descriptor, beside the cells' copy
-  bool ok = mbar_wait_bounded(&bar[wid][0], 0);
+  bool ok = mbar_wait_bounded(&bar[wid][0], 0, m.wait_limit);
   int k = 0, pending = 0;
   if (__all_sync(0xffffffffu, ok)) {
     for (; k < my_boxes; k += 2) {
@@ -1098,7 +1106,7 @@ k_restrict_warp(Meta m, BoxSet bs, T* __restrict__ phi, const T* __restrict__ rh
   }
   if (k < my_boxes && lane == 0) {  // gave up: drain this warp's copies
     atomicExch(m.err, 1);
-    for (int j = pending; j < issued; ++j) mbar_wait_bounded(&bar[wid][j % S], (j / S) & 1);
+    for (int j = pending; j < issued; ++j) mbar_wait_bounded(&bar[wid][j % S], (j / S) & 1, kDrainLimitCycles);
   }
 }
 
@@ -1213,7 +1221,7 @@ k_coarse_warp(Meta m, BoxSet bs, T* __restrict__ phi, T* __restrict__ rhs, T* __
     if (lane == 0 && k + S - 1 < my_boxes) issue(k + S - 1);
     bool ok = true;
     if (k + 1 < my_boxes) {
-      ok = mbar_wait_bounded(&bar[wid][(k + 1) % S], ((k + 1) / S) & 1);
+      ok = mbar_wait_bounded(&bar[wid][(k + 1) % S], ((k + 1) / S) & 1, m.wait_limit);
       if (ok) fetch(k + 1, g1, t1, a1);
     }
     if (!__all_sync(0xffffffffu, ok)) return false;
@@ -1270,7 +1278,7 @@ k_coarse_warp(Meta m, BoxSet bs, T* __restrict__ phi, T* __restrict__ rhs, T* __
   T ga[C::GPL], gb[C::GPL], ta[C::CPL], tb[C::CPL];
   int aa = 0, ab = 0;
   fetch(0, ga, ta, aa);  // from the staged descriptor, beside the cells' copy
-  bool ok = mbar_wait_bounded(&bar[wid][0], 0);
+  bool ok = mbar_wait_bounded(&bar[wid][0], 0, m.wait_limit);
   int k = 0, pending = 0;
   if (__all_sync(0xffffffffu, ok)) {
     for (; k < my_boxes; k += 2) {
@@ -1284,7 +1292,7 @@ k_coarse_warp(Meta m, BoxSet bs, T* __restrict__ phi, T* __restrict__ rhs, T* __
   }
   if (k < my_boxes && lane == 0) {  // gave up: drain this warp's copies
     atomicExch(m.err, 1);
-    for (int j = pending; j < issued; ++j) mbar_wait_bounded(&bar[wid][j % S], (j / S) & 1);
+    for (int j = pending; j < issued; ++j) mbar_wait_bounded(&bar[wid][j % S], (j / S) & 1, kDrainLimitCycles);
   }
 }
 
@@ -1487,7 +1495,7 @@ k_correct_warp(Meta m, BoxSet bs, T* __restrict__ phi, T* __restrict__ tmp, int 
     if (lane == 0 && k + S - 1 < my_boxes) issue(k + S - 1);
     bool ok = true;
     if (k + 1 < my_boxes) {
-      ok = mbar_wait_bounded(&bar[wid][(k + 1) % S], ((k + 1) / S) & 1);
+      ok = mbar_wait_bounded(&bar[wid][(k + 1) % S], ((k + 1) / S) & 1, m.wait_limit);
       if (ok) fetch(k + 1, g1, co1, a1);
     }
     if (!__all_sync(0xffffffffu, ok)) return false;
@@ -1567,7 +1575,7 @@ k_correct_warp(Meta m, BoxSet bs, T* __restrict__ phi, T* __restrict__ tmp, int 
   long long oa = 0, ob = 0;
   int aa = 0, ab = 0;
   fetch(0, ga, oa, aa);  // from the staged descriptor, beside the cells' copy
-  bool ok = mbar_wait_bounded(&bar[wid][0], 0);
+  bool ok = mbar_wait_bounded(&bar[wid][0], 0, m.wait_limit);
   int k = 0, pending = 0;
   if (__all_sync(0xffffffffu, ok)) {
     for (; k < my_boxes; k += 2) {
@@ -1581,7 +1589,7 @@ k_correct_warp(Meta m, BoxSet bs, T* __restrict__ phi, T* __restrict__ tmp, int 
   }
   if (k < my_boxes && lane == 0) {  // gave up: drain this warp's copies
     atomicExch(m.err, 1);
-    for (int j = pending; j < issued; ++j) mbar_wait_bounded(&bar[wid][j % S], (j / S) & 1);
+    for (int j = pending; j < issued; ++j) mbar_wait_bounded(&bar[wid][j % S], (j / S) & 1, kDrainLimitCycles);
   }
 }
 

@@ -2,8 +2,8 @@
 // memory: the same reduction as Forest::max_abs (the GPU form of
 // a$D_tree_max_cc, src/m_aX_utils.f90:468-519), for callers that must not
 // allocate. Its scratch is a file-scope __device__ array; its address is taken
-// once per device with cudaGetSymbolAddress, and every call clears what it
-// uses with cudaMemsetAsync. Nothing here calls an allocating routine.
+// with cudaGetSymbolAddress once per device and context (again after a device
+// reset), and every call clears what it uses with cudaMemsetAsync. Nothing here calls an allocating routine.
 // Included at the end of solver.cu (one translation unit for the kernels).
 #pragma once
 #include <cstring>
@@ -34,13 +34,45 @@ struct StaticScratch {
 constexpr int kMaxDevices = 64;
 std::mutex g_setup_mutex;
 bool g_ready[kMaxDevices] = {};
+unsigned long long g_ctx_id[kMaxDevices] = {};
 StaticScratch g_scratch[kMaxDevices];
 
-// Address of the static scratch on the current device (set up on first use).
+// Unique id of the calling thread's current CUDA context (cuCtxGetId through
+// the runtime's driver entry points, so the library links no driver library).
+// A device reset or a rebuilt primary context gets a new id, and with it the
+// module's static arrays may sit at new addresses.
+int current_context_id(unsigned long long& id, std::string& err) {
+  typedef int (*CtxGetCurrent)(void**);
+  typedef int (*CtxGetId)(void*, unsigned long long*);
+  static CtxGetCurrent get_current = nullptr;
+  static CtxGetId get_id = nullptr;
+  if (!get_current || !get_id) {
+    void* a = nullptr;
+    void* b = nullptr;
+    cudaDriverEntryPointQueryResult qa, qb;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &a, 12000, cudaEnableDefault, &qa) != cudaSuccess ||
+        cudaGetDriverEntryPointByVersion("cuCtxGetId", &b, 12000, cudaEnableDefault, &qb) != cudaSuccess ||
+        qa != cudaDriverEntryPointSuccess || qb != cudaDriverEntryPointSuccess || !a || !b)
+      return err = "cuCtxGetCurrent / cuCtxGetId not available", AFV_ERR_CUDA;
+    get_current = reinterpret_cast<CtxGetCurrent>(a);
+    get_id = reinterpret_cast<CtxGetId>(b);
+  }
+  void* ctx = nullptr;
+  if (get_current(&ctx) != 0 || !ctx || get_id(ctx, &id) != 0)
+    return err = "no current CUDA context", AFV_ERR_CUDA;
+  return AFV_OK;
+}
+
+// Address of the static scratch in the current context (device `device` is
+// current). Taken with cudaGetSymbolAddress the first time a context uses it
+// and again whenever the context changes; the cached addresses serve every
+// other call.
 int static_scratch(int device, StaticScratch& out, std::string& err) {
   if (device < 0 || device >= kMaxDevices) return err = "device ordinal out of range", AFV_ERR_INVALID;
   std::lock_guard<std::mutex> lock(g_setup_mutex);
-  if (!g_ready[device]) {
+  unsigned long long ctx = 0;
+  if (int rc = current_context_id(ctx, err)) return rc;
+  if (!g_ready[device] || g_ctx_id[device] != ctx) {
     StaticScratch s;
     cudaError_t e1 = cudaGetSymbolAddress((void**)&s.stripes, g_stripes);
     cudaError_t e2 = cudaGetSymbolAddress((void**)&s.red, g_red);
@@ -50,6 +82,7 @@ int static_scratch(int device, StaticScratch& out, std::string& err) {
       return err = std::string("cudaGetSymbolAddress failed: ") + cudaGetErrorString(e), AFV_ERR_CUDA;
     }
     g_scratch[device] = s;
+    g_ctx_id[device] = ctx;
     g_ready[device] = true;
   }
   out = g_scratch[device];
@@ -104,6 +137,7 @@ int Forest::max_abs_static(int t, int var, double* out, std::string& err) {
   m.desc = meta.desc;
   m.nbo2 = meta.nbo2;
   m.err = meta.err;
+  m.wait_limit = meta.wait_limit;
   const double* v = var == AFV_PHI ? d64.phi : var == AFV_RHS ? d64.rhs : d64.tmp;
   for (int l = plan.min_lvl; l <= plan.max_lvl; ++l) {
     int nl = n_leaves(l);

@@ -56,6 +56,7 @@ static Meta meta_of(const DevMeta& d) {
   m.desc = d.desc;
   m.nbo2 = d.nbo2;
   m.err = d.err;
+  m.wait_limit = d.wait_limit;
   return m;
 }
 
@@ -1523,7 +1524,7 @@ int Forest::solve(const MgOpts& mg, int precision, double tol, int max_cycles, S
     n_failed += h_failed[t] != 0;
   }
   const int n_active = h_count[0];
-  st.status = n_failed ? AFV_ERR_DIVERGED : n_active > 0 ? AFV_ERR_TIMEOUT : AFV_OK;
+  st.status = n_failed ? AFV_ERR_DIVERGED : n_active > 0 ? AFV_ERR_NOT_CONVERGED : AFV_OK;
   if (n_failed)
     err = std::to_string(n_failed) + " tree(s) diverged (non-finite residual)";
   else if (n_active > 0)

@@ -16,6 +16,7 @@ module m_afivo_gb300
   integer(c_int), parameter :: AFV_ERR_STATE = -6
   integer(c_int), parameter :: AFV_ERR_BUDGET = -7
   integer(c_int), parameter :: AFV_ERR_DIVERGED = -8
+  integer(c_int), parameter :: AFV_ERR_NOT_CONVERGED = -9
 
   integer(c_int), parameter :: AFV_RM_REF = -1, AFV_KEEP_REF = 0, AFV_DO_REF = 1
   integer(c_int), parameter :: AFV_PHI = 0, AFV_RHS = 1, AFV_TMP = 2

@@ -38,10 +38,12 @@ enum {
   AFV_ERR_CUDA = -2,        /* a CUDA runtime call failed                */
   AFV_ERR_NOMEM = -3,       /* host or device allocation failed          */
   AFV_ERR_UNSUPPORTED = -4, /* valid request this build does not support */
-  AFV_ERR_TIMEOUT = -5,     /* a bounded device wait gave up             */
+  AFV_ERR_TIMEOUT = -5,     /* a bounded device wait gave up (the device
+                               error word was set; it is cleared on report) */
   AFV_ERR_STATE = -6,       /* call out of order (e.g. before set_base)  */
   AFV_ERR_BUDGET = -7,      /* over the memory budget (box_limit, HBM)   */
-  AFV_ERR_DIVERGED = -8     /* a solve produced a non-finite residual    */
+  AFV_ERR_DIVERGED = -8,    /* a solve produced a non-finite residual    */
+  AFV_ERR_NOT_CONVERGED = -9 /* a solve ran max_cycles without reaching tol */
 };
 
 /* Refinement flags, src/m_aX_t.f90:17-24. */
@@ -203,7 +205,8 @@ int afv_tree_max_abs_cc(afv_forest* f, int tree, int var, double* out);
  * bytes per device, which limits it to forests of at most 1024 trees
  * (larger ones get AFV_ERR_INVALID). The first call on a device takes the
  * array's address (cudaGetSymbolAddress) and should come before any stream
- * capture; every call clears the scratch it uses on the forest's stream.
+ * capture; so does the first call after a device reset, which takes it
+ * again. Every call clears the scratch it uses on the forest's stream.
  * Calls that overlap in time on one device (two host threads, or two forests
  * on different streams) share the scratch and race: serialise them. For
  * callers that cannot allocate at the time of the call: a request loop whose
@@ -215,8 +218,9 @@ int afv_tree_max_abs_cc_noalloc(afv_forest* f, int tree, int var, double* out);
  * from the current phi, with FP64 V-cycles (AFV_PREC_FP64) or FP64 defect
  * correction around FP32 V-cycles (AFV_PREC_MIXED). cycles[t] and rel_res[t]
  * (n_trees entries, may be NULL) receive per-tree results. Returns
- * AFV_ERR_TIMEOUT if a tree is not converged after max_cycles and
- * AFV_ERR_DIVERGED if a tree's residual stopped being finite. */
+ * AFV_ERR_NOT_CONVERGED if a tree is not converged after max_cycles,
+ * AFV_ERR_DIVERGED if a tree's residual stopped being finite, and
+ * AFV_ERR_TIMEOUT if a bounded device wait gave up during the solve. */
 int afv_mg_solve(afv_forest* f, const afv_mg_opts* mg, int precision, double tol, int max_cycles,
                  int* cycles, double* rel_res);
 
@@ -274,7 +278,12 @@ int afv_forest_profile_read(afv_forest* f, int kind, long long* launches, double
  * (0). AFV_OPT_SWEEP_KERNEL 3..5 are other warp and stage counts of 1.
  * AFV_OPT_COARSE_END: 1 (default) runs the mixed solve's correction cycle on
  * levels <= 1 (one box per tree each) in one launch, one block per tree;
- * 0 launches its operators one by one. */
+ * 0 launches its operators one by one. AFV_OPT_WAIT_LIMIT_US: how long
+ * (microseconds, default 2000000) a kernel waits for one of its own copies
+ * into shared memory before it gives up, sets the device error word and
+ * returns once its copies in flight have landed; the call then reports
+ * AFV_ERR_TIMEOUT and clears the word. 0 makes every such wait give up at
+ * once, which exercises that path without a stuck copy. */
 enum {
   AFV_OPT_SWEEP_KERNEL = 0,
   AFV_OPT_GRAPHS = 1,
@@ -282,7 +291,8 @@ enum {
   AFV_OPT_SMALL_SWEEPS = 3,
   AFV_OPT_PROFILE_LEAD_US = 4,
   AFV_OPT_DEFECT_KERNEL = 5,
-  AFV_OPT_COARSE_END = 6
+  AFV_OPT_COARSE_END = 6,
+  AFV_OPT_WAIT_LIMIT_US = 7
 };
 int afv_forest_set_option(afv_forest* f, int option, int value);
 int afv_forest_get_option(afv_forest* f, int option, int* value);

@@ -96,3 +96,51 @@ def setup_pair(afv, spec, mixed=False, bc_gauss=False):
     if bc_gauss:
         f.set_bc(0, afv.AFV_BC_DIRICHLET, gauss=spec["gauss"], lpl=False)
     return f, ot, pt
+
+
+def leaf_interiors(flat, t, n_cell, dim):
+    """Interior values of the leaves only, concatenated over the levels, from
+    a ghosted host-layout array (boxes in level-list order)."""
+    boxes = split_boxes(flat, t, n_cell, dim)
+    parts = []
+    for l, arr in boxes.items():
+        ids, leaves, _ = t.level(l)
+        if not len(leaves):
+            continue
+        nc = n_cell if l >= 1 else n_cell >> (1 - l)
+        rows = np.isin(ids, leaves)
+        parts.append(arr[rows][:, interior_mask(nc, dim)].ravel())
+    return np.concatenate(parts) if parts else np.zeros(0)
+
+
+def leaf_error(gpu_flat, ora_flat, t, n_cell, dim):
+    """max |gpu - oracle| over leaf interiors / max |oracle| there: the error
+    of a solution against the oracle's, relative to the solution's size."""
+    g = leaf_interiors(gpu_flat, t, n_cell, dim)
+    o = leaf_interiors(ora_flat, t, n_cell, dim)
+    return float(np.abs(g - o).max() / max(np.abs(o).max(), 1e-300))
+
+
+def oracle_solve(ot, tol, max_cycles=80):
+    """The reference's solve loop (examples/poisson_basic_2d.f90:84-92) on the
+    oracle: V-cycles with the residual until max |r| <= tol * max |f| over the
+    leaves; returns the number of V-cycles."""
+    fmax = ot.max_abs(O.I_RHS)
+    ot.residual_all()
+    n = 0
+    while ot.max_abs_residual() > tol * fmax and n < max_cycles:
+        ot.vcycle(set_residual=True)
+        n += 1
+    return n
+
+
+def same_tree(a, o):
+    """The library's host tree equals the oracle's bit for bit: per-id
+    topology (lvl, ix, parent, children, neighbours, n_cell, dr, r_min,
+    in_use) and the level lists (ids, leaves, parents)."""
+    ba, bo = a.boxes(), o.boxes()
+    for k in bo:
+        assert np.array_equal(ba[k], bo[k]), k
+    for l in range(o.min_lvl, o.highest_lvl + 2):
+        for x, y in zip(a.level(l), o.level(l)):
+            assert np.array_equal(x, y), l

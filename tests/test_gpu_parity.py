@@ -6,7 +6,7 @@ import numpy as np
 import pytest
 
 import oracle as O
-from helpers import compare_var, oracle_tree, oracle_var, setup_pair
+from helpers import compare_var, oracle_solve, oracle_tree, oracle_var, setup_pair
 from afivo_gb300 import workloads as W
 
 pytestmark = pytest.mark.gpu
@@ -477,3 +477,44 @@ def test_pinned_host_exchange(gpu):
             assert np.array_equal(back, src.numpy())
         else:
             assert np.array_equal(back, src.numpy())
+
+
+def test_wait_limit_error_path(gpu):
+    """A wait limit of 0 makes every kernel's wait for its own copies give up
+    at once: the kernels set the device error word and return after their
+    copies in flight have landed, the solve stops and reports AFV_ERR_TIMEOUT
+    and the word is cleared. With the default limit back, the next solve
+    succeeds and matches the oracle, bit for bit in FP64."""
+    spec = W.c2_poisson_3d(thr=3e-3, lvl_max=5)
+    f, ot, _ = setup_pair(gpu, spec, mixed=True)
+    default = f.get_option(gpu.AFV_OPT_WAIT_LIMIT_US)
+    assert default == 2000000
+    for prec in (gpu.AFV_PREC_MIXED, gpu.AFV_PREC_FP64):
+        f.set_option(gpu.AFV_OPT_WAIT_LIMIT_US, 0)
+        cyc, rel, rc = f.solve(prec, tol=1e-8, max_cycles=5, check=False)
+        assert rc == gpu.AFV_ERR_TIMEOUT, rc
+        with pytest.raises(gpu.AfivoError) as e:
+            f.vcycle()
+        assert e.value.code == gpu.AFV_ERR_TIMEOUT
+        f.set_option(gpu.AFV_OPT_WAIT_LIMIT_US, default)
+        f.zero(gpu.AFV_PHI)
+        f.zero(gpu.AFV_TMP)
+        cyc, rel, rc = f.solve(prec, tol=1e-8, max_cycles=40)
+        assert rc == 0 and rel[0] <= 1e-8
+    # FP64 solve from zero again, against the oracle's loop
+    n = oracle_solve(ot, 1e-8)
+    f.zero(gpu.AFV_PHI)
+    f.zero(gpu.AFV_TMP)
+    cyc, rel, rc = f.solve(gpu.AFV_PREC_FP64, tol=1e-8, max_cycles=40)
+    assert rc == 0 and int(cyc[0]) == n
+    assert compare_var(f.get_var(0, gpu.AFV_PHI), oracle_var(ot, O.I_PHI, 8), ot, 8, 3, False) <= TOL
+
+
+def test_not_converged_is_its_own_code(gpu):
+    """Running out of cycles is AFV_ERR_NOT_CONVERGED, not a timeout."""
+    spec = W.c1_poisson_2d()
+    f, ot, _ = setup_pair(gpu, spec, mixed=True)
+    for prec in (gpu.AFV_PREC_MIXED, gpu.AFV_PREC_FP64):
+        f.zero(gpu.AFV_PHI)
+        cyc, rel, rc = f.solve(prec, tol=1e-8, max_cycles=2, check=False)
+        assert rc == gpu.AFV_ERR_NOT_CONVERGED and int(cyc[0]) == 2 and rel[0] > 1e-8

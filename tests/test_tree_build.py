@@ -6,7 +6,7 @@ import numpy as np
 import pytest
 
 import oracle as O
-from helpers import oracle_tree
+from helpers import oracle_tree, same_tree
 from afivo_gb300 import workloads as W
 
 
@@ -38,15 +38,6 @@ def check_invariants(t):
                     ix = b["ix"][cid - 1]
                     ic = nch - sum((int(ix[d]) & 1) << d for d in range(dim))
                     assert ic == c + 1
-
-
-def same_tree(a, o):
-    ba, bo = a.boxes(), o.boxes()
-    for k in bo:
-        assert np.array_equal(ba[k], bo[k]), k
-    for l in range(o.min_lvl, o.highest_lvl + 2):
-        for x, y in zip(a.level(l), o.level(l)):
-            assert np.array_equal(x, y), l
 
 
 SPECS = [W.c1_poisson_2d(), W.c3_uniform_2d(5), W.c2_poisson_3d(thr=3e-3, lvl_max=7)] + \
@@ -139,3 +130,19 @@ def test_python_callback_matches_builtin(afv):
         if na == 0:
             break
     assert t.info()["n_leaves"] == a.info()["n_leaves"]
+
+
+@pytest.mark.parametrize("which", ["c2_full", "c3_lvl9", "c4_256"])
+def test_library_tree_matches_oracle_full_size(afv, oracle_lib, which):
+    """The trees the benchmark runs on, at their full sizes: the 3-D adaptive
+    tree (34,907 boxes), the 4096^2 uniform tree (87,384 boxes) and all 256
+    random trees of the batched workload, bit for bit."""
+    specs = {"c2_full": [W.c2_poisson_3d()], "c3_lvl9": [W.c3_uniform_2d(9)],
+             "c4_256": W.c4_random_2d()}[which]
+    boxes = 0
+    for spec in specs:
+        o = oracle_tree(spec)
+        a = W.build_tree(spec)
+        same_tree(a, o)
+        boxes += a.info()["n_boxes"]
+    assert boxes == {"c2_full": 34907, "c3_lvl9": 87384, "c4_256": 1166416}[which]

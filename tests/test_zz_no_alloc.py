@@ -13,8 +13,15 @@ pytestmark = pytest.mark.gpu
 REL_TOL = 0.0
 
 
-def _forest(afv):
-    specs = W.c4_random_2d(3, small=True)
+def _specs(which):
+    if which == "2d":
+        return W.c4_random_2d(3, small=True)
+    # 3-D trees of different depth (leaves on levels 2 to 5) in one forest
+    return [W.c2_poisson_3d(seed=s, thr=3e-3, lvl_max=l) for s, l in ((2, 5), (3, 4), (5, 3))]
+
+
+def _forest(afv, which="2d"):
+    specs = _specs(which)
     trees = [W.build_tree(s) for s in specs]
     f = afv.Forest(trees)
     rng = np.random.default_rng(11)
@@ -26,8 +33,9 @@ def _forest(afv):
     return f, len(trees)
 
 
-def test_noalloc_matches_max_abs_twice(gpu):
-    f, nt = _forest(gpu)
+@pytest.mark.parametrize("which", ["2d", "3d"])
+def test_noalloc_matches_max_abs_twice(gpu, which):
+    f, nt = _forest(gpu, which)
     for var in (gpu.AFV_PHI, gpu.AFV_RHS, gpu.AFV_TMP):
         for t in range(nt):
             want = f.max_abs(t, var)
