@@ -43,6 +43,8 @@ AFV_PREC_FP64, AFV_PREC_MIXED = 0, 1
 AFV_OPT_SWEEP_KERNEL, AFV_OPT_GRAPHS, AFV_OPT_RESTRICT_KERNEL, AFV_OPT_SMALL_SWEEPS = 0, 1, 2, 3
 AFV_OPT_PROFILE_LEAD_US, AFV_OPT_DEFECT_KERNEL, AFV_OPT_COARSE_END = 4, 5, 6
 AFV_OPT_WAIT_LIMIT_US = 7
+AFV_RB_MG, AFV_RB_PROLONG0, AFV_RB_INTERP, AFV_RB_INTERP_LIM = 0, 1, 2, 3
+AFV_BCM_TABLE, AFV_BCM_DIRICHLET_ZERO, AFV_BCM_NEUMANN_ZERO = 0, -1, -2
 KERNEL_KINDS = ("sweep", "fill", "restrict", "coarse_rhs", "correct", "residual", "defect",
                 "accumulate", "coarse_end")
 
@@ -147,6 +149,17 @@ def lib():
             "afv_mg_residual_all": (I, [P]),
             "afv_forest_profile": (I, [P, I]),
             "afv_forest_profile_read": (I, [P, I, llp, dp, dp]),
+            "afv_forest_add_vars": (I, [P, I, I]),
+            "afv_forest_set_fc": (I, [P, I, I, dp, LL]),
+            "afv_forest_get_fc": (I, [P, I, I, dp, LL]),
+            "afv_prolong_from_level": (I, [P, I, I, I, I, I]),
+            "afv_restrict_tree": (I, [P, I, I]),
+            "afv_gc_tree_var": (I, [P, I, I, I]),
+            "afv_gc2_level": (I, [P, I, I, I, dp, LL]),
+            "afv_consistent_fluxes": (I, [P, I, ip]),
+            "afv_write_vtk": (I, [P, I, ctypes.c_char_p, I, Dd, I, ip,
+                                  ctypes.POINTER(ctypes.c_char_p), I, ip,
+                                  ctypes.POINTER(ctypes.c_char_p), ctypes.c_char_p]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -434,6 +447,64 @@ class Forest:
         if check and rc != AFV_OK:
             _check(rc)
         return cyc, rel, rc
+
+    # general ghost cells, transfers and output (src/m_aX_gc.f90,
+    # m_aX_prolong.f90, m_aX_restrict.f90, m_aX_core.f90, m_aX_io.f90)
+    def add_vars(self, n_cc=0, n_fc=0):
+        """Extra cell variables (numbered 3, 4, ...) and face variables."""
+        _check(lib().afv_forest_add_vars(self.h, n_cc, n_fc))
+        self.__dict__["_n_fc"] = self.__dict__.get("_n_fc", 0) + n_fc
+
+    def fc_count(self, tree):
+        t = self.trees[tree]
+        n = 0
+        for lvl in range(t.min_lvl, t.highest_lvl + 1):
+            nc = t.n_cell_at(lvl)
+            n += len(t.level(lvl)[0]) * self.dim * (nc + 1) * nc ** (self.dim - 1)
+        return n
+
+    def set_fc(self, tree, ifc, values):
+        a = np.ascontiguousarray(values, dtype=np.float64).ravel()
+        _check(lib().afv_forest_set_fc(self.h, tree, ifc, _dp(a), a.size))
+
+    def get_fc(self, tree, ifc):
+        a = np.empty(self.fc_count(tree))
+        _check(lib().afv_forest_get_fc(self.h, tree, ifc, _dp(a), a.size))
+        return a
+
+    def prolong(self, lvl_parent, iv, iv_to=None, order=2, add=False):
+        """a$D_prolong{order}_from on every parent of lvl_parent."""
+        iv_to = iv if iv_to is None else iv_to
+        _check(lib().afv_prolong_from_level(self.h, lvl_parent, iv, iv_to, order, int(add)))
+
+    def restrict_tree(self, iv, iv_to=None):
+        _check(lib().afv_restrict_tree(self.h, iv, iv if iv_to is None else iv_to))
+
+    def gc_tree_var(self, iv, rb=AFV_RB_MG, bc=AFV_BCM_TABLE):
+        _check(lib().afv_gc_tree_var(self.h, iv, rb, bc))
+
+    def gc2_level(self, tree, lvl, iv):
+        t = self.trees[tree]
+        nc = t.n_cell_at(lvl)
+        n = len(t.level(lvl)[0]) * 2 * self.dim * nc ** (self.dim - 1)
+        out = np.empty(n)
+        _check(lib().afv_gc2_level(self.h, tree, lvl, iv, _dp(out), n))
+        return out
+
+    def consistent_fluxes(self, f_ixs):
+        ix = np.ascontiguousarray(f_ixs, dtype=np.int32)
+        _check(lib().afv_consistent_fluxes(self.h, ix.size, _ip(ix)))
+
+    def write_vtk(self, tree, filename, ixs_cc, cc_names, ixs_fc=(), fc_names=(), n_cycle=0,
+                  time=0.0, dir=None):
+        """a$D_write_vtk: leaves of one tree to filename.vtu."""
+        icc = np.ascontiguousarray(ixs_cc, dtype=np.int32)
+        ifc = np.ascontiguousarray(ixs_fc, dtype=np.int32)
+        cn = (ctypes.c_char_p * max(1, len(cc_names)))(*[n.encode() for n in cc_names])
+        fn = (ctypes.c_char_p * max(1, len(fc_names)))(*[n.encode() for n in fc_names])
+        _check(lib().afv_write_vtk(self.h, tree, filename.encode(), n_cycle, float(time), icc.size,
+                                   _ip(icc), cn, ifc.size, _ip(ifc), fn,
+                                   None if dir is None else dir.encode()))
 
     # single operators
     def gsrb_level(self, lvl, n_cycle):

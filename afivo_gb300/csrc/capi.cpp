@@ -53,6 +53,20 @@ afv::MgOpts mg_of(const afv_mg_opts* o) {
 }
 }  // namespace
 
+namespace afv {
+int forest_add_vars(Forest& F, int n_cc, int n_fc, std::string& err);
+int forest_fc_exchange(Forest& F, int t, int ifc, double* host, bool to_dev, std::string& err);
+long long forest_fc_count(const Forest& F, int t);
+int forest_prolong(Forest& F, int lp, int iv, int iv_to, int order, int add, std::string& err);
+int forest_restrict_tree(Forest& F, int iv, int iv_to, std::string& err);
+int forest_gc_tree_var(Forest& F, int iv, int rb, int bc, std::string& err);
+int forest_gc2_level(Forest& F, int tree, int lvl, int iv, double* host_out, long long n_out, std::string& err);
+int forest_consistent_fluxes(Forest& F, int n, const int* f_ixs, std::string& err);
+int forest_write_vtk(Forest& F, int tree, const char* filename, int n_cycle, double time, int n_cc, const int* ixs_cc,
+                     const char* const* cc_names, int n_fcv, const int* ixs_fc, const char* const* fc_names,
+                     const char* dir, std::string& err);
+}  // namespace afv
+
 extern "C" {
 
 const char* afv_last_error(void) { return g_err.c_str(); }
@@ -469,6 +483,56 @@ int afv_forest_get_option(afv_forest* f, int option, int* value) {
     case AFV_OPT_WAIT_LIMIT_US: *value = (int)(f->f.meta.wait_limit / 2000LL); return AFV_OK;
   }
   return fail(AFV_ERR_INVALID, "unknown option");
+}
+
+int afv_forest_add_vars(afv_forest* f, int n_cc, int n_fc) {
+  FOREST_CALL(f, return afv::forest_add_vars(f->f, n_cc, n_fc, err));
+}
+
+static int fc_exchange(afv_forest* f, int tree, int ifc, double* host, long long n, bool to_dev) {
+  if (!f || !host) return fail(AFV_ERR_INVALID, "NULL argument");
+  cudaSetDevice(f->f.device);
+  return guarded([&](std::string& err) -> int {
+    if (tree < 0 || tree >= f->f.plan.n_trees) return err = "tree index out of range", AFV_ERR_INVALID;
+    if (n != afv::forest_fc_count(f->f, tree)) return err = "value count does not match the tree", AFV_ERR_INVALID;
+    return afv::forest_fc_exchange(f->f, tree, ifc, host, to_dev, err);
+  });
+}
+
+int afv_forest_set_fc(afv_forest* f, int tree, int ifc, const double* host, long long n) {
+  return fc_exchange(f, tree, ifc, const_cast<double*>(host), n, true);
+}
+
+int afv_forest_get_fc(afv_forest* f, int tree, int ifc, double* host, long long n) {
+  return fc_exchange(f, tree, ifc, host, n, false);
+}
+
+int afv_prolong_from_level(afv_forest* f, int lvl_parent, int iv, int iv_to, int order, int add) {
+  FOREST_CALL(f, return afv::forest_prolong(f->f, lvl_parent, iv, iv_to, order, add, err));
+}
+
+int afv_restrict_tree(afv_forest* f, int iv, int iv_to) {
+  FOREST_CALL(f, return afv::forest_restrict_tree(f->f, iv, iv_to, err));
+}
+
+int afv_gc_tree_var(afv_forest* f, int iv, int rb_method, int bc_method) {
+  FOREST_CALL(f, return afv::forest_gc_tree_var(f->f, iv, rb_method, bc_method, err));
+}
+
+int afv_gc2_level(afv_forest* f, int tree, int lvl, int iv, double* host_out, long long n_out) {
+  if (!host_out) return fail(AFV_ERR_INVALID, "NULL argument");
+  FOREST_CALL(f, return afv::forest_gc2_level(f->f, tree, lvl, iv, host_out, n_out, err));
+}
+
+int afv_consistent_fluxes(afv_forest* f, int n_fc, const int* f_ixs) {
+  FOREST_CALL(f, return afv::forest_consistent_fluxes(f->f, n_fc, f_ixs, err));
+}
+
+int afv_write_vtk(afv_forest* f, int tree, const char* filename, int n_cycle, double time, int n_cc,
+                  const int* ixs_cc, const char* const* cc_names, int n_fc, const int* ixs_fc,
+                  const char* const* fc_names, const char* dir) {
+  FOREST_CALL(f, return afv::forest_write_vtk(f->f, tree, filename, n_cycle, time, n_cc, ixs_cc, cc_names, n_fc,
+                                              ixs_fc, fc_names, dir, err));
 }
 
 int afv_forest_autotune(afv_forest* f, int* choice, float* ms3) {

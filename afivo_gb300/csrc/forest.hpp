@@ -105,6 +105,28 @@ class Forest {
   double* base_rhs64 = nullptr;
   bool mixed = false;
   // level lists on the device
+  // Variables beyond phi, rhs and tmp (afv_forest_add_vars): ghosted FP64
+  // cell-centred variables numbered 3, 4, ... in phi's layout, and face
+  // variables, per slot D blocks of (nc+1) * nc^(D-1) values (fx, fy, fz),
+  // at fc + (ifc * n_slots + slot) * fc_stride.
+  std::vector<double*> xcc;
+  int n_fc = 0;
+  double* fc = nullptr;
+  long long fc_stride = 0;
+  // Slot tables the general utilities read, uploaded on first use: the
+  // neighbour slot per face (-1 refinement boundary, -2 physical), level and
+  // child-number bits per slot.
+  int* d_nb = nullptr;
+  int* d_lvl = nullptr;
+  int* d_qd = nullptr;
+  int n_cc_vars() const { return 3 + (int)xcc.size(); }
+  // Device array of cell variable iv (0 phi, 1 rhs, 2 tmp, 3.. extra).
+  double* var_ptr(int iv) const {
+    if (iv == 0) return d64.phi;
+    if (iv == 1) return d64.rhs;
+    if (iv == 2) return d64.tmp;
+    return (iv >= 3 && iv < n_cc_vars()) ? xcc[iv - 3] : nullptr;
+  }
   int* d_lists = nullptr;
   std::vector<int> leaves_off, parents_off;  // offsets in d_lists per level
   int all_leaves_off = 0;

@@ -160,6 +160,10 @@ Forest::~Forest() {
                   d_fmax, d_count, d_failed, d_cycles, d_final, d_stage, d_stage_slots};
   for (void* p : ptrs)
     if (p) cudaFreeAsync(p, stream);
+  for (double* p : xcc)
+    if (p) cudaFreeAsync(p, stream);
+  for (void* p : {(void*)fc, (void*)d_nb, (void*)d_lvl, (void*)d_qd})
+    if (p) cudaFreeAsync(p, stream);
   if (stream) cudaStreamSynchronize(stream);
   for (const ProfEntry& p : prof) {
     cudaEventDestroy(p.start);
@@ -487,7 +491,7 @@ static int exchange(Forest& F, int t, int var, double* host, int interior_only, 
                     std::string& err) {
   const Plan& p = F.plan;
   if (t < 0 || t >= p.n_trees) return err = "tree index out of range", AFV_ERR_INVALID;
-  if (var < AFV_PHI || var > AFV_TMP) return err = "unknown variable", AFV_ERR_INVALID;
+  if (var < AFV_PHI || var >= F.n_cc_vars()) return err = "unknown variable", AFV_ERR_INVALID;
   if (int rc = exchange_plan(F, err)) return rc;
   const int D = p.dim;
   const long long total = F.xfer_total[t][interior_only ? 0 : 1];
@@ -517,7 +521,7 @@ static int exchange(Forest& F, int t, int var, double* host, int interior_only, 
     cudaMemcpyAsync(F.d_stage, host, sizeof(double) * total, cudaMemcpyHostToDevice, st);
   Meta m = meta_of(F.meta);
   bool ghosted = var != AFV_RHS;
-  double* dvar = var == AFV_PHI ? F.d64.phi : var == AFV_RHS ? F.d64.rhs : F.d64.tmp;
+  double* dvar = F.var_ptr(var);
   long long off = 0;
   for (const Forest::XferRun& r : F.xfer_runs[t]) {
     const int nc = p.nc_at(r.lvl);
@@ -545,6 +549,8 @@ static int exchange(Forest& F, int t, int var, double* host, int interior_only, 
 }  // namespace afv
 
 namespace afv {
+
+int forest_exchange_plan(Forest& F, std::string& err) { return exchange_plan(F, err); }
 
 int forest_set_var(Forest& F, int t, int var, const double* host, int interior_only, std::string& err) {
   return exchange(F, t, var, const_cast<double*>(host), interior_only, true, err);

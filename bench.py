@@ -157,22 +157,42 @@ class OracleSolver:
     max |f - L phi| <= TOL * max |f|, the reference's own loop
     (examples/poisson_basic_2d.f90:84-92)."""
 
-    def __init__(self, spec, threads):
+    def __init__(self, spec, threads, rhs_interior=None):
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
         sys.path.insert(0, os.path.join(ROOT, "tests"))
         import oracle as O
-        from helpers import oracle_tree
+        from helpers import interior_to_ghosted, oracle_tree
         O.build()
         O.set_threads(threads)
         self.O = O
         self.ot = oracle_tree(spec)
-        self.ot.fill_gauss(O.I_RHS, spec["gauss"], lpl=True)
+        if rhs_interior is None:
+            self.ot.fill_gauss(O.I_RHS, spec["gauss"], lpl=True)
+        else:  # a host-layout interior-only right-hand side
+            g = interior_to_ghosted(rhs_interior, self.ot, spec["n_cell"], spec["dim"])
+            off = 0
+            for lvl in range(self.ot.min_lvl, self.ot.highest_lvl + 1):
+                a = self.ot.get_level(lvl, O.I_RHS, spec["n_cell"])
+                self.ot.set_level(lvl, O.I_RHS, g[off:off + a.size].reshape(a.shape))
+                off += a.size
         self.ot.mg_init()
+        self.spec = spec
         self.fmax = self.ot.max_abs(O.I_RHS)
         nc, D = spec["n_cell"], spec["dim"]
         self.leaves = sum(len(self.ot.level(l)[1]) for l in range(self.ot.min_lvl, self.ot.highest_lvl + 1))
         self.boxes = sum(len(self.ot.level(l)[0]) for l in range(self.ot.min_lvl, self.ot.highest_lvl + 1))
         self.cells = self.leaves * nc ** D
+
+    def phi(self):
+        """The oracle's phi in the host layout (ghosted)."""
+        from helpers import oracle_var
+        return oracle_var(self.ot, self.O.I_PHI, self.spec["n_cell"])
+
+    def error_of(self, gpu_phi):
+        """max |gpu - oracle| over leaf interiors / max |oracle phi| there, for
+        a ghosted host-layout GPU solution."""
+        from helpers import leaf_error
+        return leaf_error(gpu_phi, self.phi(), self.ot, self.spec["n_cell"], self.spec["dim"])
 
     def solve(self, max_cycles=60):
         """One solve; returns (V-cycles, seconds, relative residual)."""
@@ -236,7 +256,7 @@ def run_reference(args, spec):
     print(json.dumps(line))
 
 
-def run_batched(afv, W, local, rank, world, n_trees=256):
+def run_batched(afv, W, local, rank, world, n_trees=256, check_errors=False):
     """Batched 2-D solves: 256 independent random quadtrees in one forest per
     GPU (trees placed over the ranks), one launch per level and operator for
     all of them, autotuned sweep kernel, mixed-precision solve to 1e-8."""
@@ -274,14 +294,34 @@ def run_batched(afv, W, local, rank, world, n_trees=256):
     unknowns = sum(float(t.leaf_cells()) * c for t, c in zip([trees[i] for i in mine], cyc))
     unknowns = sum_over_ranks(unknowns, world)
     total_cells = sum_over_ranks(float(cells), world)
+    errors = None
+    if check_errors:
+        errors = batched_errors(afv, forest, specs, mine)
     out = {"workload": "random2d_256trees_seed4", "trees": n_trees, "leaf_cells": int(total_cells),
            "boxes": int(sum_over_ranks(float(forest.info()["n_boxes"]), world)),
            "ms_per_solve": ms, "unknowns_per_s": unknowns / (ms / 1e3),
            "cycles_min": int(min(cyc)), "cycles_max": int(max(cyc)), "rel_res_max": float(max(rel)),
            "sweep_kernel": choice, "autotune_ms_per_vcycle": {str(k): round(v, 3) for k, v in tune_ms.items()},
-           "tree_build_s": round(t_build, 2)}
+           "tree_build_s": round(t_build, 2), "err_vs_fp64_oracle": errors}
     forest.close()
     return out
+
+
+def batched_errors(afv, forest, specs, mine):
+    """Per tree, the mixed solution in the forest against the oracle's FP64
+    solve of the same tree to the same tolerance (max over leaf interiors,
+    relative to max |phi|)."""
+    cores = os.cpu_count() or 1
+    errs = []
+    for k, i in enumerate(mine):
+        s = OracleSolver(specs[i], cores)
+        s.solve()
+        errs.append(s.error_of(forest.get_var(k, afv.AFV_PHI)))
+    worst = int(np.argmax(errs))
+    return {"max": float(max(errs)), "median": float(np.median(errs)), "worst_tree": mine[worst],
+            "per_tree": [float("%.3g" % e) for e in errs],
+            "note": "mixed solution vs the oracle's FP64 solve to the same tolerance, max over "
+                    "leaf interiors / max |phi|"}
 
 
 def run_serving(afv, W, local, rank, world, n_requests=64):
@@ -309,7 +349,7 @@ def run_serving(afv, W, local, rank, world, n_requests=64):
     return out, reqs
 
 
-def run_uniform(afv, W, local, rank, world):
+def run_uniform(afv, W, local, rank, world, check_errors=False):
     """2-D uniform periodic case: 16x16 boxes, 4096^2 cells, white-noise
     source with zero mean (seed 3); FMG followed by V-cycles to 1e-8, FP64
     and mixed, with the per-kernel bandwidth of one mixed solve. The
@@ -328,9 +368,11 @@ def run_uniform(afv, W, local, rank, world):
         parts.append(rng.standard_normal(n) if lvl == tree.highest_lvl else np.zeros(n))
     top = parts[-1]
     top -= top.mean()
-    forest.set_var(0, afv.AFV_RHS, np.concatenate(parts), interior_only=True)
+    rhs_int = np.concatenate(parts)
+    forest.set_var(0, afv.AFV_RHS, rhs_int, interior_only=True)
     ext = torch.cuda.ExternalStream(forest.stream())
     out = {"workload": spec["name"], "leaf_cells": info["leaf_cells"], "boxes": info["n_boxes"]}
+    solutions = {}
     for name, prec in (("mixed", afv.AFV_PREC_MIXED), ("fp64", afv.AFV_PREC_FP64)):
         def run():
             forest.zero(afv.AFV_PHI)
@@ -347,6 +389,18 @@ def run_uniform(afv, W, local, rank, world):
         ms = e0.elapsed_time(e1)
         out[name] = {"fmg_then_cycles": cyc, "rel_res": rel, "status": rc, "ms": round(ms, 3),
                      "unknowns_per_s": info["leaf_cells"] * (cyc + 1) / (ms / 1e3)}
+        if check_errors:
+            solutions[name] = forest.get_var(0, afv.AFV_PHI)
+    if check_errors:
+        # the oracle's FP64 FMG followed by V-cycles to the same tolerance
+        s = OracleSolver(spec, os.cpu_count() or 1, rhs_interior=rhs_int)
+        s.ot.fmg(set_residual=True, have_guess=False)
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        from helpers import oracle_solve
+        n = oracle_solve(s.ot, TOL)
+        for name, phi in solutions.items():
+            out[name]["err_vs_fp64_oracle"] = s.error_of(phi)
+        out["oracle_fmg_then_cycles"] = n
     forest.profile((1 << len(afv.KERNEL_KINDS)) - 1)
     forest.zero(afv.AFV_PHI)
     forest.solve(afv.AFV_PREC_MIXED, tol=TOL, max_cycles=60, check=False)
@@ -539,9 +593,12 @@ def main():
     e2e_s = max_over_ranks(time.perf_counter() - t0, world)
     e2e_value = cells * sum_over_ranks(float(e2e_cycles), world) / e2e_s
 
-    batched = None if args.no_batched else run_batched(afv, W, local, rank, world)
+    # The solutions are checked against the oracle's FP64 solves on the host
+    # cores (rank 0 of a single-GPU run, beside the CPU baseline).
+    check = rank == 0 and world == 1 and not args.no_cpu_baseline
+    batched = None if args.no_batched else run_batched(afv, W, local, rank, world, check_errors=check)
     served, reqs = (None, None) if args.no_serving else run_serving(afv, W, local, rank, world)
-    uniform = None if args.no_uniform else run_uniform(afv, W, local, rank, world)
+    uniform = None if args.no_uniform else run_uniform(afv, W, local, rank, world, check_errors=check)
 
     peak, peak_kind = load_peaks()
     achieved = sweep_bytes / (sweep_ms / 1e3) / 1e9 if sweep_ms > 0 else None
@@ -549,14 +606,21 @@ def main():
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cores = os.cpu_count() or 1
-        v, dt, n, _s = cpu_baseline_sample(spec, cores)
+        v, dt, n, osolve = cpu_baseline_sample(spec, cores)
         cpu = {"value": v, "unit": "unknowns/s", "cores": cores, "kind": "port",
                "sample": f"{n} FP64 solves of the full tree to {TOL:g} on the oracle "
                          f"({dt:.1f} s, {cores} threads; median rate)"}
+        # the headline's solution (the last end-to-end mixed solve) and a GPU
+        # FP64 solve against the oracle's FP64 solution of the same tree
+        err_mixed = osolve.error_of(forest.get_var(0, afv.AFV_PHI))
+        solve(afv.AFV_PREC_FP64)
+        err_fp64 = osolve.error_of(forest.get_var(0, afv.AFV_PHI))
         if served is not None:
             served["cpu_oracle"] = cpu_serving_sample(reqs, cores)
     if rank != 0:
         return
+    errs = {} if cpu is None else {"err_vs_fp64_oracle": err_mixed}
+    errs64 = {} if cpu is None else {"err_vs_oracle": err_fp64}
     line = {
         "metric": METRIC, "value": value, "unit": "unknowns/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
@@ -565,9 +629,10 @@ def main():
         "config": config_of(spec, cells, info["n_boxes"]),
         "method": "mixed: FP32 FAS V(2,2) cycles inside FP64 defect correction; CUDA graphs",
         "solve": {"cycles": cyc, "rel_res": max(rels), "ms_p50": float(np.percentile(per, 50)),
-                  "ms_p99": float(np.percentile(per, 99)), "ms_each": [round(x, 3) for x in per]},
+                  "ms_p99": float(np.percentile(per, 99)), "ms_each": [round(x, 3) for x in per],
+                  **errs},
         "fp64": {"value": value64, "unit": "unknowns/s", "cycles": cyc64, "rel_res": max(rels64),
-                 "ms_per_solve": ms64 / len(cyc64)},
+                 "ms_per_solve": ms64 / len(cyc64), **errs64},
         "mixed_vs_fp64_solve_speedup": (ms64 / len(cyc64)) / (ms / args.steps),
         "roofline": {"bound": "hbm", "kernel": "k_sweep_warp<3,8,float>",
                      "achieved": achieved, "peak": peak, "unit": "GB/s",

@@ -236,6 +236,62 @@ int afv_mg_correct_children(afv_forest* f, int lvl_parent);
 /* residual_box on every box of every level, src/m_aX_mg.f90:243-254 */
 int afv_mg_residual_all(afv_forest* f);
 
+/* ---- general ghost cells, transfers and output ------------------------------ */
+
+/* Refinement-boundary methods of afv_gc_tree_var (the reference's sides_rb
+ * hooks): mg$D_sides_rb (src/m_aX_mg.f90:262-350), a$D_gc_prolong0
+ * (src/m_aX_gc.f90:135-151), a$D_gc_interp (:155-245) and a$D_gc_interp_lim
+ * (:249-358). */
+enum { AFV_RB_MG = 0, AFV_RB_PROLONG0 = 1, AFV_RB_INTERP = 2, AFV_RB_INTERP_LIM = 3 };
+/* Physical-boundary methods of afv_gc_tree_var: the forest's sampled sides_bc
+ * records (afv_forest_set_bc / _set_bc_faces), or a$D_bc_dirichlet_zero /
+ * a$D_bc_neumann_zero (src/m_aX_gc.f90:361-378). */
+enum { AFV_BCM_TABLE = 0, AFV_BCM_DIRICHLET_ZERO = -1, AFV_BCM_NEUMANN_ZERO = -2 };
+
+/* The n_var_cell / n_var_face arguments of a$D_init (src/m_aX_core.f90:24-50)
+ * for a forest: adds n_cc cell-centred FP64 variables (numbered 3, 4, ...,
+ * ghosted like phi, exchanged with afv_forest_set_var / _get_var) and n_fc
+ * face variables (fx, fy[, fz] of box$D_t, src/m_aX_t.f90:153-177),
+ * zero-initialised. Face variables can be added once. */
+int afv_forest_add_vars(afv_forest* f, int n_cc, int n_fc);
+/* Face variable ifc of one tree to or from the host: per box in the host
+ * exchange order, fx(1:nc+1,1:nc[,1:nc]), then fy, then fz, x fastest;
+ * n = the total count (checked). */
+int afv_forest_set_fc(afv_forest* f, int tree, int ifc, const double* host, long long n);
+int afv_forest_get_fc(afv_forest* f, int tree, int ifc, double* host, long long n);
+/* a$D_prolong0_from / a$D_prolong1_from / a$D_prolong2_from
+ * (src/m_aX_prolong.f90:22-37, 112-127, 226-241) for order 0 / 1 / 2 on every
+ * parent of level lvl_parent of every tree: cell variable iv of the parents
+ * into iv_to of their children, added to the old values when add != 0. The
+ * parents' ghost cells must be valid for orders 1 and 2. */
+int afv_prolong_from_level(afv_forest* f, int lvl_parent, int iv, int iv_to, int order, int add);
+/* a$D_restrict_tree, src/m_aX_restrict.f90:54-64 (iv into iv_to on every
+ * parent, finest level first). */
+int afv_restrict_tree(afv_forest* f, int iv, int iv_to);
+/* a$D_gc_tree(tree, iv, subr_rb, subr_bc), src/m_aX_gc.f90:28-46, with
+ * subr_rb one of AFV_RB_* and subr_bc one of AFV_BCM_*, for a ghosted cell
+ * variable iv. */
+int afv_gc_tree_var(afv_forest* f, int iv, int rb_method, int bc_method);
+/* a$D_gc2_box (src/m_aX_gc.f90:420-440) with subr_rb = a$D_gc2_prolong1 and
+ * subr_bc = a$D_bc2_neumann_zero, for every box of one tree on level lvl
+ * (>= 1), in level-list order: host_out receives per box gc_data(nc[,nc],
+ * 2D), the second layer of ghost cells per face. n_out must be boxes x 2D x
+ * nc^(D-1). */
+int afv_gc2_level(afv_forest* f, int tree, int lvl, int iv, double* host_out, long long n_out);
+/* a$D_consistent_fluxes, src/m_aX_core.f90:811-945 (Cartesian): face
+ * variables f_ixs[0..n_fc-1] of leaves next to refined neighbours become the
+ * averages of the neighbours' fine fluxes. */
+int afv_consistent_fluxes(afv_forest* f, int n_fc, const int* f_ixs);
+/* a$D_write_vtk, src/m_aX_io.f90:115-310: the leaves of levels 1..highest of
+ * one tree as a VTK unstructured grid, file filename.vtu (in dir, if given),
+ * with the cell variables ixs_cc (names cc_names) and the cell averages of
+ * the face variables ixs_fc (names fc_names + "_x", "_y"[, "_z"]). The file
+ * layout is that of src/m_vtk.f90 (appended raw data); the TIME and CYCLE
+ * values are written as %.17E and %d text. */
+int afv_write_vtk(afv_forest* f, int tree, const char* filename, int n_cycle, double time, int n_cc,
+                  const int* ixs_cc, const char* const* cc_names, int n_fc, const int* ixs_fc,
+                  const char* const* fc_names, const char* dir);
+
 /* ---- measurement ------------------------------------------------------------ */
 
 /* Kernel kinds of the event profiler. */

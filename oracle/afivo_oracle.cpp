@@ -36,6 +36,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <string>
 #include <vector>
 #ifdef _OPENMP
 #include <omp.h>
@@ -105,6 +106,20 @@ template <int D> struct Box {
   double r_min[D] = {};
   int n_var = 0;
   std::vector<double> cc;  // (n_cell+2)^D per variable, x fastest
+  // Face variables fx, fy[, fz] (box$D_t, src/m_aX_t.f90:153-177): per
+  // variable D blocks, direction d with n_cell+1 values along d and n_cell
+  // along the others, x fastest.
+  int n_fc = 0;
+  std::vector<double> fc;
+  long long fblock() const {
+    long long n = n_cell + 1;
+    for (int d = 1; d < D; ++d) n *= n_cell;
+    return n;
+  }
+  double& f_at(int ifc, int dim, int i, int j, int k) {
+    const int sx = dim == 0 ? n_cell + 1 : n_cell, sy = dim == 1 ? n_cell + 1 : n_cell;
+    return fc[((size_t)ifc * D + dim) * fblock() + (i - 1) + (size_t)sx * ((j - 1) + (size_t)sy * (D == 3 ? k - 1 : 0))];
+  }
 
   int ng() const { return n_cell + 2; }
   int nvol() const {
@@ -1327,6 +1342,525 @@ template <int D> double leaf_mean(Tree<D>& t, int iv) {
 // ---------------------------------------------------------------------------
 using namespace orc;
 
+// ---------------------------------------------------------------------------
+// General ghost-cell, transfer and output routines used by codes other than
+// the multigrid solver: src/m_aX_prolong.f90, m_aX_restrict.f90:21-64,
+// m_aX_gc.f90:28-358, 420-634, m_aX_core.f90:811-945, m_aX_io.f90:115-310,
+// m_vtk.f90.
+// ---------------------------------------------------------------------------
+
+// n_var_cell / n_var_face of a$D_init (core:24-131) grown on a built tree:
+// n_cc more cell variables after the existing ones and n_fc face variables,
+// zero-initialised.
+template <int D> void add_vars(Tree<D>& t, int n_cc, int n_fc) {
+  t.n_var_cell += n_cc;
+  for (size_t id = 1; id < t.boxes.size(); ++id) {
+    Box<D>& b = t.boxes[id];
+    if (!b.in_use) continue;
+    b.n_var += n_cc;
+    b.cc.resize((size_t)b.nvol() * b.n_var, 0.0);
+    if (n_fc) {
+      b.n_fc = n_fc;
+      b.fc.assign((size_t)n_fc * D * b.fblock(), 0.0);
+    }
+  }
+}
+
+// a$D_prolong0 / a$D_prolong1 / a$D_prolong2 of a whole child (prolong:39-348)
+template <int D> void prolong_box(Box<D>& p, Box<D>& c, int iv, int ivc, int order, bool add) {
+  const int nc = c.n_cell, hnc = nc >> 1;
+  int off[D];
+  child_offset(c, off);
+  if (order == 0) {
+    const int kmax = D == 3 ? nc : 1;
+    for (int k = 1; k <= kmax; ++k) {
+      const int k_c1 = D == 3 ? off[D - 1] + ((k + 1) >> 1) : 0;
+      for (int j = 1; j <= nc; ++j) {
+        const int j_c1 = off[1] + ((j + 1) >> 1);
+        for (int i = 1; i <= nc; ++i) {
+          const int i_c1 = off[0] + ((i + 1) >> 1);
+          double& o = D == 2 ? c.at(i, j, ivc) : c.at(i, j, k, ivc);
+          const double v = D == 2 ? p.at(i_c1, j_c1, iv) : p.at(i_c1, j_c1, k_c1, iv);
+          o = add ? o + v : v;
+        }
+      }
+    }
+    return;
+  }
+  if (!add) {  // box_c%cc(1:nc, 1:nc[, 1:nc], ivc) = 0
+    const int kmax = D == 3 ? nc : 1;
+    for (int k = 1; k <= kmax; ++k)
+      for (int j = 1; j <= nc; ++j)
+        for (int i = 1; i <= nc; ++i) (D == 2 ? c.at(i, j, ivc) : c.at(i, j, k, ivc)) = 0;
+  }
+  if (order == 2) {  // onto the zeroed interior unless add, as the reference does
+    prolong2_add<D>(p, c, iv, ivc);
+    return;
+  }
+  // order 1: 2-1-1 (2D) and 1-1-1-1 (3D) interpolation, prolong:129-222
+  if constexpr (D == 2) {
+    for (int j = 1; j <= hnc; ++j) {
+      const int j_c = j + off[1], j_f = 2 * j - 1;
+      for (int i = 1; i <= hnc; ++i) {
+        const int i_c = i + off[0], i_f = 2 * i - 1;
+        const double f0 = 0.5 * p.at(i_c, j_c, iv);
+        const double flx = 0.25 * p.at(i_c - 1, j_c, iv);
+        const double fhx = 0.25 * p.at(i_c + 1, j_c, iv);
+        const double fly = 0.25 * p.at(i_c, j_c - 1, iv);
+        const double fhy = 0.25 * p.at(i_c, j_c + 1, iv);
+        c.at(i_f, j_f, ivc) = f0 + flx + fly + c.at(i_f, j_f, ivc);
+        c.at(i_f + 1, j_f, ivc) = f0 + fhx + fly + c.at(i_f + 1, j_f, ivc);
+        c.at(i_f, j_f + 1, ivc) = f0 + flx + fhy + c.at(i_f, j_f + 1, ivc);
+        c.at(i_f + 1, j_f + 1, ivc) = f0 + fhx + fhy + c.at(i_f + 1, j_f + 1, ivc);
+      }
+    }
+  } else {
+    for (int k = 1; k <= hnc; ++k) {
+      const int k_c = k + off[2], k_f = 2 * k - 1;
+      for (int j = 1; j <= hnc; ++j) {
+        const int j_c = j + off[1], j_f = 2 * j - 1;
+        for (int i = 1; i <= hnc; ++i) {
+          const int i_c = i + off[0], i_f = 2 * i - 1;
+          const double f0 = 0.25 * p.at(i_c, j_c, k_c, iv);
+          const double flx = 0.25 * p.at(i_c - 1, j_c, k_c, iv);
+          const double fhx = 0.25 * p.at(i_c + 1, j_c, k_c, iv);
+          const double fly = 0.25 * p.at(i_c, j_c - 1, k_c, iv);
+          const double fhy = 0.25 * p.at(i_c, j_c + 1, k_c, iv);
+          const double flz = 0.25 * p.at(i_c, j_c, k_c - 1, iv);
+          const double fhz = 0.25 * p.at(i_c, j_c, k_c + 1, iv);
+          c.at(i_f, j_f, k_f, ivc) = f0 + flx + fly + flz + c.at(i_f, j_f, k_f, ivc);
+          c.at(i_f + 1, j_f, k_f, ivc) = f0 + fhx + fly + flz + c.at(i_f + 1, j_f, k_f, ivc);
+          c.at(i_f, j_f + 1, k_f, ivc) = f0 + flx + fhy + flz + c.at(i_f, j_f + 1, k_f, ivc);
+          c.at(i_f + 1, j_f + 1, k_f, ivc) = f0 + fhx + fhy + flz + c.at(i_f + 1, j_f + 1, k_f, ivc);
+          c.at(i_f, j_f, k_f + 1, ivc) = f0 + flx + fly + fhz + c.at(i_f, j_f, k_f + 1, ivc);
+          c.at(i_f + 1, j_f, k_f + 1, ivc) = f0 + fhx + fly + fhz + c.at(i_f + 1, j_f, k_f + 1, ivc);
+          c.at(i_f, j_f + 1, k_f + 1, ivc) = f0 + flx + fhy + fhz + c.at(i_f, j_f + 1, k_f + 1, ivc);
+          c.at(i_f + 1, j_f + 1, k_f + 1, ivc) = f0 + fhx + fhy + fhz + c.at(i_f + 1, j_f + 1, k_f + 1, ivc);
+        }
+      }
+    }
+  }
+}
+
+// a$D_prolong{0,1,2}_from (prolong:22-37, 112-127, 226-241) on the parents of a level
+template <int D> void prolong_from_level(Tree<D>& t, int lvl, int iv, int ivc, int order, bool add) {
+  using T = Topo<D>;
+  for (int id : t.L(lvl).parents)
+    for (int i_c = 0; i_c < T::NCH; ++i_c) {
+      const int c_id = t.boxes[id].children[i_c];
+      if (c_id == a5_no_box) continue;
+      prolong_box<D>(t.boxes[id], t.boxes[c_id], iv, ivc, order, add);
+    }
+}
+
+// a$D_restrict_box with iv_to (restrict:67-132, Cartesian)
+template <int D> void restrict_box_to(Box<D>& c, Box<D>& p, int iv, int ivt) {
+  const int hnc = c.n_cell >> 1;
+  int off[D];
+  child_offset(c, off);
+  const int kmax = D == 3 ? hnc : 1;
+  for (int k = 1; k <= kmax; ++k)
+    for (int j = 1; j <= hnc; ++j)
+      for (int i = 1; i <= hnc; ++i) {
+        const int i_f = 2 * i - 1, j_f = 2 * j - 1, k_f = 2 * k - 1;
+        double s = 0.0;
+        if constexpr (D == 2) {
+          s = s + c.at(i_f, j_f, iv);
+          s = s + c.at(i_f + 1, j_f, iv);
+          s = s + c.at(i_f, j_f + 1, iv);
+          s = s + c.at(i_f + 1, j_f + 1, iv);
+          p.at(off[0] + i, off[1] + j, ivt) = 0.25 * s;
+        } else {
+          for (int kk = 0; kk < 2; ++kk)
+            for (int jj = 0; jj < 2; ++jj)
+              for (int ii = 0; ii < 2; ++ii) s = s + c.at(i_f + ii, j_f + jj, k_f + kk, iv);
+          p.at(off[0] + i, off[1] + j, off[2] + k, ivt) = 0.125 * s;
+        }
+      }
+}
+
+// a$D_restrict_tree (restrict:54-64): a$D_restrict_to_boxes on the parents
+// of every level, from highest_lvl - 1 down to the coarsest
+template <int D> void restrict_tree(Tree<D>& t, int iv, int ivt) {
+  using T = Topo<D>;
+  for (int lvl = t.highest_lvl - 1; lvl >= t.min_lvl; --lvl)
+    for (int id : t.L(lvl).parents)
+      for (int i_c = 0; i_c < T::NCH; ++i_c) {
+        const int c_id = t.boxes[id].children[i_c];
+        if (c_id == a5_no_box) continue;
+        restrict_box_to<D>(t.boxes[c_id], t.boxes[id], iv, ivt);
+      }
+}
+
+// a$D_gc_interp / a$D_gc_interp_lim (gc:155-358)
+template <int D> void gc_interp(Tree<D>& t, int id, int nb, int iv, bool lim) {
+  using T = Topo<D>;
+  Box<D>& b = t.boxes[id];
+  const int nc = b.n_cell;
+  const int p_id = b.parent;
+  Box<D>& pn = t.boxes[t.boxes[p_id].neighbors[nb - 1]];
+  int off[D];
+  child_offset(b, off);  // the tangential offsets (a$D_get_child_offset with nb differs in the normal one only)
+  int ix, ix_f, ix_c;
+  if (T::neighb_low(nb)) {
+    ix = 0;
+    ix_f = 1;
+    ix_c = nc;
+  } else {
+    ix = nc + 1;
+    ix_f = nc;
+    ix_c = 1;
+  }
+  const double sixth = 1 / 6.0, third = 1 / 3.0;
+  auto clip = [&](double& g, double c1) {
+    if (lim && g > 2 * c1) g = 2 * c1;
+  };
+  if constexpr (D == 2) {
+    for (int a = 1; a <= nc; ++a) {
+      const int a_c1 = (T::neighb_dim(nb) == 0 ? off[1] : off[0]) + ((a + 1) >> 1);
+      const int a_c2 = a_c1 + 1 - 2 * (a & 1);
+      if (T::neighb_dim(nb) == 0) {
+        const double c1 = pn.at(ix_c, a_c1, iv), c2 = pn.at(ix_c, a_c2, iv);
+        double& g = b.at(ix, a, iv);
+        g = 0.5 * c1 + sixth * c2 + third * b.at(ix_f, a, iv);
+        clip(g, c1);
+      } else {
+        const double c1 = pn.at(a_c1, ix_c, iv), c2 = pn.at(a_c2, ix_c, iv);
+        double& g = b.at(a, ix, iv);
+        g = 0.5 * c1 + sixth * c2 + third * b.at(a, ix_f, iv);
+        clip(g, c1);
+      }
+    }
+  } else {
+    for (int m = 1; m <= nc; ++m)
+      for (int n = 1; n <= nc; ++n) {
+        switch (T::neighb_dim(nb)) {
+          case 0: {  // n = j, m = k
+            const int j_c1 = off[1] + ((n + 1) >> 1), j_c2 = j_c1 + 1 - 2 * (n & 1);
+            const int k_c1 = off[2] + ((m + 1) >> 1), k_c2 = k_c1 + 1 - 2 * (m & 1);
+            const double c1 = pn.at(ix_c, j_c1, k_c1, iv), c2 = pn.at(ix_c, j_c2, k_c1, iv),
+                         c3 = pn.at(ix_c, j_c1, k_c2, iv);
+            double& g = b.at(ix, n, m, iv);
+            g = third * c1 + sixth * c2 + sixth * c3 + third * b.at(ix_f, n, m, iv);
+            clip(g, c1);
+            break;
+          }
+          case 1: {  // n = i, m = k
+            const int i_c1 = off[0] + ((n + 1) >> 1), i_c2 = i_c1 + 1 - 2 * (n & 1);
+            const int k_c1 = off[2] + ((m + 1) >> 1), k_c2 = k_c1 + 1 - 2 * (m & 1);
+            const double c1 = pn.at(i_c1, ix_c, k_c1, iv), c2 = pn.at(i_c2, ix_c, k_c1, iv),
+                         c3 = pn.at(i_c1, ix_c, k_c2, iv);
+            double& g = b.at(n, ix, m, iv);
+            g = third * c1 + sixth * c2 + sixth * c3 + third * b.at(n, ix_f, m, iv);
+            clip(g, c1);
+            break;
+          }
+          default: {  // n = i, m = j
+            const int i_c1 = off[0] + ((n + 1) >> 1), i_c2 = i_c1 + 1 - 2 * (n & 1);
+            const int j_c1 = off[1] + ((m + 1) >> 1), j_c2 = j_c1 + 1 - 2 * (m & 1);
+            const double c1 = pn.at(i_c1, j_c1, ix_c, iv), c2 = pn.at(i_c1, j_c2, ix_c, iv),
+                         c3 = pn.at(i_c2, j_c1, ix_c, iv);
+            double& g = b.at(n, m, ix, iv);
+            g = third * c1 + sixth * c2 + sixth * c3 + third * b.at(n, m, ix_f, iv);
+            clip(g, c1);
+            break;
+          }
+        }
+      }
+  }
+}
+
+enum { RB_MG = 0, RB_PROLONG0 = 1, RB_INTERP = 2, RB_INTERP_LIM = 3 };
+enum { BCM_TABLE = 0, BCM_DIRICHLET_ZERO = -1, BCM_NEUMANN_ZERO = -2 };
+
+// a$D_gc_box (gc:50-69) for any variable, with the chosen sides_rb and sides_bc
+template <int D> void gc_box_var(Tree<D>& t, int id, int iv, int rb, int bcm, const MG& mg) {
+  using T = Topo<D>;
+  for (int nb = 1; nb <= T::NNB; ++nb) {
+    const int nb_id = t.boxes[id].neighbors[nb - 1];
+    if (nb_id > a5_no_box) {
+      sides_from_nb(t.boxes[id], t.boxes[nb_id], nb, iv);
+    } else if (nb_id == a5_no_box) {
+      switch (rb) {
+        case RB_MG: sides_rb(t, id, nb, iv); break;
+        case RB_PROLONG0: gc_prolong0(t, id, nb, iv); break;
+        default: gc_interp(t, id, nb, iv, rb == RB_INTERP_LIM); break;
+      }
+    } else if (bcm == BCM_TABLE) {
+      const int bc_type = sides_bc(t.boxes[id], id, nb, iv, mg);
+      bc_to_gc(t.boxes[id], nb, iv, bc_type);
+    } else {  // a$D_bc_dirichlet_zero / a$D_bc_neumann_zero, gc:361-378
+      Box<D>& b = t.boxes[id];
+      const int nc = b.n_cell, cmax = D == 3 ? nc : 1;
+      for (int c = 1; c <= cmax; ++c)
+        for (int a = 1; a <= nc; ++a) (&face_ghost<D>(b, nb, a, c))[(size_t)iv * b.nvol()] = 0.0;
+      bc_to_gc(b, nb, iv, bcm == BCM_NEUMANN_ZERO ? a5_bc_neumann : a5_bc_dirichlet);
+    }
+  }
+}
+
+// a$D_gc_tree (gc:28-46)
+template <int D> void gc_tree_var(Tree<D>& t, int iv, int rb, int bcm, const MG& mg) {
+  for (int lvl = t.min_lvl; lvl <= t.highest_lvl; ++lvl)
+    for (int id : t.L(lvl).ids) gc_box_var<D>(t, id, iv, rb, bcm, mg);
+}
+
+// a$D_gc2_box (gc:420-440) with sides2_from_nb (:443-478), a$D_gc2_prolong1
+// (:481-583) and a$D_bc2_neumann_zero (:586-632); gc_data is
+// (nc[, nc], 2D), first index fastest
+template <int D> void gc2_box(Tree<D>& t, int id, int iv, double* gc_data) {
+  using T = Topo<D>;
+  Box<D>& b = t.boxes[id];
+  const int nc = b.n_cell;
+  const int nf = D == 2 ? nc : nc * nc;
+  for (int nb = 1; nb <= T::NNB; ++nb) {
+    const int nb_id = b.neighbors[nb - 1];
+    const int dim = T::neighb_dim(nb);
+    double* side = gc_data + (size_t)(nb - 1) * nf;
+    for (int m = 1; m <= (D == 3 ? nc : 1); ++m)
+      for (int n = 1; n <= nc; ++n) {
+        int c[3] = {0, 0, 0};
+        {
+          int tang[2] = {n, m}, e = 0;
+          for (int d = 0; d < D; ++d)
+            if (d != dim) c[d] = tang[e++];
+        }
+        double val;
+        if (nb_id > a5_no_box) {
+          c[dim] = T::neighb_low(nb) ? nc - 1 : 2;
+          Box<D>& o = t.boxes[nb_id];
+          val = D == 2 ? o.at(c[0], c[1], iv) : o.at(c[0], c[1], c[2], iv);
+        } else if (nb_id == a5_no_box) {
+          const int p_id = b.parent;
+          Box<D>& pn = t.boxes[t.boxes[p_id].neighbors[nb - 1]];
+          int off[D];
+          child_offset(b, off);
+          // a$D_get_child_offset(box, nb): minus neighb_dix * n_cell (lvl > 1)
+          // or * n_cell/2 (sub-levels) in the normal direction
+          off[dim] -= T::neighb_high_pm(nb) * (b.lvl > 1 ? nc : nc >> 1);
+          const int ix = T::neighb_high_01(nb) * (nc + 3) - 1;
+          int c1[3] = {0, 0, 0}, c2[3] = {0, 0, 0};
+          for (int d = 0; d < D; ++d) {
+            const int x = d == dim ? ix : c[d];
+            c1[d] = off[d] + ((x + 1) >> 1);
+            c2[d] = c1[d] + 1 - 2 * (x & 1);
+          }
+          if constexpr (D == 2)
+            val = 0.5 * pn.at(c1[0], c1[1], iv) + 0.25 * pn.at(c2[0], c1[1], iv) + 0.25 * pn.at(c1[0], c2[1], iv);
+          else
+            val = 0.25 * pn.at(c1[0], c1[1], c1[2], iv) + 0.25 * pn.at(c2[0], c1[1], c1[2], iv) +
+                  0.25 * pn.at(c1[0], c2[1], c1[2], iv) + 0.25 * pn.at(c1[0], c1[1], c2[2], iv);
+        } else {
+          c[dim] = T::neighb_low(nb) ? 2 : nc - 1;
+          val = D == 2 ? b.at(c[0], c[1], iv) : b.at(c[0], c[1], c[2], iv);
+        }
+        side[(size_t)(n - 1) + (size_t)nc * (m - 1)] = val;
+      }
+  }
+}
+
+// flux_from_children (core:841-945, Cartesian): neighbour nb of box id has
+// no children; its fluxes on the shared face become averages of the children's
+template <int D> void flux_from_children(Tree<D>& t, int id, int nb, const std::vector<int>& f_ixs) {
+  using T = Topo<D>;
+  Box<D>& b = t.boxes[id];
+  const int nc = b.n_cell, nch = nc >> 1;
+  const int d = T::neighb_dim(nb);
+  const int n_chnb = 1 << (D - 1);
+  const int nb_id = b.neighbors[nb - 1];
+  Box<D>& o = t.boxes[nb_id];
+  const int i = T::neighb_low(nb) ? 1 : nc + 1, i_nb = T::neighb_low(nb) ? nc + 1 : 1;
+  for (int ic = 0; ic < n_chnb; ++ic) {
+    const int i_ch = T::child_adj_nb(ic, nb);
+    Box<D>& c = t.boxes[b.children[i_ch - 1]];
+    int ioff[D];
+    for (int e = 0; e < D; ++e) ioff[e] = nch * T::child_dix(i_ch, e);
+    for (int f : f_ixs) {
+      if constexpr (D == 2) {
+        for (int n = 1; n <= nch; ++n) {
+          if (d == 0)
+            o.f_at(f, 0, i_nb, ioff[1] + n, 1) = 0.5 * (c.f_at(f, 0, i, 2 * n - 1, 1) + c.f_at(f, 0, i, 2 * n, 1));
+          else
+            o.f_at(f, 1, ioff[0] + n, i_nb, 1) = 0.5 * (c.f_at(f, 1, 2 * n - 1, i, 1) + c.f_at(f, 1, 2 * n, i, 1));
+        }
+      } else {
+        for (int m = 1; m <= nch; ++m)
+          for (int n = 1; n <= nch; ++n) {
+            const int a = 2 * n - 1, bb = 2 * m - 1;
+            switch (d) {
+              case 0:
+                o.f_at(f, 0, i_nb, ioff[1] + n, ioff[2] + m) =
+                    0.25 * (c.f_at(f, 0, i, a, bb) + c.f_at(f, 0, i, a + 1, bb) + c.f_at(f, 0, i, a, bb + 1) +
+                            c.f_at(f, 0, i, a + 1, bb + 1));
+                break;
+              case 1:
+                o.f_at(f, 1, ioff[0] + n, i_nb, ioff[2] + m) =
+                    0.25 * (c.f_at(f, 1, a, i, bb) + c.f_at(f, 1, a + 1, i, bb) + c.f_at(f, 1, a, i, bb + 1) +
+                            c.f_at(f, 1, a + 1, i, bb + 1));
+                break;
+              default:
+                o.f_at(f, 2, ioff[0] + n, ioff[1] + m, i_nb) =
+                    0.25 * (c.f_at(f, 2, a, bb, i) + c.f_at(f, 2, a + 1, bb, i) + c.f_at(f, 2, a, bb + 1, i) +
+                            c.f_at(f, 2, a + 1, bb + 1, i));
+                break;
+            }
+          }
+      }
+    }
+  }
+}
+
+// a$D_consistent_fluxes (core:811-838)
+template <int D> void consistent_fluxes(Tree<D>& t, const std::vector<int>& f_ixs) {
+  using T = Topo<D>;
+  for (int lvl = t.min_lvl; lvl <= t.highest_lvl - 1; ++lvl)
+    for (int id : t.L(lvl).parents)
+      for (int nb = 1; nb <= T::NNB; ++nb) {
+        const int nb_id = t.boxes[id].neighbors[nb - 1];
+        if (nb_id > a5_no_box && t.boxes[nb_id].children[0] == a5_no_box) flux_from_children<D>(t, id, nb, f_ixs);
+      }
+}
+
+// a$D_write_vtk (io:115-310) with the m_vtk.f90 writer; the TIME and CYCLE
+// field values are written as %.17E and %d text
+template <int D>
+int write_vtk(Tree<D>& t, const char* path, int n_cycle, double time, const std::vector<int>& icc,
+              const std::vector<std::string>& cc_names, const std::vector<int>& ifc,
+              const std::vector<std::string>& fc_names) {
+  const int bc = t.n_cell, bn = t.n_cell + 1;
+  const long long nodes_per_box = D == 2 ? bn * bn : bn * bn * bn;
+  const long long cells_per_box = D == 2 ? bc * bc : bc * bc * bc;
+  long long n_grids = 0;
+  for (int lvl = 1; lvl <= t.highest_lvl; ++lvl) n_grids += (long long)t.L(lvl).leaves.size();
+  const long long n_nodes = nodes_per_box * n_grids, n_cells = cells_per_box * n_grids;
+  const int n_cc = (int)icc.size(), n_fc = (int)ifc.size(), ncol = n_cc + D * n_fc;
+  std::vector<double> coords((size_t)(D * n_nodes));
+  std::vector<double> cc_vars((size_t)(n_cells * ncol));  // column-major (cell, var)
+  std::vector<int> offsets((size_t)n_cells), types((size_t)n_cells, D == 2 ? 8 : 11);
+  std::vector<int> connects((size_t)((1 << D) * n_cells));
+  long long ig = 0;
+  const long long bn2 = (long long)bn * bn;
+  for (int lvl = 1; lvl <= t.highest_lvl; ++lvl)
+    for (int id : t.L(lvl).leaves) {
+      Box<D>& b = t.boxes[id];
+      ++ig;
+      const long long cell_ix = (ig - 1) * cells_per_box, node_ix = (ig - 1) * nodes_per_box;
+      for (int k = 1; k <= (D == 3 ? bn : 1); ++k)
+        for (int j = 1; j <= bn; ++j)
+          for (int i = 1; i <= bn; ++i) {
+            const long long n_ix = D * (node_ix + (k - 1) * bn2 + (long long)(j - 1) * bn + i);
+            const int ijk[3] = {i - 1, j - 1, k - 1};
+            for (int d = 0; d < D; ++d) coords[(size_t)(n_ix - D + d)] = b.r_min[d] + ijk[d] * b.dr;
+          }
+      for (int k = 1; k <= (D == 3 ? bc : 1); ++k)
+        for (int j = 1; j <= bc; ++j)
+          for (int i = 1; i <= bc; ++i) {
+            const long long n_ix = node_ix + (k - 1) * bn2 + (long long)(j - 1) * bn + i - 1;
+            const long long c_ix = cell_ix + (long long)(k - 1) * bc * bc + (long long)(j - 1) * bc + i;
+            for (int v = 0; v < n_cc; ++v)
+              cc_vars[(size_t)(v * n_cells + c_ix - 1)] = D == 2 ? b.at(i, j, icc[v]) : b.at(i, j, k, icc[v]);
+            for (int v = 0; v < n_fc; ++v)
+              for (int d = 0; d < D; ++d) {
+                double s = 0.0;
+                s = s + b.f_at(ifc[v], d, i, j, k);
+                s = s + b.f_at(ifc[v], d, i + (d == 0), j + (d == 1), k + (d == 2));
+                cc_vars[(size_t)((n_cc + v * D + d) * n_cells + c_ix - 1)] = 0.5 * s;
+              }
+            offsets[(size_t)(c_ix - 1)] = (1 << D) * (int)c_ix;
+            int* cn = &connects[(size_t)((1 << D) * (c_ix - 1))];
+            cn[0] = (int)n_ix;
+            cn[1] = (int)(n_ix + 1);
+            cn[2] = (int)(n_ix + bn);
+            cn[3] = (int)(n_ix + bn + 1);
+            if (D == 3) {
+              cn[4] = (int)(n_ix + bn2);
+              cn[5] = (int)(n_ix + bn2 + 1);
+              cn[6] = (int)(n_ix + bn2 + bn);
+              cn[7] = (int)(n_ix + bn2 + bn + 1);
+            }
+          }
+    }
+  // m_vtk.f90: vtk_ini_xml .. vtk_end_xml
+  std::string xml;
+  std::vector<char> scratch;
+  int indent = 0;
+  long long offset = 0;
+  auto w = [&](const std::string& s) { xml += std::string(indent, ' ') + s + "\n"; };
+  auto dat = [&](const std::string& n, bool open) {
+    if (open) {
+      w("<" + n + ">");
+      indent += 2;
+    } else {
+      indent -= 2;
+      w("</" + n + ">");
+    }
+  };
+  auto raw = [&](const void* p, long long n_bytes) {
+    const int nb = (int)n_bytes;
+    scratch.insert(scratch.end(), (const char*)&nb, (const char*)&nb + 4);
+    scratch.insert(scratch.end(), (const char*)p, (const char*)p + n_bytes);
+    offset += 4 + n_bytes;
+  };
+  xml = "<?xml version=\"1.0\"?>\n<VTKFile type=\"UnstructuredGrid\" version=\"0.1\" byte_order=\"LittleEndian\">\n";
+  indent = 2;
+  dat("UnstructuredGrid", true);
+  std::vector<float> wr((size_t)(3 * n_nodes), 0.0f);
+  dat("FieldData", true);
+  w("<DataArray type=\"Float64\" Name=\"TIME\" NumberOfTuples=\"1\" format=\"ascii\">");
+  indent += 2;
+  char buf[64];
+  std::snprintf(buf, sizeof buf, "%.17E", time);
+  w(buf);
+  dat("DataArray", false);
+  w("<DataArray type=\"Int32\" Name=\"CYCLE\" NumberOfTuples=\"1\" format=\"ascii\">");
+  indent += 2;
+  w(std::to_string(n_cycle));
+  dat("DataArray", false);
+  dat("FieldData", false);
+  for (int d = 0; d < D; ++d)
+    for (long long n = 0; n < n_nodes; ++n) wr[(size_t)(3 * n + d)] = (float)coords[(size_t)(D * n + d)];
+  w("<Piece NumberOfPoints=\"" + std::to_string(n_nodes) + "\" NumberOfCells=\"" + std::to_string(n_cells) + "\">");
+  indent += 2;
+  dat("Points", true);
+  w("<DataArray type=\"Float32\" NumberOfComponents=\"3\" Name=\"Points\" format=\"appended\" offset=\"" +
+    std::to_string(offset) + "\"/>");
+  raw(wr.data(), 3 * n_nodes * 4);
+  dat("Points", false);
+  dat("Cells", true);
+  w("<DataArray type=\"Int32\" Name=\"connectivity\" format=\"appended\" offset=\"" + std::to_string(offset) + "\"/>");
+  raw(connects.data(), (n_cells ? (long long)offsets[(size_t)(n_cells - 1)] : 0) * 4);
+  w("<DataArray type=\"Int32\" Name=\"offsets\" format=\"appended\" offset=\"" + std::to_string(offset) + "\"/>");
+  raw(offsets.data(), n_cells * 4);
+  w("<DataArray type=\"Int32\" Name=\"types\" format=\"appended\" offset=\"" + std::to_string(offset) + "\"/>");
+  raw(types.data(), n_cells * 4);
+  dat("Cells", false);
+  dat("CellData", true);
+  std::vector<std::string> names(cc_names);
+  const char* sfx[3] = {"_x", "_y", "_z"};
+  for (int v = 0; v < n_fc; ++v)
+    for (int d = 0; d < D; ++d) names.push_back(fc_names[(size_t)v] + sfx[d]);
+  for (int c = 0; c < ncol; ++c) {
+    w("<DataArray type=\"Float64\" Name=\"" + names[(size_t)c] +
+      "\" NumberOfComponents=\"1\" format=\"appended\" offset=\"" + std::to_string(offset) + "\"/>");
+    raw(cc_vars.data() + (size_t)c * n_cells, n_cells * 8);
+  }
+  dat("CellData", false);
+  dat("Piece", false);  // vtk_unstr_geo_xml_close
+  dat("UnstructuredGrid", false);
+  w("<AppendedData encoding=\"raw\">");
+  FILE* fp = std::fopen(path, "wb");
+  if (!fp) return -1;
+  std::fwrite(xml.data(), 1, xml.size(), fp);
+  std::fputc('_', fp);
+  if (!scratch.empty()) std::fwrite(scratch.data(), 1, scratch.size(), fp);
+  std::string tail = "\n" + std::string(indent, ' ') + "</AppendedData>\n";
+  indent -= 2;
+  tail += std::string(indent, ' ') + "</VTKFile>\n";
+  std::fwrite(tail.data(), 1, tail.size(), fp);
+  std::fclose(fp);
+  return 0;
+}
+
 struct OrcHandle {
   int dim;
   void* tree;
@@ -1700,6 +2234,92 @@ int orc_neighb_dix(int dim, int d, int nb) {
 }
 int orc_ix_to_ichild(int dim, const int* ix) {
   return dim == 2 ? Topo<2>::ix_to_ichild(ix) : Topo<3>::ix_to_ichild(ix);
+}
+
+
+// General ghost-cell, transfer and output routines (see above).
+void orc_add_vars(OrcHandle* h, int n_cc, int n_fc) {
+  if (h->dim == 2)
+    add_vars<2>(TT<2>(h), n_cc, n_fc);
+  else
+    add_vars<3>(TT<3>(h), n_cc, n_fc);
+}
+static long long fc_io(OrcHandle* h, int ifc, double* buf, bool get) {
+  long long off = 0;
+  auto go = [&](auto& t) {
+    for (int lvl = t.min_lvl; lvl <= t.highest_lvl; ++lvl)
+      for (int id : t.L(lvl).ids) {
+        auto& b = t.boxes[id];
+        const long long n = (long long)(h->dim) * b.fblock();
+        double* v = b.fc.data() + (size_t)ifc * n;
+        if (buf) {
+          if (get)
+            std::copy(v, v + n, buf + off);
+          else
+            std::copy(buf + off, buf + off + n, v);
+        }
+        off += n;
+      }
+  };
+  if (h->dim == 2)
+    go(TT<2>(h));
+  else
+    go(TT<3>(h));
+  return off;
+}
+long long orc_fc_count(OrcHandle* h) { return fc_io(h, 0, nullptr, true); }
+void orc_get_fc(OrcHandle* h, int ifc, double* out) { fc_io(h, ifc, out, true); }
+void orc_set_fc(OrcHandle* h, int ifc, double* in) { fc_io(h, ifc, in, false); }
+void orc_prolong_from_level(OrcHandle* h, int lvl, int iv, int iv_to, int order, int add) {
+  if (h->dim == 2)
+    prolong_from_level<2>(TT<2>(h), lvl, iv, iv_to, order, add != 0);
+  else
+    prolong_from_level<3>(TT<3>(h), lvl, iv, iv_to, order, add != 0);
+}
+void orc_restrict_tree(OrcHandle* h, int iv, int iv_to) {
+  if (h->dim == 2)
+    restrict_tree<2>(TT<2>(h), iv, iv_to);
+  else
+    restrict_tree<3>(TT<3>(h), iv, iv_to);
+}
+void orc_gc_tree_var(OrcHandle* h, int iv, int rb, int bcm) {
+  if (h->dim == 2)
+    gc_tree_var<2>(TT<2>(h), iv, rb, bcm, h->mg);
+  else
+    gc_tree_var<3>(TT<3>(h), iv, rb, bcm, h->mg);
+}
+// a$D_gc2_box on every box of a level (level-list order), (nc[,nc], 2D) each
+void orc_gc2_level(OrcHandle* h, int lvl, int iv, double* out) {
+  auto go = [&](auto& t, int D) {
+    const int nc = t.n_cell;
+    const long long per = 2LL * D * (D == 2 ? nc : nc * nc);
+    long long off = 0;
+    for (int id : t.L(lvl).ids) {
+      if (D == 2)
+        gc2_box<2>(TT<2>(h), id, iv, out + off);
+      else
+        gc2_box<3>(TT<3>(h), id, iv, out + off);
+      off += per;
+    }
+  };
+  if (h->dim == 2)
+    go(TT<2>(h), 2);
+  else
+    go(TT<3>(h), 3);
+}
+void orc_consistent_fluxes(OrcHandle* h, int n, const int* f_ixs) {
+  std::vector<int> f(f_ixs, f_ixs + n);
+  if (h->dim == 2)
+    consistent_fluxes<2>(TT<2>(h), f);
+  else
+    consistent_fluxes<3>(TT<3>(h), f);
+}
+int orc_write_vtk(OrcHandle* h, const char* path, int n_cycle, double time, int n_cc, const int* icc,
+                  const char* const* cc_names, int n_fc, const int* ifc, const char* const* fc_names) {
+  std::vector<int> a(icc, icc + n_cc), b(ifc, ifc + n_fc);
+  std::vector<std::string> an(cc_names, cc_names + n_cc), bn(fc_names, fc_names + n_fc);
+  return h->dim == 2 ? write_vtk<2>(TT<2>(h), path, n_cycle, time, a, an, b, bn)
+                     : write_vtk<3>(TT<3>(h), path, n_cycle, time, a, an, b, bn);
 }
 
 }  // extern "C"

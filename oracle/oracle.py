@@ -75,6 +75,19 @@ def lib():
         L.orc_morton_to_ix.argtypes = [ctypes.c_int, ctypes.c_ulonglong, ip]
         L.orc_ix_to_ichild.argtypes = [ctypes.c_int, ip]
         L.orc_set_threads.argtypes = [ctypes.c_int]
+        L.orc_add_vars.argtypes = [P, ctypes.c_int, ctypes.c_int]
+        L.orc_fc_count.argtypes = [P]
+        L.orc_fc_count.restype = ctypes.c_longlong
+        L.orc_get_fc.argtypes = [P, ctypes.c_int, dp]
+        L.orc_set_fc.argtypes = [P, ctypes.c_int, dp]
+        L.orc_prolong_from_level.argtypes = [P] + [ctypes.c_int] * 5
+        L.orc_restrict_tree.argtypes = [P, ctypes.c_int, ctypes.c_int]
+        L.orc_gc_tree_var.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+        L.orc_gc2_level.argtypes = [P, ctypes.c_int, ctypes.c_int, dp]
+        L.orc_consistent_fluxes.argtypes = [P, ctypes.c_int, ip]
+        cpp = ctypes.POINTER(ctypes.c_char_p)
+        L.orc_write_vtk.argtypes = [P, ctypes.c_char_p, ctypes.c_int, ctypes.c_double,
+                                    ctypes.c_int, ip, cpp, ctypes.c_int, ip, cpp]
         _lib = L
     return _lib
 
@@ -239,6 +252,49 @@ class OracleTree:
 
     def leaf_mean(self, iv):
         return lib().orc_leaf_mean(self.h, iv)
+
+    # general ghost cells, transfers and output ---------------------------------
+    def add_vars(self, n_cc=0, n_fc=0):
+        lib().orc_add_vars(self.h, n_cc, n_fc)
+
+    def get_fc(self, ifc):
+        out = np.zeros(lib().orc_fc_count(self.h))
+        lib().orc_get_fc(self.h, ifc, _dp(out))
+        return out
+
+    def set_fc(self, ifc, values):
+        a = np.ascontiguousarray(values, dtype=np.float64)
+        lib().orc_set_fc(self.h, ifc, _dp(a))
+
+    def prolong(self, lvl_parent, iv, iv_to=None, order=2, add=False):
+        lib().orc_prolong_from_level(self.h, lvl_parent, iv, iv if iv_to is None else iv_to,
+                                     order, int(add))
+
+    def restrict_tree(self, iv, iv_to=None):
+        lib().orc_restrict_tree(self.h, iv, iv if iv_to is None else iv_to)
+
+    def gc_tree_var(self, iv, rb=0, bc=0):
+        lib().orc_gc_tree_var(self.h, iv, rb, bc)
+
+    def gc2_level(self, lvl, iv, n_cell):
+        n = len(self.level(lvl)[0]) * 2 * self.dim * n_cell ** (self.dim - 1)
+        out = np.zeros(n)
+        lib().orc_gc2_level(self.h, lvl, iv, _dp(out))
+        return out
+
+    def consistent_fluxes(self, f_ixs):
+        a = np.ascontiguousarray(f_ixs, dtype=np.int32)
+        lib().orc_consistent_fluxes(self.h, a.size, _ip(a))
+
+    def write_vtk(self, path, ixs_cc, cc_names, ixs_fc=(), fc_names=(), n_cycle=0, time=0.0):
+        icc = np.ascontiguousarray(ixs_cc, dtype=np.int32)
+        ifc = np.ascontiguousarray(ixs_fc, dtype=np.int32)
+        cn = (ctypes.c_char_p * max(1, len(cc_names)))(*[n.encode() for n in cc_names])
+        fn = (ctypes.c_char_p * max(1, len(fc_names)))(*[n.encode() for n in fc_names])
+        rc = lib().orc_write_vtk(self.h, path.encode(), n_cycle, float(time), icc.size, _ip(icc),
+                                 cn, ifc.size, _ip(ifc), fn)
+        if rc != 0:
+            raise OSError(f"cannot write {path}")
 
 
 def morton_from_ix(ix):

@@ -144,3 +144,18 @@ def same_tree(a, o):
     for l in range(o.min_lvl, o.highest_lvl + 2):
         for x, y in zip(a.level(l), o.level(l)):
             assert np.array_equal(x, y), l
+
+
+def interior_to_ghosted(flat_int, t, n_cell, dim):
+    """A host-layout interior-only array (cc(1:nc,...) per box) spread into the
+    ghosted layout, ghost cells zero."""
+    parts, off = [], 0
+    for l in range(t.min_lvl, t.highest_lvl + 1):
+        n = len(t.level(l)[0])
+        nc = n_cell if l >= 1 else n_cell >> (1 - l)
+        g = np.zeros((n,) + (nc + 2,) * dim)
+        sl = (slice(None),) + (slice(1, nc + 1),) * dim
+        g[sl] = flat_int[off:off + n * nc ** dim].reshape((n,) + (nc,) * dim)
+        off += n * nc ** dim
+        parts.append(g.ravel())
+    return np.concatenate(parts)

@@ -491,8 +491,10 @@ def test_wait_limit_error_path(gpu):
     assert default == 2000000
     for prec in (gpu.AFV_PREC_MIXED, gpu.AFV_PREC_FP64):
         f.set_option(gpu.AFV_OPT_WAIT_LIMIT_US, 0)
+        assert f.get_option(gpu.AFV_OPT_WAIT_LIMIT_US) == 0
+        f.zero(gpu.AFV_PHI)
         cyc, rel, rc = f.solve(prec, tol=1e-8, max_cycles=5, check=False)
-        assert rc == gpu.AFV_ERR_TIMEOUT, rc
+        assert rc == gpu.AFV_ERR_TIMEOUT, (prec, rc, cyc, rel)
         with pytest.raises(gpu.AfivoError) as e:
             f.vcycle()
         assert e.value.code == gpu.AFV_ERR_TIMEOUT
