@@ -45,6 +45,7 @@ AFV_OPT_PROFILE_LEAD_US, AFV_OPT_DEFECT_KERNEL, AFV_OPT_COARSE_END = 4, 5, 6
 AFV_OPT_WAIT_LIMIT_US = 7
 AFV_RB_MG, AFV_RB_PROLONG0, AFV_RB_INTERP, AFV_RB_INTERP_LIM = 0, 1, 2, 3
 AFV_BCM_TABLE, AFV_BCM_DIRICHLET_ZERO, AFV_BCM_NEUMANN_ZERO = 0, -1, -2
+AFV_OP_LPL, AFV_OP_LPLD, AFV_OP_AUTO = 0, 1, 2
 KERNEL_KINDS = ("sweep", "fill", "restrict", "coarse_rhs", "correct", "residual", "defect",
                 "accumulate", "coarse_end")
 
@@ -150,6 +151,7 @@ def lib():
             "afv_forest_profile": (I, [P, I]),
             "afv_forest_profile_read": (I, [P, I, llp, dp, dp]),
             "afv_forest_add_vars": (I, [P, I, I]),
+            "afv_mg_set_operator": (I, [P, I, I]),
             "afv_forest_set_fc": (I, [P, I, I, dp, LL]),
             "afv_forest_get_fc": (I, [P, I, I, dp, LL]),
             "afv_prolong_from_level": (I, [P, I, I, I, I, I]),
@@ -454,6 +456,10 @@ class Forest:
         """Extra cell variables (numbered 3, 4, ...) and face variables."""
         _check(lib().afv_forest_add_vars(self.h, n_cc, n_fc))
         self.__dict__["_n_fc"] = self.__dict__.get("_n_fc", 0) + n_fc
+
+    def set_operator(self, op, i_eps=-1):
+        """mg%box_op / box_gsrb / box_corr and mg%i_eps (AFV_OP_*)."""
+        _check(lib().afv_mg_set_operator(self.h, op, i_eps))
 
     def fc_count(self, tree):
         t = self.trees[tree]

@@ -485,6 +485,10 @@ int afv_forest_get_option(afv_forest* f, int option, int* value) {
   return fail(AFV_ERR_INVALID, "unknown option");
 }
 
+int afv_mg_set_operator(afv_forest* f, int op, int i_eps) {
+  FOREST_CALL(f, return f->f.set_operator(op, i_eps, err));
+}
+
 int afv_forest_add_vars(afv_forest* f, int n_cc, int n_fc) {
   FOREST_CALL(f, return afv::forest_add_vars(f->f, n_cc, n_fc, err));
 }

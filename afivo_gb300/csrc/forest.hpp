@@ -119,6 +119,21 @@ class Forest {
   int* d_nb = nullptr;
   int* d_lvl = nullptr;
   int* d_qd = nullptr;
+  // Operator of the FP64 multigrid routines (afv_mg_set_operator): AFV_OP_LPL
+  // (the fused constant-coefficient kernels), AFV_OP_LPLD or AFV_OP_AUTO (the
+  // generic kernels of operators.cu, with eps in cell variable i_eps and the
+  // per-box tags of the auto dispatch in d_tags).
+  int op = AFV_OP_LPL;
+  int i_eps = -1;
+  int* d_tags = nullptr;
+  int set_operator(int new_op, int new_i_eps, std::string& err);
+  const double* eps_ptr() const;
+  void gen_gsrb_boxes(int lvl, int n_cycle);
+  void gen_update_coarse(int lvl, bool copy_tmp);
+  void gen_correct(int lvl_parent);
+  void gen_residual(int lvl, unsigned long long* norm);
+  void gen_vcycle(const MgOpts& mg, int highest, bool set_residual);
+  void fill64(int lvl);  // ghost fill of the FP64 phi of a level (mg sides_rb, sides_bc)
   int n_cc_vars() const { return 3 + (int)xcc.size(); }
   // Device array of cell variable iv (0 phi, 1 rhs, 2 tmp, 3.. extra).
   double* var_ptr(int iv) const {

@@ -2167,7 +2167,7 @@ __device__ __forceinline__ void box_max_atomic(V v, unsigned long long* dst, V* 
   }
 }
 
-__global__ void k_stripe_reduce(int n_trees, const unsigned long long* __restrict__ norm,
+static __global__ void k_stripe_reduce(int n_trees, const unsigned long long* __restrict__ norm,
                                 unsigned long long* __restrict__ out) {
   pdl_wait();
   pdl_trigger();
@@ -2923,7 +2923,7 @@ __global__ void k_gather(Meta m, const int* __restrict__ slots, int n, const T* 
 // ahead of each solve iteration, so that the host has enqueued the
 // iteration's launches before the device reaches them and the events time the
 // kernels, not the rate at which the host launches them.
-__global__ void k_hold(long long ns) {
+static __global__ void k_hold(long long ns) {
   unsigned long long t0, t;
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
   for (long long r = 0; r < ns / 1000 + 1000; ++r) {
@@ -2935,7 +2935,7 @@ __global__ void k_hold(long long ns) {
 
 // Per-tree convergence bookkeeping on the device: a tree stays active while
 // max|r| > tol * max|f|; a non-finite residual stops it and marks it failed.
-__global__ void k_check(int n_trees, const unsigned long long* __restrict__ rnorm,
+static __global__ void k_check(int n_trees, const unsigned long long* __restrict__ rnorm,
                         const double* __restrict__ fmax, double tol, int* __restrict__ active,
                         int* __restrict__ failed, int* __restrict__ n_active_out, const int* __restrict__ err,
                         int* __restrict__ cycles, unsigned long long* __restrict__ final_r, int count_cycle) {
@@ -2962,7 +2962,7 @@ __global__ void k_check(int n_trees, const unsigned long long* __restrict__ rnor
 }
 
 // Sets n ints to v (activity flags).
-__global__ void k_set_int(int* __restrict__ a, int n, int v) {
+static __global__ void k_set_int(int* __restrict__ a, int n, int v) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) a[i] = v;
 }
 
@@ -2972,11 +2972,11 @@ __global__ void k_set_int(int* __restrict__ a, int n, int v) {
 // run. k_loop_start enters the loop if a tree is active; k_loop_step, at the
 // end of every iteration, repeats it while one is, below max_cycles
 // iterations and without a device error.
-__global__ void k_loop_start(cudaGraphConditionalHandle h, int* __restrict__ count, int max_cycles) {
+static __global__ void k_loop_start(cudaGraphConditionalHandle h, int* __restrict__ count, int max_cycles) {
   count[2] = 0;
   cudaGraphSetConditional(h, (count[0] > 0 && max_cycles > 0) ? 1u : 0u);
 }
-__global__ void k_loop_step(cudaGraphConditionalHandle h, int* __restrict__ count, int max_cycles) {
+static __global__ void k_loop_step(cudaGraphConditionalHandle h, int* __restrict__ count, int max_cycles) {
   const int c = count[2] + 1;
   count[2] = c;
   cudaGraphSetConditional(h, (count[0] > 0 && c < max_cycles && count[1] == 0) ? 1u : 0u);

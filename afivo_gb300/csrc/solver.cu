@@ -162,7 +162,7 @@ Forest::~Forest() {
     if (p) cudaFreeAsync(p, stream);
   for (double* p : xcc)
     if (p) cudaFreeAsync(p, stream);
-  for (void* p : {(void*)fc, (void*)d_nb, (void*)d_lvl, (void*)d_qd})
+  for (void* p : {(void*)fc, (void*)d_nb, (void*)d_lvl, (void*)d_qd, (void*)d_tags})
     if (p) cudaFreeAsync(p, stream);
   if (stream) cudaStreamSynchronize(stream);
   for (const ProfEntry& p : prof) {
@@ -991,7 +991,14 @@ void Forest::vcycle_t(const Arrays<T>& a, const MgOpts& mg, int highest, bool ho
 // FP64 entry points
 // ---------------------------------------------------------------------------
 
+void Forest::fill64(int lvl) { fill(d64, lvl, false); }
+
 int Forest::gsrb_level(int lvl, int n_cycle, std::string& err) {
+  if (op != AFV_OP_LPL) {
+    gen_gsrb_boxes(lvl, n_cycle);
+    if (int rc = check(err, "gsrb_level")) return rc;
+    return check_device_error(err);
+  }
   gsrb_boxes(d64, lvl, n_cycle, false);
   if (int rc = check(err, "gsrb_level")) return rc;
   return check_device_error(err);
@@ -1002,25 +1009,39 @@ int Forest::fill_level(int lvl, std::string& err) {
 }
 int Forest::update_coarse(int lvl, std::string& err) {
   if (lvl <= plan.min_lvl || lvl > plan.max_lvl) return err = "level out of range", AFV_ERR_INVALID;
-  update_coarse_t(d64, lvl, false, true);
+  if (op != AFV_OP_LPL)
+    gen_update_coarse(lvl, true);
+  else
+    update_coarse_t(d64, lvl, false, true);
   return check(err, "update_coarse");
 }
 int Forest::correct_children(int lp, std::string& err) {
   if (lp < plan.min_lvl || lp >= plan.max_lvl) return err = "level out of range", AFV_ERR_INVALID;
-  correct(d64, lp);
+  if (op != AFV_OP_LPL)
+    gen_correct(lp);
+  else
+    correct(d64, lp);
   return check(err, "correct_children");
 }
 int Forest::residual_all(unsigned long long* norm, std::string& err) {
-  for (int l = plan.min_lvl; l <= plan.max_lvl; ++l) residual(d64, l, norm, true);
+  for (int l = plan.min_lvl; l <= plan.max_lvl; ++l)
+    if (op != AFV_OP_LPL)
+      gen_residual(l, norm);
+    else
+      residual(d64, l, norm, true);
   return check(err, "residual");
 }
 
 int Forest::vcycle(const MgOpts& mg, int highest, bool set_residual, std::string& err) {
   if (highest < plan.min_lvl) return err = "highest_lvl below the coarsest level", AFV_ERR_INVALID;
   highest = std::min(highest, plan.max_lvl);
-  vcycle_t(d64, mg, highest, false, false);
-  if (set_residual)
-    for (int l = plan.min_lvl; l <= highest; ++l) residual(d64, l, nullptr, true);
+  if (op != AFV_OP_LPL) {
+    gen_vcycle(mg, highest, set_residual);
+  } else {
+    vcycle_t(d64, mg, highest, false, false);
+    if (set_residual)
+      for (int l = plan.min_lvl; l <= highest; ++l) residual(d64, l, nullptr, true);
+  }
   if (int rc = check(err, "vcycle")) return rc;
   return check_device_error(err);
 }
@@ -1125,7 +1146,10 @@ int Forest::fmg(const MgOpts& mg, bool set_residual, bool have_guess, std::strin
         fill(d64, l, false);
         set_active_host(all);
       }
-      update_coarse_t(d64, l, false, false);
+      if (op != AFV_OP_LPL)
+        gen_update_coarse(l, false);
+      else
+        update_coarse_t(d64, l, false, false);
     }
   } else {
     // init_phi_rhs: phi = 0 on levels > min_lvl, rhs restricted downwards.
@@ -1172,10 +1196,16 @@ int Forest::fmg(const MgOpts& mg, bool set_residual, bool have_guess, std::strin
       });
     }
     if (l > l0) {
-      correct(d64, l - 1);
+      if (op != AFV_OP_LPL)
+        gen_correct(l - 1);
+      else
+        correct(d64, l - 1);
       fill(d64, l, false);
     }
-    vcycle_t(d64, mg, l, false, false);
+    if (op != AFV_OP_LPL)
+      gen_vcycle(mg, l, false);
+    else
+      vcycle_t(d64, mg, l, false, false);
     if (set_residual) {
       std::vector<int> fin(plan.n_trees, 0);
       bool any = false;
@@ -1183,7 +1213,11 @@ int Forest::fmg(const MgOpts& mg, bool set_residual, bool have_guess, std::strin
         if (plan.tree_highest[t] == l) fin[t] = 1, any = true;
       if (any) {
         set_active_host(fin);
-        for (int k = l0; k <= l; ++k) residual(d64, k, nullptr, true);
+        for (int k = l0; k <= l; ++k)
+          if (op != AFV_OP_LPL)
+            gen_residual(k, nullptr);
+          else
+            residual(d64, k, nullptr, true);
       }
     }
   }
@@ -1269,6 +1303,8 @@ void Forest::enqueue_residual_check(int precision, double tol, int count_cycle) 
                  d64.phi, d64.rhs, d32.rhs, d_norm);
       }
     });
+  } else if (op != AFV_OP_LPL) {
+    for (int l = plan.min_lvl; l <= plan.max_lvl; ++l) gen_residual(l, d_norm);
   } else {
     for (int l = plan.min_lvl; l <= plan.max_lvl; ++l) residual(d64, l, d_norm, true);
   }
@@ -1339,7 +1375,10 @@ void Forest::enqueue_iteration(const MgOpts& mg, int precision, double tol) {
     enqueue_residual_check(precision, tol);
     join();
   } else {
-    vcycle_t(d64, mg, plan.max_lvl, false, false);
+    if (op != AFV_OP_LPL)
+      gen_vcycle(mg, plan.max_lvl, false);
+    else
+      vcycle_t(d64, mg, plan.max_lvl, false, false);
     enqueue_residual_check(precision, tol);
   }
 }
@@ -1493,6 +1532,8 @@ int Forest::solve(const MgOpts& mg, int precision, double tol, int max_cycles, S
   const int nt = plan.n_trees;
   if (precision == AFV_PREC_MIXED && !mixed)
     return err = "forest created without mixed_buffers", AFV_ERR_STATE;
+  if (precision == AFV_PREC_MIXED && op != AFV_OP_LPL)
+    return err = "mixed-precision solves take the constant-coefficient operator only", AFV_ERR_UNSUPPORTED;
   st.cycles.assign(nt, 0);
   st.rel_res.assign(nt, 0.0);
   const bool graph = use_graphs && prof_mask == 0;

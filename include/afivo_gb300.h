@@ -191,6 +191,24 @@ int afv_forest_get_stream(afv_forest* f, void** stream);
 
 /* mg$D_init_mg, src/m_aX_mg.f90:130-154. */
 int afv_mg_init(afv_mg_opts* mg);
+/* Operators of the multigrid routines (mg%box_op, mg%box_gsrb, mg%box_corr;
+ * mg%box_rstr stays mg$D_box_rstr_lpl): AFV_OP_LPL, the constant-coefficient
+ * Laplacian (mg$D_box_*_lpl, the default); AFV_OP_LPLD, the variable-
+ * coefficient operator div(eps grad phi) on every box (mg$D_box_gsrb_lpld,
+ * mg$D_box_lpld, mg$D_box_corr_lpld, src/m_aX_mg.f90:810-985); AFV_OP_AUTO,
+ * the per-box dispatch of mg$D_auto_gsrb / _op / _corr (:562-669), boxes
+ * whose eps is 1 everywhere taking the AFV_OP_LPL operators. */
+enum { AFV_OP_LPL = 0, AFV_OP_LPLD = 1, AFV_OP_AUTO = 2 };
+/* Sets mg%box_op / box_gsrb / box_corr and mg%i_eps of a forest. eps is the
+ * extra cell variable i_eps (>= 3, afv_forest_add_vars); as with the
+ * reference, the caller fills its ghost cells and coarse levels (for instance
+ * afv_gc_tree_var and afv_restrict_tree). For AFV_OP_AUTO the per-box tags of
+ * mg$D_set_box_tag (:672-706, min and max of eps over the box, ghost cells
+ * included) are taken by this call, where the reference takes each box's tag
+ * at its first use: call it again after changing eps. The operator applies to
+ * the FP64 routines (V-cycle, FMG, single operators, FP64 solves); a mixed-
+ * precision solve with a variable coefficient returns AFV_ERR_UNSUPPORTED. */
+int afv_mg_set_operator(afv_forest* f, int op, int i_eps);
 /* mg$D_fas_vcycle, src/m_aX_mg.f90:208-255 (all trees of the forest). */
 int afv_mg_fas_vcycle(afv_forest* f, const afv_mg_opts* mg, int highest_lvl, int set_residual);
 /* mg$D_fas_fmg, src/m_aX_mg.f90:164-203. */

@@ -172,7 +172,15 @@ template <int D> struct Tree {
   int n_boxes_capacity() const { return (int)boxes.size() - 1; }
 };
 
+// Operators of the multigrid routines (mg%box_op / box_gsrb / box_corr):
+// the constant-coefficient Laplacian, the variable-coefficient lpld
+// operators, or the per-box auto dispatch (src/m_aX_mg.f90:562-706, 810-985).
+enum { OP_LPL = 0, OP_LPLD = 1, OP_AUTO = 2 };
+enum { MG_NORMAL_BOX = 1, MG_LSF_BOX = 2, MG_CEPS_BOX = 3, MG_VEPS_BOX = 4 };
+
 struct MG {
+  int op = OP_LPL;
+  int i_eps = -1;
   int i_phi = 0, i_rhs = 1, i_tmp = 2;
   int n_cycle_down = 2, n_cycle_up = 2, n_cycle_base = 2;
   int bc_kind = BC_DIRICHLET_ZERO;
@@ -1109,6 +1117,128 @@ template <int D> void box_lpl(Box<D>& b, int i_out, const MG& mg) {
   }
 }
 
+// mg$D_set_box_tag (mg:672-706) without the level-set part: min and max of
+// eps over the whole box, ghost cells included
+template <int D> void set_box_tag(Box<D>& b, const MG& mg) {
+  bool is_eps = false, is_deps = false;
+  if (mg.i_eps != -1) {
+    const double* e = b.var(mg.i_eps);
+    double a = e[0], c = e[0];
+    for (int n = 0; n < b.nvol(); ++n) {
+      a = std::min(a, e[n]);
+      c = std::max(c, e[n]);
+    }
+    is_deps = c > a;
+    if (!is_deps) is_eps = (a < 1 || a > 1);
+  }
+  b.tag = MG_NORMAL_BOX;
+  if (is_eps) b.tag = MG_CEPS_BOX;
+  if (is_deps) b.tag = MG_VEPS_BOX;
+}
+
+// Neighbour values of cell (i,j[,k]) in the reference's order (i-1, i+1,
+// j-1, j+1[, k-1, k+1]).
+template <int D> void nb_vals(Box<D>& b, int iv, int i, int j, int k, double* out) {
+  if constexpr (D == 2) {
+    out[0] = b.at(i - 1, j, iv);
+    out[1] = b.at(i + 1, j, iv);
+    out[2] = b.at(i, j - 1, iv);
+    out[3] = b.at(i, j + 1, iv);
+  } else {
+    out[0] = b.at(i - 1, j, k, iv);
+    out[1] = b.at(i + 1, j, k, iv);
+    out[2] = b.at(i, j - 1, k, iv);
+    out[3] = b.at(i, j + 1, k, iv);
+    out[4] = b.at(i, j, k - 1, iv);
+    out[5] = b.at(i, j, k + 1, iv);
+  }
+}
+
+// mg$D_box_gsrb_lpld, mg:810-859
+template <int D> void box_gsrb_lpld(Box<D>& b, int redblack_cntr, const MG& mg) {
+  const double dx2 = b.dr * b.dr;
+  const int nc = b.n_cell, ip = mg.i_phi, ie = mg.i_eps, ir = mg.i_rhs;
+  const int kmax = D == 3 ? nc : 1;
+  for (int k = 1; k <= kmax; ++k)
+    for (int j = 1; j <= nc; ++j) {
+      const int i0 = 2 - ((redblack_cntr ^ (D == 3 ? k + j : j)) & 1);
+      for (int i = i0; i <= nc; i += 2) {
+        double u[6], a[6], c[6];
+        const double a0 = D == 2 ? b.at(i, j, ie) : b.at(i, j, k, ie);
+        nb_vals<D>(b, ip, i, j, k, u);
+        nb_vals<D>(b, ie, i, j, k, a);
+        for (int n = 0; n < 2 * D; ++n) c[n] = 2 * a0 * a[n] / (a0 + a[n]);
+        double scu = 0.0, sc = 0.0;
+        for (int n = 0; n < 2 * D; ++n) scu = scu + c[n] * u[n];
+        for (int n = 0; n < 2 * D; ++n) sc = sc + c[n];
+        double& o = D == 2 ? b.at(i, j, ip) : b.at(i, j, k, ip);
+        o = (scu - dx2 * (D == 2 ? b.at(i, j, ir) : b.at(i, j, k, ir))) / sc;
+      }
+    }
+}
+
+// mg$D_box_lpld, mg:861-905
+template <int D> void box_lpld(Box<D>& b, int i_out, const MG& mg) {
+  const int nc = b.n_cell, ip = mg.i_phi, ie = mg.i_eps;
+  const double inv_dr_sq = 1 / (b.dr * b.dr);
+  const int kmax = D == 3 ? nc : 1;
+  for (int k = 1; k <= kmax; ++k)
+    for (int j = 1; j <= nc; ++j)
+      for (int i = 1; i <= nc; ++i) {
+        double u[6], a[6];
+        const double u0 = D == 2 ? b.at(i, j, ip) : b.at(i, j, k, ip);
+        const double a0 = D == 2 ? b.at(i, j, ie) : b.at(i, j, k, ie);
+        nb_vals<D>(b, ip, i, j, k, u);
+        nb_vals<D>(b, ie, i, j, k, a);
+        double s = 0.0;
+        for (int n = 0; n < 2 * D; ++n) s = s + a0 * a[n] / (a0 + a[n]) * (u[n] - u0);
+        (D == 2 ? b.at(i, j, i_out) : b.at(i, j, k, i_out)) = inv_dr_sq * 2 * s;
+      }
+}
+
+// mg$D_box_corr_lpld, mg:907-985
+template <int D> void box_corr_lpld(Box<D>& p, Box<D>& c, const MG& mg) {
+  const int nc = c.n_cell, ip = mg.i_phi, it = mg.i_tmp, ie = mg.i_eps;
+  int off[D];
+  child_offset(c, off);
+  const double third = 1 / 3.0;
+  const int kmax = D == 3 ? nc : 1;
+  for (int k = 1; k <= kmax; ++k) {
+    const int k_c1 = D == 3 ? off[D - 1] + ((k + 1) >> 1) : 0;
+    const int k_c2 = k_c1 + 1 - 2 * (k & 1);
+    for (int j = 1; j <= nc; ++j) {
+      const int j_c1 = off[1] + ((j + 1) >> 1), j_c2 = j_c1 + 1 - 2 * (j & 1);
+      for (int i = 1; i <= nc; ++i) {
+        const int i_c1 = off[0] + ((i + 1) >> 1), i_c2 = i_c1 + 1 - 2 * (i & 1);
+        if constexpr (D == 2) {
+          const double u0 = p.at(i_c1, j_c1, it), a0 = p.at(i_c1, j_c1, ie);
+          const double u[2] = {p.at(i_c2, j_c1, it), p.at(i_c1, j_c2, it)};
+          const double a[2] = {p.at(i_c2, j_c1, ie), p.at(i_c1, j_c2, ie)};
+          double s = 0.0;
+          for (int n = 0; n < 2; ++n) s = s + (a0 * u0 + a[n] * u[n]) / (a0 + a[n]);
+          c.at(i, j, ip) = c.at(i, j, ip) + 0.5 * s;
+        } else {
+          const double u0 = p.at(i_c1, j_c1, k_c1, it), a0 = p.at(i_c1, j_c1, k_c1, ie);
+          const double u[3] = {p.at(i_c2, j_c1, k_c1, it), p.at(i_c1, j_c2, k_c1, it), p.at(i_c1, j_c1, k_c2, it)};
+          const double a[3] = {p.at(i_c2, j_c1, k_c1, ie), p.at(i_c1, j_c2, k_c1, ie), p.at(i_c1, j_c1, k_c2, ie)};
+          double s = 0.0;
+          for (int n = 0; n < 3; ++n) s = s + (a0 * u0 + a[n] * (1.5 * u[n] - 0.5 * u0)) / (a0 + a[n]);
+          c.at(i, j, k, ip) = c.at(i, j, k, ip) + third * s;
+        }
+      }
+    }
+  }
+}
+
+// The operator hooks as the driver calls them: mg%box_gsrb, mg%box_op
+// (mg$D_auto_gsrb / mg$D_auto_op, mg:562-622, choose by the box's own tag).
+template <int D> bool use_lpld(Box<D>& b, const MG& mg) {
+  if (mg.op == OP_LPL) return false;
+  if (mg.op == OP_LPLD) return true;
+  if (b.tag == a5_init_tag) set_box_tag<D>(b, mg);
+  return b.tag != MG_NORMAL_BOX;
+}
+
 // Interior / full-array helpers, utils:262-352
 template <int D> void interior_for(Box<D>& b, int iv_a, int iv_b, int mode) {
   // mode 0: b = a - b ; mode 1: b = a (interior only)
@@ -1134,8 +1264,28 @@ template <int D> void interior_for(Box<D>& b, int iv_a, int iv_b, int mode) {
 }
 
 // residual_box, mg:545-559
+template <int D> void box_op(Box<D>& b, int i_out, const MG& mg) {
+  if (use_lpld<D>(b, mg))
+    box_lpld<D>(b, i_out, mg);
+  else
+    box_lpl<D>(b, i_out, mg);
+}
+template <int D> void box_gsrb(Box<D>& b, int n, const MG& mg) {
+  if (use_lpld<D>(b, mg))
+    box_gsrb_lpld<D>(b, n, mg);
+  else
+    box_gsrb_lpl<D>(b, n, mg);
+}
+// mg%box_corr: mg$D_auto_corr (mg:645-669) chooses by the child's tag
+template <int D> void box_corr(Box<D>& p, Box<D>& c, const MG& mg) {
+  if (use_lpld<D>(c, mg))
+    box_corr_lpld<D>(p, c, mg);
+  else
+    prolong2_add<D>(p, c, mg.i_tmp, mg.i_phi);
+}
+
 template <int D> void residual_box(Box<D>& b, const MG& mg) {
-  box_lpl(b, mg.i_tmp, mg);
+  box_op(b, mg.i_tmp, mg);
   interior_for(b, mg.i_rhs, mg.i_tmp, 0);
 }
 
@@ -1174,7 +1324,7 @@ template <int D> void correct_children(Tree<D>& t, const std::vector<int>& ids, 
     for (int ic = 0; ic < Topo<D>::NCH; ++ic) {
       int c_id = p.children[ic];
       if (c_id == a5_no_box) continue;
-      prolong2_add(p, t.boxes[c_id], mg.i_tmp, mg.i_phi);
+      box_corr<D>(p, t.boxes[c_id], mg);
     }
   }
 }
@@ -1184,7 +1334,7 @@ void gsrb_boxes(Tree<D>& t, const std::vector<int>& ids, const MG& mg, int n_cyc
 #pragma omp parallel
   for (int n = 1; n <= 2 * n_cycle; ++n) {
 #pragma omp for
-    for (int i = 0; i < (int)ids.size(); ++i) box_gsrb_lpl(t.boxes[ids[i]], n, mg);
+    for (int i = 0; i < (int)ids.size(); ++i) box_gsrb<D>(t.boxes[ids[i]], n, mg);
 #pragma omp for
     for (int i = 0; i < (int)ids.size(); ++i) gc_box(t, ids[i], mg.i_phi, mg);
   }
@@ -1210,7 +1360,7 @@ template <int D> void update_coarse(Tree<D>& t, int lvl, const MG& mg) {
 #pragma omp parallel for
   for (int i = 0; i < (int)par.size(); ++i) {
     Box<D>& p = t.boxes[par[i]];
-    box_lpl(p, mg.i_rhs, mg);
+    box_op<D>(p, mg.i_rhs, mg);
     box_add_cc(p, mg.i_tmp, mg.i_rhs);
     box_copy_cc(p, mg.i_phi, mg.i_tmp);
   }
@@ -1232,7 +1382,7 @@ template <int D> void set_coarse_phi_rhs(Tree<D>& t, int lvl, const MG& mg) {
 #pragma omp parallel for
   for (int i = 0; i < (int)par.size(); ++i) {
     Box<D>& p = t.boxes[par[i]];
-    box_lpl(p, mg.i_rhs, mg);
+    box_op<D>(p, mg.i_rhs, mg);
     box_add_cc(p, mg.i_tmp, mg.i_rhs);
   }
 }
@@ -2320,6 +2470,21 @@ int orc_write_vtk(OrcHandle* h, const char* path, int n_cycle, double time, int 
   std::vector<std::string> an(cc_names, cc_names + n_cc), bn(fc_names, fc_names + n_fc);
   return h->dim == 2 ? write_vtk<2>(TT<2>(h), path, n_cycle, time, a, an, b, bn)
                      : write_vtk<3>(TT<3>(h), path, n_cycle, time, a, an, b, bn);
+}
+
+
+// mg%box_op / box_gsrb / box_corr and mg%i_eps; box tags are taken again at
+// their next use (the reference's a5_init_tag state).
+void orc_mg_set_operator(OrcHandle* h, int op, int i_eps) {
+  h->mg.op = op;
+  h->mg.i_eps = i_eps;
+  auto reset = [](auto& t) {
+    for (size_t id = 1; id < t.boxes.size(); ++id) t.boxes[id].tag = a5_init_tag;
+  };
+  if (h->dim == 2)
+    reset(TT<2>(h));
+  else
+    reset(TT<3>(h));
 }
 
 }  // extern "C"

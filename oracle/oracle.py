@@ -76,6 +76,7 @@ def lib():
         L.orc_ix_to_ichild.argtypes = [ctypes.c_int, ip]
         L.orc_set_threads.argtypes = [ctypes.c_int]
         L.orc_add_vars.argtypes = [P, ctypes.c_int, ctypes.c_int]
+        L.orc_mg_set_operator.argtypes = [P, ctypes.c_int, ctypes.c_int]
         L.orc_fc_count.argtypes = [P]
         L.orc_fc_count.restype = ctypes.c_longlong
         L.orc_get_fc.argtypes = [P, ctypes.c_int, dp]
@@ -252,6 +253,10 @@ class OracleTree:
 
     def leaf_mean(self, iv):
         return lib().orc_leaf_mean(self.h, iv)
+
+    def set_operator(self, op, i_eps=-1):
+        """mg%box_op / box_gsrb / box_corr: 0 lpl, 1 lpld, 2 auto (i_eps = eps)."""
+        lib().orc_mg_set_operator(self.h, op, i_eps)
 
     # general ghost cells, transfers and output ---------------------------------
     def add_vars(self, n_cc=0, n_fc=0):
