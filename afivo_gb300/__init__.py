@@ -151,6 +151,12 @@ def lib():
             "afv_forest_profile": (I, [P, I]),
             "afv_forest_profile_read": (I, [P, I, llp, dp, dp]),
             "afv_forest_add_vars": (I, [P, I, I]),
+            "afv_dtree_create": (I, [P, I, ctypes.POINTER(P)]),
+            "afv_dtree_destroy": (None, [P]),
+            "afv_dtree_adjust_builtin": (I, [P, ctypes.POINTER(RefCrit), ip, ip]),
+            "afv_dtree_refine_builtin": (I, [P, ctypes.POINTER(RefCrit), I, ip]),
+            "afv_dtree_download": (I, [P, P]),
+            "afv_dtree_get_info": (I, [P, ip]),
             "afv_mg_set_operator": (I, [P, I, I]),
             "afv_forest_set_fc": (I, [P, I, I, dp, LL]),
             "afv_forest_get_fc": (I, [P, I, I, dp, LL]),
@@ -311,6 +317,54 @@ class Tree:
     def leaf_cells(self):
         i = self.info()
         return i["n_leaves"] * i["n_cell"] ** self.dim
+
+
+class DeviceTree:
+    """A copy of a host tree in device memory, refined there
+    (afv_dtree_*): a$D_adjust_refinement with the built-in criteria."""
+
+    def __init__(self, tree, device=0):
+        self.dim = tree.dim
+        h = ctypes.c_void_p()
+        _check(lib().afv_dtree_create(tree.h, device, ctypes.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.afv_dtree_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def adjust_builtin(self, kind, lvl_max, thr=0.0, prob=0.0, seed=0, gauss=None, lpl=False):
+        c, _keep = _crit(kind, lvl_max, thr, prob, seed, gauss, lpl)
+        if gauss is not None:
+            c.n_gauss = len(gauss) // (2 + self.dim)
+        na, nr = ctypes.c_int(0), ctypes.c_int(0)
+        _check(lib().afv_dtree_adjust_builtin(self.h, ctypes.byref(c), ctypes.byref(na),
+                                              ctypes.byref(nr)))
+        return na.value, nr.value
+
+    def refine_builtin(self, kind, lvl_max, thr=0.0, prob=0.0, seed=0, gauss=None, lpl=False,
+                       max_passes=100):
+        c, _keep = _crit(kind, lvl_max, thr, prob, seed, gauss, lpl)
+        if gauss is not None:
+            c.n_gauss = len(gauss) // (2 + self.dim)
+        n = ctypes.c_int(0)
+        _check(lib().afv_dtree_refine_builtin(self.h, ctypes.byref(c), max_passes, ctypes.byref(n)))
+        return n.value
+
+    def download(self, tree):
+        """Copy the device tree's state into host tree `tree`."""
+        _check(lib().afv_dtree_download(self.h, tree.h))
+        return tree
+
+    def info(self):
+        out = np.zeros(5, np.int32)
+        _check(lib().afv_dtree_get_info(self.h, _ip(out)))
+        return dict(zip(("highest_lvl", "highest_id", "passes", "n_boxes", "n_leaves"),
+                        (int(x) for x in out)))
 
 
 def a2_init(n_cell, dr, r_min=None, lvl_limit=30, coarsen_to=-1, mem_limit_gb=64.0):

@@ -20,6 +20,22 @@ struct afv_forest {
   afv::Forest f;
 };
 
+namespace afv {
+class DevTree;
+int dtree_create(const HostTree& h, int device, DevTree** out, std::string& err);
+void dtree_destroy(DevTree* t);
+int dtree_adjust(DevTree* t, const afv_ref_crit* c, int* n_add, int* n_rm, std::string& err);
+int dtree_download(const DevTree* t, HostTree& h, std::string& err);
+int dtree_info(const DevTree* t, int* out5);
+}  // namespace afv
+
+struct afv_dtree {
+  afv::DevTree* t = nullptr;
+  ~afv_dtree() {
+    if (t) afv::dtree_destroy(t);
+  }
+};
+
 namespace {
 thread_local std::string g_err;
 
@@ -131,6 +147,51 @@ int afv_tree_refine_builtin(afv_tree* t, const afv_ref_crit* crit, int max_passe
 }
 
 void afv_tree_destroy(afv_tree* t) { delete t; }
+
+int afv_dtree_create(const afv_tree* t, int device, afv_dtree** out) {
+  if (!t || !out) return fail(AFV_ERR_INVALID, "NULL argument");
+  *out = nullptr;
+  return guarded([&](std::string& err) -> int {
+    std::unique_ptr<afv_dtree> d(new afv_dtree());
+    if (int rc = afv::dtree_create(t->t, device, &d->t, err)) return rc;
+    *out = d.release();
+    return AFV_OK;
+  });
+}
+
+void afv_dtree_destroy(afv_dtree* t) { delete t; }
+
+int afv_dtree_adjust_builtin(afv_dtree* t, const afv_ref_crit* crit, int* n_add, int* n_rm) {
+  if (!t || !crit) return fail(AFV_ERR_INVALID, "NULL argument");
+  if (crit->kind == AFV_REF_SOURCE && (crit->n_gauss <= 0 || !crit->gauss))
+    return fail(AFV_ERR_INVALID, "source criterion needs Gaussians");
+  return guarded([&](std::string& err) -> int { return afv::dtree_adjust(t->t, crit, n_add, n_rm, err); });
+}
+
+int afv_dtree_refine_builtin(afv_dtree* t, const afv_ref_crit* crit, int max_passes, int* n_passes) {
+  int passes = 0;
+  for (; passes < max_passes; ++passes) {
+    int na = 0, nr = 0;
+    int rc = afv_dtree_adjust_builtin(t, crit, &na, &nr);
+    if (rc) return rc;
+    if (na == 0) {
+      ++passes;
+      break;
+    }
+  }
+  if (n_passes) *n_passes = passes;
+  return AFV_OK;
+}
+
+int afv_dtree_download(const afv_dtree* t, afv_tree* host) {
+  if (!t || !host) return fail(AFV_ERR_INVALID, "NULL argument");
+  return guarded([&](std::string& err) -> int { return afv::dtree_download(t->t, host->t, err); });
+}
+
+int afv_dtree_get_info(const afv_dtree* t, int* out5) {
+  if (!t || !out5) return fail(AFV_ERR_INVALID, "NULL argument");
+  return afv::dtree_info(t->t, out5);
+}
 
 int afv_tree_get_info(const afv_tree* t, int* out8) {
   if (!t || !out8) return fail(AFV_ERR_INVALID, "NULL argument");

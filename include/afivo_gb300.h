@@ -143,6 +143,30 @@ int afv_tree_export(const afv_tree* t, int* lvl, int* ix, int* parent, int* chil
  * sizes3 receives the three lengths; the list pointers may be NULL. */
 int afv_tree_level(const afv_tree* t, int lvl, int* sizes3, int* ids, int* leaves, int* parents);
 
+/* ---- tree build on the device ------------------------------------------------ */
+
+typedef struct afv_dtree afv_dtree; /* a tree held and refined in device memory */
+
+/* No counterpart in the reference (its tree lives in host memory): a device
+ * copy of a host tree (after a$D_set_base or any refinement), for refining
+ * without moving the tree through host memory. */
+int afv_dtree_create(const afv_tree* t, int device, afv_dtree** out);
+void afv_dtree_destroy(afv_dtree* t);
+/* a$D_adjust_refinement on the device (src/m_aX_core.f90:452-541, with
+ * consistent_ref_flags :628-725, add_children / remove_children :728-787,
+ * set_neighbs :387-422 and a$D_tidy_up :238-314), for a built-in criterion
+ * (at most 16 Gaussians): the same ids, links and level lists as
+ * afv_tree_adjust_builtin on the host. Only list sizes and counts come back
+ * to the host during a pass. */
+int afv_dtree_adjust_builtin(afv_dtree* t, const afv_ref_crit* crit, int* n_add, int* n_rm);
+/* afv_tree_refine_builtin's loop with afv_dtree_adjust_builtin. */
+int afv_dtree_refine_builtin(afv_dtree* t, const afv_ref_crit* crit, int max_passes, int* n_passes);
+/* Replaces the state of host tree `host` by the device tree's (for instance
+ * to create a forest from it). */
+int afv_dtree_download(const afv_dtree* t, afv_tree* host);
+/* out[5] = highest_lvl, highest_id, adjust passes made, boxes in use, leaves. */
+int afv_dtree_get_info(const afv_dtree* t, int* out5);
+
 /* ---- device forest ----------------------------------------------------------- */
 
 /* Uploads the topology of n_trees trees (same dim, n_cell, coarsen_to) and
