@@ -143,6 +143,8 @@ def lib():
             "afv_forest_get_option": (I, [P, I, ip]),
             "afv_tree_max_abs_cc_noalloc": (I, [P, I, I, dp]),
             "afv_mg_solve": (I, [P, ctypes.POINTER(MgOpts), I, Dd, I, ip, dp]),
+            "afv_mg_solve_trees": (I, [P, ctypes.POINTER(MgOpts), I, Dd, I, ip, ip, dp]),
+            "afv_forest_zero_tree": (I, [P, I, I]),
             "afv_mg_gsrb_level": (I, [P, I, I]),
             "afv_fill_gc_level": (I, [P, I]),
             "afv_mg_update_coarse": (I, [P, I]),
@@ -458,6 +460,9 @@ class Forest:
     def zero(self, var):
         _check(lib().afv_forest_zero(self.h, var))
 
+    def zero_tree(self, tree, var):
+        _check(lib().afv_forest_zero_tree(self.h, tree, var))
+
     def sync(self):
         _check(lib().afv_forest_sync(self.h))
 
@@ -493,13 +498,22 @@ class Forest:
         _check(lib().afv_tree_max_abs_cc_noalloc(self.h, tree, var, ctypes.byref(out)))
         return out.value
 
-    def solve(self, precision=AFV_PREC_FP64, tol=1e-8, max_cycles=50, mg=None, check=True):
+    def solve(self, precision=AFV_PREC_FP64, tol=1e-8, max_cycles=50, mg=None, check=True,
+              mask=None):
+        """Solve every tree (or the trees with a nonzero mask entry)."""
         mg = mg or MgOpts()
         n = len(self.trees)
         cyc = np.zeros(n, np.int32)
         rel = np.zeros(n)
-        rc = lib().afv_mg_solve(self.h, ctypes.byref(mg), precision, float(tol), max_cycles,
-                                _ip(cyc), _dp(rel))
+        if mask is None:
+            rc = lib().afv_mg_solve(self.h, ctypes.byref(mg), precision, float(tol), max_cycles,
+                                    _ip(cyc), _dp(rel))
+        else:
+            m = np.ascontiguousarray(mask, dtype=np.int32)
+            if m.size != n:
+                raise ValueError("mask must have one entry per tree")
+            rc = lib().afv_mg_solve_trees(self.h, ctypes.byref(mg), precision, float(tol),
+                                          max_cycles, _ip(m), _ip(cyc), _dp(rel))
         if check and rc != AFV_OK:
             _check(rc)
         return cyc, rel, rc

@@ -412,6 +412,11 @@ int afv_mg_fas_fmg(afv_forest* f, const afv_mg_opts* mg, int set_residual, int h
 
 int afv_gc_tree(afv_forest* f) { FOREST_CALL(f, return f->f.gc_tree(err)); }
 
+int afv_forest_zero_tree(afv_forest* f, int tree, int var) {
+  FOREST_CALL(f, return f->f.zero_tree(tree, var, err));
+}
+
+
 int afv_tree_max_abs_cc(afv_forest* f, int tree, int var, double* out) {
   if (!out) return fail(AFV_ERR_INVALID, "out is NULL");
   FOREST_CALL(f, return f->f.max_abs(tree, var, out, err));
@@ -424,12 +429,17 @@ int afv_tree_max_abs_cc_noalloc(afv_forest* f, int tree, int var, double* out) {
 
 int afv_mg_solve(afv_forest* f, const afv_mg_opts* mg, int precision, double tol, int max_cycles,
                  int* cycles, double* rel_res) {
+  return afv_mg_solve_trees(f, mg, precision, tol, max_cycles, nullptr, cycles, rel_res);
+}
+
+int afv_mg_solve_trees(afv_forest* f, const afv_mg_opts* mg, int precision, double tol, int max_cycles,
+                       const int* mask, int* cycles, double* rel_res) {
   if (precision != AFV_PREC_FP64 && precision != AFV_PREC_MIXED)
     return fail(AFV_ERR_INVALID, "unknown precision");
   if (!(tol > 0) || max_cycles < 0) return fail(AFV_ERR_INVALID, "bad tolerance or cycle limit");
   FOREST_CALL(f, {
     afv::SolveStats st;
-    int rc = f->f.solve(mg_of(mg), precision, tol, max_cycles, st, err);
+    int rc = f->f.solve(mg_of(mg), precision, tol, max_cycles, st, err, mask);
     for (int t = 0; t < f->f.plan.n_trees; ++t) {
       if (cycles) cycles[t] = st.cycles.empty() ? 0 : st.cycles[t];
       if (rel_res) rel_res[t] = st.rel_res.empty() ? 0 : st.rel_res[t];

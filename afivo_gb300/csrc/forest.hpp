@@ -153,6 +153,8 @@ class Forest {
   // iterations of the current solve (graph loop), unused
   int* d_count = nullptr;
   int* d_failed = nullptr;               // [n_trees] nonzero: residual not finite
+  int* d_solve_mask = nullptr;           // [n_trees] trees a solve takes part in
+  int* h_solve_mask = nullptr;           // pinned [n_trees]
   int* d_cycles = nullptr;               // [n_trees] V-cycles of the current solve
   unsigned long long* d_final = nullptr; // [n_trees] residual norm at the tree's last check (double bits)
   int* h_count = nullptr;                // pinned [4]: copy of d_count
@@ -235,8 +237,11 @@ class Forest {
   int max_abs(int tree, int var, double* out, std::string& err);
   // max_abs with its scratch in static device memory (noalloc.cuh)
   int max_abs_static(int tree, int var, double* out, std::string& err);
+  // mask (n_trees entries, may be null = every tree): the trees the solve
+  // takes part in; the others are left as they are
   int solve(const MgOpts& mg, int precision, double tol, int max_cycles, SolveStats& st,
-            std::string& err);
+            std::string& err, const int* mask = nullptr);
+  int zero_tree(int tree, int var, std::string& err);
 
   // Generic-precision pieces.
   template <class T> void sweep(const Arrays<T>& a, int lvl, int n, bool pull, bool homog);

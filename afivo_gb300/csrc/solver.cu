@@ -157,7 +157,7 @@ Forest::~Forest() {
   void* ptrs[] = {meta.parent, meta.first_child, meta.tree, meta.offg, meta.offi, meta.bcval,
                   meta.active, meta.desc, meta.nbo2, meta.err, meta.rmin, d64.phi, d64.rhs,
                   d64.tmp, d32.phi, d32.rhs, d32.tmp, base_phi64, base_rhs64, d_lists, d_norm, d_red,
-                  d_fmax, d_count, d_failed, d_cycles, d_final, d_stage, d_stage_slots};
+                  d_fmax, d_count, d_failed, d_cycles, d_final, d_stage, d_stage_slots, d_solve_mask};
   for (void* p : ptrs)
     if (p) cudaFreeAsync(p, stream);
   for (double* p : xcc)
@@ -171,7 +171,8 @@ Forest::~Forest() {
   }
   for (cudaEvent_t e : event_pool) cudaEventDestroy(e);
   drop_graphs();
-  for (void* p : {(void*)h_count, (void*)h_norm, (void*)h_cycles, (void*)h_final, (void*)h_failed, (void*)h_fmax})
+  for (void* p : {(void*)h_count, (void*)h_norm, (void*)h_cycles, (void*)h_final, (void*)h_failed, (void*)h_fmax,
+                  (void*)h_solve_mask})
     if (p) cudaFreeHost(p);
   if (ev_fork) cudaEventDestroy(ev_fork);
   if (ev_join) cudaEventDestroy(ev_join);
@@ -345,6 +346,7 @@ int Forest::create(const std::vector<const HostTree*>& trees, const afv_forest_o
   if ((rc = upload_bc(err))) return rc;
   std::vector<int> act(p.n_trees, 1);
   if ((rc = dupload(&meta.active, act, bytes, stream))) return err = "device allocation failed", rc;
+  if ((rc = dupload(&d_solve_mask, act, bytes, stream))) return err = "device allocation failed", rc;
   host_active = act;
 
   if (dmalloc(&d64.phi, p.n_elem_g, bytes, stream) || dmalloc(&d64.tmp, p.n_elem_g, bytes, stream) ||
@@ -391,7 +393,8 @@ int Forest::create(const std::vector<const HostTree*>& trees, const afv_forest_o
       cudaMallocHost((void**)&h_cycles, sizeof(int) * p.n_trees) != cudaSuccess ||
       cudaMallocHost((void**)&h_final, sizeof(unsigned long long) * p.n_trees) != cudaSuccess ||
       cudaMallocHost((void**)&h_failed, sizeof(int) * p.n_trees) != cudaSuccess ||
-      cudaMallocHost((void**)&h_fmax, sizeof(double) * p.n_trees) != cudaSuccess)
+      cudaMallocHost((void**)&h_fmax, sizeof(double) * p.n_trees) != cudaSuccess ||
+      cudaMallocHost((void**)&h_solve_mask, sizeof(int) * p.n_trees) != cudaSuccess)
     return err = "pinned allocation failed", AFV_ERR_NOMEM;
   if (cudaStreamSynchronize(stream) != cudaSuccess) return check(err, "forest create");
   return AFV_OK;
@@ -1121,6 +1124,30 @@ int Forest::set_source_device(int t, int lpl, int n_gauss, const double* gauss, 
   return check(err, "set_source_device");
 }
 
+// cc(..., var) := 0 on every box of one tree, ghost cells included (a
+// tree's boxes of one level are consecutive slots).
+int Forest::zero_tree(int t, int var, std::string& err) {
+  if (t < 0 || t >= plan.n_trees) return err = "tree index out of range", AFV_ERR_INVALID;
+  double* v = var_ptr(var);
+  if (!v) return err = "unknown variable", AFV_ERR_INVALID;
+  for (int l = plan.min_lvl; l <= plan.max_lvl; ++l) {
+    const int lo = plan.lvl_lo[plan.L(l)], n = plan.lvl_n[plan.L(l)];
+    int a = -1, b = -1;
+    for (int k = 0; k < n; ++k)
+      if (plan.tree[lo + k] == t) {
+        if (a < 0) a = lo + k;
+        b = lo + k;
+      }
+    if (a < 0) continue;
+    long long per = 1;
+    for (int d = 0; d < plan.dim; ++d) per *= var == AFV_RHS ? plan.nc_at(l) : plan.nc_at(l) + 2;
+    const long long o0 = var == AFV_RHS ? plan.offi[a] : plan.offg[a];
+    const long long o1 = (var == AFV_RHS ? plan.offi[b] : plan.offg[b]) + per;
+    cudaMemsetAsync(v + o0, 0, sizeof(double) * (o1 - o0), stream);
+  }
+  return check(err, "zero_tree");
+}
+
 int Forest::gc_tree(std::string& err) {
   for (int l = plan.min_lvl; l <= plan.max_lvl; ++l) fill(d64, l, false);
   return check(err, "gc_tree");
@@ -1391,8 +1418,8 @@ void Forest::enqueue_iteration(const MgOpts& mg, int precision, double tol) {
 void Forest::enqueue_solve_begin(int precision, double tol, int max_cycles, const cudaGraphConditionalHandle* h) {
   const int nt = plan.n_trees;
   Meta m = meta_of(meta);
-  dev::k_set_int<<<(nt + 255) / 256, 256, 0, stream>>>(meta.active, nt, 1);
-  ++n_launches;
+  // the trees this solve takes part in
+  cudaMemcpyAsync(meta.active, d_solve_mask, sizeof(int) * nt, cudaMemcpyDeviceToDevice, stream);
   cudaMemsetAsync(d_cycles, 0, sizeof(int) * nt, stream);
   cudaMemsetAsync(d_failed, 0, sizeof(int) * nt, stream);
   norm_reset();
@@ -1528,8 +1555,10 @@ int Forest::build_solve_graph(GraphCache& gc, const MgOpts& mg, int precision, d
 // graph does not change while the set of active trees shrinks. Otherwise the
 // host drives the loop, one iteration at a time.
 int Forest::solve(const MgOpts& mg, int precision, double tol, int max_cycles, SolveStats& st,
-                  std::string& err) {
+                  std::string& err, const int* mask) {
   const int nt = plan.n_trees;
+  for (int t = 0; t < nt; ++t) h_solve_mask[t] = mask ? (mask[t] != 0) : 1;
+  cudaMemcpyAsync(d_solve_mask, h_solve_mask, sizeof(int) * nt, cudaMemcpyHostToDevice, stream);
   if (precision == AFV_PREC_MIXED && !mixed)
     return err = "forest created without mixed_buffers", AFV_ERR_STATE;
   if (precision == AFV_PREC_MIXED && op != AFV_OP_LPL)
@@ -1564,6 +1593,7 @@ int Forest::solve(const MgOpts& mg, int precision, double tol, int max_cycles, S
   if (h_count[1]) return check_device_error(err);  // a bounded wait gave up
   int n_failed = 0;
   for (int t = 0; t < nt; ++t) {
+    if (!h_solve_mask[t]) continue;  // left out of this solve
     double r;
     std::memcpy(&r, &h_final[t], sizeof(double));
     st.cycles[t] = h_cycles[t];

@@ -206,6 +206,9 @@ int afv_forest_set_bc(afv_forest* f, int tree, int bc_type, int src_lpl, int n_g
 int afv_forest_set_bc_faces(afv_forest* f, int tree, long long n_faces, const int* bc_type,
                             long long n_values, const double* values);
 int afv_forest_zero(afv_forest* f, int var);
+/* No counterpart in the reference: a$D_box_clear_cc (src/m_aX_utils.f90:
+ * 262-270) on every box of one tree of the forest. */
+int afv_forest_zero_tree(afv_forest* f, int tree, int var);
 int afv_forest_sync(afv_forest* f);
 /* No counterpart in the reference: the cudaStream_t that orders this
  * forest's work, for callers that time it or order their own work after it. */
@@ -265,6 +268,12 @@ int afv_tree_max_abs_cc_noalloc(afv_forest* f, int tree, int var, double* out);
  * AFV_ERR_TIMEOUT if a bounded device wait gave up during the solve. */
 int afv_mg_solve(afv_forest* f, const afv_mg_opts* mg, int precision, double tol, int max_cycles,
                  int* cycles, double* rel_res);
+/* No counterpart in the reference: afv_mg_solve on the trees whose mask
+ * entry is nonzero (mask may be NULL: every tree); the other trees' cell
+ * data is left as it is and their cycles / rel_res entries are 0. A forest
+ * whose trees are request slots solves the occupied slots only. */
+int afv_mg_solve_trees(afv_forest* f, const afv_mg_opts* mg, int precision, double tol, int max_cycles,
+                       const int* mask, int* cycles, double* rel_res);
 
 /* Single operators of the V-cycle, one level of every tree. */
 /* gsrb_boxes, src/m_aX_mg.f90:397-420 */
