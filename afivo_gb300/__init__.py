@@ -140,6 +140,7 @@ def lib():
             "afv_forest_set_option": (I, [P, I, I]),
             "afv_forest_set_source_device": (I, [P, I, I, I, dp]),
             "afv_forest_autotune": (I, [P, ip, ctypes.POINTER(ctypes.c_float)]),
+            "afv_forest_autotune_all": (I, [P, ip, ctypes.POINTER(ctypes.c_float)]),
             "afv_forest_get_option": (I, [P, I, ip]),
             "afv_tree_max_abs_cc_noalloc": (I, [P, I, I, dp]),
             "afv_mg_solve": (I, [P, ctypes.POINTER(MgOpts), I, Dd, I, ip, dp]),
@@ -607,6 +608,17 @@ class Forest:
         ms = (ctypes.c_float * 3)()
         _check(lib().afv_forest_autotune(self.h, ctypes.byref(c), ms))
         return c.value, {1: ms[0], 2: ms[1], 0: ms[2]}
+
+    def autotune_all(self):
+        """Full tuning pass: (sweep kernel, small sweeps, coarse end) chosen,
+        and the ms per FP32 V-cycle of every setting timed."""
+        c = np.zeros(3, np.int32)
+        ms = (ctypes.c_float * 10)()
+        _check(lib().afv_forest_autotune_all(self.h, _ip(c), ms))
+        times = {"sweep_kernel_%d" % k: ms[k] for k in range(6)}
+        for k in range(4):
+            times["small_%d_coarse_end_%d" % (k >> 1, k & 1)] = ms[6 + k]
+        return {"sweep_kernel": int(c[0]), "small_sweeps": int(c[1]), "coarse_end": int(c[2])}, times
 
     def set_option(self, option, value):
         _check(lib().afv_forest_set_option(self.h, option, int(value)))

@@ -614,6 +614,11 @@ int afv_forest_autotune(afv_forest* f, int* choice, float* ms3) {
   FOREST_CALL(f, return f->f.autotune(choice, ms3, err));
 }
 
+int afv_forest_autotune_all(afv_forest* f, int* choice3, float* ms10) {
+  if (!choice3) return fail(AFV_ERR_INVALID, "NULL argument");
+  FOREST_CALL(f, return f->f.autotune_all(&choice3[0], &choice3[1], &choice3[2], ms10, err));
+}
+
 int afv_forest_set_source_device(afv_forest* f, int tree, int src_lpl, int n_gauss, const double* gauss) {
   if (n_gauss < 0 || (n_gauss > 0 && !gauss)) return fail(AFV_ERR_INVALID, "bad arguments");
   FOREST_CALL(f, return f->f.set_source_device(tree, src_lpl, n_gauss, gauss, err));

@@ -231,6 +231,7 @@ class Forest {
   int residual_all(unsigned long long* norm, std::string& err);
   int vcycle(const MgOpts& mg, int highest, bool set_residual, std::string& err);
   int autotune(int* choice, float* ms3, std::string& err);
+  int autotune_all(int* sweep, int* small, int* coarse_end, float* ms10, std::string& err);
   int set_source_device(int tree, int lpl, int n_gauss, const double* gauss, std::string& err);
   int fmg(const MgOpts& mg, bool set_residual, bool have_guess, std::string& err);
   int gc_tree(std::string& err);

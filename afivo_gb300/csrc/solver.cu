@@ -1049,44 +1049,96 @@ int Forest::vcycle(const MgOpts& mg, int highest, bool set_residual, std::string
   return check_device_error(err);
 }
 
-// Times the sweep kernel variants on this forest (two FP32 correction
-// V-cycles each, on the mixed scratch state, which every solve
-// re-initialises) and keeps the fastest. Needs the mixed buffers.
-int Forest::autotune(int* choice, float* ms_out, std::string& err) {
+// Times the kernel variants on this forest (FP32 correction V-cycles on the
+// mixed scratch state, which every solve re-initialises) and keeps the
+// fastest: first the sweep kernel (block-pipelined, warp-per-box with bulk
+// copies in four warp / stage shapes, warp-per-box with per-lane copies),
+// then, with it, the small-level sweep fusion and the one-launch coarse end
+// (both on / off). Needs the mixed buffers. ms receives the ms per V-cycle of
+// sweep kernels 0..5, then of the four (small sweeps, coarse end) settings
+// (0,0), (0,1), (1,0), (1,1).
+int Forest::autotune_all(int* sweep_out, int* small_out, int* coarse_out, float* ms_out, std::string& err) {
   if (!mixed) return err = "autotune needs a forest created with mixed_buffers", AFV_ERR_STATE;
   MgOpts mg;
   mg.n_down = mg.n_up = mg.n_base = 2;
-  const int candidates[3] = {1, 2, 0};
-  const int saved = sweep_kernel, saved_mask = prof_mask;
+  const int saved_mask = prof_mask;
   prof_mask = 0;
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
-  int best = saved;
-  float best_ms = 1e30f;
-  for (int c = 0; c < 3; ++c) {
-    sweep_kernel = candidates[c];
+  auto time_cycles = [&]() -> float {
     vcycle_t(d32, mg, plan.max_lvl, true, true, true);  // warm-up (first launches set attributes)
     cudaEventRecord(e0, stream);
-    for (int r = 0; r < 2; ++r) vcycle_t(d32, mg, plan.max_lvl, true, true, true);
+    for (int r = 0; r < 3; ++r) vcycle_t(d32, mg, plan.max_lvl, true, true, true);
     cudaEventRecord(e1, stream);
     cudaEventSynchronize(e1);
     float ms = 0;
     cudaEventElapsedTime(&ms, e0, e1);
-    if (ms_out) ms_out[c] = ms / 2;
+    return ms / 3;
+  };
+  float best_ms = 1e30f;
+  int best = sweep_kernel;
+  for (int c = 0; c <= 5; ++c) {
+    sweep_kernel = c;
+    const float ms = time_cycles();
+    if (ms_out) ms_out[c] = ms;
     if (ms < best_ms) {
       best_ms = ms;
-      best = candidates[c];
+      best = c;
     }
   }
+  sweep_kernel = best;
+  bool best_small = use_small_sweeps, best_ce = use_coarse_end;
+  best_ms = 1e30f;
+  for (int k = 0; k < 4; ++k) {
+    use_small_sweeps = (k >> 1) & 1;
+    use_coarse_end = k & 1;
+    coarse_end_levels = -1;
+    const float ms = time_cycles();
+    if (ms_out) ms_out[6 + k] = ms;
+    if (ms < best_ms) {
+      best_ms = ms;
+      best_small = use_small_sweeps;
+      best_ce = use_coarse_end;
+    }
+  }
+  use_small_sweeps = best_small;
+  use_coarse_end = best_ce;
+  coarse_end_levels = -1;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  sweep_kernel = best;
   prof_mask = saved_mask;
   drop_graphs();
-  if (choice) *choice = best;
+  if (sweep_out) *sweep_out = sweep_kernel;
+  if (small_out) *small_out = use_small_sweeps ? 1 : 0;
+  if (coarse_out) *coarse_out = use_coarse_end ? 1 : 0;
   if (int rc = check(err, "autotune")) return rc;
   return check_device_error(err);
+}
+
+// The sweep kernel alone (the first part of autotune_all): variants 1, 2, 0.
+int Forest::autotune(int* choice, float* ms_out, std::string& err) {
+  if (!mixed) return err = "autotune needs a forest created with mixed_buffers", AFV_ERR_STATE;
+  float ms[10];
+  const bool small = use_small_sweeps, ce = use_coarse_end;
+  int rc = autotune_all(choice, nullptr, nullptr, ms, err);
+  use_small_sweeps = small;  // this entry point tunes the sweep kernel only
+  use_coarse_end = ce;
+  coarse_end_levels = -1;
+  if (ms_out) {
+    ms_out[0] = ms[1];
+    ms_out[1] = ms[2];
+    ms_out[2] = ms[0];
+  }
+  if (!rc && choice && *choice > 2) {  // keep the documented choice among 0..2
+    int c = 1;
+    for (int k : {0, 2})
+      if (ms[k] < ms[c]) c = k;
+    sweep_kernel = c;
+    *choice = c;
+  }
+  drop_graphs();
+  return rc;
 }
 
 // rhs of one tree := sum of Gaussians (or their Laplacian) at the cell

@@ -271,7 +271,7 @@ def run_batched(afv, W, local, rank, world, n_trees=256, check_errors=False):
     forest = afv.Forest([trees[i] for i in mine], device=local, mixed=True)
     for k, i in enumerate(mine):
         forest.set_source(k, specs[i]["gauss"], lpl=True)
-    choice, tune_ms = forest.autotune()
+    choice, tune_ms = forest.autotune_all()
     ext = torch.cuda.ExternalStream(forest.stream())
 
     def solve():
@@ -294,6 +294,27 @@ def run_batched(afv, W, local, rank, world, n_trees=256, check_errors=False):
     unknowns = sum(float(t.leaf_cells()) * c for t, c in zip([trees[i] for i in mine], cyc))
     unknowns = sum_over_ranks(unknowns, world)
     total_cells = sum_over_ranks(float(cells), world)
+    # per-kernel bandwidth of one profiled solve (kernel by kernel, each
+    # iteration behind a 5 ms device-side wait so that the events time the
+    # kernels), and the sweep's roofline
+    forest.set_option(afv.AFV_OPT_PROFILE_LEAD_US, 5000)
+    forest.profile((1 << len(afv.KERNEL_KINDS)) - 1)
+    forest.zero(afv.AFV_PHI)
+    forest.solve(afv.AFV_PREC_MIXED, tol=TOL, max_cycles=60, check=False)
+    kern = {}
+    for k, kname in enumerate(afv.KERNEL_KINDS):
+        n, kms, kb = forest.profile_read(k)
+        if n and kms > 0:
+            kern[kname] = {"launches": int(n), "ms": round(kms, 4), "GB/s": round(kb / (kms / 1e3) / 1e9, 1)}
+    forest.profile(0)
+    forest.set_option(afv.AFV_OPT_PROFILE_LEAD_US, 0)
+    peak, peak_kind = load_peaks()
+    sw = kern.get("sweep")
+    roof = None
+    if sw:
+        roof = {"kernel": "sweep (chosen variant %d)" % choice["sweep_kernel"], "achieved": sw["GB/s"],
+                "peak": peak, "unit": "GB/s", "frac": sw["GB/s"] / peak,
+                "peak_kind": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)"}
     errors = None
     if check_errors:
         errors = batched_errors(afv, forest, specs, mine)
@@ -301,7 +322,8 @@ def run_batched(afv, W, local, rank, world, n_trees=256, check_errors=False):
            "boxes": int(sum_over_ranks(float(forest.info()["n_boxes"]), world)),
            "ms_per_solve": ms, "unknowns_per_s": unknowns / (ms / 1e3),
            "cycles_min": int(min(cyc)), "cycles_max": int(max(cyc)), "rel_res_max": float(max(rel)),
-           "sweep_kernel": choice, "autotune_ms_per_vcycle": {str(k): round(v, 3) for k, v in tune_ms.items()},
+           "autotune_choice": choice, "autotune_ms_per_vcycle": {k: round(v, 3) for k, v in tune_ms.items()},
+           "kernels_mixed_solve": kern, "roofline": roof,
            "tree_build_s": round(t_build, 2), "err_vs_fp64_oracle": errors}
     forest.close()
     return out
@@ -324,29 +346,53 @@ def batched_errors(afv, forest, specs, mine):
                     "leaf interiors / max |phi|"}
 
 
-def run_serving(afv, W, local, rank, world, n_requests=64):
+def _leaf_cells(spec):
+    """Leaf cells of a uniform request tree (8^3 boxes to level lvl_max)."""
+    side = spec["n_cell"] * 2 ** (spec["lvl_max"] - 1)
+    return float(side ** spec["dim"])
+
+
+def run_serving(afv, W, local, rank, world, n_requests=500, keep_ids=()):
     """Served 3-D requests (Poisson arrivals, mean 200/s; uniform octrees of
-    8^3 boxes from 32^3 to 256^3 cells): continuous batching under an HBM
-    budget, mixed and FP64, p50/p99 latency and solves/s."""
+    8^3 boxes from 32^3 to 256^3 cells): resident per-shape forests under an
+    HBM budget, continuous batching, mixed and FP64. Each rate's run follows
+    one run that warms the resident forests; p50/p99 latency with its
+    queueing and service parts, solves/s; then the same stream at half the
+    served rate (below capacity)."""
     from afivo_gb300 import placement, serving
     reqs = W.c5_requests(n=n_requests)
-    t0 = time.time()
-    trees = [W.build_tree(r) for r in reqs]
-    t_build = time.time() - t0
-    work = [float(t.leaf_cells()) for t in trees]
+    work = [_leaf_cells(r) for r in reqs]
     mine = placement.shard(list(range(len(reqs))), work, rank, world)
-    out = {"workload": "poisson3d_requests_seed5", "requests": len(reqs), "tree_build_s": round(t_build, 2)}
+    mreqs = [reqs[i] for i in mine]
+    out = {"workload": "poisson3d_requests_seed5", "requests": len(reqs),
+           "shapes": len({serving.shape_key(r) for r in reqs})}
+    kept = {}
     for name, prec in (("mixed", afv.AFV_PREC_MIXED), ("fp64", afv.AFV_PREC_FP64)):
-        srv = serving.Server(device=local, budget_bytes=32 << 30, slots=4, max_batch=8, precision=prec)
-        srv.serve([reqs[i] for i in mine[:4]], [trees[i] for i in mine[:4]], realtime=False)  # warm-up
-        res = srv.serve([reqs[i] for i in mine], [trees[i] for i in mine], realtime=True)
+        keep = {k for k, i in enumerate(mine) if i in keep_ids}
+        srv = serving.Server(device=local, budget_bytes=32 << 30, slots=4, max_batch=8, precision=prec,
+                             keep_phi=keep)
+        srv.serve(mreqs, realtime=False)  # builds the resident forests (a server that has been running)
+        res = srv.serve(mreqs, realtime=True)
         summ = serving.summary(res)
-        summ["p99_ms"] = max_over_ranks(summ["p99_ms"], world)
-        summ["solves_per_s"] = sum_over_ranks(summ["solves_per_s"], world)
-        summ["unknowns_per_s"] = sum_over_ranks(summ["unknowns_per_s"], world)
+        rate = float(len(mreqs) / (mreqs[-1]["arrival"] - mreqs[0]["arrival"]))
+        low = 0.5 * min(summ["solves_per_s"], rate)
+        slow = [dict(r, arrival=r["arrival"] * rate / low) for r in mreqs]
+        res_low = srv.serve(slow, realtime=True)
+        summ_low = serving.summary(res_low)
+        for sm in (summ, summ_low):
+            sm["p99_ms"] = max_over_ranks(sm["p99_ms"], world)
+            sm["solves_per_s"] = sum_over_ranks(sm["solves_per_s"], world)
+            sm["unknowns_per_s"] = sum_over_ranks(sm["unknowns_per_s"], world)
+        summ["offered_per_s"] = rate
+        summ_low["offered_per_s"] = low
         summ["peak_device_bytes"] = srv.last_peak_bytes
-        out[name] = {k: (float("%.6g" % v) if isinstance(v, float) else v) for k, v in summ.items()}
-    return out, reqs
+        f6 = lambda v: float("%.6g" % v) if isinstance(v, float) else v  # noqa: E731
+        out[name] = {k: f6(v) for k, v in summ.items()}
+        out[name]["below_capacity"] = {k: f6(v) for k, v in summ_low.items()}
+        if name == "mixed":
+            kept = {mine[k]: res[k].phi for k in keep}
+        srv.close()
+    return out, reqs, kept
 
 
 def run_uniform(afv, W, local, rank, world, check_errors=False):
@@ -415,20 +461,31 @@ def run_uniform(afv, W, local, rank, world, check_errors=False):
     return out
 
 
-def cpu_serving_sample(reqs, threads, n=4):
-    """The oracle's solve time per request on the host cores for a sample of
-    the requests (solved one after another, as a CPU server would)."""
-    picks = list(range(0, len(reqs), max(1, len(reqs) // n)))[:n]
-    times, cells = [], []
+def serving_picks(n_requests, n=8):
+    return list(range(0, n_requests, max(1, n_requests // n)))[:n]
+
+
+def cpu_serving_sample(reqs, threads, picks, served_phi):
+    """The oracle's FP64 solve of a sample of the requests on the host cores
+    (one after another, as a CPU server would): its time per request, and the
+    served mixed-precision solution's error against it (max over leaf
+    interiors / max |phi|)."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from helpers import interior_to_ghosted
+    times, cells, errs = [], [], []
     for i in picks:
         s = OracleSolver(reqs[i], threads)
         c, dt, _ = s.solve()
         times.append(dt * 1e3)
         cells.append(s.cells * c)
+        if served_phi.get(i) is not None:
+            errs.append(s.error_of(interior_to_ghosted(served_phi[i], s.ot, 8, 3)))
     return {"sample": f"requests {picks}, solved one at a time on {threads} threads",
             "ms_p50": float(np.percentile(times, 50)), "ms_max": float(max(times)),
             "solves_per_s": len(times) / (sum(times) / 1e3),
-            "unknowns_per_s": sum(cells) / (sum(times) / 1e3)}
+            "unknowns_per_s": sum(cells) / (sum(times) / 1e3),
+            "err_vs_fp64_oracle": {"max": float(max(errs)) if errs else None,
+                                   "per_request": [float("%.3g" % e) for e in errs]}}
 
 
 def profile_solves(spec, n):
@@ -597,7 +654,9 @@ def main():
     # cores (rank 0 of a single-GPU run, beside the CPU baseline).
     check = rank == 0 and world == 1 and not args.no_cpu_baseline
     batched = None if args.no_batched else run_batched(afv, W, local, rank, world, check_errors=check)
-    served, reqs = (None, None) if args.no_serving else run_serving(afv, W, local, rank, world)
+    picks = serving_picks(500)
+    served, reqs, served_phi = (None, None, {}) if args.no_serving else run_serving(
+        afv, W, local, rank, world, keep_ids=set(picks) if check else ())
     uniform = None if args.no_uniform else run_uniform(afv, W, local, rank, world, check_errors=check)
 
     peak, peak_kind = load_peaks()
@@ -616,7 +675,7 @@ def main():
         solve(afv.AFV_PREC_FP64)
         err_fp64 = osolve.error_of(forest.get_var(0, afv.AFV_PHI))
         if served is not None:
-            served["cpu_oracle"] = cpu_serving_sample(reqs, cores)
+            served["cpu_oracle"] = cpu_serving_sample(reqs, cores, picks, served_phi)
     if rank != 0:
         return
     errs = {} if cpu is None else {"err_vs_fp64_oracle": err_mixed}

@@ -409,6 +409,15 @@ int afv_forest_get_option(afv_forest* f, int option, int* value);
  * choice receives it; ms3 (may be NULL) the ms per V-cycle of variants 1, 2
  * and 0 in that order. */
 int afv_forest_autotune(afv_forest* f, int* choice, float* ms3);
+/* No counterpart in the reference: the full tuning pass. Times the six sweep
+ * kernels (AFV_OPT_SWEEP_KERNEL 0..5: the block-pipelined level kernel, the
+ * warp-per-box kernel with bulk copies in four warp / stage shapes, the one
+ * with per-lane copies), keeps the fastest, then times AFV_OPT_SMALL_SWEEPS
+ * and AFV_OPT_COARSE_END on and off with it and keeps the fastest pair.
+ * choice3 receives (sweep kernel, small sweeps, coarse end); ms10 (may be
+ * NULL) the ms per FP32 V-cycle of sweep kernels 0..5, then of the (small,
+ * coarse end) settings (0,0), (0,1), (1,0), (1,1). Needs mixed_buffers. */
+int afv_forest_autotune_all(afv_forest* f, int* choice3, float* ms10);
 
 /* No counterpart in the reference: the profiled event pairs one by one (up
  * to max; n_total receives how many were recorded): kernel kind, level,

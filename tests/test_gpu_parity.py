@@ -293,8 +293,8 @@ def test_mixed_batch_alone_vs_mix(gpu):
 @pytest.mark.parametrize("which", ["c1", "3d"])
 def test_sweep_kernel_variants_agree(gpu, which):
     """Every sweep kernel variant (block-pipelined, warp-per-box with bulk
-    copies, warp-per-box with per-lane copies) gives the oracle's bits, FP64
-    and mixed."""
+    copies in four warp / stage shapes, warp-per-box with per-lane copies)
+    gives the oracle's bits, FP64 and mixed."""
     spec = W.c1_poisson_2d() if which == "c1" else W.c2_poisson_3d(thr=3e-3, lvl_max=5)
     f, ot, _ = setup_pair(gpu, spec)
     for _ in range(2):
@@ -302,7 +302,7 @@ def test_sweep_kernel_variants_agree(gpu, which):
     ref = oracle_var(ot, O.I_PHI, spec["n_cell"])
     rhs = f.get_var(0, gpu.AFV_RHS)
     mixed = []
-    for sk in (0, 1, 2):
+    for sk in (0, 1, 2, 3, 4, 5):
         g = gpu.Forest([W.build_tree(spec)], mixed=True)
         g.set_var(0, gpu.AFV_RHS, rhs)
         g.set_option(gpu.AFV_OPT_SWEEP_KERNEL, sk)
@@ -313,7 +313,8 @@ def test_sweep_kernel_variants_agree(gpu, which):
         g.solve(gpu.AFV_PREC_MIXED, tol=1e-8, max_cycles=30)
         mixed.append(g.get_var(0, gpu.AFV_PHI))
         g.close()
-    assert np.array_equal(mixed[0], mixed[1]) and np.array_equal(mixed[0], mixed[2])
+    for m in mixed[1:]:
+        assert np.array_equal(mixed[0], m)
 
 
 @pytest.mark.parametrize("which", ["c1", "3d"])
@@ -520,3 +521,27 @@ def test_not_converged_is_its_own_code(gpu):
         f.zero(gpu.AFV_PHI)
         cyc, rel, rc = f.solve(prec, tol=1e-8, max_cycles=2, check=False)
         assert rc == gpu.AFV_ERR_NOT_CONVERGED and int(cyc[0]) == 2 and rel[0] > 1e-8
+
+
+def test_autotune_all_keeps_results(gpu):
+    """The full tuning pass picks a sweep kernel and the two fusion switches,
+    reports a time for every setting, and a solve with the choice gives the
+    same bits as one with the defaults."""
+    specs = W.c4_random_2d(3, small=True)
+    out = []
+    for tune in (False, True):
+        g = gpu.Forest([W.build_tree(s) for s in specs], mixed=True)
+        for k, s in enumerate(specs):
+            g.set_source(k, s["gauss"], lpl=True)
+        if tune:
+            choice, times = g.autotune_all()
+            assert 0 <= choice["sweep_kernel"] <= 5 and len(times) == 10
+            assert all(t > 0 for t in times.values())
+            assert g.get_option(gpu.AFV_OPT_SWEEP_KERNEL) == choice["sweep_kernel"]
+            assert g.get_option(gpu.AFV_OPT_SMALL_SWEEPS) == choice["small_sweeps"]
+            assert g.get_option(gpu.AFV_OPT_COARSE_END) == choice["coarse_end"]
+        cyc, rel, rc = g.solve(gpu.AFV_PREC_MIXED, tol=1e-8, max_cycles=60)
+        out.append([g.get_var(k, gpu.AFV_PHI) for k in range(len(specs))])
+        g.close()
+    for a, b in zip(out[0], out[1]):
+        assert np.array_equal(a, b)
