@@ -11,6 +11,14 @@
 !>  * uploads phi, rhs and tmp of every box, runs the cycle, and downloads
 !>    phi, rhs and tmp, so the tree ends as the reference's routine leaves it.
 !>
+!> Lean mode (gb$D_lean = .true.): the device keeps phi, rhs and tmp between
+!> calls. A call uploads (and samples sides_bc) only when the refinement
+!> changed or the caller bumped gb$D_data_gen since the last upload (after
+!> changing phi, rhs, tmp or the boundary hook on the host), and downloads
+!> phi only, plus tmp when set_residual is true. The host's rhs and tmp are
+!> then out of date where the cycle changed them (the coarse levels' rhs,
+!> tmp without set_residual); gb$D_sync downloads all three.
+!>
 !> Only the constant-coefficient Laplacian is on the device: mg%box_op,
 !> box_gsrb, box_corr, box_rstr and sides_rb must be the defaults that
 !> mg$D_init_mg sets, else the call stops.
@@ -31,6 +39,8 @@ module m_a$D_gb300
      type(c_ptr)          :: tree = c_null_ptr
      type(c_ptr)          :: forest = c_null_ptr
      integer(c_long_long) :: stamp(4) = -1
+     !> gb$D_data_gen at the last upload (-1: none)
+     integer(c_long_long) :: gen = -1
      !> reference ids of the mirror's boxes in the host exchange order
      integer, allocatable :: order(:)
   end type gb_mirror_t
@@ -40,10 +50,15 @@ module m_a$D_gb300
 
   !> CUDA device the mirror is created on
   integer, public :: gb$D_device = 0
+  !> Keep the state on the device between calls (see above)
+  logical, public :: gb$D_lean = .false.
+  !> Bumped by the caller whenever it changes phi, rhs, tmp or sides_bc
+  integer(c_long_long), public :: gb$D_data_gen = 0
 
   public :: mg$D_fas_vcycle
   public :: mg$D_fas_fmg
   public :: gb$D_release
+  public :: gb$D_sync
 
 contains
 
@@ -58,7 +73,7 @@ contains
     call prepare(tree, mg, opts)
     call afv_check(afv_mg_fas_vcycle(mirror%forest, opts, int(highest_lvl, c_int), &
          merge(1_c_int, 0_c_int, set_residual)), "mg$D_fas_vcycle")
-    call download_all(tree, mg)
+    call download_after(tree, mg, set_residual)
   end subroutine mg$D_fas_vcycle
 
   !> mg$D_fas_fmg (src/m_aX_mg.f90:164-203) on the device
@@ -72,8 +87,16 @@ contains
     call prepare(tree, mg, opts)
     call afv_check(afv_mg_fas_fmg(mirror%forest, opts, merge(1_c_int, 0_c_int, set_residual), &
          merge(1_c_int, 0_c_int, have_guess)), "mg$D_fas_fmg")
-    call download_all(tree, mg)
+    call download_after(tree, mg, set_residual)
   end subroutine mg$D_fas_fmg
+
+  !> Download phi, rhs and tmp of the mirror into the tree (after lean calls)
+  subroutine gb$D_sync(tree, mg)
+    type(a$D_t), intent(inout) :: tree
+    type(mg$D_t), intent(in)   :: mg
+    if (.not. c_associated(mirror%forest)) return
+    call download_all(tree, mg)
+  end subroutine gb$D_sync
 
   !> Free the device mirror (the next call builds it again)
   subroutine gb$D_release()
@@ -82,6 +105,7 @@ contains
     mirror%forest = c_null_ptr
     mirror%tree = c_null_ptr
     mirror%stamp = -1
+    mirror%gen = -1
     if (allocated(mirror%order)) deallocate(mirror%order)
   end subroutine gb$D_release
 
@@ -104,14 +128,31 @@ contains
        call build_mirror(tree)
        mirror%stamp = stamp
     end if
-    call sample_bc(tree, mg)
-    call upload(tree, mg%i_phi, AFV_PHI)
-    call upload(tree, mg%i_rhs, AFV_RHS)
-    call upload(tree, mg%i_tmp, AFV_TMP)
+    if (.not. gb$D_lean .or. mirror%gen /= gb$D_data_gen) then
+       call sample_bc(tree, mg)
+       call upload(tree, mg%i_phi, AFV_PHI)
+       call upload(tree, mg%i_rhs, AFV_RHS)
+       call upload(tree, mg%i_tmp, AFV_TMP)
+       mirror%gen = gb$D_data_gen
+    end if
     opts%n_cycle_down = mg%n_cycle_down
     opts%n_cycle_up = mg%n_cycle_up
     opts%n_cycle_base = mg%n_cycle_base
   end subroutine prepare
+
+  !> What a call hands back: everything, or in lean mode phi (and tmp when
+  !> the residual was asked for)
+  subroutine download_after(tree, mg, set_residual)
+    type(a$D_t), intent(inout) :: tree
+    type(mg$D_t), intent(in)   :: mg
+    logical, intent(in)        :: set_residual
+    if (.not. gb$D_lean) then
+       call download_all(tree, mg)
+    else
+       call download(tree, mg%i_phi, AFV_PHI)
+       if (set_residual) call download(tree, mg%i_tmp, AFV_TMP)
+    end if
+  end subroutine download_after
 
   subroutine download_all(tree, mg)
     type(a$D_t), intent(inout) :: tree
