@@ -46,6 +46,8 @@ AFV_OPT_WAIT_LIMIT_US = 7
 AFV_RB_MG, AFV_RB_PROLONG0, AFV_RB_INTERP, AFV_RB_INTERP_LIM = 0, 1, 2, 3
 AFV_BCM_TABLE, AFV_BCM_DIRICHLET_ZERO, AFV_BCM_NEUMANN_ZERO = 0, -1, -2
 AFV_OP_LPL, AFV_OP_LPLD, AFV_OP_AUTO = 0, 1, 2
+AFV_OP_CLPL, AFV_OP_CLPLD, AFV_OP_LPLLSF = 3, 4, 5
+AFV_COORD_XYZ, AFV_COORD_CYL = 0, 1
 KERNEL_KINDS = ("sweep", "fill", "restrict", "coarse_rhs", "correct", "residual", "defect",
                 "accumulate", "coarse_end")
 
@@ -112,6 +114,7 @@ def lib():
             "afv_version": (I, []),
             "afv_tree_create": (I, [I, I, Dd, dp, I, I, Dd, ctypes.POINTER(P)]),
             "afv_tree_set_base": (I, [P, I, ip, ip]),
+            "afv_tree_set_coord": (I, [P, I]),
             "afv_tree_adjust_refinement": (I, [P, REF_FN, P, ip, ip]),
             "afv_tree_adjust_builtin": (I, [P, ctypes.POINTER(RefCrit), ip, ip]),
             "afv_tree_refine_builtin": (I, [P, ctypes.POINTER(RefCrit), I, ip]),
@@ -161,6 +164,7 @@ def lib():
             "afv_dtree_download": (I, [P, P]),
             "afv_dtree_get_info": (I, [P, ip]),
             "afv_mg_set_operator": (I, [P, I, I]),
+            "afv_mg_set_operator_lsf": (I, [P, I, I, I, I]),
             "afv_forest_set_fc": (I, [P, I, I, dp, LL]),
             "afv_forest_get_fc": (I, [P, I, I, dp, LL]),
             "afv_prolong_from_level": (I, [P, I, I, I, I, I]),
@@ -218,6 +222,11 @@ class Tree:
         if getattr(self, "h", None) and _lib is not None:
             _lib.afv_tree_destroy(self.h)
             self.h = None
+
+    def set_coord(self, coord):
+        """a$D_init's coord (AFV_COORD_XYZ or AFV_COORD_CYL); before set_base."""
+        _check(lib().afv_tree_set_coord(self.h, coord))
+        return self
 
     def set_base(self, ix_list, nb_list):
         ix = np.ascontiguousarray(np.asarray(ix_list, dtype=np.int32).reshape(-1, self.dim))
@@ -526,9 +535,13 @@ class Forest:
         _check(lib().afv_forest_add_vars(self.h, n_cc, n_fc))
         self.__dict__["_n_fc"] = self.__dict__.get("_n_fc", 0) + n_fc
 
-    def set_operator(self, op, i_eps=-1):
-        """mg%box_op / box_gsrb / box_corr and mg%i_eps (AFV_OP_*)."""
-        _check(lib().afv_mg_set_operator(self.h, op, i_eps))
+    def set_operator(self, op, i_eps=-1, i_lsf=-1, i_bval=-1):
+        """mg%box_op / box_gsrb / box_corr / box_rstr with mg%i_eps, mg%i_lsf
+        and mg%i_bval (AFV_OP_*)."""
+        if i_lsf < 0 and i_bval < 0:
+            _check(lib().afv_mg_set_operator(self.h, op, i_eps))
+        else:
+            _check(lib().afv_mg_set_operator_lsf(self.h, op, i_eps, i_lsf, i_bval))
 
     def fc_count(self, tree):
         t = self.trees[tree]

@@ -101,6 +101,14 @@ int afv_tree_create(int dim, int n_cell, double dr, const double* r_min, int lvl
   });
 }
 
+int afv_tree_set_coord(afv_tree* t, int coord) {
+  if (!t) return fail(AFV_ERR_INVALID, "tree is NULL");
+  if (coord != AFV_COORD_XYZ && coord != AFV_COORD_CYL) return fail(AFV_ERR_INVALID, "unknown coordinate system");
+  if (coord == AFV_COORD_CYL && t->t.dim != 2) return fail(AFV_ERR_INVALID, "cylindrical coordinates need a 2-D tree");
+  t->t.coord = coord;
+  return AFV_OK;
+}
+
 int afv_tree_set_base(afv_tree* t, int n_boxes, const int* ix_list, const int* nb_list) {
   if (!t || !ix_list || !nb_list) return fail(AFV_ERR_INVALID, "NULL argument");
   return guarded([&](std::string& err) -> int {
@@ -556,8 +564,10 @@ int afv_forest_get_option(afv_forest* f, int option, int* value) {
   return fail(AFV_ERR_INVALID, "unknown option");
 }
 
-int afv_mg_set_operator(afv_forest* f, int op, int i_eps) {
-  FOREST_CALL(f, return f->f.set_operator(op, i_eps, err));
+int afv_mg_set_operator(afv_forest* f, int op, int i_eps) { return afv_mg_set_operator_lsf(f, op, i_eps, -1, -1); }
+
+int afv_mg_set_operator_lsf(afv_forest* f, int op, int i_eps, int i_lsf, int i_bval) {
+  FOREST_CALL(f, return f->f.set_operator(op, i_eps, i_lsf, i_bval, err));
 }
 
 int afv_forest_add_vars(afv_forest* f, int n_cc, int n_fc) {

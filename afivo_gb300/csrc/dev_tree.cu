@@ -423,6 +423,7 @@ class DevTree {
   int device = 0;
   cudaStream_t st = nullptr;
   int dim = 2, nch = 4, nnb = 4, n_cell = 8, min_lvl = 1, lvl_limit = 30, box_limit = 0;
+  int coord = 0;  // the host tree's coordinate system, carried to downloads
   int highest_lvl = 0, highest_id = 0, n_adjust = 0;
   bool ready = false;
   double dr_base = 0, r_base[3] = {0, 0, 0};
@@ -542,6 +543,7 @@ int DevTree::init(const HostTree& h, int dev, std::string& err) {
   if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess)
     return err = "cudaStreamCreate failed", AFV_ERR_CUDA;
   dim = h.dim;
+  coord = h.coord;
   nch = h.nch;
   nnb = h.nnb;
   n_cell = h.n_cell;
@@ -770,6 +772,7 @@ int DevTree::adjust(const afv_ref_crit* crit, int* n_add, int* n_rm, std::string
 int DevTree::download(HostTree& h, std::string& err) const {
   cudaSetDevice(device);
   h.dim = dim;
+  h.coord = coord;
   h.nch = nch;
   h.nnb = nnb;
   h.n_cell = n_cell;

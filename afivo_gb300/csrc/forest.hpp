@@ -12,6 +12,9 @@
 
 namespace afv {
 
+namespace opdev {
+struct Op;
+}
 namespace dev {
 struct BoxSet;
 }
@@ -120,14 +123,23 @@ class Forest {
   int* d_lvl = nullptr;
   int* d_qd = nullptr;
   // Operator of the FP64 multigrid routines (afv_mg_set_operator): AFV_OP_LPL
-  // (the fused constant-coefficient kernels), AFV_OP_LPLD or AFV_OP_AUTO (the
-  // generic kernels of operators.cu, with eps in cell variable i_eps and the
-  // per-box tags of the auto dispatch in d_tags).
+  // (the fused constant-coefficient kernels in Cartesian trees), or one of
+  // AFV_OP_LPLD, AFV_OP_CLPL, AFV_OP_CLPLD, AFV_OP_LPLLSF, AFV_OP_AUTO (the
+  // generic kernels of operators.cu, with eps in cell variable i_eps, the
+  // level set and its boundary value in i_lsf / i_bval, and the per-box tags
+  // of the auto dispatch in d_tags).
   int op = AFV_OP_LPL;
-  int i_eps = -1;
+  int i_eps = -1, i_lsf = -1, i_bval = -1;
   int* d_tags = nullptr;
-  int set_operator(int new_op, int new_i_eps, std::string& err);
+  int* d_ix = nullptr;  // [slot*D + d] the boxes' ix (cylindrical radial factors)
+  int set_operator(int new_op, int new_i_eps, int new_i_lsf, int new_i_bval, std::string& err);
   const double* eps_ptr() const;
+  opdev::Op op_args() const;  // what the generic kernels read
+  // The FP64 routines take the generic kernels of operators.cu: an operator
+  // other than the Laplacian, or cylindrical coordinates (whose restriction
+  // is weighted).
+  bool generic() const { return op != AFV_OP_LPL || plan.cyl; }
+  void gen_init_phi_rhs();  // init_phi_rhs (FMG without a guess)
   void gen_gsrb_boxes(int lvl, int n_cycle);
   void gen_update_coarse(int lvl, bool copy_tmp);
   void gen_correct(int lvl_parent);

@@ -34,6 +34,7 @@ uint64_t morton_key(int dim, const int* ix0);
 class HostTree {
  public:
   int dim = 2;
+  int coord = 0;  // 0 Cartesian, 1 cylindrical (a$D_init's coord, src/m_aX_core.f90:58-70)
   int nch = 4;  // 2^dim
   int nnb = 4;  // 2*dim
   int n_cell = 8;

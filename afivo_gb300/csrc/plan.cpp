@@ -21,13 +21,14 @@ int build_plan(const std::vector<const HostTree*>& trees, Plan& p, std::string& 
   p.dim = t0.dim;
   p.nc = t0.n_cell;
   p.min_lvl = t0.min_lvl;
+  p.cyl = t0.coord == 1;
   p.n_trees = (int)trees.size();
   const int D = p.dim, NCH = 1 << D, NNB = 2 * D;
   int max_lvl = 1;
   for (const HostTree* t : trees) {
     if (!t->ready) return err = "tree without base (set_base not called)", AFV_ERR_STATE;
-    if (t->dim != D || t->n_cell != p.nc || t->min_lvl != p.min_lvl)
-      return err = "trees of one forest need the same dim, n_cell and coarsen_to", AFV_ERR_INVALID;
+    if (t->dim != D || t->n_cell != p.nc || t->min_lvl != p.min_lvl || t->coord != t0.coord)
+      return err = "trees of one forest need the same dim, n_cell, coarsen_to and coordinates", AFV_ERR_INVALID;
     max_lvl = std::max(max_lvl, t->highest_lvl);
   }
   p.max_lvl = max_lvl;

@@ -30,6 +30,7 @@ struct BcSpec {
 
 struct Plan {
   int dim = 2, nc = 8, min_lvl = 1, max_lvl = 1, n_trees = 0, n_slots = 0;
+  int cyl = 0;  // the trees' coordinates are cylindrical (2-D)
   // per slot
   std::vector<int> nb;           // [s*2D+f]: slot, -1 refinement boundary, -2 physical
   std::vector<int> parent;       // slot or -1

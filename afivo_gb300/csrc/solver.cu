@@ -162,7 +162,7 @@ Forest::~Forest() {
     if (p) cudaFreeAsync(p, stream);
   for (double* p : xcc)
     if (p) cudaFreeAsync(p, stream);
-  for (void* p : {(void*)fc, (void*)d_nb, (void*)d_lvl, (void*)d_qd, (void*)d_tags})
+  for (void* p : {(void*)fc, (void*)d_nb, (void*)d_lvl, (void*)d_qd, (void*)d_tags, (void*)d_ix})
     if (p) cudaFreeAsync(p, stream);
   if (stream) cudaStreamSynchronize(stream);
   for (const ProfEntry& p : prof) {
@@ -997,7 +997,7 @@ void Forest::vcycle_t(const Arrays<T>& a, const MgOpts& mg, int highest, bool ho
 void Forest::fill64(int lvl) { fill(d64, lvl, false); }
 
 int Forest::gsrb_level(int lvl, int n_cycle, std::string& err) {
-  if (op != AFV_OP_LPL) {
+  if (generic()) {
     gen_gsrb_boxes(lvl, n_cycle);
     if (int rc = check(err, "gsrb_level")) return rc;
     return check_device_error(err);
@@ -1012,7 +1012,7 @@ int Forest::fill_level(int lvl, std::string& err) {
 }
 int Forest::update_coarse(int lvl, std::string& err) {
   if (lvl <= plan.min_lvl || lvl > plan.max_lvl) return err = "level out of range", AFV_ERR_INVALID;
-  if (op != AFV_OP_LPL)
+  if (generic())
     gen_update_coarse(lvl, true);
   else
     update_coarse_t(d64, lvl, false, true);
@@ -1020,7 +1020,7 @@ int Forest::update_coarse(int lvl, std::string& err) {
 }
 int Forest::correct_children(int lp, std::string& err) {
   if (lp < plan.min_lvl || lp >= plan.max_lvl) return err = "level out of range", AFV_ERR_INVALID;
-  if (op != AFV_OP_LPL)
+  if (generic())
     gen_correct(lp);
   else
     correct(d64, lp);
@@ -1028,7 +1028,7 @@ int Forest::correct_children(int lp, std::string& err) {
 }
 int Forest::residual_all(unsigned long long* norm, std::string& err) {
   for (int l = plan.min_lvl; l <= plan.max_lvl; ++l)
-    if (op != AFV_OP_LPL)
+    if (generic())
       gen_residual(l, norm);
     else
       residual(d64, l, norm, true);
@@ -1038,7 +1038,7 @@ int Forest::residual_all(unsigned long long* norm, std::string& err) {
 int Forest::vcycle(const MgOpts& mg, int highest, bool set_residual, std::string& err) {
   if (highest < plan.min_lvl) return err = "highest_lvl below the coarsest level", AFV_ERR_INVALID;
   highest = std::min(highest, plan.max_lvl);
-  if (op != AFV_OP_LPL) {
+  if (generic()) {
     gen_vcycle(mg, highest, set_residual);
   } else {
     vcycle_t(d64, mg, highest, false, false);
@@ -1225,11 +1225,13 @@ int Forest::fmg(const MgOpts& mg, bool set_residual, bool have_guess, std::strin
         fill(d64, l, false);
         set_active_host(all);
       }
-      if (op != AFV_OP_LPL)
+      if (generic())
         gen_update_coarse(l, false);
       else
         update_coarse_t(d64, l, false, false);
     }
+  } else if (generic()) {
+    gen_init_phi_rhs();
   } else {
     // init_phi_rhs: phi = 0 on levels > min_lvl, rhs restricted downwards.
     for (int l = plan.max_lvl; l >= l0 + 1; --l) {
@@ -1275,13 +1277,13 @@ int Forest::fmg(const MgOpts& mg, bool set_residual, bool have_guess, std::strin
       });
     }
     if (l > l0) {
-      if (op != AFV_OP_LPL)
+      if (generic())
         gen_correct(l - 1);
       else
         correct(d64, l - 1);
       fill(d64, l, false);
     }
-    if (op != AFV_OP_LPL)
+    if (generic())
       gen_vcycle(mg, l, false);
     else
       vcycle_t(d64, mg, l, false, false);
@@ -1293,7 +1295,7 @@ int Forest::fmg(const MgOpts& mg, bool set_residual, bool have_guess, std::strin
       if (any) {
         set_active_host(fin);
         for (int k = l0; k <= l; ++k)
-          if (op != AFV_OP_LPL)
+          if (generic())
             gen_residual(k, nullptr);
           else
             residual(d64, k, nullptr, true);
@@ -1382,7 +1384,7 @@ void Forest::enqueue_residual_check(int precision, double tol, int count_cycle) 
                  d64.phi, d64.rhs, d32.rhs, d_norm);
       }
     });
-  } else if (op != AFV_OP_LPL) {
+  } else if (generic()) {
     for (int l = plan.min_lvl; l <= plan.max_lvl; ++l) gen_residual(l, d_norm);
   } else {
     for (int l = plan.min_lvl; l <= plan.max_lvl; ++l) residual(d64, l, d_norm, true);
@@ -1454,7 +1456,7 @@ void Forest::enqueue_iteration(const MgOpts& mg, int precision, double tol) {
     enqueue_residual_check(precision, tol);
     join();
   } else {
-    if (op != AFV_OP_LPL)
+    if (generic())
       gen_vcycle(mg, plan.max_lvl, false);
     else
       vcycle_t(d64, mg, plan.max_lvl, false, false);
@@ -1613,8 +1615,8 @@ int Forest::solve(const MgOpts& mg, int precision, double tol, int max_cycles, S
   cudaMemcpyAsync(d_solve_mask, h_solve_mask, sizeof(int) * nt, cudaMemcpyHostToDevice, stream);
   if (precision == AFV_PREC_MIXED && !mixed)
     return err = "forest created without mixed_buffers", AFV_ERR_STATE;
-  if (precision == AFV_PREC_MIXED && op != AFV_OP_LPL)
-    return err = "mixed-precision solves take the constant-coefficient operator only", AFV_ERR_UNSUPPORTED;
+  if (precision == AFV_PREC_MIXED && generic())
+    return err = "mixed-precision solves take the Cartesian constant-coefficient operator only", AFV_ERR_UNSUPPORTED;
   st.cycles.assign(nt, 0);
   st.rel_res.assign(nt, 0.0);
   const bool graph = use_graphs && prof_mask == 0;

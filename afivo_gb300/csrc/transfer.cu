@@ -41,7 +41,19 @@ struct XT {
   const long long* offg;    // [s]
   const SlotDesc* desc;     // [s]
   const double* bcval;      // boundary values of the sampled sides_bc records
+  const double* rmin;       // [s*D+d] lower corner of each box
+  int cyl;                  // cylindrical trees (2-D)
 };
+
+// a2_cyl_child_weights (src/m_aX_t.f90:516-528): weights of the inner and
+// outer child at cell index i of a box with lower radius r0 and cell size dr
+// (the cell centre's radius, a2_cyl_radius_cc, :508-514).
+__device__ __forceinline__ void cyl_weights(double r0, double dr, int i, double& inner, double& outer) {
+  const double r = r0 + (i - 0.5) * dr;
+  const double tmp = 0.25 * dr / r;
+  inner = 1 - tmp;
+  outer = 1 + tmp;
+}
 
 template <int D>
 __device__ __forceinline__ long long gi(int ng, int i, int j, int k) {
@@ -138,9 +150,11 @@ __global__ void k_prolong(XT t, const int* __restrict__ parents, int np, int nch
   }
 }
 
-// a$D_restrict_box (Cartesian) for every child of the parents of a level,
+// a$D_restrict_box for every child of the parents of a level,
 // src/m_aX_restrict.f90:67-132: the average of the 2^D fine cells, summed in
-// Fortran's column-major order starting from zero.
+// Fortran's column-major order starting from zero; in cylindrical trees the
+// inner and outer pairs weighted at the parent's radius of index i (the
+// reference's index within the child's quadrant, :90-103).
 template <int D>
 __global__ void k_restrict(XT t, const int* __restrict__ parents, int np, int nch, int ncp, int ncc,
                            const double* __restrict__ src, double* __restrict__ dst) {
@@ -159,6 +173,17 @@ __global__ void k_restrict(XT t, const int* __restrict__ parents, int np, int nc
     const int kc = D == 3 ? k + child_off(t, C, 2, hnc) : 0;
     const double* c = src + t.offg[C];
     const int i_f = 2 * i - 1, j_f = 2 * j - 1, k_f = D == 3 ? 2 * k - 1 : 0;
+    if (D == 2 && t.cyl) {
+      double w1, w2;
+      cyl_weights(t.rmin[(size_t)P * D], t.desc[P].dr, i, w1, w2);
+      double s1 = 0.0, s2 = 0.0;
+      s1 = s1 + c[gi<D>(ngc, i_f, j_f, 0)];
+      s1 = s1 + c[gi<D>(ngc, i_f, j_f + 1, 0)];
+      s2 = s2 + c[gi<D>(ngc, i_f + 1, j_f, 0)];
+      s2 = s2 + c[gi<D>(ngc, i_f + 1, j_f + 1, 0)];
+      dst[t.offg[P] + gi<D>(ngp, ic, jc, kc)] = 0.25 * (w1 * s1 + w2 * s2);
+      continue;
+    }
     double s = 0.0;
     for (int kk = 0; kk < (D == 3 ? 2 : 1); ++kk)
       for (int jj = 0; jj < 2; ++jj)
@@ -378,9 +403,11 @@ __global__ void k_gc2_level(XT t, const int* __restrict__ slots, int nbx, int nc
 }
 
 // a$D_consistent_fluxes for the parents of one level (src/m_aX_core.f90:
-// 811-945, Cartesian): where a parent's neighbour across face f exists and has
-// no children, the neighbour's face fluxes on that face become the average of
-// the adjacent children's fine fluxes. One thread per coarse face value.
+// 811-945): where a parent's neighbour across face f exists and has no
+// children, the neighbour's face fluxes on that face become the average of
+// the adjacent children's fine fluxes, in cylindrical trees with the radial
+// weights of the neighbour's cell for the axial fluxes (:881-895). One thread
+// per coarse face value.
 template <int D>
 __global__ void k_flux_level(XT t, const int* __restrict__ parents, int np, int nc, double* __restrict__ fc,
                              long long stride, const int* __restrict__ ifc, int nfc, long long per_var) {
@@ -429,7 +456,13 @@ __global__ void k_flux_level(XT t, const int* __restrict__ parents, int np, int 
     if constexpr (D == 2) {
       const int e = 1 - dim;
       b[e] = a[e] + 1;
-      val = 0.5 * (cf[fidx(a[0], a[1], 1)] + cf[fidx(b[0], b[1], 1)]);
+      if (dim == 1 && t.cyl) {
+        double w1, w2;
+        cyl_weights(t.rmin[(size_t)nbs * D], t.desc[nbs].dr, cc[0], w1, w2);
+        val = 0.5 * (w1 * cf[fidx(a[0], a[1], 1)] + w2 * cf[fidx(b[0], b[1], 1)]);
+      } else {
+        val = 0.5 * (cf[fidx(a[0], a[1], 1)] + cf[fidx(b[0], b[1], 1)]);
+      }
     } else {
       const int e1 = dim == 0 ? 1 : 0, e2 = dim == 2 ? 1 : 2;
       int a2[3] = {a[0], a[1], a[2]}, a3[3] = {a[0], a[1], a[2]}, a4[3] = {a[0], a[1], a[2]};
@@ -517,6 +550,8 @@ xdev::XT tables(const Forest& F) {
   t.offg = F.meta.offg;
   t.desc = F.meta.desc;
   t.bcval = F.meta.bcval;
+  t.rmin = F.meta.rmin;
+  t.cyl = F.plan.cyl;
   return t;
 }
 
@@ -880,7 +915,8 @@ int forest_write_vtk(Forest& F, int tree, const char* filename, int n_cycle, dou
   }
   std::vector<std::string> names;
   for (int k = 0; k < n_cc; ++k) names.push_back(cc_names[k]);
-  static const char* sfx[3] = {"_x", "_y", "_z"};
+  const bool cyl = D == 2 && F.plan.cyl;  // a$D_write_vtk names r, z in cylindrical trees
+  const char* sfx[3] = {cyl ? "_r" : "_x", cyl ? "_z" : "_y", "_z"};
   for (int k = 0; k < n_fcv; ++k)
     for (int d = 0; d < D; ++d) names.push_back(std::string(fc_names[k]) + sfx[d]);
   // the file, in the order of vtk_ini_xml .. vtk_end_xml

@@ -98,6 +98,8 @@ def c5_requests(n=64, seed=5, small=False):
 def build_tree(spec, max_passes=100):
     """Build the host tree of a workload with the library's tree builder."""
     t = Tree(spec["dim"], spec["n_cell"], spec["dr"], coarsen_to=spec["coarsen_to"])
+    if spec.get("coord", 0):
+        t.set_coord(spec["coord"])
     t.set_base(spec["ix"], spec["nb"])
     if spec["crit"] == AFV_REF_RANDOM and "target_cells" in spec:
         for _ in range(max_passes):

@@ -119,6 +119,11 @@ int afv_version(void);
  * coarsen_to <= 0 means no coarse sub-levels). */
 int afv_tree_create(int dim, int n_cell, double dr, const double* r_min, int lvl_limit,
                     int coarsen_to, double mem_limit_gb, afv_tree** out);
+/* a$D_init's coord argument (src/m_aX_core.f90:58-70, 102): AFV_COORD_CYL
+ * makes a 2-D tree cylindrical (x the radius, y the axis). Set it before
+ * afv_tree_set_base; every box inherits it (core:772). */
+enum { AFV_COORD_XYZ = 0, AFV_COORD_CYL = 1 };
+int afv_tree_set_coord(afv_tree* t, int coord);
 /* a$D_set_base, src/m_aX_core.f90:152-235. ix_list: n_boxes*dim, nb_list:
  * n_boxes*2*dim, both box-major. */
 int afv_tree_set_base(afv_tree* t, int n_boxes, const int* ix_list, const int* nb_list);
@@ -218,24 +223,37 @@ int afv_forest_get_stream(afv_forest* f, void** stream);
 
 /* mg$D_init_mg, src/m_aX_mg.f90:130-154. */
 int afv_mg_init(afv_mg_opts* mg);
-/* Operators of the multigrid routines (mg%box_op, mg%box_gsrb, mg%box_corr;
- * mg%box_rstr stays mg$D_box_rstr_lpl): AFV_OP_LPL, the constant-coefficient
- * Laplacian (mg$D_box_*_lpl, the default); AFV_OP_LPLD, the variable-
- * coefficient operator div(eps grad phi) on every box (mg$D_box_gsrb_lpld,
- * mg$D_box_lpld, mg$D_box_corr_lpld, src/m_aX_mg.f90:810-985); AFV_OP_AUTO,
- * the per-box dispatch of mg$D_auto_gsrb / _op / _corr (:562-669), boxes
- * whose eps is 1 everywhere taking the AFV_OP_LPL operators. */
-enum { AFV_OP_LPL = 0, AFV_OP_LPLD = 1, AFV_OP_AUTO = 2 };
-/* Sets mg%box_op / box_gsrb / box_corr and mg%i_eps of a forest. eps is the
- * extra cell variable i_eps (>= 3, afv_forest_add_vars); as with the
- * reference, the caller fills its ghost cells and coarse levels (for instance
- * afv_gc_tree_var and afv_restrict_tree). For AFV_OP_AUTO the per-box tags of
- * mg$D_set_box_tag (:672-706, min and max of eps over the box, ghost cells
- * included) are taken by this call, where the reference takes each box's tag
- * at its first use: call it again after changing eps. The operator applies to
- * the FP64 routines (V-cycle, FMG, single operators, FP64 solves); a mixed-
- * precision solve with a variable coefficient returns AFV_ERR_UNSUPPORTED. */
+/* Operators of the multigrid routines (mg%box_op, mg%box_gsrb, mg%box_corr,
+ * mg%box_rstr): AFV_OP_LPL, the constant-coefficient Laplacian
+ * (mg$D_box_*_lpl, the default); AFV_OP_LPLD, the variable-coefficient
+ * operator div(eps grad phi) on every box (mg$D_box_gsrb_lpld, mg$D_box_lpld,
+ * mg$D_box_corr_lpld, src/m_aX_mg.f90:810-985); AFV_OP_CLPL / AFV_OP_CLPLD,
+ * their cylindrical forms (mg2_box_*_clpl, mg2_box_*_clpld, :1323-1443;
+ * cylindrical 2-D trees only); AFV_OP_LPLLSF, the Laplacian with internal
+ * boundaries where a level set changes sign (mg$D_box_*_lpllsf with
+ * mg$D_box_rstr_lpllsf, :987-1321); AFV_OP_AUTO, the per-box dispatch of
+ * mg$D_auto_gsrb / _op / _corr / _rstr (:562-669) by the tags of
+ * mg$D_set_box_tag. In cylindrical trees every operator restricts with the
+ * radial weights of a2_restrict_box (src/m_aX_restrict.f90:90-103). */
+enum { AFV_OP_LPL = 0, AFV_OP_LPLD = 1, AFV_OP_AUTO = 2, AFV_OP_CLPL = 3, AFV_OP_CLPLD = 4, AFV_OP_LPLLSF = 5 };
+/* Sets mg%box_op / box_gsrb / box_corr / box_rstr and mg%i_eps of a forest
+ * (mg%i_lsf = mg%i_bval = -1). eps is the extra cell variable i_eps (>= 3,
+ * afv_forest_add_vars); as with the reference, the caller fills its ghost
+ * cells and coarse levels (for instance afv_gc_tree_var and
+ * afv_restrict_tree). For AFV_OP_AUTO the per-box tags of mg$D_set_box_tag
+ * (:672-706, min and max of eps and of the level set over the box, ghost
+ * cells included) are taken by this call, where the reference takes each
+ * box's tag at its first use: call it again after changing eps or the level
+ * set. A box that would take two tags is refused with AFV_ERR_INVALID, where
+ * the reference stops. The operator applies to the FP64 routines (V-cycle,
+ * FMG, single operators, FP64 solves); a mixed-precision solve with another
+ * operator than the Cartesian Laplacian returns AFV_ERR_UNSUPPORTED. */
 int afv_mg_set_operator(afv_forest* f, int op, int i_eps);
+/* As afv_mg_set_operator, with mg%i_lsf and mg%i_bval (both >= 3 or both
+ * -1, mg$D_init_mg's check, src/m_aX_mg.f90:136-137): the level set and the
+ * boundary value at the interface, extra cell variables with filled ghost
+ * cells. AFV_OP_LPLLSF needs both; AFV_OP_AUTO needs eps or the level set. */
+int afv_mg_set_operator_lsf(afv_forest* f, int op, int i_eps, int i_lsf, int i_bval);
 /* mg$D_fas_vcycle, src/m_aX_mg.f90:208-255 (all trees of the forest). */
 int afv_mg_fas_vcycle(afv_forest* f, const afv_mg_opts* mg, int highest_lvl, int set_residual);
 /* mg$D_fas_fmg, src/m_aX_mg.f90:164-203. */

@@ -97,6 +97,7 @@ template <int D> struct Box {
   int lvl = 0;
   bool in_use = false;
   int tag = a5_init_tag;
+  int coord = 0;  // a5_xyz (0) or a5_cyl (1), src/m_aX_t.f90:42-43
   int ix[D] = {};
   int parent = 0;
   int children[NCH] = {};
@@ -168,19 +169,23 @@ template <int D> struct Tree {
   std::vector<Lvl> lvls;            // lvl = min_lvl .. lvl_limit+1
   std::vector<Box<D>> boxes;        // 1-based, boxes[0] unused
   int n_adjust = 0;                 // number of adjust_refinement calls so far
+  int coord = 0;  // a5_xyz or a5_cyl (a$D_init's coord argument, core:58, 102)
   Lvl& L(int lvl) { return lvls[lvl - min_lvl]; }
   int n_boxes_capacity() const { return (int)boxes.size() - 1; }
 };
 
-// Operators of the multigrid routines (mg%box_op / box_gsrb / box_corr):
-// the constant-coefficient Laplacian, the variable-coefficient lpld
-// operators, or the per-box auto dispatch (src/m_aX_mg.f90:562-706, 810-985).
-enum { OP_LPL = 0, OP_LPLD = 1, OP_AUTO = 2 };
+// Operators of the multigrid routines (mg%box_op / box_gsrb / box_corr /
+// box_rstr): the constant-coefficient Laplacian, the variable-coefficient
+// lpld operators, the per-box auto dispatch (src/m_aX_mg.f90:562-706,
+// 810-985), the cylindrical clpl / clpld (:1323-1443) and the level-set
+// lpllsf operators (:987-1321).
+enum { OP_LPL = 0, OP_LPLD = 1, OP_AUTO = 2, OP_CLPL = 3, OP_CLPLD = 4, OP_LPLLSF = 5 };
 enum { MG_NORMAL_BOX = 1, MG_LSF_BOX = 2, MG_CEPS_BOX = 3, MG_VEPS_BOX = 4 };
 
 struct MG {
   int op = OP_LPL;
   int i_eps = -1;
+  int i_lsf = -1, i_bval = -1;  // level set and its boundary value (mg$D_t, mg:40-45)
   int i_phi = 0, i_rhs = 1, i_tmp = 2;
   int n_cycle_down = 2, n_cycle_up = 2, n_cycle_base = 2;
   int bc_kind = BC_DIRICHLET_ZERO;
@@ -400,6 +405,7 @@ int set_base(Tree<D>& t, int n_boxes, const int* ix_list, int* nb_list) {
       b.lvl = lvl;
       for (int d = 0; d < D; ++d) b.ix[d] = ix_list[(i - 1) * D + d];
       b.dr = t.dr_base * std::pow(0.5, lvl - 1);
+      b.coord = t.coord;
       for (int d = 0; d < D; ++d)
         b.r_min[d] = t.r_base[d] + (b.ix[d] - 1) * t.dr_base * t.n_cell;
       int nc = t.n_cell / (1 << (1 - lvl));
@@ -622,6 +628,7 @@ void add_children(std::vector<Box<D>>& boxes, int id, const int* c_ids, int n_va
     for (int k = 0; k < T::NCH; ++k) c.children[k] = a5_no_box;
     for (int k = 0; k < T::NNB; ++k) c.neighbors[k] = a5_no_box;
     c.dr = 0.5 * p.dr;
+    c.coord = p.coord;  // core:772
     for (int d = 0; d < D; ++d)
       c.r_min[d] = p.r_min[d] + 0.5 * p.dr * T::child_dix(i, d) * p.n_cell;
     init_box(c, p.n_cell, n_var);
@@ -1033,12 +1040,41 @@ template <int D> void prolong2_add(Box<D>& p, Box<D>& c, int iv, int ivc) {
   }
 }
 
-// a$D_restrict_box (Cartesian branch), restrict:67-132. The Fortran sum() of a
-// 2^D section accumulates column-major from zero.
+// a2_cyl_child_weights, src/m_aX_t.f90:516-528: the inner and outer
+// children's weights at cell index i of a box with lower radius r_min0 and
+// cell size dr (the cell centre's radius, a2_cyl_radius_cc, :508-514).
+inline void cyl_child_weights(double r_min0, double dr, int i, double& inner, double& outer) {
+  const double r = r_min0 + (i - 0.5) * dr;
+  const double tmp = 0.25 * dr / r;
+  inner = 1 - tmp;
+  outer = 1 + tmp;
+}
+
+// a$D_restrict_box, restrict:67-132. The Fortran sum() of a 2^D section
+// accumulates column-major from zero. In cylindrical trees the inner and
+// outer pairs take the parent's weights at index i (:90-103; the index
+// within the quadrant, as the reference passes it).
 template <int D> void restrict_box(Box<D>& c, Box<D>& p, int iv) {
   int hnc = c.n_cell >> 1;
   int off[D];
   child_offset(c, off);
+  if (D == 2 && p.coord == 1) {
+    for (int j = 1; j <= hnc; ++j) {
+      int j_c = off[1] + j, j_f = 2 * j - 1;
+      for (int i = 1; i <= hnc; ++i) {
+        int i_c = off[0] + i, i_f = 2 * i - 1;
+        double w1, w2;
+        cyl_child_weights(p.r_min[0], p.dr, i, w1, w2);
+        double s1 = 0.0, s2 = 0.0;
+        s1 = s1 + c.at(i_f, j_f, 0, iv);
+        s1 = s1 + c.at(i_f, j_f + 1, 0, iv);
+        s2 = s2 + c.at(i_f + 1, j_f, 0, iv);
+        s2 = s2 + c.at(i_f + 1, j_f + 1, 0, iv);
+        p.at(i_c, j_c, 0, iv) = 0.25 * (w1 * s1 + w2 * s2);
+      }
+    }
+    return;
+  }
   if constexpr (D == 2) {
     for (int j = 1; j <= hnc; ++j) {
       int j_c = off[1] + j, j_f = 2 * j - 1;
@@ -1117,23 +1153,36 @@ template <int D> void box_lpl(Box<D>& b, int i_out, const MG& mg) {
   }
 }
 
-// mg$D_set_box_tag (mg:672-706) without the level-set part: min and max of
-// eps over the whole box, ghost cells included
-template <int D> void set_box_tag(Box<D>& b, const MG& mg) {
-  bool is_eps = false, is_deps = false;
-  if (mg.i_eps != -1) {
-    const double* e = b.var(mg.i_eps);
-    double a = e[0], c = e[0];
+// mg$D_set_box_tag (mg:672-706): min and max of lsf and eps over the whole
+// box, ghost cells included. Returns false where the reference stops (a box
+// that would take two tags).
+template <int D> bool set_box_tag(Box<D>& b, const MG& mg) {
+  bool is_lsf = false, is_eps = false, is_deps = false;
+  auto minmax = [&](int iv, double& a, double& c) {
+    const double* e = b.var(iv);
+    a = e[0];
+    c = e[0];
     for (int n = 0; n < b.nvol(); ++n) {
       a = std::min(a, e[n]);
       c = std::max(c, e[n]);
     }
+  };
+  if (mg.i_lsf != -1) {
+    double a, c;
+    minmax(mg.i_lsf, a, c);
+    is_lsf = a * c < 0;
+  }
+  if (mg.i_eps != -1) {
+    double a, c;
+    minmax(mg.i_eps, a, c);
     is_deps = c > a;
     if (!is_deps) is_eps = (a < 1 || a > 1);
   }
   b.tag = MG_NORMAL_BOX;
+  if (is_lsf) b.tag = MG_LSF_BOX;
   if (is_eps) b.tag = MG_CEPS_BOX;
   if (is_deps) b.tag = MG_VEPS_BOX;
+  return (int)is_lsf + (int)is_eps + (int)is_deps <= 1;
 }
 
 // Neighbour values of cell (i,j[,k]) in the reference's order (i-1, i+1,
@@ -1230,13 +1279,249 @@ template <int D> void box_corr_lpld(Box<D>& p, Box<D>& c, const MG& mg) {
   }
 }
 
-// The operator hooks as the driver calls them: mg%box_gsrb, mg%box_op
-// (mg$D_auto_gsrb / mg$D_auto_op, mg:562-622, choose by the box's own tag).
-template <int D> bool use_lpld(Box<D>& b, const MG& mg) {
-  if (mg.op == OP_LPL) return false;
-  if (mg.op == OP_LPLD) return true;
+// mg2_box_gsrb_clpl / mg2_box_clpl / mg2_box_clpld / mg2_box_gsrb_clpld,
+// mg:1323-1443 (2-D only): the cylindrical operators, radial factors
+// rfac = [i+ioff-1, i+ioff] / (i+ioff-0.5) with ioff = (ix(1)-1) * nc.
+template <int D> void box_gsrb_clpl(Box<D>& b, int redblack_cntr, const MG& mg) {
+  if constexpr (D == 2) {
+    const double dx2 = b.dr * b.dr;
+    const int nc = b.n_cell, ip = mg.i_phi, ir = mg.i_rhs, ioff = (b.ix[0] - 1) * nc;
+    for (int j = 1; j <= nc; ++j) {
+      const int i0 = 2 - ((redblack_cntr ^ j) & 1);
+      for (int i = i0; i <= nc; i += 2) {
+        const double r1 = (i + ioff - 1) / (i + ioff - 0.5), r2 = (i + ioff) / (i + ioff - 0.5);
+        b.at(i, j, ip) = 0.25 * (r1 * b.at(i - 1, j, ip) + r2 * b.at(i + 1, j, ip) + b.at(i, j + 1, ip) +
+                                 b.at(i, j - 1, ip) - dx2 * b.at(i, j, ir));
+      }
+    }
+  }
+}
+template <int D> void box_clpl(Box<D>& b, int i_out, const MG& mg) {
+  if constexpr (D == 2) {
+    const double inv_dr_sq = 1 / (b.dr * b.dr);
+    const int nc = b.n_cell, ip = mg.i_phi, ioff = (b.ix[0] - 1) * nc;
+    for (int j = 1; j <= nc; ++j)
+      for (int i = 1; i <= nc; ++i) {
+        const double r1 = (i + ioff - 1) / (i + ioff - 0.5), r2 = (i + ioff) / (i + ioff - 0.5);
+        b.at(i, j, i_out) = (r1 * b.at(i - 1, j, ip) + r2 * b.at(i + 1, j, ip) + b.at(i, j - 1, ip) +
+                             b.at(i, j + 1, ip) - 4 * b.at(i, j, ip)) *
+                            inv_dr_sq;
+      }
+  }
+}
+template <int D> void box_clpld(Box<D>& b, int i_out, const MG& mg) {
+  if constexpr (D == 2) {
+    const double inv_dr_sq = 1 / (b.dr * b.dr);
+    const int nc = b.n_cell, ip = mg.i_phi, ie = mg.i_eps, ioff = (b.ix[0] - 1) * nc;
+    for (int j = 1; j <= nc; ++j)
+      for (int i = 1; i <= nc; ++i) {
+        const double rfac[4] = {(i + ioff - 1) / (i + ioff - 0.5), (i + ioff) / (i + ioff - 0.5), 1, 1};
+        double u[4], a[4];
+        const double u0 = b.at(i, j, ip), a0 = b.at(i, j, ie);
+        nb_vals<D>(b, ip, i, j, 0, u);
+        nb_vals<D>(b, ie, i, j, 0, a);
+        double s = 0.0;
+        for (int n = 0; n < 4; ++n) s = s + rfac[n] * a0 * a[n] / (a0 + a[n]) * (u[n] - u0);
+        b.at(i, j, i_out) = inv_dr_sq * 2 * s;
+      }
+  }
+}
+template <int D> void box_gsrb_clpld(Box<D>& b, int redblack_cntr, const MG& mg) {
+  if constexpr (D == 2) {
+    const double dx2 = b.dr * b.dr;
+    const int nc = b.n_cell, ip = mg.i_phi, ie = mg.i_eps, ir = mg.i_rhs, ioff = (b.ix[0] - 1) * nc;
+    for (int j = 1; j <= nc; ++j) {
+      const int i0 = 2 - ((redblack_cntr ^ j) & 1);
+      for (int i = i0; i <= nc; i += 2) {
+        const double rfac[4] = {(i + ioff - 1) / (i + ioff - 0.5), (i + ioff) / (i + ioff - 0.5), 1, 1};
+        double u[4], a[4], c[4];
+        const double a0 = b.at(i, j, ie);
+        nb_vals<D>(b, ip, i, j, 0, u);
+        nb_vals<D>(b, ie, i, j, 0, a);
+        for (int n = 0; n < 4; ++n) c[n] = 2 * a0 * a[n] / (a0 + a[n]);
+        double s1 = 0.0, s2 = 0.0;
+        for (int n = 0; n < 4; ++n) s1 = s1 + c[n] * rfac[n] * u[n];
+        for (int n = 0; n < 4; ++n) s2 = s2 + c[n] * rfac[n];
+        b.at(i, j, ip) = (s1 - dx2 * b.at(i, j, ir)) / s2;
+      }
+    }
+  }
+}
+
+// lsf_dist_val, mg:993-1019: distance (0..1) to a neighbour and the value
+// there, or at the interface between when the level set changes sign.
+// a and b hold (level set, value, boundary value).
+inline void lsf_dist_val(const double* a, const double* b, double& dist, double& val) {
+  const double lsf_a = a[0], lsf_b = b[0];
+  if (lsf_a * lsf_b < 0) {
+    dist = lsf_a / (lsf_a - lsf_b);
+    val = a[2] * (1 - dist) + b[2] * dist;
+  } else {
+    dist = 1;
+    val = b[1];
+  }
+}
+template <int D> void lsf_triple(Box<D>& b, const MG& mg, int i, int j, int k, double* v) {
+  const int iv[3] = {mg.i_lsf, mg.i_phi, mg.i_bval};
+  for (int n = 0; n < 3; ++n) v[n] = D == 2 ? b.at(i, j, iv[n]) : b.at(i, j, k, iv[n]);
+}
+// The 2D neighbours' distances and values (i-1, i+1, j-1, j+1[, k-1, k+1]).
+template <int D> void lsf_stencil(Box<D>& b, const MG& mg, int i, int j, int k, double* dd, double* val) {
+  double va[3], vb[3];
+  lsf_triple<D>(b, mg, i, j, k, va);
+  const int di[6] = {-1, 1, 0, 0, 0, 0}, dj[6] = {0, 0, -1, 1, 0, 0}, dk[6] = {0, 0, 0, 0, -1, 1};
+  for (int n = 0; n < 2 * D; ++n) {
+    lsf_triple<D>(b, mg, i + di[n], j + dj[n], k + dk[n], vb);
+    lsf_dist_val(va, vb, dd[n], val[n]);
+  }
+}
+
+// mg$D_box_gsrb_lpllsf, mg:1102-1181
+template <int D> void box_gsrb_lpllsf(Box<D>& b, int redblack_cntr, const MG& mg) {
+  const double dx2 = b.dr * b.dr;
+  const int nc = b.n_cell, ip = mg.i_phi, ir = mg.i_rhs;
+  const int kmax = D == 3 ? nc : 1;
+  for (int k = 1; k <= kmax; ++k)
+    for (int j = 1; j <= nc; ++j) {
+      const int i0 = 2 - ((redblack_cntr ^ (D == 3 ? k + j : j)) & 1);
+      for (int i = i0; i <= nc; i += 2) {
+        double dd[6], val[6];
+        lsf_stencil<D>(b, mg, i, j, k, dd, val);
+        if constexpr (D == 2) {
+          double prod = 1;
+          for (int n = 0; n < 4; ++n) prod = prod * dd[n];
+          b.at(i, j, ip) = 1 / (dd[0] * dd[1] + dd[2] * dd[3]) *
+                           ((dd[1] * val[0] + dd[0] * val[1]) * dd[2] * dd[3] / (dd[0] + dd[1]) +
+                            (dd[3] * val[2] + dd[2] * val[3]) * dd[0] * dd[1] / (dd[2] + dd[3]) -
+                            0.5 * prod * dx2 * b.at(i, j, ir));
+        } else {
+          b.at(i, j, k, ip) =
+              1 / (1 / (dd[0] * dd[1]) + 1 / (dd[2] * dd[3]) + 1 / (dd[4] * dd[5])) *
+              ((dd[1] * val[0] + dd[0] * val[1]) / ((dd[0] + dd[1]) * dd[0] * dd[1]) +
+               (dd[3] * val[2] + dd[2] * val[3]) / ((dd[2] + dd[3]) * dd[2] * dd[3]) +
+               (dd[5] * val[4] + dd[4] * val[5]) / ((dd[4] + dd[5]) * dd[4] * dd[5]) - 0.5 * dx2 * b.at(i, j, k, ir));
+        }
+      }
+    }
+}
+
+// mg$D_box_lpllsf, mg:1184-1253
+template <int D> void box_lpllsf(Box<D>& b, int i_out, const MG& mg) {
+  const double inv_dr_sq = 1 / (b.dr * b.dr);
+  const int nc = b.n_cell, ip = mg.i_phi;
+  const int kmax = D == 3 ? nc : 1;
+  for (int k = 1; k <= kmax; ++k)
+    for (int j = 1; j <= nc; ++j)
+      for (int i = 1; i <= nc; ++i) {
+        double dd[6], val[6];
+        lsf_stencil<D>(b, mg, i, j, k, dd, val);
+        const double f0 = D == 2 ? b.at(i, j, ip) : b.at(i, j, k, ip);
+        double s = (dd[1] * val[0] + dd[0] * val[1] - (dd[0] + dd[1]) * f0) / ((dd[0] + dd[1]) * dd[0] * dd[1]) +
+                   (dd[3] * val[2] + dd[2] * val[3] - (dd[2] + dd[3]) * f0) / ((dd[2] + dd[3]) * dd[2] * dd[3]);
+        if constexpr (D == 3)
+          s = s + (dd[5] * val[4] + dd[4] * val[5] - (dd[4] + dd[5]) * f0) / ((dd[4] + dd[5]) * dd[4] * dd[5]);
+        (D == 2 ? b.at(i, j, i_out) : b.at(i, j, k, i_out)) = 2 * inv_dr_sq * s;
+      }
+}
+
+// mg$D_box_corr_lpllsf, mg:1021-1099
+template <int D> void box_corr_lpllsf(Box<D>& p, Box<D>& c, const MG& mg) {
+  const int nc = c.n_cell, ip = mg.i_phi, icr = mg.i_tmp, il = mg.i_lsf;
+  int off[D];
+  child_offset(c, off);
+  const int kmax = D == 3 ? nc : 1;
+  for (int k = 1; k <= kmax; ++k) {
+    const int k_c1 = D == 3 ? off[D - 1] + ((k + 1) >> 1) : 0, k_c2 = k_c1 + 1 - 2 * (k & 1);
+    for (int j = 1; j <= nc; ++j) {
+      const int j_c1 = off[1] + ((j + 1) >> 1), j_c2 = j_c1 + 1 - 2 * (j & 1);
+      for (int i = 1; i <= nc; ++i) {
+        const int i_c1 = off[0] + ((i + 1) >> 1), i_c2 = i_c1 + 1 - 2 * (i & 1);
+        auto P = [&](int a, int b, int e, int iv) { return D == 2 ? p.at(a, b, iv) : p.at(a, b, e, iv); };
+        double va[3], vb[3], dist[4], val[4];
+        va[0] = D == 2 ? c.at(i, j, il) : c.at(i, j, k, il);
+        va[1] = D == 2 ? c.at(i, j, icr) : c.at(i, j, k, icr);
+        va[2] = 0.0;
+        vb[2] = 0.0;
+        const int pts[4][3] = {{i_c1, j_c1, k_c1}, {i_c2, j_c1, k_c1}, {i_c1, j_c2, k_c1}, {i_c1, j_c1, k_c2}};
+        for (int n = 0; n <= D; ++n) {
+          vb[0] = P(pts[n][0], pts[n][1], pts[n][2], il);
+          vb[1] = P(pts[n][0], pts[n][1], pts[n][2], icr);
+          lsf_dist_val(va, vb, dist[n], val[n]);
+        }
+        double cw[4];
+        if constexpr (D == 2) {
+          cw[0] = 2 * dist[1] * dist[2];
+          cw[1] = dist[0] * dist[2];
+          cw[2] = dist[0] * dist[1];
+        } else {
+          cw[0] = dist[1] * dist[2] * dist[3];
+          cw[1] = dist[0] * dist[2] * dist[3];
+          cw[2] = dist[0] * dist[1] * dist[3];
+          cw[3] = dist[0] * dist[1] * dist[2];
+        }
+        double s1 = 0.0, s2 = 0.0;
+        for (int n = 0; n <= D; ++n) s1 = s1 + cw[n] * val[n];
+        for (int n = 0; n <= D; ++n) s2 = s2 + cw[n];
+        double& o = D == 2 ? c.at(i, j, ip) : c.at(i, j, k, ip);
+        o = o + s1 / s2;
+      }
+    }
+  }
+}
+
+// mg$D_box_rstr_lpllsf, mg:1256-1320: children on the parent's side of the
+// interface only; 1 / n_ch is an integer division in the reference.
+template <int D> void box_rstr_lpllsf(Box<D>& c, Box<D>& p, int iv, const MG& mg) {
+  const int hnc = c.n_cell >> 1, il = mg.i_lsf, nch = 1 << D;
+  int off[D];
+  child_offset(c, off);
+  const int kmax = D == 3 ? hnc : 1;
+  for (int k = 1; k <= kmax; ++k)
+    for (int j = 1; j <= hnc; ++j)
+      for (int i = 1; i <= hnc; ++i) {
+        const int i_c = off[0] + i, j_c = off[1] + j, k_c = D == 3 ? off[D - 1] + k : 0;
+        const int i_f = 2 * i - 1, j_f = 2 * j - 1, k_f = 2 * k - 1;
+        const double lp = D == 2 ? p.at(i_c, j_c, il) : p.at(i_c, j_c, k_c, il);
+        int n_ch = 0;
+        double sm = 0.0, sa = 0.0;
+        for (int kk = 0; kk < (D == 3 ? 2 : 1); ++kk)
+          for (int jj = 0; jj < 2; ++jj)
+            for (int ii = 0; ii < 2; ++ii) {
+              const double lc = D == 2 ? c.at(i_f + ii, j_f + jj, il) : c.at(i_f + ii, j_f + jj, k_f + kk, il);
+              const double v = D == 2 ? c.at(i_f + ii, j_f + jj, iv) : c.at(i_f + ii, j_f + jj, k_f + kk, iv);
+              sa = sa + v;
+              if (lp * lc > 0) {
+                ++n_ch;
+                sm = sm + v;
+              }
+            }
+        double& o = D == 2 ? p.at(i_c, j_c, iv) : p.at(i_c, j_c, k_c, iv);
+        if (n_ch < nch && n_ch > 0)
+          o = (double)(1 / n_ch) * sm;
+        else
+          o = (D == 2 ? 0.25 : 0.125) * sa;
+      }
+}
+
+// The operator of a box as the driver calls mg%box_gsrb / box_op / box_corr
+// / box_rstr: the fixed choice, or mg$D_auto_* by the box's tag (mg:562-669;
+// the tag is taken at first use).
+enum { K_LPL = 0, K_LPLD = 1, K_CLPL = 2, K_CLPLD = 3, K_LSF = 4 };
+template <int D> int box_kind(Box<D>& b, const MG& mg) {
+  switch (mg.op) {
+    case OP_LPL: return K_LPL;
+    case OP_LPLD: return K_LPLD;
+    case OP_CLPL: return K_CLPL;
+    case OP_CLPLD: return K_CLPLD;
+    case OP_LPLLSF: return K_LSF;
+  }
   if (b.tag == a5_init_tag) set_box_tag<D>(b, mg);
-  return b.tag != MG_NORMAL_BOX;
+  const bool cyl = D == 2 && b.coord == 1;
+  switch (b.tag) {
+    case MG_NORMAL_BOX: return cyl ? K_CLPL : K_LPL;
+    case MG_LSF_BOX: return K_LSF;
+    default: return cyl ? K_CLPLD : K_LPLD;
+  }
 }
 
 // Interior / full-array helpers, utils:262-352
@@ -1265,23 +1550,40 @@ template <int D> void interior_for(Box<D>& b, int iv_a, int iv_b, int mode) {
 
 // residual_box, mg:545-559
 template <int D> void box_op(Box<D>& b, int i_out, const MG& mg) {
-  if (use_lpld<D>(b, mg))
-    box_lpld<D>(b, i_out, mg);
-  else
-    box_lpl<D>(b, i_out, mg);
+  switch (box_kind<D>(b, mg)) {
+    case K_LPL: box_lpl<D>(b, i_out, mg); break;
+    case K_LPLD: box_lpld<D>(b, i_out, mg); break;
+    case K_CLPL: box_clpl<D>(b, i_out, mg); break;
+    case K_CLPLD: box_clpld<D>(b, i_out, mg); break;
+    default: box_lpllsf<D>(b, i_out, mg); break;
+  }
 }
 template <int D> void box_gsrb(Box<D>& b, int n, const MG& mg) {
-  if (use_lpld<D>(b, mg))
-    box_gsrb_lpld<D>(b, n, mg);
-  else
-    box_gsrb_lpl<D>(b, n, mg);
+  switch (box_kind<D>(b, mg)) {
+    case K_LPL: box_gsrb_lpl<D>(b, n, mg); break;
+    case K_LPLD: box_gsrb_lpld<D>(b, n, mg); break;
+    case K_CLPL: box_gsrb_clpl<D>(b, n, mg); break;
+    case K_CLPLD: box_gsrb_clpld<D>(b, n, mg); break;
+    default: box_gsrb_lpllsf<D>(b, n, mg); break;
+  }
 }
-// mg%box_corr: mg$D_auto_corr (mg:645-669) chooses by the child's tag
+// mg%box_corr: mg$D_auto_corr (mg:645-669) chooses by the child's tag; the
+// cylindrical operators take the Cartesian corrections
 template <int D> void box_corr(Box<D>& p, Box<D>& c, const MG& mg) {
-  if (use_lpld<D>(c, mg))
-    box_corr_lpld<D>(p, c, mg);
+  switch (box_kind<D>(c, mg)) {
+    case K_LPL:
+    case K_CLPL: prolong2_add<D>(p, c, mg.i_tmp, mg.i_phi); break;
+    case K_LSF: box_corr_lpllsf<D>(p, c, mg); break;
+    default: box_corr_lpld<D>(p, c, mg); break;
+  }
+}
+// mg%box_rstr: mg$D_auto_rstr (mg:625-642) by the child's tag, lpllsf's
+// masked average for level-set boxes, a$D_restrict_box otherwise
+template <int D> void box_rstr(Box<D>& c, Box<D>& p, int iv, const MG& mg) {
+  if (box_kind<D>(c, mg) == K_LSF)
+    box_rstr_lpllsf<D>(c, p, iv, mg);
   else
-    prolong2_add<D>(p, c, mg.i_tmp, mg.i_phi);
+    restrict_box<D>(c, p, iv);
 }
 
 template <int D> void residual_box(Box<D>& b, const MG& mg) {
@@ -1350,8 +1652,8 @@ template <int D> void update_coarse(Tree<D>& t, int lvl, const MG& mg) {
     int p_id = b.parent;
     std::vector<double> save(t.boxes[id].var(mg.i_tmp), t.boxes[id].var(mg.i_tmp) + b.nvol());
     residual_box(b, mg);
-    restrict_box(b, t.boxes[p_id], mg.i_tmp);
-    restrict_box(b, t.boxes[p_id], mg.i_phi);
+    box_rstr<D>(b, t.boxes[p_id], mg.i_tmp, mg);
+    box_rstr<D>(b, t.boxes[p_id], mg.i_phi, mg);
     // restore the interior of tmp (the ghost cells of tmp are not touched above)
     std::copy(save.begin(), save.end(), b.var(mg.i_tmp));
   }
@@ -1374,8 +1676,8 @@ template <int D> void set_coarse_phi_rhs(Tree<D>& t, int lvl, const MG& mg) {
   for (int i = 0; i < (int)ids.size(); ++i) {
     Box<D>& b = t.boxes[ids[i]];
     residual_box(b, mg);
-    restrict_box(b, t.boxes[b.parent], mg.i_tmp);
-    restrict_box(b, t.boxes[b.parent], mg.i_phi);
+    box_rstr<D>(b, t.boxes[b.parent], mg.i_tmp, mg);
+    box_rstr<D>(b, t.boxes[b.parent], mg.i_phi, mg);
   }
   fill_gc_phi(t, t.L(lvl - 1).ids, mg);
   const std::vector<int>& par = t.L(lvl - 1).parents;
@@ -1396,7 +1698,7 @@ template <int D> void init_phi_rhs(Tree<D>& t, const MG& mg) {
     for (int i = 0; i < (int)ids.size(); ++i) {
       Box<D>& b = t.boxes[ids[i]];
       box_clear_cc(b, mg.i_phi);
-      restrict_box(b, t.boxes[b.parent], mg.i_rhs);
+      box_rstr<D>(b, t.boxes[b.parent], mg.i_rhs, mg);
     }
   }
 }
@@ -1603,11 +1905,26 @@ template <int D> void prolong_from_level(Tree<D>& t, int lvl, int iv, int ivc, i
     }
 }
 
-// a$D_restrict_box with iv_to (restrict:67-132, Cartesian)
+// a$D_restrict_box with iv_to (restrict:67-132)
 template <int D> void restrict_box_to(Box<D>& c, Box<D>& p, int iv, int ivt) {
   const int hnc = c.n_cell >> 1;
   int off[D];
   child_offset(c, off);
+  if (D == 2 && p.coord == 1) {  // cylindrical branch, restrict:90-103
+    for (int j = 1; j <= hnc; ++j)
+      for (int i = 1; i <= hnc; ++i) {
+        const int i_f = 2 * i - 1, j_f = 2 * j - 1;
+        double w1, w2;
+        cyl_child_weights(p.r_min[0], p.dr, i, w1, w2);
+        double s1 = 0.0, s2 = 0.0;
+        s1 = s1 + c.at(i_f, j_f, 0, iv);
+        s1 = s1 + c.at(i_f, j_f + 1, 0, iv);
+        s2 = s2 + c.at(i_f + 1, j_f, 0, iv);
+        s2 = s2 + c.at(i_f + 1, j_f + 1, 0, iv);
+        p.at(off[0] + i, off[1] + j, 0, ivt) = 0.25 * (w1 * s1 + w2 * s2);
+      }
+    return;
+  }
   const int kmax = D == 3 ? hnc : 1;
   for (int k = 1; k <= kmax; ++k)
     for (int j = 1; j <= hnc; ++j)
@@ -1830,8 +2147,14 @@ template <int D> void flux_from_children(Tree<D>& t, int id, int nb, const std::
         for (int n = 1; n <= nch; ++n) {
           if (d == 0)
             o.f_at(f, 0, i_nb, ioff[1] + n, 1) = 0.5 * (c.f_at(f, 0, i, 2 * n - 1, 1) + c.f_at(f, 0, i, 2 * n, 1));
-          else
+          else if (o.coord == 1) {  // cylindrical: weighted average (core:881-895)
+            double w1, w2;
+            cyl_child_weights(o.r_min[0], o.dr, ioff[0] + n, w1, w2);
+            o.f_at(f, 1, ioff[0] + n, i_nb, 1) =
+                0.5 * (w1 * c.f_at(f, 1, 2 * n - 1, i, 1) + w2 * c.f_at(f, 1, 2 * n, i, 1));
+          } else {
             o.f_at(f, 1, ioff[0] + n, i_nb, 1) = 0.5 * (c.f_at(f, 1, 2 * n - 1, i, 1) + c.f_at(f, 1, 2 * n, i, 1));
+          }
         }
       } else {
         for (int m = 1; m <= nch; ++m)
@@ -1986,7 +2309,8 @@ int write_vtk(Tree<D>& t, const char* path, int n_cycle, double time, const std:
   dat("Cells", false);
   dat("CellData", true);
   std::vector<std::string> names(cc_names);
-  const char* sfx[3] = {"_x", "_y", "_z"};
+  const bool cyl = D == 2 && t.coord == 1;  // io:174-176
+  const char* sfx[3] = {cyl ? "_r" : "_x", cyl ? "_z" : "_y", "_z"};
   for (int v = 0; v < n_fc; ++v)
     for (int d = 0; d < D; ++d) names.push_back(fc_names[(size_t)v] + sfx[d]);
   for (int c = 0; c < ncol; ++c) {
@@ -2473,18 +2797,38 @@ int orc_write_vtk(OrcHandle* h, const char* path, int n_cycle, double time, int 
 }
 
 
-// mg%box_op / box_gsrb / box_corr and mg%i_eps; box tags are taken again at
-// their next use (the reference's a5_init_tag state).
-void orc_mg_set_operator(OrcHandle* h, int op, int i_eps) {
+// mg%box_op / box_gsrb / box_corr / box_rstr with mg%i_eps, mg%i_lsf and
+// mg%i_bval; box tags are taken again at their next use (the reference's
+// a5_init_tag state). Returns -1 when a box would take two tags (where
+// mg$D_set_box_tag stops).
+int orc_mg_set_operator(OrcHandle* h, int op, int i_eps, int i_lsf, int i_bval) {
   h->mg.op = op;
   h->mg.i_eps = i_eps;
-  auto reset = [](auto& t) {
-    for (size_t id = 1; id < t.boxes.size(); ++id) t.boxes[id].tag = a5_init_tag;
+  h->mg.i_lsf = i_lsf;
+  h->mg.i_bval = i_bval;
+  int ok = 1;
+  auto reset = [&](auto& t) {
+    for (size_t id = 1; id < t.boxes.size(); ++id) {
+      t.boxes[id].tag = a5_init_tag;
+      if (op == OP_AUTO && t.boxes[id].in_use && !set_box_tag(t.boxes[id], h->mg)) ok = 0;
+      t.boxes[id].tag = a5_init_tag;
+    }
   };
   if (h->dim == 2)
     reset(TT<2>(h));
   else
     reset(TT<3>(h));
+  return ok ? 0 : -1;
+}
+
+// a$D_init's coord argument (core:58-70, 102, 198): a5_cyl for a 2-D tree,
+// set on the tree and its boxes.
+int orc_set_coord(OrcHandle* h, int coord) {
+  if (h->dim != 2 && coord == 1) return -1;
+  auto& t = TT<2>(h);
+  t.coord = coord;
+  for (size_t id = 1; id < t.boxes.size(); ++id) t.boxes[id].coord = coord;
+  return 0;
 }
 
 }  // extern "C"

@@ -76,7 +76,10 @@ def lib():
         L.orc_ix_to_ichild.argtypes = [ctypes.c_int, ip]
         L.orc_set_threads.argtypes = [ctypes.c_int]
         L.orc_add_vars.argtypes = [P, ctypes.c_int, ctypes.c_int]
-        L.orc_mg_set_operator.argtypes = [P, ctypes.c_int, ctypes.c_int]
+        L.orc_mg_set_operator.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+        L.orc_mg_set_operator.restype = ctypes.c_int
+        L.orc_set_coord.argtypes = [P, ctypes.c_int]
+        L.orc_set_coord.restype = ctypes.c_int
         L.orc_fc_count.argtypes = [P]
         L.orc_fc_count.restype = ctypes.c_longlong
         L.orc_get_fc.argtypes = [P, ctypes.c_int, dp]
@@ -254,9 +257,16 @@ class OracleTree:
     def leaf_mean(self, iv):
         return lib().orc_leaf_mean(self.h, iv)
 
-    def set_operator(self, op, i_eps=-1):
-        """mg%box_op / box_gsrb / box_corr: 0 lpl, 1 lpld, 2 auto (i_eps = eps)."""
-        lib().orc_mg_set_operator(self.h, op, i_eps)
+    def set_operator(self, op, i_eps=-1, i_lsf=-1, i_bval=-1):
+        """mg%box_op / box_gsrb / box_corr / box_rstr: 0 lpl, 1 lpld, 2 auto,
+        3 clpl, 4 clpld, 5 lpllsf, with mg%i_eps, mg%i_lsf, mg%i_bval.
+        Returns False when a box would take two auto tags."""
+        return lib().orc_mg_set_operator(self.h, op, i_eps, i_lsf, i_bval) == 0
+
+    def set_coord(self, coord):
+        """a$D_init's coord: 0 Cartesian, 1 cylindrical (2-D; before refinement)."""
+        if lib().orc_set_coord(self.h, coord) != 0:
+            raise ValueError("cylindrical coordinates need a 2-D tree")
 
     # general ghost cells, transfers and output ---------------------------------
     def add_vars(self, n_cc=0, n_fc=0):

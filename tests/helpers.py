@@ -9,6 +9,8 @@ from afivo_gb300 import workloads as W
 def oracle_tree(spec, max_passes=100):
     t = O.OracleTree(spec["dim"], spec["n_cell"], spec["dr"], spec["ix"], spec["nb"],
                      coarsen_to=spec["coarsen_to"])
+    if spec.get("coord", 0):
+        t.set_coord(spec["coord"])
     if "target_cells" in spec:
         for _ in range(max_passes):
             if leaf_boxes(t) * spec["n_cell"] ** spec["dim"] >= spec["target_cells"]:
@@ -159,3 +161,65 @@ def interior_to_ghosted(flat_int, t, n_cell, dim):
         off += n * nc ** dim
         parts.append(g.ravel())
     return np.concatenate(parts)
+
+
+def centres(t, lvl, nc, dim):
+    """Cell-centre coordinates of every box of a level of the oracle tree,
+    ghost cells included: array (boxes, (nc+2)^dim..., dim), x fastest."""
+    b = t.boxes()
+    ids, _, _ = t.level(lvl)
+    g = np.arange(nc + 2) - 0.5
+    out = np.zeros((len(ids),) + (nc + 2,) * dim + (dim,))
+    grids = np.meshgrid(*([g] * dim), indexing="ij")[::-1]
+    for n, i in enumerate(ids):
+        for d in range(dim):
+            out[n, ..., d] = b["r_min"][i - 1][d] + grids[d] * b["dr"][i - 1]
+    return out
+
+
+def fill_from_centres(t, iv, fn, n_cell):
+    """Variable iv of every box (ghost cells included) as fn(centres); returns
+    the concatenation over levels (the library's host layout)."""
+    parts = []
+    for lvl in range(t.min_lvl, t.highest_lvl + 1):
+        nc = t.n_cell_at(lvl, n_cell)
+        v = np.ascontiguousarray(fn(centres(t, lvl, nc, t.dim)), dtype=np.float64)
+        t.set_level(lvl, iv, v)
+        parts.append(v.ravel())
+    return np.concatenate(parts)
+
+
+def cyl_spec(lvl_max=6):
+    """The 2-D Gaussian workload in cylindrical coordinates (x the radius
+    from the axis at 0, y the axis), as examples/poisson_cyl.f90 sets up."""
+    s = W.c1_poisson_2d()
+    s.update(name="poisson2d_cyl_nc8_lvl%d" % lvl_max, coord=1, lvl_max=lvl_max)
+    return s
+
+
+def cyl_bc_table(tree):
+    """poisson_cyl's sides_bc: Neumann 0 on the axis (the low-x faces at
+    r = 0), Dirichlet with smooth values on the other faces."""
+    ids, faces, types, vals = [], [], [], []
+    for i, fc, cen in tree.bc_faces():
+        ids.append(i)
+        faces.append(fc)
+        types.append(-2 if fc == 0 else -1)
+        vals.append(np.zeros(len(cen)) if fc == 0 else 0.1 * np.cos(2.0 * cen[:, 1]) + 0.05 * cen[:, 0])
+    return ids, faces, types, np.concatenate(vals)
+
+
+LSF_CENTRE = (0.45, 0.55, 0.5)
+LSF_RADIUS = 0.23
+
+
+def lsf_sphere(r):
+    """Level set of a sphere (circle) around LSF_CENTRE: negative inside."""
+    d = r.shape[-1]
+    c = np.asarray(LSF_CENTRE[:d])
+    return np.sqrt(((r - c) ** 2).sum(-1)) - LSF_RADIUS
+
+
+def bval_field(r):
+    """Boundary value at the interface, position dependent: 1 + 0.5 x."""
+    return 1.0 + 0.5 * r[..., 0]

@@ -2,7 +2,7 @@
 the oracle's restatement of the reference: a$D_gc_tree with every built-in
 refinement-boundary and boundary method, a$D_prolong{0,1,2}_from with and
 without add, a$D_restrict_tree, a$D_gc2_box, a$D_consistent_fluxes and
-a$D_write_vtk. Inputs are seeded random values in an extra cell variable (and
+a$D_write_vtk, in Cartesian and cylindrical trees. Inputs are seeded random values in an extra cell variable (and
 face variables) on every box, ghost cells included, on both sides; outputs
 must be bit-identical (the VTK file byte for byte)."""
 import os
@@ -11,7 +11,7 @@ import numpy as np
 import pytest
 
 import oracle as O
-from helpers import oracle_tree, oracle_var
+from helpers import cyl_spec, oracle_tree, oracle_var
 from afivo_gb300 import workloads as W
 
 pytestmark = pytest.mark.gpu
@@ -20,6 +20,7 @@ CASES = {
     "c1_2d": lambda: [W.c1_poisson_2d()],
     "adaptive_3d": lambda: [W.c2_poisson_3d(thr=3e-3, lvl_max=5)],
     "forest_2d": lambda: W.c4_random_2d(3, small=True),
+    "cyl_2d": lambda: [cyl_spec(lvl_max=6)],  # weighted restriction and fluxes, r/z names
 }
 
 
