@@ -665,8 +665,6 @@ int Forest::set_operator(int new_op, int new_i_eps, int new_i_lsf, int new_i_bva
     return err = "lsf and bval must be extra cell variables (afv_forest_add_vars)", AFV_ERR_INVALID;
   if (new_op == AFV_OP_AUTO && new_i_eps >= 0 && !is_var(new_i_eps))
     return err = "eps must be an extra cell variable (afv_forest_add_vars)", AFV_ERR_INVALID;
-  if (new_op == AFV_OP_AUTO && new_i_eps < 0 && new_i_lsf < 0)
-    return err = "auto needs eps or a level set", AFV_ERR_INVALID;
   drop_graphs();
   if (!d_tags) {
     if (cudaMallocAsync((void**)&d_tags, sizeof(int) * std::max(1, plan.n_slots), stream) != cudaSuccess)

@@ -252,7 +252,8 @@ int afv_mg_set_operator(afv_forest* f, int op, int i_eps);
 /* As afv_mg_set_operator, with mg%i_lsf and mg%i_bval (both >= 3 or both
  * -1, mg$D_init_mg's check, src/m_aX_mg.f90:136-137): the level set and the
  * boundary value at the interface, extra cell variables with filled ghost
- * cells. AFV_OP_LPLLSF needs both; AFV_OP_AUTO needs eps or the level set. */
+ * cells. AFV_OP_LPLLSF needs both; AFV_OP_AUTO without eps or a level set
+ * tags every box normal (examples/poisson_cyl.f90). */
 int afv_mg_set_operator_lsf(afv_forest* f, int op, int i_eps, int i_lsf, int i_bval);
 /* mg$D_fas_vcycle, src/m_aX_mg.f90:208-255 (all trees of the forest). */
 int afv_mg_fas_vcycle(afv_forest* f, const afv_mg_opts* mg, int highest_lvl, int set_residual);

@@ -24,11 +24,6 @@ def _eps_jump(r):
     return np.where(r[..., 0] > 0.53, 100.0, 1.0)
 
 
-def _eps_far(r):
-    """eps = 2 beyond x = 0.9, away from the level set's interface."""
-    return np.where(r[..., 0] > 0.9, 2.0, 1.0)
-
-
 def _pair(afv, spec, op, eps=None, lsf=False, cyl_bc=False):
     nc = spec["n_cell"]
     ot = oracle_tree(spec)
@@ -36,7 +31,7 @@ def _pair(afv, spec, op, eps=None, lsf=False, cyl_bc=False):
     ot.mg_init()
     ot.add_vars(3, 0)
     tree = W.build_tree(spec)
-    f = afv.Forest([tree])
+    f = afv.Forest([tree], mixed=True)
     f.add_vars(3, 0)
     i_eps = i_lsf = i_bval = -1
     if eps is not None:
@@ -118,9 +113,9 @@ def _lsf_spec(dim):
 
 
 # (operator, eps) with the level set: lpllsf on every box, auto with the
-# level set only (normal and lsf boxes), auto with eps far from the
-# interface as well (normal, lsf and eps boxes)
-LSF = {"lpllsf": (5, None), "auto_lsf": (2, None), "auto_lsf_eps": (2, _eps_far)}
+# level set (normal and lsf boxes). A varying eps cannot join a level set
+# under auto: the coarsest box holds both and mg$D_set_box_tag stops.
+LSF = {"lpllsf": (5, None), "auto_lsf": (2, None)}
 
 
 @pytest.mark.parametrize("dim", [2, 3])
@@ -138,7 +133,7 @@ def test_level_set_cycles_match_oracle(gpu, dim, case):
 @pytest.mark.parametrize("dim", [2, 3])
 def test_level_set_fmg_and_solve(gpu, dim):
     spec = _lsf_spec(dim)
-    ot, f = _pair(gpu, spec, 2, eps=_eps_far, lsf=True)
+    ot, f = _pair(gpu, spec, 2, lsf=True)
     for i in range(2):
         ot.fmg(set_residual=True, have_guess=i > 0)
         f.fmg(set_residual=True, have_guess=i > 0)
@@ -152,7 +147,7 @@ def test_level_set_fmg_and_solve(gpu, dim):
 
 def test_single_operators_level_set_2d(gpu):
     spec = _lsf_spec(2)
-    ot, f = _pair(gpu, spec, 2, eps=_eps_far, lsf=True)
+    ot, f = _pair(gpu, spec, 2, lsf=True)
     ot.vcycle()
     f.vcycle()
     top = ot.highest_lvl
