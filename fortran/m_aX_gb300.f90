@@ -14,14 +14,19 @@
 !> Lean mode (gb$D_lean = .true.): the device keeps phi, rhs and tmp between
 !> calls. A call uploads (and samples sides_bc) only when the refinement
 !> changed or the caller bumped gb$D_data_gen since the last upload (after
-!> changing phi, rhs, tmp or the boundary hook on the host), and downloads
+!> changing phi, rhs, tmp, eps, the level set, the boundary or operator hooks
+!> on the host), and downloads
 !> phi only, plus tmp when set_residual is true. The host's rhs and tmp are
 !> then out of date where the cycle changed them (the coarse levels' rhs,
 !> tmp without set_residual); gb$D_sync downloads all three.
 !>
-!> Only the constant-coefficient Laplacian is on the device: mg%box_op,
-!> box_gsrb, box_corr, box_rstr and sides_rb must be the defaults that
-!> mg$D_init_mg sets, else the call stops.
+!> The operator hooks may be any of the reference's built-in sets: the
+!> Laplacian (the defaults of mg$D_init_mg), mg$D_box_*_lpld,
+!> mg2_box_*_clpl(d), mg$D_box_*_lpllsf, or mg$D_auto_* (with
+!> mg$D_auto_rstr, or mg$D_box_rstr_lpl when there is no level set), with
+!> mg%i_eps, mg%i_lsf and mg%i_bval uploaded beside phi; cylindrical trees
+!> (coord_t = a5_cyl) are mirrored as such. Other hooks, and a sides_rb other
+!> than mg$D_sides_rb, stop the call.
 !>
 !> This file is a template like the reference's m_aX_*.f90: the Makefile
 !> beside it expands $D to 2 and 3 (sed, then cpp).
@@ -30,7 +35,13 @@ module m_a$D_gb300
   use m_afivo_gb300
   use m_a$D_t
   use m_a$D_mg, only: mg$D_t, mg$D_box_lpl, mg$D_box_gsrb_lpl, &
-       mg$D_box_corr_lpl, mg$D_box_rstr_lpl, mg$D_sides_rb
+       mg$D_box_corr_lpl, mg$D_box_rstr_lpl, mg$D_sides_rb, &
+       mg$D_box_lpld, mg$D_box_gsrb_lpld, mg$D_box_corr_lpld, &
+       mg$D_box_lpllsf, mg$D_box_gsrb_lpllsf, mg$D_box_corr_lpllsf, mg$D_box_rstr_lpllsf, &
+#if $D == 2
+       mg$D_box_clpl, mg$D_box_gsrb_clpl, mg$D_box_clpld, mg$D_box_gsrb_clpld, &
+#endif
+       mg$D_auto_op, mg$D_auto_gsrb, mg$D_auto_corr, mg$D_auto_rstr
   implicit none
   private
 
@@ -43,6 +54,8 @@ module m_a$D_gb300
      integer(c_long_long) :: gen = -1
      !> reference ids of the mirror's boxes in the host exchange order
      integer, allocatable :: order(:)
+     !> extra cell variables added to the forest (eps, lsf, bval)
+     logical              :: has_extra = .false.
   end type gb_mirror_t
 
   type(gb_mirror_t), save      :: mirror
@@ -52,7 +65,8 @@ module m_a$D_gb300
   integer, public :: gb$D_device = 0
   !> Keep the state on the device between calls (see above)
   logical, public :: gb$D_lean = .false.
-  !> Bumped by the caller whenever it changes phi, rhs, tmp or sides_bc
+  !> Bumped by the caller whenever it changes phi, rhs, tmp, sides_bc, the
+  !> operator hooks or their variables (eps, lsf, bval)
   integer(c_long_long), public :: gb$D_data_gen = 0
 
   public :: mg$D_fas_vcycle
@@ -106,6 +120,7 @@ contains
     mirror%tree = c_null_ptr
     mirror%stamp = -1
     mirror%gen = -1
+    mirror%has_extra = .false.
     if (allocated(mirror%order)) deallocate(mirror%order)
   end subroutine gb$D_release
 
@@ -115,13 +130,12 @@ contains
     type(afv_mg_opts), intent(out)     :: opts
     integer(c_long_long)               :: stamp(4)
 
+    integer(c_int)                     :: op
+
     if (.not. mg%initialized) stop "afivo_gb300: call mg$D_init_mg first"
-    if (.not. (associated(mg%box_op, mg$D_box_lpl) .and. &
-         associated(mg%box_gsrb, mg$D_box_gsrb_lpl) .and. &
-         associated(mg%box_corr, mg$D_box_corr_lpl) .and. &
-         associated(mg%box_rstr, mg$D_box_rstr_lpl) .and. &
-         associated(mg%sides_rb, mg$D_sides_rb))) &
-         stop "afivo_gb300: only the default Laplacian operators run on the device"
+    if (.not. associated(mg%sides_rb, mg$D_sides_rb)) &
+         stop "afivo_gb300: only mg$D_sides_rb runs on the device"
+    op = operator_of(mg)
 
     call tree_stamp(tree, stamp)
     if (any(stamp /= mirror%stamp)) then
@@ -133,12 +147,59 @@ contains
        call upload(tree, mg%i_phi, AFV_PHI)
        call upload(tree, mg%i_rhs, AFV_RHS)
        call upload(tree, mg%i_tmp, AFV_TMP)
+       if (op /= AFV_OP_LPL .and. .not. mirror%has_extra) then
+          call afv_check(afv_forest_add_vars(mirror%forest, 3_c_int, 0_c_int), "afv_forest_add_vars")
+          mirror%has_extra = .true.
+       end if
+       ! eps, lsf and bval as the forest's cell variables 3, 4 and 5; the
+       ! auto tags are taken from them by afv_mg_set_operator_lsf
+       if (mg%i_eps > 0 .and. op /= AFV_OP_LPL) call upload(tree, mg%i_eps, 3_c_int)
+       if (mg%i_lsf > 0 .and. op /= AFV_OP_LPL) then
+          call upload(tree, mg%i_lsf, 4_c_int)
+          call upload(tree, mg%i_bval, 5_c_int)
+       end if
+       call afv_check(afv_mg_set_operator_lsf(mirror%forest, op, &
+            merge(3_c_int, -1_c_int, mg%i_eps > 0 .and. op /= AFV_OP_LPL), &
+            merge(4_c_int, -1_c_int, mg%i_lsf > 0 .and. op /= AFV_OP_LPL), &
+            merge(5_c_int, -1_c_int, mg%i_lsf > 0 .and. op /= AFV_OP_LPL)), "afv_mg_set_operator_lsf")
        mirror%gen = gb$D_data_gen
     end if
     opts%n_cycle_down = mg%n_cycle_down
     opts%n_cycle_up = mg%n_cycle_up
     opts%n_cycle_base = mg%n_cycle_base
   end subroutine prepare
+
+  !> The library's operator for the caller's hooks (mg%box_op, box_gsrb,
+  !> box_corr, box_rstr), or a stop when the set is not a built-in one
+  integer(c_int) function operator_of(mg) result(op)
+    type(mg$D_t), intent(in) :: mg
+    logical                  :: rstr_lpl
+    rstr_lpl = associated(mg%box_rstr, mg$D_box_rstr_lpl)
+    op = -1
+    if (associated(mg%box_op, mg$D_box_lpl) .and. associated(mg%box_gsrb, mg$D_box_gsrb_lpl) .and. &
+         associated(mg%box_corr, mg$D_box_corr_lpl) .and. rstr_lpl) then
+       op = AFV_OP_LPL
+    else if (associated(mg%box_op, mg$D_box_lpld) .and. associated(mg%box_gsrb, mg$D_box_gsrb_lpld) .and. &
+         associated(mg%box_corr, mg$D_box_corr_lpld) .and. rstr_lpl) then
+       op = AFV_OP_LPLD
+    else if (associated(mg%box_op, mg$D_box_lpllsf) .and. associated(mg%box_gsrb, mg$D_box_gsrb_lpllsf) .and. &
+         associated(mg%box_corr, mg$D_box_corr_lpllsf) .and. associated(mg%box_rstr, mg$D_box_rstr_lpllsf)) then
+       op = AFV_OP_LPLLSF
+    else if (associated(mg%box_op, mg$D_auto_op) .and. associated(mg%box_gsrb, mg$D_auto_gsrb) .and. &
+         associated(mg%box_corr, mg$D_auto_corr) .and. (associated(mg%box_rstr, mg$D_auto_rstr) .or. &
+         (rstr_lpl .and. mg%i_lsf < 0))) then
+       op = AFV_OP_AUTO
+#if $D == 2
+    else if (associated(mg%box_op, mg$D_box_clpl) .and. associated(mg%box_gsrb, mg$D_box_gsrb_clpl) .and. &
+         associated(mg%box_corr, mg$D_box_corr_lpl) .and. rstr_lpl) then
+       op = AFV_OP_CLPL
+    else if (associated(mg%box_op, mg$D_box_clpld) .and. associated(mg%box_gsrb, mg$D_box_gsrb_clpld) .and. &
+         associated(mg%box_corr, mg$D_box_corr_lpld) .and. rstr_lpl) then
+       op = AFV_OP_CLPLD
+#endif
+    end if
+    if (op < 0) stop "afivo_gb300: these operator hooks do not run on the device"
+  end function operator_of
 
   !> What a call hands back: everything, or in lean mode phi (and tmp when
   !> the residual was asked for)
@@ -244,6 +305,8 @@ contains
     call afv_check(afv_tree_create($D, int(tree%n_cell, c_int), real(tree%dr_base, c_double), &
          real(tree%r_base, c_double), int(tree%lvl_limit, c_int), int(coarsen_to, c_int), &
          1024.0_c_double, mirror%tree), "afv_tree_create")
+    if (tree%coord_t == a5_cyl) &
+         call afv_check(afv_tree_set_coord(mirror%tree, AFV_COORD_CYL), "afv_tree_set_coord")
 
     ! Base boxes in the order of the caller's level-1 list; neighbours as
     ! positions in that list, physical boundaries unchanged.

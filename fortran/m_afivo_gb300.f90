@@ -22,6 +22,9 @@ module m_afivo_gb300
   integer(c_int), parameter :: AFV_PHI = 0, AFV_RHS = 1, AFV_TMP = 2
   integer(c_int), parameter :: AFV_BC_DIRICHLET = -1, AFV_BC_NEUMANN = -2
   integer(c_int), parameter :: AFV_PREC_FP64 = 0, AFV_PREC_MIXED = 1
+  integer(c_int), parameter :: AFV_OP_LPL = 0, AFV_OP_LPLD = 1, AFV_OP_AUTO = 2
+  integer(c_int), parameter :: AFV_OP_CLPL = 3, AFV_OP_CLPLD = 4, AFV_OP_LPLLSF = 5
+  integer(c_int), parameter :: AFV_COORD_XYZ = 0, AFV_COORD_CYL = 1
 
   !> What a refinement callback sees of a box (afv_box_view)
   type, bind(C) :: afv_box_view
@@ -59,6 +62,13 @@ module m_afivo_gb300
        type(c_ptr), intent(out)   :: tree
        integer(c_int)             :: rc
      end function afv_tree_create
+
+     function afv_tree_set_coord(tree, coord) bind(C, name="afv_tree_set_coord") result(rc)
+       import :: c_int, c_ptr
+       type(c_ptr), value    :: tree
+       integer(c_int), value :: coord
+       integer(c_int)        :: rc
+     end function afv_tree_set_coord
 
      function afv_tree_set_base(tree, n_boxes, ix_list, nb_list) &
           bind(C, name="afv_tree_set_base") result(rc)
@@ -125,6 +135,21 @@ module m_afivo_gb300
        import :: c_ptr
        type(c_ptr), value :: forest
      end subroutine afv_forest_destroy
+
+     function afv_forest_add_vars(forest, n_cc, n_fc) bind(C, name="afv_forest_add_vars") result(rc)
+       import :: c_int, c_ptr
+       type(c_ptr), value    :: forest
+       integer(c_int), value :: n_cc, n_fc
+       integer(c_int)        :: rc
+     end function afv_forest_add_vars
+
+     function afv_mg_set_operator_lsf(forest, op, i_eps, i_lsf, i_bval) &
+          bind(C, name="afv_mg_set_operator_lsf") result(rc)
+       import :: c_int, c_ptr
+       type(c_ptr), value    :: forest
+       integer(c_int), value :: op, i_eps, i_lsf, i_bval
+       integer(c_int)        :: rc
+     end function afv_mg_set_operator_lsf
 
      function afv_forest_set_var(forest, tree, var, host, interior_only) &
           bind(C, name="afv_forest_set_var") result(rc)
