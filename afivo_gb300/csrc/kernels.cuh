@@ -1726,6 +1726,72 @@ k_sweep_small(Meta m, BoxSet bs, T* __restrict__ phi, const T* __restrict__ rhs,
   }
 }
 
+// ---------------------------------------------------------------------------
+// Half-sweep of a small level with one thread per updated cell and no
+// staging (k_sweep_direct): on a level of a few dozen boxes the staged and
+// pipelined sweeps are bound by their chain of dependent copies, not by
+// bytes. Each thread reads its cell's neighbours straight from global memory;
+// a neighbour across the box face is the ghost value this colour reads, made
+// from the current state exactly as a pulled ghost (ghost_value): it depends
+// on the cell itself (read before it is written, by the same thread) and on
+// cells of the other colour, which no thread writes in this half-sweep. So
+// the values are those of k_sweep_small and the staged sweeps, bit for bit.
+// Without pull the stored ghost cells are read.
+// ---------------------------------------------------------------------------
+template <int D, int NC, class T>
+__global__ void __launch_bounds__(kThreads)
+k_sweep_direct(Meta m, BoxSet bs, T* phi, const T* rhs, int nsw, int pull, int homog) {
+  pdl_trigger();
+  using G = Geo<D, NC>;
+  constexpr int HALF = G::SI / 2;
+  // one item per thread (the launch covers the level); the slot's tree and
+  // descriptor never change, so they are read before the previous kernel ends
+  const long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const bool mine = x < (long long)bs.n * HALF;
+  const int b = mine ? (int)(x / HALF) : 0, q = mine ? (int)(x % HALF) : 0;
+  const int s = mine ? box_at(bs, b) : 0;
+  const int tr = mine ? m.tree[s] : 0;
+  SlotDesc d;
+  if (mine) d = m.desc[s];
+  pdl_wait();
+  if (!mine || !m.active[tr]) return;
+  const int p = q % (NC / 2);
+  int i, j, k;
+  if constexpr (D == 2) {
+    j = q / (NC / 2) + 1;
+    k = 0;
+    i = 2 * p + 1 + ((1 + j + nsw) & 1);
+  } else {
+    j = (q / (NC / 2)) % NC + 1;
+    k = q / ((NC / 2) * NC) + 1;
+    i = 2 * p + 1 + ((1 + j + k + nsw) & 1);
+  }
+  T* u = phi + d.offg;
+  auto own = [&](int a, int bb, int c) { return u[G::g(a, bb, c)]; };
+  // the neighbour of (i, j, k) in direction e (0: +x, 1: -x, 2: +y, 3: -y, 4: +z, 5: -z)
+  auto nbv = [&](int e) -> T {
+    const int dim = e >> 1, up = (e & 1) == 0;
+    int c3[3] = {i, j, k};
+    c3[dim] += up ? 1 : -1;
+    const int x0 = c3[dim];
+    if (x0 >= 1 && x0 <= NC) return u[G::g(c3[0], c3[1], c3[2])];
+    if (!pull) return u[G::g(c3[0], c3[1], c3[2])];
+    const int f = 2 * dim + (up ? 1 : 0);
+    const int a = dim == 0 ? j : i, c = dim == 2 ? j : k;
+    return ghost_value<D, NC, T>(m, d, phi, f, a, c, homog != 0, own);
+  };
+  const T f = rhs[d.offi + G::in(i, j, D == 3 ? k : 1)];
+  const T dx2 = Sc<T>::dx2(d);
+  T v;
+  if constexpr (D == 2) {
+    v = (T)0.25 * (nbv(0) + nbv(1) + nbv(2) + nbv(3) - dx2 * f);
+  } else {
+    const T sixth = (T)(1 / 6.0);
+    v = sixth * (nbv(0) + nbv(1) + nbv(2) + nbv(3) + nbv(4) + nbv(5) - dx2 * f);
+  }
+  u[G::g(i, j, k)] = v;
+}
+
 // Loads a group of BPC boxes of a set into shared memory (whole ghosted
 // boxes, vectorised) and their slots into s_slot; returns the count.
 template <int D, int NC, class T, int BPC>
@@ -2487,7 +2553,7 @@ k_defect(Meta m, BoxSet bs, const double* __restrict__ u, const double* __restri
 // iteration of a 256-thread block and a three-deep software pipeline, so that
 // every load of a leaf is in flight while the block computes the leaf before
 // it: at iteration k the block waits for the copies issued at k - 1 (leaf k's
-// ghosted u, leaf k + 1's descriptor), issues leaf k + 1's u and leaf k + 2's
+// u, interior rows only, leaf k + 1's descriptor), issues leaf k + 1's u and leaf k + 2's
 // descriptor (cp.async), loads leaf k + 1's ghost sources and f into
 // registers, and computes leaf k: ghost cells from the sources and its own
 // cells, the largest exponent of the cells the stencil reads, those cells in
@@ -2503,8 +2569,9 @@ struct DefectFxCfg {
   static constexpr int NEED = 2 * D * G::NF;          // face ghosts
   static constexpr int IPT = (NEED + T - 1) / T;      // face ghosts per thread
   static constexpr int SPT = (G::SG + T - 1) / T;     // ghosted cells per thread
-  static constexpr int CH = G::SG * 8 / 16;           // 16-byte chunks of a box
-  static constexpr bool OK = T % 32 == 0 && G::SI % T == 0 && (G::SG * 8) % 16 == 0 && SPT <= 32;
+  static constexpr int NPL = D == 3 ? NC : 1;         // interior planes of a box
+  static constexpr int PCH = NC * G::NG * 8 / 16;     // 16-byte chunks of a plane's interior rows
+  static constexpr bool OK = T % 32 == 0 && G::SI % T == 0 && (G::NG * 8) % 16 == 0 && SPT <= 32;
 };
 
 template <int D, int NC>
@@ -2538,10 +2605,17 @@ k_defect_fx(Meta m, BoxSet bs, const double* __restrict__ u, const double* __res
       cp_async16(reinterpret_cast<char*>(&sd[k % 3]) + 16 * tid,
                  reinterpret_cast<const char*>(m.desc + s) + 16 * tid);
   };
+  // Leaf k's rows j = 1..NC of the planes k = 1..NC (the one plane in 2-D):
+  // its interior with the x ghosts between the rows, contiguous per plane.
+  // The ghost planes and rows are not read: every face ghost the stencil
+  // reads is computed from its sources below, edges and corners are unused.
   auto copy_box = [&](int k) {
     const char* src = reinterpret_cast<const char*>(u + sd[k % 3].offg);
     char* dst = reinterpret_cast<char*>(sb[k & 1]);
-    for (int c = tid; c < C::CH; c += C::T) cp_async16(dst + 16 * c, src + 16 * c);
+    for (int c = tid; c < C::NPL * C::PCH; c += C::T) {
+      const int off = 8 * (G::NG + (D == 3 ? (c / C::PCH + 1) * G::NG * G::NG : 0)) + 16 * (c % C::PCH);
+      cp_async16(dst + off, src + off);
+    }
   };
   // This thread's face ghosts (fixed for every leaf): face (-1: none), ghost,
   // neighbour's and adjacent cell positions, index in the face; and its cells.

@@ -697,7 +697,11 @@ void Forest::sweep(const Arrays<T>& a, int lvl, int n, bool pull, bool homog) {
     using G = dev::Geo<D, NC>;
     // read phi and f, write phi over the interior
     ProfScope ps(this, kProfSweep, 3.0 * nbx * G::SI * sizeof(T));
-    if (sweep_kernel == 0) {
+    if (nbx <= direct_limit<T>() && (long long)nbx * (G::SI / 2) <= (1LL << 24)) {
+      const long long items = (long long)nbx * (G::SI / 2);
+      launch_k(dev::k_sweep_direct<D, NC, T>, (int)((items + 255) / 256), 256, 0, stream, m, bs, a.phi,
+               (const T*)a.rhs, n, pull ? 1 : 0, homog ? 1 : 0);
+    } else if (sweep_kernel == 0) {
       launch_level<D, NC, T, dev::kModeSweep>(*this, m, bs, a.phi, a.rhs, n, pull, homog);
     } else if constexpr (std::is_same<T, float>::value) {
       switch (sweep_kernel) {

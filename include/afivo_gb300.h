@@ -409,7 +409,11 @@ int afv_forest_profile_read(afv_forest* f, int kind, long long* launches, double
  * into shared memory before it gives up, sets the device error word and
  * returns once its copies in flight have landed; the call then reports
  * AFV_ERR_TIMEOUT and clears the word. 0 makes every such wait give up at
- * once, which exercises that path without a stuck copy. */
+ * once, which exercises that path without a stuck copy.
+ * AFV_OPT_DIRECT_BOXES: levels of at most this many boxes (0: none) take the
+ * unstaged half-sweep, one thread per updated cell reading its neighbours
+ * and pulled ghosts straight from memory (same values); -1 (default): FP64
+ * sweeps of levels of at most 4096 boxes, FP32 sweeps never. */
 enum {
   AFV_OPT_SWEEP_KERNEL = 0,
   AFV_OPT_GRAPHS = 1,
@@ -418,7 +422,8 @@ enum {
   AFV_OPT_PROFILE_LEAD_US = 4,
   AFV_OPT_DEFECT_KERNEL = 5,
   AFV_OPT_COARSE_END = 6,
-  AFV_OPT_WAIT_LIMIT_US = 7
+  AFV_OPT_WAIT_LIMIT_US = 7,
+  AFV_OPT_DIRECT_BOXES = 8
 };
 int afv_forest_set_option(afv_forest* f, int option, int value);
 int afv_forest_get_option(afv_forest* f, int option, int* value);

@@ -365,12 +365,25 @@ def test_small_level_sweeps_agree(gpu, which):
         assert np.array_equal(a, b)
 
 
-@pytest.mark.parametrize("which", ["c1", "3d"])
+def _steep_spec(dim):
+    """A near-delta source the tree does not resolve: one Gaussian of width
+    0.01 centred on a cell centre (its Laplacian as the source, values
+    spanning many orders of magnitude inside a box) on a tree refined to
+    level 4 (2-D, cells of 0.016) or 3 (3-D, 0.031) uniformly."""
+    c = (0.5078125, 0.4921875, 0.5078125)[:dim]
+    base = W.c1_poisson_2d() if dim == 2 else W.c2_poisson_3d()
+    return dict(base, name="steep%dd" % dim, gauss=W.gauss_records([c], [1.0], [0.01]),
+                crit=W.AFV_REF_UNIFORM, lvl_max=4 if dim == 2 else 3)
+
+
+@pytest.mark.parametrize("which", ["c1", "3d", "steep2d", "steep3d"])
 def test_defect_kernels_agree(gpu, which):
     """The mixed solve's defect with the fixed-point Laplacian (default) and
     with the FP64 sum: same cycle counts, residuals within float rounding,
-    solutions within the solve tolerance of each other and of the oracle."""
-    spec = W.c1_poisson_2d() if which == "c1" else W.c2_poisson_3d(thr=3e-3, lvl_max=5)
+    solutions within the solve tolerance of each other and of the oracle,
+    also for a source with steep jumps inside boxes."""
+    spec = {"c1": W.c1_poisson_2d, "3d": lambda: W.c2_poisson_3d(thr=3e-3, lvl_max=5),
+            "steep2d": lambda: _steep_spec(2), "steep3d": lambda: _steep_spec(3)}[which]()
     f, ot, _ = setup_pair(gpu, spec)
     rhs = f.get_var(0, gpu.AFV_RHS)
     out = []
@@ -542,6 +555,34 @@ def test_autotune_all_keeps_results(gpu):
             assert g.get_option(gpu.AFV_OPT_COARSE_END) == choice["coarse_end"]
         cyc, rel, rc = g.solve(gpu.AFV_PREC_MIXED, tol=1e-8, max_cycles=60)
         out.append([g.get_var(k, gpu.AFV_PHI) for k in range(len(specs))])
+        g.close()
+    for a, b in zip(out[0], out[1]):
+        assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("which", ["c1", "3d", "batch"])
+def test_direct_sweeps_agree(gpu, which):
+    """The unstaged half-sweep (AFV_OPT_DIRECT_BOXES) on every level and the
+    staged sweeps give the same bits: FP64 V-cycles and mixed solves, with
+    refinement boundaries, coarsened levels and a forest of trees."""
+    if which == "batch":
+        specs = W.c4_random_2d(3, small=True)
+    else:
+        specs = [W.c1_poisson_2d() if which == "c1" else W.c2_poisson_3d(thr=3e-3, lvl_max=5)]
+    out = []
+    for nb in (0, 1 << 30):
+        g = gpu.Forest([W.build_tree(s) for s in specs], mixed=True)
+        for k, s in enumerate(specs):
+            g.set_source(k, s["gauss"], lpl=True)
+        g.set_option(gpu.AFV_OPT_DIRECT_BOXES, nb)
+        assert g.get_option(gpu.AFV_OPT_DIRECT_BOXES) == nb
+        for _ in range(2):
+            g.vcycle(set_residual=True)
+        v = [g.get_var(k, x) for k in range(len(specs)) for x in (gpu.AFV_PHI, gpu.AFV_TMP)]
+        g.zero(gpu.AFV_PHI)
+        g.solve(gpu.AFV_PREC_MIXED, tol=1e-8, max_cycles=30)
+        v += [g.get_var(k, gpu.AFV_PHI) for k in range(len(specs))]
+        out.append(v)
         g.close()
     for a, b in zip(out[0], out[1]):
         assert np.array_equal(a, b)
