@@ -70,3 +70,75 @@ def test_placement_respects_capacity():
     assert max(used) <= 7
     with pytest.raises(ValueError):
         placement.place([5, 5, 5], 2, capacity=6, need=[5, 5, 5])
+
+
+def test_admission_rule():
+    """Least outstanding work among the ranks with room; FIFO wait when no
+    rank has room; completions admit the waiting requests in order."""
+    from afivo_gb300.dispatch import Admission
+    a = Admission(2, budget_bytes=10)
+    assert a.arrive(0, work=5, need=6) == [(0, 0)]
+    assert a.arrive(1, work=3, need=6) == [(1, 1)]
+    assert a.arrive(2, work=1, need=6) == []          # no rank has room: waits
+    assert a.arrive(3, work=1, need=2) == []          # behind request 2 (first in, first out)
+    assert a.complete(1) == [(2, 1), (3, 1)] or a.where  # rank 1 freed: 2 and then 3 fit there
+    assert a.where[2][0] == 1 and a.where[3][0] == 1 and a.used[1] == 8
+    assert max(a.peak) <= 10 and a.waited == 2
+    with pytest.raises(ValueError):
+        a.arrive(9, work=1, need=11)
+
+
+def _serve_main(rank, world, port, q, budget):
+    sys.path.insert(0, ROOT)
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank),
+                      WORLD_SIZE=str(world), LOCAL_RANK=str(rank))
+    import time as _t
+    import torch.distributed as dist
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    from afivo_gb300.dispatch import serve_ranks
+    reqs = [dict(arrival=0.0005 * i, work=float(1 + (5 * i) % 7), need=1 + (3 * i) % 5, id=i)
+            for i in range(60)]
+
+    def solve(r):  # stands in for a solve on this rank's GPU
+        _t.sleep(0.0004 * r["work"])
+        return 2 * r["id"]
+
+    out = serve_ranks(reqs, solve, rank, world, budget, realtime=True)
+    dist.barrier()
+    dist.destroy_process_group()
+    if rank == 0:
+        q.put((rank, {k: (v["rank"], v["result"]) for k, v in out["requests"].items()},
+               out["peak_bytes"], out["waited"]))
+    else:
+        q.put((rank, sorted(out), None, None))
+
+
+@pytest.mark.parametrize("world,budget", [(2, 6), (3, 100)])
+def test_serve_ranks_gloo(world, budget):
+    """Online admission across ranks on CPU (gloo): every request is solved
+    once, by the rank the admission chose, never above the per-rank budget;
+    rank 0 solves its share too."""
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_serve_main, args=(r, world, port, q, budget)) for r in range(world)]
+    for p in procs:
+        p.start()
+    got = {}
+    for _ in range(world):
+        r, a, b, c = q.get(timeout=180)
+        got[r] = (a, b, c)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    placed, peak, waited = got[0]
+    assert sorted(placed) == list(range(60))
+    assert max(peak) <= budget
+    for rid, (r, res) in placed.items():
+        if r == 0:
+            assert res == 2 * rid
+    for r in range(1, world):
+        assert got[r][0] == sorted(i for i, (o, _) in placed.items() if o == r)
+    assert all(any(o == r for o, _ in placed.values()) for r in range(world))
+    if budget == 6:
+        assert waited > 0
