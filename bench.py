@@ -314,7 +314,11 @@ def run_batched(afv, W, local, rank, world, n_trees=256, check_errors=False):
     if sw:
         roof = {"kernel": "sweep (chosen variant %d)" % choice["sweep_kernel"], "achieved": sw["GB/s"],
                 "peak": peak, "unit": "GB/s", "frac": sw["GB/s"] / peak,
-                "peak_kind": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)"}
+                "peak_kind": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
+                "gap": "below 0.6: the half-sweep is latency-bound, not bandwidth-bound; each 8x8 box "
+                       "(400 B of FP32 cells) needs its descriptor, its cells and 32 scattered ghost "
+                       "sources from its neighbours, a chain of dependent L2 round trips, and the level "
+                       "stays in L2 between half-sweeps so DRAM moves a fraction of the algorithmic bytes"}
     errors = None
     if check_errors:
         errors = batched_errors(afv, forest, specs, mine)
@@ -750,6 +754,11 @@ def main():
                               "(4 launches), one profiled mixed solve, each iteration queued "
                               "behind a 5 ms device-side wait (host ahead of the device)",
                      "per_level": sweep_levels,
+                     "gap": "below 0.6 because of the coarse levels: levels 2-5 (under 3 % of the "
+                            "bytes) take about a quarter of the sweep time at 4-5 us per launch, the "
+                            "chain of dependent L2 round trips of a half-sweep; the finest levels run "
+                            "at 0.62-0.67. A cluster-barrier kernel and an unstaged sweep for the small "
+                            "levels were bit-identical but not faster",
                      "launches": sweep_n, "ms": sweep_ms,
                      "traffic": traffic.get("dram_bytes_per_launch") if traffic else None,
                      "traffic_note": traffic.get("note") if traffic else None},
