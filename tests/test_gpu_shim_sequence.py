@@ -55,3 +55,35 @@ def test_default_and_lean_sequences_match_the_oracle(gpu):
         if set_residual:
             assert compare_var(lean_host[gpu.AFV_TMP], oracle_var(ot, O.I_TMP, 8), ot, 8, 2, True) <= TOL
     assert uploads == 2
+
+
+def test_operator_hooks_sequence_matches_the_oracle(gpu):
+    """The drop-in's sequence for the reference's built-in operator hooks in
+    a cylindrical tree (examples/poisson_cyl.f90 with mg2_auto_*, and eps):
+    extra variables 3-5 added once, eps uploaded beside phi, rhs and tmp with
+    every upload, the operator set after it (tags from the uploaded eps),
+    then the cycle; phi after every V-cycle is the oracle's."""
+    from helpers import cyl_spec, fill_from_centres, oracle_tree
+    spec = cyl_spec(lvl_max=6)
+    nc = spec["n_cell"]
+    ot = oracle_tree(spec)
+    ot.fill_gauss(O.I_RHS, spec["gauss"], lpl=True)
+    ot.mg_init()
+    ot.add_vars(3, 0)
+    eps = fill_from_centres(ot, 3, lambda r: np.where(r[..., 0] > 0.53, 100.0, 1.0), nc)
+    assert ot.set_operator(2, 3)  # mg2_auto_op / _gsrb / _corr with mg%i_eps
+    f = gpu.Forest([W.build_tree(spec)])
+    host = {v: oracle_var(ot, v, nc) for v in (gpu.AFV_PHI, gpu.AFV_RHS, gpu.AFV_TMP)}
+    added = False
+    for cycle in range(4):
+        for v, a in host.items():
+            f.set_var(0, v, a)
+        if not added:
+            f.add_vars(3, 0)
+            added = True
+        f.set_var(0, 3, eps)
+        f.set_operator(gpu.AFV_OP_AUTO, 3, -1, -1)
+        f.vcycle(set_residual=True)
+        host = {v: f.get_var(0, v) for v in host}
+        ot.vcycle(set_residual=True)
+        assert compare_var(host[gpu.AFV_PHI], oracle_var(ot, O.I_PHI, nc), ot, nc, 2, False) <= TOL
