@@ -76,12 +76,13 @@ def serve_ranks(requests, solve, rank, world, budget_bytes, group=None, realtime
     """Serve `requests` (dicts with "arrival" in s, "work" and "need" in
     bytes) over the ranks of `group` (a gloo group; None: the default group).
     Every rank calls this with the same list. `solve(request)` runs one
-    request on the calling rank and returns its result.
+    request on the calling rank and returns its result; a solve that raises
+    is reported with its request (as "error") instead of stopping the run.
 
     Returns on rank 0 a dict: per request its rank, start and done times (s
-    from the start) and result, plus the admission's per-rank peak bytes and
-    the count of requests that waited for room; on the other ranks the
-    results of the requests they solved."""
+    from the start), result (rank 0's own requests) and error (or None), plus
+    the admission's per-rank peak bytes and the count of requests that waited
+    for room; on the other ranks the results of the requests they solved."""
     import torch
     import torch.distributed as dist
 
@@ -90,8 +91,14 @@ def serve_ranks(requests, solve, rank, world, budget_bytes, group=None, realtime
 
     def run_one(rid):
         start = now()
-        res = solve(requests[rid])
-        return rid, start, now(), res
+        try:
+            res, err = solve(requests[rid]), None
+        except Exception as exc:  # reported to rank 0 with the request
+            res, err = None, repr(exc)
+        return rid, start, now(), res, err
+
+    def send(value, dst):
+        dist.send(torch.tensor([value], dtype=torch.int64), dst=dst, group=group)
 
     if rank != 0:
         done = {}
@@ -100,13 +107,13 @@ def serve_ranks(requests, solve, rank, world, budget_bytes, group=None, realtime
             dist.recv(msg, src=0, group=group)
             rid = int(msg.item())
             if rid < 0:  # stop: acknowledge, which ends rank 0's receiver for this rank
-                dist.send(torch.tensor([-1], dtype=torch.int64), dst=0, group=group)
+                send(-1, 0)
                 return done
-            rid, start, end, res = run_one(rid)
+            rid, _start, _end, res, err = run_one(rid)
             done[rid] = res
-            dist.send(torch.tensor([rid], dtype=torch.int64), dst=0, group=group)
+            send(rid if err is None else -2 - rid, 0)  # a failed request travels as -2 - rid
 
-    # rank 0: the admission, its own worker thread, and the other ranks' completions
+    # rank 0: the admission, its own worker thread, and one receiver per other rank
     adm = Admission(world, budget_bytes)
     local_q, finished = queue.Queue(), queue.Queue()
     out = {}
@@ -116,16 +123,17 @@ def serve_ranks(requests, solve, rank, world, budget_bytes, group=None, realtime
             rid = local_q.get()
             if rid is None:
                 return
-            finished.put(run_one(rid) + (0,))
+            finished.put(run_one(rid))
 
     def receiver(r):  # completions of rank r, until its acknowledgement of the stop
         buf = torch.zeros(1, dtype=torch.int64)
         while True:
             dist.recv(buf, src=r, group=group)
-            rid = int(buf.item())
-            if rid < 0:
+            v = int(buf.item())
+            if v == -1:
                 return
-            finished.put((rid, None, now(), None, r))
+            rid, err = (v, None) if v >= 0 else (-2 - v, "failed on rank %d" % r)
+            finished.put((rid, None, now(), None, err))
 
     threads = [threading.Thread(target=local_worker, daemon=True)]
     threads += [threading.Thread(target=receiver, args=(r,), daemon=True) for r in range(1, world)]
@@ -140,7 +148,7 @@ def serve_ranks(requests, solve, rank, world, budget_bytes, group=None, realtime
                 local_q.put(rid)
             else:
                 remote_start[rid] = now()
-                dist.send(torch.tensor([rid], dtype=torch.int64), dst=r, group=group)
+                send(rid, r)
 
     order = sorted(range(len(requests)), key=lambda i: (requests[i]["arrival"], i))
     nxt, n_done = 0, 0
@@ -155,17 +163,17 @@ def serve_ranks(requests, solve, rank, world, budget_bytes, group=None, realtime
         if nxt < len(order) and realtime:
             wait = max(0.0, requests[order[nxt]]["arrival"] - now())
         try:
-            rid, start, end, res, r = finished.get(timeout=wait)
+            rid, start, end, res, err = finished.get(timeout=wait)
         except queue.Empty:
             continue
         if start is None:
             start = remote_start.pop(rid)
-        out[rid].update(start=start, done=end, result=res)
+        out[rid].update(start=start, done=end, result=res, error=err)
         n_done += 1
         assign(adm.complete(rid))
     local_q.put(None)
     for r in range(1, world):
-        dist.send(torch.tensor([-1], dtype=torch.int64), dst=r, group=group)
+        send(-1, r)
     for th in threads:
         th.join()
     return {"requests": out, "peak_bytes": list(adm.peak), "waited": adm.waited}

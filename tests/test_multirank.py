@@ -99,15 +99,17 @@ def _serve_main(rank, world, port, q, budget):
     reqs = [dict(arrival=0.0005 * i, work=float(1 + (5 * i) % 7), need=1 + (3 * i) % 5, id=i)
             for i in range(60)]
 
-    def solve(r):  # stands in for a solve on this rank's GPU
+    def solve(r):  # stands in for a solve on this rank's GPU; one request fails
         _t.sleep(0.0004 * r["work"])
+        if r["id"] == 17:
+            raise RuntimeError("request 17 does not converge")
         return 2 * r["id"]
 
     out = serve_ranks(reqs, solve, rank, world, budget, realtime=True)
     dist.barrier()
     dist.destroy_process_group()
     if rank == 0:
-        q.put((rank, {k: (v["rank"], v["result"]) for k, v in out["requests"].items()},
+        q.put((rank, {k: (v["rank"], v["result"], v["error"]) for k, v in out["requests"].items()},
                out["peak_bytes"], out["waited"]))
     else:
         q.put((rank, sorted(out), None, None))
@@ -117,7 +119,8 @@ def _serve_main(rank, world, port, q, budget):
 def test_serve_ranks_gloo(world, budget):
     """Online admission across ranks on CPU (gloo): every request is solved
     once, by the rank the admission chose, never above the per-rank budget;
-    rank 0 solves its share too."""
+    rank 0 solves its share too; a request whose solve raises is reported and
+    the others go on."""
     ctx = mp.get_context("spawn")
     q = ctx.Queue()
     port = _free_port()
@@ -134,11 +137,12 @@ def test_serve_ranks_gloo(world, budget):
     placed, peak, waited = got[0]
     assert sorted(placed) == list(range(60))
     assert max(peak) <= budget
-    for rid, (r, res) in placed.items():
-        if r == 0:
+    for rid, (r, res, err) in placed.items():
+        assert (err is None) == (rid != 17)          # the failure is reported, the run goes on
+        if r == 0 and rid != 17:
             assert res == 2 * rid
     for r in range(1, world):
-        assert got[r][0] == sorted(i for i, (o, _) in placed.items() if o == r)
-    assert all(any(o == r for o, _ in placed.values()) for r in range(world))
+        assert got[r][0] == sorted(i for i, (o, _, _) in placed.items() if o == r)
+    assert all(any(o == r for o, _, _ in placed.values()) for r in range(world))
     if budget == 6:
         assert waited > 0
