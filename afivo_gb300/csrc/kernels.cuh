@@ -2874,6 +2874,13 @@ k_restrict_increment(Meta m, BoxSet bs, double* __restrict__ u, float* __restric
 // Right-hand side from a sum of Gaussians a*exp(-|r-c|^2/s^2), or their
 // Laplacian (lpl), at the cell centres of a slot range of one tree
 // (the source of examples/m_gaussians.f90:64-102), evaluated on the device.
+// A Gaussian factors over the axes, exp(-|x|^2) = exp(-x^2) exp(-y^2)
+// exp(-z^2), and a box's cell centres lie on NC coordinates per axis: one
+// block per box evaluates the 1-D factors and squares (D * NC exponentials
+// and divisions per Gaussian instead of NC^D) and each cell takes their
+// products. GB300 runs FP64 exponentials and divisions slowly; this way the
+// source of a 256^3 tree takes about a tenth of the time. The product differs
+// from exp of the sum by a few roundings (relative 1e-15).
 constexpr int kMaxGauss = 16;
 struct GaussSet {
   int n, lpl;
@@ -2887,29 +2894,41 @@ k_source(Meta m, BoxSet bs, int tree, const double* __restrict__ rmin, GaussSet 
   pdl_wait();
   pdl_trigger();
   using G = Geo<D, NC>;
-  const long long total = (long long)bs.n * G::SI;
-  for (long long x = blockIdx.x * (long long)blockDim.x + threadIdx.x; x < total;
-       x += (long long)gridDim.x * blockDim.x) {
-    const int bi = (int)(x / G::SI), q = (int)(x % G::SI);
+  __shared__ double s_sq[kMaxGauss][3][NC];  // ((r_d - c_d) / s)^2 at the box's NC coordinates
+  __shared__ double s_ex[kMaxGauss][3][NC];  // exp(-that)
+  __shared__ double s_c4[kMaxGauss];         // 4 / s^2 of each Gaussian
+  for (int k = threadIdx.x; k < gs.n; k += blockDim.x) s_c4[k] = 4 / (gs.g[k * (2 + D) + 1] * gs.g[k * (2 + D) + 1]);
+  for (int bi = blockIdx.x; bi < bs.n; bi += gridDim.x) {
     const int s = bs.lo + bi;
-    if (m.tree[s] != tree) continue;
-    const int cix[3] = {q % NC + 1, (q / NC) % NC + 1, (D == 3) ? q / (NC * NC) + 1 : 1};
+    if (m.tree[s] != tree) continue;  // the same for the whole block
     const double dr = m.desc[s].dr;
-    double v = 0;
-    for (int k = 0; k < gs.n; ++k) {
+    __syncthreads();  // the previous box's factors are no longer read
+    for (int e = threadIdx.x; e < gs.n * D * NC; e += blockDim.x) {
+      const int k = e / (D * NC), d = (e / NC) % D, i = e % NC + 1;
       const double* p = gs.g + k * (2 + D);
-      double xr2 = 0;
-#pragma unroll
-      for (int d = 0; d < D; ++d) {
-        const double xx = (rmin[(size_t)s * D + d] + (cix[d] - 0.5) * dr - p[2 + d]) / p[1];
-        xr2 = xr2 + xx * xx;
-      }
-      if (gs.lpl)
-        v = v + p[0] * (4 / (p[1] * p[1]) * (xr2 - 0.5 * D) * exp(-xr2));
-      else
-        v = v + p[0] * exp(-xr2);
+      const double xx = (rmin[(size_t)s * D + d] + (i - 0.5) * dr - p[2 + d]) / p[1];
+      s_sq[k][d][i - 1] = xx * xx;
+      s_ex[k][d][i - 1] = exp(-(xx * xx));
     }
-    rhs[bs.i0 + (long long)bi * G::SI + q] = v;
+    __syncthreads();
+    for (int q = threadIdx.x; q < G::SI; q += blockDim.x) {
+      const int cix[3] = {q % NC, (q / NC) % NC, (D == 3) ? q / (NC * NC) : 0};
+      double v = 0;
+      for (int k = 0; k < gs.n; ++k) {
+        const double* p = gs.g + k * (2 + D);
+        double xr2 = 0, ex = 1;
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+          xr2 = xr2 + s_sq[k][d][cix[d]];
+          ex = ex * s_ex[k][d][cix[d]];
+        }
+        if (gs.lpl)
+          v = v + p[0] * (s_c4[k] * (xr2 - 0.5 * D) * ex);
+        else
+          v = v + p[0] * ex;
+      }
+      rhs[bs.i0 + (long long)bi * G::SI + q] = v;
+    }
   }
 }
 

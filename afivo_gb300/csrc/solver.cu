@@ -1173,7 +1173,7 @@ int Forest::set_source_device(int t, int lpl, int n_gauss, const double* gauss, 
       using G = dev::Geo<D, NC>;
       long long items = (long long)bs.n * G::SI;
       ProfScope ps(this, kProfOther, 8.0 * items);
-      launch_k(dev::k_source<D, NC>, grid_for((items + 255) / 256, n_sm), 256, 0, stream, m, bs, t,
+      launch_k(dev::k_source<D, NC>, grid_for(bs.n, n_sm), dev::kThreads, 0, stream, m, bs, t,
                (const double*)meta.rmin, gs, d64.rhs);
     });
   }
