@@ -6,6 +6,7 @@
 
 #include <array>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "plan.hpp"
@@ -306,6 +307,11 @@ class Forest {
   int n_parents(int l) const {
     return (l < plan.min_lvl || l > plan.max_lvl) ? 0 : (int)plan.parents[plan.L(l)].size();
   }
+  // First and last slot of tree t on level l ({-1, -1}: none); a level's
+  // slots are tree-major, so a tree's are contiguous. The table is built on
+  // first use.
+  std::pair<int, int> tree_level_range(int t, int l);
+  std::vector<int> tl_first, tl_last;  // [t * levels + (l - min_lvl)]
 };
 
 }  // namespace afv

@@ -2876,11 +2876,12 @@ k_restrict_increment(Meta m, BoxSet bs, double* __restrict__ u, float* __restric
 // (the source of examples/m_gaussians.f90:64-102), evaluated on the device.
 // A Gaussian factors over the axes, exp(-|x|^2) = exp(-x^2) exp(-y^2)
 // exp(-z^2), and a box's cell centres lie on NC coordinates per axis: one
-// block per box evaluates the 1-D factors and squares (D * NC exponentials
-// and divisions per Gaussian instead of NC^D) and each cell takes their
-// products. GB300 runs FP64 exponentials and divisions slowly; this way the
-// source of a 256^3 tree takes about a tenth of the time. The product differs
-// from exp of the sum by a few roundings (relative 1e-15).
+// block per box evaluates the factors and squares along each axis (D * NC
+// exponentials and divisions per Gaussian instead of NC^D), combines those
+// of y and z over the transverse positions, and each cell takes one sum and
+// one product of them. GB300 runs FP64 exponentials and divisions slowly; this way the
+// source of a 256^3 tree takes a fraction of the time. The factored form
+// differs from exp of the sum by a few roundings (relative 1e-15).
 constexpr int kMaxGauss = 16;
 struct GaussSet {
   int n, lpl;
@@ -2894,8 +2895,11 @@ k_source(Meta m, BoxSet bs, int tree, const double* __restrict__ rmin, GaussSet 
   pdl_wait();
   pdl_trigger();
   using G = Geo<D, NC>;
+  constexpr int NT = D == 3 ? NC * NC : NC;  // transverse (y, z) positions of a box
   __shared__ double s_sq[kMaxGauss][3][NC];  // ((r_d - c_d) / s)^2 at the box's NC coordinates
   __shared__ double s_ex[kMaxGauss][3][NC];  // exp(-that)
+  __shared__ double s_sqt[kMaxGauss][NT];    // summed over y (and z)
+  __shared__ double s_ext[kMaxGauss][NT];    // multiplied over y (and z)
   __shared__ double s_c4[kMaxGauss];         // 4 / s^2 of each Gaussian
   for (int k = threadIdx.x; k < gs.n; k += blockDim.x) s_c4[k] = 4 / (gs.g[k * (2 + D) + 1] * gs.g[k * (2 + D) + 1]);
   for (int bi = blockIdx.x; bi < bs.n; bi += gridDim.x) {
@@ -2911,21 +2915,28 @@ k_source(Meta m, BoxSet bs, int tree, const double* __restrict__ rmin, GaussSet 
       s_ex[k][d][i - 1] = exp(-(xx * xx));
     }
     __syncthreads();
+    for (int e = threadIdx.x; e < gs.n * NT; e += blockDim.x) {
+      const int k = e / NT, t = e % NT, j = t % NC;
+      if constexpr (D == 3) {
+        const int kz = t / NC;
+        s_sqt[k][t] = s_sq[k][1][j] + s_sq[k][2][kz];
+        s_ext[k][t] = s_ex[k][1][j] * s_ex[k][2][kz];
+      } else {
+        s_sqt[k][t] = s_sq[k][1][j];
+        s_ext[k][t] = s_ex[k][1][j];
+      }
+    }
+    __syncthreads();
     for (int q = threadIdx.x; q < G::SI; q += blockDim.x) {
-      const int cix[3] = {q % NC, (q / NC) % NC, (D == 3) ? q / (NC * NC) : 0};
+      const int i = q % NC, t = q / NC;
       double v = 0;
       for (int k = 0; k < gs.n; ++k) {
-        const double* p = gs.g + k * (2 + D);
-        double xr2 = 0, ex = 1;
-#pragma unroll
-        for (int d = 0; d < D; ++d) {
-          xr2 = xr2 + s_sq[k][d][cix[d]];
-          ex = ex * s_ex[k][d][cix[d]];
-        }
+        const double xr2 = s_sq[k][0][i] + s_sqt[k][t];
+        const double ex = s_ex[k][0][i] * s_ext[k][t];
         if (gs.lpl)
-          v = v + p[0] * (s_c4[k] * (xr2 - 0.5 * D) * ex);
+          v = v + gs.g[k * (2 + D)] * (s_c4[k] * (xr2 - 0.5 * D) * ex);
         else
-          v = v + p[0] * ex;
+          v = v + gs.g[k * (2 + D)] * ex;
       }
       rhs[bs.i0 + (long long)bi * G::SI + q] = v;
     }

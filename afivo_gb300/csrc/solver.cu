@@ -1159,13 +1159,7 @@ int Forest::set_source_device(int t, int lpl, int n_gauss, const double* gauss, 
   for (int k = 0; k < n_gauss * (2 + plan.dim); ++k) gs.g[k] = gauss[k];
   Meta m = meta_of(meta);
   for (int l = plan.min_lvl; l <= plan.max_lvl; ++l) {
-    const int lo = plan.lvl_lo[plan.L(l)], n = plan.lvl_n[plan.L(l)];
-    int a = -1, b = -1;
-    for (int k = 0; k < n; ++k)
-      if (plan.tree[lo + k] == t) {
-        if (a < 0) a = lo + k;
-        b = lo + k;
-      }
+    const auto [a, b] = tree_level_range(t, l);
     if (a < 0) continue;
     BoxSet bs{nullptr, a, b - a + 1, plan.offg[a], plan.offi[a]};
     with_nc(plan.dim, plan.nc_at(l), [&](auto d_, auto nc_) {
@@ -1182,18 +1176,31 @@ int Forest::set_source_device(int t, int lpl, int n_gauss, const double* gauss, 
 
 // cc(..., var) := 0 on every box of one tree, ghost cells included (a
 // tree's boxes of one level are consecutive slots).
+std::pair<int, int> Forest::tree_level_range(int t, int l) {
+  const int nlev = plan.max_lvl - plan.min_lvl + 1;
+  if (tl_first.empty()) {
+    tl_first.assign((size_t)plan.n_trees * nlev, -1);
+    tl_last.assign((size_t)plan.n_trees * nlev, -1);
+    for (int ll = plan.min_lvl; ll <= plan.max_lvl; ++ll) {
+      const int lo = plan.lvl_lo[plan.L(ll)], n = plan.lvl_n[plan.L(ll)];
+      for (int k = 0; k < n; ++k) {
+        const size_t i = (size_t)plan.tree[lo + k] * nlev + (ll - plan.min_lvl);
+        if (tl_first[i] < 0) tl_first[i] = lo + k;
+        tl_last[i] = lo + k;
+      }
+    }
+  }
+  if (l < plan.min_lvl || l > plan.max_lvl) return {-1, -1};
+  const size_t i = (size_t)t * nlev + (l - plan.min_lvl);
+  return {tl_first[i], tl_last[i]};
+}
+
 int Forest::zero_tree(int t, int var, std::string& err) {
   if (t < 0 || t >= plan.n_trees) return err = "tree index out of range", AFV_ERR_INVALID;
   double* v = var_ptr(var);
   if (!v) return err = "unknown variable", AFV_ERR_INVALID;
   for (int l = plan.min_lvl; l <= plan.max_lvl; ++l) {
-    const int lo = plan.lvl_lo[plan.L(l)], n = plan.lvl_n[plan.L(l)];
-    int a = -1, b = -1;
-    for (int k = 0; k < n; ++k)
-      if (plan.tree[lo + k] == t) {
-        if (a < 0) a = lo + k;
-        b = lo + k;
-      }
+    const auto [a, b] = tree_level_range(t, l);
     if (a < 0) continue;
     long long per = 1;
     for (int d = 0; d < plan.dim; ++d) per *= var == AFV_RHS ? plan.nc_at(l) : plan.nc_at(l) + 2;
