@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <array>
+#include <map>
 #include <string>
 #include <utility>
 #include <vector>
@@ -209,7 +210,11 @@ class Forest {
     long long k_pre = 0, k_body = 0, k_post = 0;
     int n_down = -1, n_up = -1, n_base = -1, max_cycles = -1;
     double tol = -1;
-  } graphs[2];
+  };
+  std::map<long long, GraphCache> graphs;  // by precision and tree_limit
+  GraphCache& graph_for(int precision, int limit) {
+    return graphs[(long long)limit * 2 + (precision == AFV_PREC_MIXED ? 1 : 0)];
+  }
   cudaStream_t loop_stream = nullptr;
   bool use_graphs = true;
   void drop_graphs();
@@ -297,15 +302,30 @@ class Forest {
   int check_device_error(std::string& err);  // reads and clears the device error word
   void norm_reset();
   void norm_fold();  // d_norm -> d_red
+  // Solves of the first tree_limit trees only (0: all): the level sets and
+  // lists below then hold those trees' boxes, a prefix of each (a solve whose
+  // mask selects leading trees sets it, see solve()).
+  int tree_limit = 0;
   int lvl_n(int l) const {
-    return (l < plan.min_lvl || l > plan.max_lvl) ? 0 : plan.lvl_n[plan.L(l)];
+    if (l < plan.min_lvl || l > plan.max_lvl) return 0;
+    return tree_limit ? plan.lvl_tprefix[(size_t)plan.L(l) * (plan.n_trees + 1) + tree_limit] : plan.lvl_n[plan.L(l)];
   }
+  int n_all_leaves() const {
+    return tree_limit ? plan.all_leaves_tprefix[tree_limit] : (int)plan.all_leaves.size();
+  }
+  int n_trees_run() const { return tree_limit ? tree_limit : plan.n_trees; }
+  void zero_correction(cudaStream_t st);  // the FP32 phi of the trees in the run
   int* leaves_list(int l) { return d_lists + leaves_off[plan.L(l)]; }
   dev_BoxSet level_set(int l) const;  // all boxes of level l (a slot range)
   int* parents_list(int l) { return d_lists + parents_off[plan.L(l)]; }
-  int n_leaves(int l) const { return (int)plan.leaves[plan.L(l)].size(); }
+  int n_leaves(int l) const {
+    return tree_limit ? plan.leaves_tprefix[(size_t)plan.L(l) * (plan.n_trees + 1) + tree_limit]
+                      : (int)plan.leaves[plan.L(l)].size();
+  }
   int n_parents(int l) const {
-    return (l < plan.min_lvl || l > plan.max_lvl) ? 0 : (int)plan.parents[plan.L(l)].size();
+    if (l < plan.min_lvl || l > plan.max_lvl) return 0;
+    return tree_limit ? plan.parents_tprefix[(size_t)plan.L(l) * (plan.n_trees + 1) + tree_limit]
+                      : (int)plan.parents[plan.L(l)].size();
   }
   // First and last slot of tree t on level l ({-1, -1}: none); a level's
   // slots are tree-major, so a tree's are contiguous. The table is built on

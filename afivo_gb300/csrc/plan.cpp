@@ -206,6 +206,30 @@ int build_plan(const std::vector<const HostTree*>& trees, Plan& p, std::string& 
       }
     }
   }
+  // all leaves tree by tree (levels, then slots, within a tree), and the
+  // counts over leading trees
+  std::stable_sort(p.all_leaves.begin(), p.all_leaves.end(),
+                   [&](int a, int b) { return p.tree[a] < p.tree[b]; });
+  const int T1 = p.n_trees + 1;
+  p.lvl_tprefix.assign((size_t)nlev * T1, 0);
+  p.leaves_tprefix.assign((size_t)nlev * T1, 0);
+  p.parents_tprefix.assign((size_t)nlev * T1, 0);
+  p.all_leaves_tprefix.assign(T1, 0);
+  for (int L = 0; L < nlev; ++L) {
+    int* lv = &p.lvl_tprefix[(size_t)L * T1];
+    for (int k = 0; k < p.lvl_n[L]; ++k) ++lv[p.tree[p.lvl_lo[L] + k] + 1];
+    int* le = &p.leaves_tprefix[(size_t)L * T1];
+    for (int sl : p.leaves[L]) ++le[p.tree[sl] + 1];
+    int* pa = &p.parents_tprefix[(size_t)L * T1];
+    for (int sl : p.parents[L]) ++pa[p.tree[sl] + 1];
+    for (int t = 0; t < p.n_trees; ++t) {
+      lv[t + 1] += lv[t];
+      le[t + 1] += le[t];
+      pa[t + 1] += pa[t];
+    }
+  }
+  for (int sl : p.all_leaves) ++p.all_leaves_tprefix[p.tree[sl] + 1];
+  for (int t = 0; t < p.n_trees; ++t) p.all_leaves_tprefix[t + 1] += p.all_leaves_tprefix[t];
   for (int t = 0; t < p.n_trees; ++t) plan_fill_bc(p, t);
   plan_build_desc(p);
   return AFV_OK;

@@ -51,7 +51,12 @@ struct Plan {
   // per level (index lvl - min_lvl): slot range and leaf / parent lists
   std::vector<int> lvl_lo, lvl_n;
   std::vector<std::vector<int>> leaves, parents;
-  std::vector<int> all_leaves;  // leaves of every level (all have n_cell = nc)
+  std::vector<int> all_leaves;  // leaves of every level (all have n_cell = nc), tree by tree
+  // Counts over the trees before t, for solves of the first t trees only:
+  // [L * (n_trees + 1) + t] slots, leaves and parents of level index L
+  // (within a level the slots, and so the lists, are tree-major), and
+  // [t] entries of all_leaves.
+  std::vector<int> lvl_tprefix, leaves_tprefix, parents_tprefix, all_leaves_tprefix;
   // per tree: slots in the tree's level-list order (the host exchange order)
   std::vector<std::vector<int>> host_order;
   std::vector<int> tree_highest;

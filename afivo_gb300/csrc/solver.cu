@@ -401,9 +401,24 @@ int Forest::create(const std::vector<const HostTree*>& trees, const afv_forest_o
 }
 
 void Forest::drop_graphs() {
-  for (auto& g : graphs) {
-    if (g.exec) cudaGraphExecDestroy(g.exec);
-    g = GraphCache();
+  for (auto& g : graphs)
+    if (g.second.exec) cudaGraphExecDestroy(g.second.exec);
+  graphs.clear();
+}
+
+// The FP32 correction of the trees in the run: one memset of the whole array,
+// or per level the slots of the leading trees.
+void Forest::zero_correction(cudaStream_t st) {
+  if (!tree_limit) {
+    cudaMemsetAsync(d32.phi, 0, sizeof(float) * plan.n_elem_g, st);
+    return;
+  }
+  for (int l = plan.min_lvl; l <= plan.max_lvl; ++l) {
+    const int n = lvl_n(l);
+    if (!n) continue;
+    const int lo = plan.lvl_lo[plan.L(l)];
+    const long long end = lo + n < plan.n_slots ? plan.offg[lo + n] : plan.n_elem_g;
+    cudaMemsetAsync(d32.phi + plan.offg[lo], 0, sizeof(float) * (end - plan.offg[lo]), st);
   }
 }
 
@@ -630,7 +645,7 @@ static void launch_correct_warp(Forest& F, const Meta& m, BoxSet bs, T* phi, T* 
 
 dev_BoxSet Forest::level_set(int lvl) const {
   const int lo = plan.lvl_lo[plan.L(lvl)];
-  return BoxSet{nullptr, lo, plan.lvl_n[plan.L(lvl)], plan.offg[lo], plan.offi[lo]};
+  return BoxSet{nullptr, lo, lvl_n(lvl), plan.offg[lo], plan.offi[lo]};
 }
 
 // Launches the warp-per-box restriction (16 warps x 3 stages in FP32,
@@ -889,11 +904,11 @@ void Forest::coarse_end(const Arrays<float>& a, const MgOpts& mg, int nl) {
   with_nc(plan.dim, plan.nc, [&](auto d_, auto nc_) {
     constexpr int D = decltype(d_)::value, NC = decltype(nc_)::value;
     using G = dev::Geo<D, NC>;
-    ProfScope ps(this, kProfCoarseEnd, 4.0 * (G::SG + 2 * G::SI) * plan.n_trees);
+    ProfScope ps(this, kProfCoarseEnd, 4.0 * (G::SG + 2 * G::SI) * n_trees_run());
     auto go = [&](auto nl_) {
       constexpr int NL = decltype(nl_)::value;
       if constexpr ((NC >> (NL - 1)) >= 2)
-        launch_k(dev::k_coarse_end<D, NC, NL>, plan.n_trees, dev::kCoarseEndThreads, 0, stream, m, sl, a.phi,
+        launch_k(dev::k_coarse_end<D, NC, NL>, n_trees_run(), dev::kCoarseEndThreads, 0, stream, m, sl, a.phi,
                  (const float*)a.rhs, mg.n_down, mg.n_up, mg.n_base);
     };
     switch (nl) {
@@ -1371,7 +1386,7 @@ void Forest::enqueue_residual_check(int precision, double tol, int count_cycle) 
   norm_reset();
   if (precision == AFV_PREC_MIXED) {
     // FP64 defect on the leaves; ghost cells are pulled inside the kernel.
-    int nl = (int)plan.all_leaves.size();
+    int nl = n_all_leaves();
     BoxSet bs{d_lists + all_leaves_off, 0, nl};
     with_nc(plan.dim, plan.nc, [&](auto d_, auto nc_) {
       constexpr int D = decltype(d_)::value, NC = decltype(nc_)::value;
@@ -1432,7 +1447,7 @@ void Forest::enqueue_iteration(const MgOpts& mg, int precision, double tol) {
   Meta m = meta_of(meta);
   if (precision == AFV_PREC_MIXED) {
     vcycle_t(d32, mg, plan.max_lvl, true, true, true);
-    int nl = (int)plan.all_leaves.size();
+    int nl = n_all_leaves();
     BoxSet bs{d_lists + all_leaves_off, 0, nl};
     with_nc(plan.dim, plan.nc, [&](auto d_, auto nc_) {
       constexpr int D = decltype(d_)::value, NC = decltype(nc_)::value;
@@ -1463,7 +1478,7 @@ void Forest::enqueue_iteration(const MgOpts& mg, int precision, double tol) {
     });
     // the next iteration's zero correction, beside this one's defect
     fork();
-    cudaMemsetAsync(d32.phi, 0, sizeof(float) * plan.n_elem_g, side);
+    zero_correction(side);
     enqueue_residual_check(precision, tol);
     join();
   } else {
@@ -1490,7 +1505,7 @@ void Forest::enqueue_solve_begin(int precision, double tol, int max_cycles, cons
   norm_reset();
   {
     // all leaves are on levels >= 1, with nc cells per side: one launch
-    const int nl = (int)plan.all_leaves.size();
+    const int nl = n_all_leaves();
     BoxSet bs{d_lists + all_leaves_off, 0, nl};
     with_nc(plan.dim, plan.nc, [&](auto d_, auto nc_) {
       constexpr int D = decltype(d_)::value, NC = decltype(nc_)::value;
@@ -1506,7 +1521,7 @@ void Forest::enqueue_solve_begin(int precision, double tol, int max_cycles, cons
   cudaMemcpyAsync(d_fmax, d_red, sizeof(double) * nt, cudaMemcpyDeviceToDevice, stream);
   if (precision == AFV_PREC_MIXED) {
     for (int l = plan.max_lvl; l >= plan.min_lvl + 1; --l) restrict_res(d64, l, false);
-    cudaMemsetAsync(d32.phi, 0, sizeof(float) * plan.n_elem_g, stream);  // the first correction
+    zero_correction(stream);  // the first correction
   }
   enqueue_residual_check(precision, tol, 0);
   if (h) {
@@ -1520,9 +1535,14 @@ void Forest::enqueue_solve_begin(int precision, double tol, int max_cycles, cons
 // the results copied to pinned host memory.
 void Forest::enqueue_solve_end(int precision) {
   const int nt = plan.n_trees;
+  if (precision == AFV_PREC_MIXED) {
+    // the parents of u and the ghost cells of the trees this solve took part
+    // in (the others stay as they were)
+    cudaMemcpyAsync(meta.active, d_solve_mask, sizeof(int) * nt, cudaMemcpyDeviceToDevice, stream);
+    restrict_tree_phi64();
+  }
   dev::k_set_int<<<(nt + 255) / 256, 256, 0, stream>>>(meta.active, nt, 1);
   ++n_launches;
-  if (precision == AFV_PREC_MIXED) restrict_tree_phi64();
   cudaMemcpyAsync(h_count, d_count, 4 * sizeof(int), cudaMemcpyDeviceToHost, stream);
   cudaMemcpyAsync(h_cycles, d_cycles, sizeof(int) * nt, cudaMemcpyDeviceToHost, stream);
   cudaMemcpyAsync(h_final, d_final, sizeof(unsigned long long) * nt, cudaMemcpyDeviceToHost, stream);
@@ -1622,6 +1642,20 @@ int Forest::build_solve_graph(GraphCache& gc, const MgOpts& mg, int precision, d
 int Forest::solve(const MgOpts& mg, int precision, double tol, int max_cycles, SolveStats& st,
                   std::string& err, const int* mask) {
   const int nt = plan.n_trees;
+  // A mask of leading trees (a forest whose first k slots hold requests):
+  // the launches cover those trees' boxes only (tree_limit).
+  int lead = 0;
+  bool prefix = mask != nullptr;
+  if (mask) {
+    while (lead < nt && mask[lead]) ++lead;
+    for (int t = lead; t < nt; ++t)
+      if (mask[t]) prefix = false;
+  }
+  struct LimitScope {
+    Forest* f;
+    ~LimitScope() { f->tree_limit = 0; }
+  } limit_scope{this};
+  tree_limit = (prefix && lead > 0 && lead < nt) ? lead : 0;
   for (int t = 0; t < nt; ++t) h_solve_mask[t] = mask ? (mask[t] != 0) : 1;
   cudaMemcpyAsync(d_solve_mask, h_solve_mask, sizeof(int) * nt, cudaMemcpyHostToDevice, stream);
   if (precision == AFV_PREC_MIXED && !mixed)
@@ -1632,7 +1666,7 @@ int Forest::solve(const MgOpts& mg, int precision, double tol, int max_cycles, S
   st.rel_res.assign(nt, 0.0);
   const bool graph = use_graphs && prof_mask == 0;
   if (graph) {
-    GraphCache& gc = graphs[precision == AFV_PREC_MIXED ? 1 : 0];
+    GraphCache& gc = graph_for(precision, tree_limit);
     if (!gc.exec || gc.n_down != mg.n_down || gc.n_up != mg.n_up || gc.n_base != mg.n_base || gc.tol != tol ||
         gc.max_cycles != max_cycles)
       if (int rc = build_solve_graph(gc, mg, precision, tol, max_cycles, err)) return rc;

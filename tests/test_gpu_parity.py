@@ -586,3 +586,43 @@ def test_direct_sweeps_agree(gpu, which):
         g.close()
     for a, b in zip(out[0], out[1]):
         assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("prec", ["mixed", "fp64"])
+def test_masked_solves_leading_and_scattered(gpu, prec):
+    """Masked solves of a 4-tree forest: a mask of leading trees (run over
+    those trees' boxes only) and a scattered mask give every selected tree
+    the bits of its solve alone, leave the other trees' phi untouched, and a
+    full solve afterwards is unaffected."""
+    p = gpu.AFV_PREC_MIXED if prec == "mixed" else gpu.AFV_PREC_FP64
+    specs = W.c4_random_2d(4, small=True)
+    alone = []
+    for s in specs:
+        f1 = gpu.Forest([W.build_tree(s)], mixed=True)
+        f1.set_source(0, s["gauss"], lpl=True)
+        c1, _, _ = f1.solve(p, tol=1e-8, max_cycles=60)
+        alone.append((int(c1[0]), f1.get_var(0, gpu.AFV_PHI)))
+        f1.close()
+    f = gpu.Forest([W.build_tree(s) for s in specs], mixed=True)
+    for k, s in enumerate(specs):
+        f.set_source(k, s["gauss"], lpl=True)
+    for mask in ([1, 1, 0, 0], [1, 0, 0, 0], [0, 1, 0, 1], [1, 1, 1, 0]):
+        f.zero(gpu.AFV_PHI)
+        marker = [f.get_var(k, gpu.AFV_PHI) + (k + 1) for k in range(4)]
+        for k in range(4):
+            if not mask[k]:
+                f.set_var(k, gpu.AFV_PHI, marker[k])  # must survive the masked solve
+        cyc, rel, rc = f.solve(p, tol=1e-8, max_cycles=60, mask=mask)
+        assert rc == 0
+        for k in range(4):
+            got = f.get_var(k, gpu.AFV_PHI)
+            if mask[k]:
+                assert int(cyc[k]) == alone[k][0]
+                assert np.array_equal(got, alone[k][1]), (mask, k)
+            else:
+                assert np.array_equal(got, marker[k]), (mask, k)
+    f.zero(gpu.AFV_PHI)
+    cyc, rel, rc = f.solve(p, tol=1e-8, max_cycles=60)
+    for k in range(4):
+        assert np.array_equal(f.get_var(k, gpu.AFV_PHI), alone[k][1])
+    f.close()
