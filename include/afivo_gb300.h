@@ -413,7 +413,7 @@ int afv_forest_profile_read(afv_forest* f, int kind, long long* launches, double
  * AFV_OPT_DIRECT_BOXES: levels of at most this many boxes (0: none) take the
  * unstaged half-sweep, one thread per updated cell reading its neighbours
  * and pulled ghosts straight from memory (same values); -1 (default): FP64
- * sweeps of levels of at most 4096 boxes, FP32 sweeps never. */
+ * sweeps on every level, FP32 sweeps never. */
 enum {
   AFV_OPT_SWEEP_KERNEL = 0,
   AFV_OPT_GRAPHS = 1,
