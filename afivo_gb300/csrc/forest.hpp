@@ -213,7 +213,9 @@ class Forest {
   };
   std::map<long long, GraphCache> graphs;  // by precision and tree_limit
   GraphCache& graph_for(int precision, int limit) {
-    return graphs[(long long)limit * 2 + (precision == AFV_PREC_MIXED ? 1 : 0)];
+    const long long key = (long long)limit * 2 + (precision == AFV_PREC_MIXED ? 1 : 0);
+    if (graphs.size() >= 32 && !graphs.count(key)) drop_graphs();  // bound the cache (many prefix lengths)
+    return graphs[key];
   }
   cudaStream_t loop_stream = nullptr;
   bool use_graphs = true;
