@@ -290,7 +290,9 @@ int afv_mg_solve(afv_forest* f, const afv_mg_opts* mg, int precision, double tol
 /* No counterpart in the reference: afv_mg_solve on the trees whose mask
  * entry is nonzero (mask may be NULL: every tree); the other trees' cell
  * data is left as it is and their cycles / rel_res entries are 0. A forest
- * whose trees are request slots solves the occupied slots only. */
+ * whose trees are request slots solves the occupied slots only; when those
+ * are the leading slots (mask 1..1 0..0) the launches cover only their boxes,
+ * so the cost follows the number of occupied slots. */
 int afv_mg_solve_trees(afv_forest* f, const afv_mg_opts* mg, int precision, double tol, int max_cycles,
                        const int* mask, int* cycles, double* rel_res);
 
