@@ -642,9 +642,12 @@ def main():
     # end to end through the C ABI: every step copies its rhs in from pinned
     # host memory, solves, and copies the solution out. Serial: one forest,
     # step after step. Pipelined (the reported e2e): two forests of the same
-    # tree, each driven by its own host thread, so that one step's copies run
-    # while the other forest solves (the C calls release the interpreter
-    # lock); every step still does all of its copies inside the timed region.
+    # tree, each driven by its own host thread (the second starting once the
+    # first step's rhs is in), so that one step's copies run beside the other
+    # forest's solve (the C calls release the interpreter lock); every step
+    # still does all of its copies inside the timed region. (Making the
+    # solves take turns on the GPU was slower: the copies' gather and scatter
+    # kernels then hold SMs the running solve needs.)
     n_in = forest._n_values(0, True)
     host_rhs = torch.empty(n_in, dtype=torch.float64, pin_memory=True)
     forest.get_var(0, afv.AFV_RHS, interior_only=True, out=host_rhs.numpy())
@@ -654,9 +657,13 @@ def main():
     pair = (forest, twin)
     host_phi = [torch.empty(n_in, dtype=torch.float64, pin_memory=True) for _ in pair]
 
+    import threading
+    first_in = threading.Event()  # the second thread starts once the first step's rhs is in
+
     def e2e_step(k):
         f = pair[k]
         f.set_var(0, afv.AFV_RHS, host_rhs.numpy(), interior_only=True)
+        first_in.set()
         f.zero(afv.AFV_PHI)
         cyc_, rel_, rc_ = f.solve(afv.AFV_PREC_MIXED, tol=TOL, max_cycles=60, check=False)
         if rc_ != 0:
@@ -674,12 +681,13 @@ def main():
     e2e_serial_s = max_over_ranks(time.perf_counter() - t0, world)
     e2e_serial = cells * sum_over_ranks(float(e2e_cycles), world) / e2e_serial_s
 
-    import threading
     done = [0, 0]
     errors = []
 
     def worker(k, n):
         try:
+            if k == 1:
+                first_in.wait(timeout=60)
             for _ in range(n):
                 done[k] += e2e_step(k)
         except Exception as exc:  # reported after the join
@@ -687,6 +695,7 @@ def main():
 
     barrier(world)
     torch.cuda.synchronize()
+    first_in.clear()
     t0 = time.perf_counter()
     threads = [threading.Thread(target=worker, args=(k, (args.steps + 1 - k) // 2)) for k in (0, 1)]
     for th in threads:
