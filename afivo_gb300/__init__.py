@@ -42,9 +42,10 @@ AFV_REF_UNIFORM, AFV_REF_SOURCE, AFV_REF_RANDOM, AFV_REF_RANDOM_RM = 0, 1, 2, 3
 AFV_PREC_FP64, AFV_PREC_MIXED = 0, 1
 AFV_OPT_SWEEP_KERNEL, AFV_OPT_GRAPHS, AFV_OPT_RESTRICT_KERNEL, AFV_OPT_SMALL_SWEEPS = 0, 1, 2, 3
 AFV_OPT_PROFILE_LEAD_US, AFV_OPT_DEFECT_KERNEL, AFV_OPT_COARSE_END = 4, 5, 6
-AFV_OPT_WAIT_LIMIT_US, AFV_OPT_DIRECT_BOXES = 7, 8
+AFV_OPT_WAIT_LIMIT_US, AFV_OPT_DIRECT_BOXES, AFV_OPT_ZERO_COPY = 7, 8, 9
 OPTION_NAMES = ("sweep_kernel", "graphs", "restrict_kernel", "small_sweeps", "profile_lead_us",
-                "defect_kernel", "coarse_end", "wait_limit_us", "direct_boxes")  # AFV_OPT_* in order
+                "defect_kernel", "coarse_end", "wait_limit_us", "direct_boxes",
+                "zero_copy")  # AFV_OPT_* in order
 AFV_RB_MG, AFV_RB_PROLONG0, AFV_RB_INTERP, AFV_RB_INTERP_LIM = 0, 1, 2, 3
 AFV_BCM_TABLE, AFV_BCM_DIRICHLET_ZERO, AFV_BCM_NEUMANN_ZERO = 0, -1, -2
 AFV_OP_LPL, AFV_OP_LPLD, AFV_OP_AUTO = 0, 1, 2

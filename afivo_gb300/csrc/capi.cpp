@@ -539,6 +539,9 @@ int afv_forest_set_option(afv_forest* f, int option, int value) {
       f->f.use_coarse_end = value != 0;
       f->f.drop_graphs();
       return AFV_OK;
+    case AFV_OPT_ZERO_COPY:
+      f->f.zero_copy = value != 0;
+      return AFV_OK;
     case AFV_OPT_DIRECT_BOXES:
       if (value < -1) return fail(AFV_ERR_INVALID, "direct boxes must be >= -1");
       f->f.direct_boxes = value;
@@ -566,6 +569,7 @@ int afv_forest_get_option(afv_forest* f, int option, int* value) {
     case AFV_OPT_COARSE_END: *value = f->f.use_coarse_end ? 1 : 0; return AFV_OK;
     case AFV_OPT_WAIT_LIMIT_US: *value = (int)(f->f.meta.wait_limit / 2000LL); return AFV_OK;
     case AFV_OPT_DIRECT_BOXES: *value = f->f.direct_boxes; return AFV_OK;
+    case AFV_OPT_ZERO_COPY: *value = f->f.zero_copy ? 1 : 0; return AFV_OK;
   }
   return fail(AFV_ERR_INVALID, "unknown option");
 }

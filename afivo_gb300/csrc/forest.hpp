@@ -101,6 +101,7 @@ class Forest {
   // 3 % faster on the 3-D and batched 2-D workloads), FP32 sweeps never (the
   // staged warp sweep is as fast there).
   int direct_boxes = -1;
+  bool zero_copy = true;  // host exchange of pinned memory by SM loads and stores, no staging buffer
   template <class T> int direct_limit() const {
     return direct_boxes >= 0 ? direct_boxes : (sizeof(T) == 8 ? (1 << 30) : 0);
   }

@@ -513,12 +513,15 @@ static int exchange(Forest& F, int t, int var, double* host, int interior_only, 
   if (int rc = exchange_plan(F, err)) return rc;
   const int D = p.dim;
   const long long total = F.xfer_total[t][interior_only ? 0 : 1];
-  // Page-locked host memory is mapped into the device's address space: the
-  // scatter / gather kernels then read or write it directly over the host
-  // link, with no staging copy. Other host memory goes through the staging
-  // buffer and cudaMemcpyAsync.
+  // With zero_copy (the default), page-locked host memory, mapped into the
+  // device's address space, is read or written by the scatter / gather
+  // kernels directly, with no staging copy; those kernels then hold SMs for
+  // the whole transfer. Otherwise (and for pageable memory) the bytes go
+  // through a device staging buffer: one cudaMemcpyAsync on the copy engines
+  // and a scatter / gather kernel at HBM speed, which leaves the SMs to other
+  // work (another forest's solve) while the bytes cross the link.
   double* mapped = nullptr;
-  {
+  if (F.zero_copy) {
     cudaPointerAttributes pa;
     if (cudaPointerGetAttributes(&pa, host) == cudaSuccess && pa.type == cudaMemoryTypeHost &&
         pa.devicePointer && pa.device == F.device)

@@ -415,7 +415,11 @@ int afv_forest_profile_read(afv_forest* f, int kind, long long* launches, double
  * AFV_OPT_DIRECT_BOXES: levels of at most this many boxes (0: none) take the
  * unstaged half-sweep, one thread per updated cell reading its neighbours
  * and pulled ghosts straight from memory (same values); -1 (default): FP64
- * sweeps on every level, FP32 sweeps never. */
+ * sweeps on every level, FP32 sweeps never. AFV_OPT_ZERO_COPY: 1 (default)
+ * exchanges page-locked host arrays (afv_forest_set_var / get_var) by kernel
+ * loads and stores over the host link, without the device staging buffer;
+ * 0 copies through the staging buffer with the copy engines, which leaves
+ * the SMs to other work (another forest's solve) during the transfer. */
 enum {
   AFV_OPT_SWEEP_KERNEL = 0,
   AFV_OPT_GRAPHS = 1,
@@ -425,7 +429,8 @@ enum {
   AFV_OPT_DEFECT_KERNEL = 5,
   AFV_OPT_COARSE_END = 6,
   AFV_OPT_WAIT_LIMIT_US = 7,
-  AFV_OPT_DIRECT_BOXES = 8
+  AFV_OPT_DIRECT_BOXES = 8,
+  AFV_OPT_ZERO_COPY = 9
 };
 int afv_forest_set_option(afv_forest* f, int option, int value);
 int afv_forest_get_option(afv_forest* f, int option, int* value);
