@@ -626,3 +626,29 @@ def test_masked_solves_leading_and_scattered(gpu, prec):
     for k in range(4):
         assert np.array_equal(f.get_var(k, gpu.AFV_PHI), alone[k][1])
     f.close()
+
+
+def test_host_exchange_routes_agree(gpu):
+    """Page-locked host arrays exchanged by kernel loads and stores
+    (AFV_OPT_ZERO_COPY 1, the default) and through the staging buffer on the
+    copy engines (0) carry the same bits, ghosted and interior-only."""
+    torch = pytest.importorskip("torch")
+    spec = W.c1_poisson_2d()
+    f = gpu.Forest([W.build_tree(spec)], mixed=True)
+    f.set_source(0, spec["gauss"], lpl=True)
+    rng = np.random.default_rng(11)
+    for interior in (True, False):
+        n = f._n_values(0, interior)
+        src = torch.from_numpy(rng.standard_normal(n)).pin_memory()
+        outs = []
+        for zc in (1, 0):
+            f.set_option(gpu.AFV_OPT_ZERO_COPY, zc)
+            assert f.get_option(gpu.AFV_OPT_ZERO_COPY) == zc
+            f.set_var(0, gpu.AFV_PHI, src.numpy(), interior_only=interior)
+            dst = torch.empty(n, dtype=torch.float64).pin_memory()
+            f.get_var(0, gpu.AFV_PHI, interior_only=interior, out=dst.numpy())
+            outs.append(dst.numpy().copy())
+        assert np.array_equal(outs[0], outs[1])
+        if interior:
+            assert np.array_equal(outs[0], src.numpy())
+    f.close()
