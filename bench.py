@@ -469,6 +469,172 @@ def serving_picks(n_requests, n=8):
     return list(range(0, n_requests, max(1, n_requests // n)))[:n]
 
 
+def run_next_rows(afv, W, local, threads):
+    """The rows beyond the solver, each on a full-size tree with the oracle
+    (the C++/OpenMP restatement, on `threads` host cores) timed beside it as
+    that row's CPU baseline, and the GPU result compared with the oracle's:
+    the device tree build (C2's tree refined on the device), the operator
+    variants (one FP64 V-cycle of lpld, auto and lpllsf on the C2 tree, clpl
+    on a cylindrical 2-D tree), the ghost-cell and transfer utilities on the
+    C2 tree, and the VTK writer (C1's leaves). GPU times include the call's
+    host side and a synchronisation."""
+    import shutil
+    import tempfile
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle as O
+    from helpers import (bval_field, compare_var, cyl_spec, fill_from_centres, lsf_sphere, oracle_tree,
+                         oracle_var)
+    O.build()
+    O.set_threads(threads)
+    out = {"cores": threads}
+
+    def timed(fn, sync, reps=1):
+        fn()
+        sync()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            fn()
+        sync()
+        return 1e3 * (time.perf_counter() - t0) / reps
+
+    def once(fn):
+        t0 = time.perf_counter()
+        fn()
+        return 1e3 * (time.perf_counter() - t0)
+
+    spec = W.c2_poisson_3d()
+    nc, D = spec["n_cell"], spec["dim"]
+
+    # device tree build: the C2 refinement from the base box
+    box = {}
+    t_host = once(lambda: box.__setitem__("host", W.build_tree(spec)))
+    base = afv.Tree(D, nc, spec["dr"], coarsen_to=spec["coarsen_to"]).set_base(spec["ix"], spec["nb"])
+    dt = afv.DeviceTree(base, device=local)
+    t_dev = once(lambda: dt.refine_builtin(spec["crit"], spec["lvl_max"], thr=spec["thr"], gauss=spec["gauss"],
+                                          lpl=spec["lpl"]))
+    n_dev = dt.info()["n_boxes"]
+    dt.close()
+    t_orc = once(lambda: box.__setitem__("oracle", oracle_tree(spec)))
+    ot = box["oracle"]
+    n_host = box["host"].info()["n_boxes"]
+    out["device_tree_build"] = {"workload": spec["name"], "boxes": n_dev, "same_box_count": n_dev == n_host,
+                                "device_ms": round(t_dev, 2), "host_ms": round(t_host, 2),
+                                "oracle_ms": round(t_orc, 2)}
+
+    # operator variants: one FP64 V-cycle from the same state on GPU and oracle
+    ops = {}
+    ot.fill_gauss(O.I_RHS, spec["gauss"], lpl=True)
+    ot.mg_init()
+    ot.add_vars(3, 0)
+    eps = fill_from_centres(ot, 3, lambda r: np.where(r[..., 0] > 0.53, 100.0, 1.0), nc)
+    lsf = fill_from_centres(ot, 4, lsf_sphere, nc)
+    bval = fill_from_centres(ot, 5, bval_field, nc)
+    rhs = oracle_var(ot, O.I_RHS, nc)
+    f = afv.Forest([box["host"]], device=local)
+    f.add_vars(3, 0)
+    for iv, a in ((3, eps), (4, lsf), (5, bval), (afv.AFV_RHS, rhs)):
+        f.set_var(0, iv, a)
+    cells = f.info()["leaf_cells"]
+    all_cells = f.info()["n_boxes"] * nc ** D
+    for name, op, args in (("lpld", 1, (3, -1, -1)), ("auto_eps", 2, (3, -1, -1)), ("lpllsf", 5, (-1, 4, 5))):
+        f.zero(afv.AFV_PHI)
+        ot.zero(O.I_PHI)
+        f.set_operator(op, *args)
+        assert ot.set_operator(op, *args)
+        g_ms = timed(lambda: f.vcycle(set_residual=False), f.sync, reps=1)  # two cycles run
+        o_ms = once(lambda: ot.vcycle(set_residual=False))
+        ot.vcycle(set_residual=False)
+        err = compare_var(f.get_var(0, afv.AFV_PHI), oracle_var(ot, O.I_PHI, nc), ot, nc, D, False)
+        ops[name] = {"gpu_ms_per_vcycle": round(g_ms, 3), "oracle_ms_per_vcycle": round(o_ms, 1),
+                     "speedup": round(o_ms / g_ms, 1), "max_rel_diff_vs_oracle": err}
+    f.set_operator(0)
+    f.close()
+    cs = cyl_spec(lvl_max=10)
+    cot = oracle_tree(cs)
+    cot.fill_gauss(O.I_RHS, cs["gauss"], lpl=True)
+    cot.mg_init()
+    cf = afv.Forest([W.build_tree(cs)], device=local)
+    cf.set_var(0, afv.AFV_RHS, oracle_var(cot, O.I_RHS, cs["n_cell"]))
+    cf.set_operator(3)
+    assert cot.set_operator(3)
+    g_ms = timed(lambda: cf.vcycle(set_residual=False), cf.sync, reps=1)
+    o_ms = once(lambda: cot.vcycle(set_residual=False))
+    cot.vcycle(set_residual=False)
+    err = compare_var(cf.get_var(0, afv.AFV_PHI), oracle_var(cot, O.I_PHI, cs["n_cell"]), cot, cs["n_cell"], 2,
+                      False)
+    ops["clpl_cylindrical_2d"] = {"leaf_cells": cf.info()["leaf_cells"], "gpu_ms_per_vcycle": round(g_ms, 3),
+                                  "oracle_ms_per_vcycle": round(o_ms, 1), "speedup": round(o_ms / g_ms, 1),
+                                  "max_rel_diff_vs_oracle": err}
+    cf.close()
+    out["operators"] = {"workload": spec["name"], "leaf_cells": cells, "cells_all_levels": all_cells, **ops}
+
+    # ghost cells, transfers and fluxes on the C2 tree, random data
+    rng = np.random.default_rng(12)
+    ot.add_vars(1, 1)  # cell variable 6, face variable 0
+    g = afv.Forest([box["host"]], device=local)
+    g.add_vars(4, 1)
+    for iv in (3, 6):
+        parts = []
+        for lvl in range(ot.min_lvl, ot.highest_lvl + 1):
+            a = rng.standard_normal(ot.get_level(lvl, iv, nc).shape)
+            ot.set_level(lvl, iv, a)
+            parts.append(a.ravel())
+        g.set_var(0, iv, np.concatenate(parts))
+    fcv = rng.standard_normal(g.fc_count(0))
+    ot.set_fc(0, fcv)
+    g.set_fc(0, 0, fcv)
+    top = ot.highest_lvl
+    ghost_vals = f_cells = 0
+    for lvl in range(ot.min_lvl, top + 1):
+        nb = len(ot.level(lvl)[0])
+        ncl = ot.n_cell_at(lvl, nc)
+        ghost_vals += nb * 2 * D * ncl ** (D - 1)
+        f_cells += nb * ncl ** D
+    tr = {}
+    steps = (
+        ("gc_tree_interp", lambda: g.gc_tree_var(3, rb=afv.AFV_RB_INTERP, bc=afv.AFV_BCM_DIRICHLET_ZERO),
+         lambda: ot.gc_tree_var(3, rb=2, bc=-1), 3, 2 * 8 * ghost_vals),
+        ("prolong2_finest", lambda: g.prolong(top - 1, 6, 6, order=2),
+         lambda: ot.prolong(top - 1, 6, 6, order=2), 6, None),
+        ("restrict_tree", lambda: g.restrict_tree(3, 6), lambda: ot.restrict_tree(3, 6), 6, None),
+        ("consistent_fluxes", lambda: g.consistent_fluxes([0]), lambda: ot.consistent_fluxes([0]), None, None),
+    )
+    for name, gf, of, iv, nbytes in steps:
+        g_ms = timed(gf, g.sync, reps=1)
+        o_ms = once(of)
+        of()  # the GPU ran it twice; so does the oracle
+        if iv is not None:
+            same = bool(np.array_equal(g.get_var(0, iv), oracle_var(ot, iv, nc)))
+        else:
+            same = bool(np.array_equal(g.get_fc(0, 0), ot.get_fc(0)))
+        tr[name] = {"gpu_ms": round(g_ms, 3), "oracle_ms": round(o_ms, 1), "speedup": round(o_ms / g_ms, 1),
+                    "bit_identical": same}
+        if nbytes:
+            tr[name]["GB/s"] = round(nbytes / (g_ms / 1e3) / 1e9, 1)
+    g.close()
+    out["transfer"] = {"workload": spec["name"], "cells_all_levels": f_cells, **tr}
+
+    # VTK output of C1's leaves (phi holding the source)
+    s1 = W.c1_poisson_2d()
+    vot = oracle_tree(s1)
+    vot.fill_gauss(O.I_PHI, s1["gauss"], lpl=True)
+    vf = afv.Forest([W.build_tree(s1)], device=local)
+    vf.set_var(0, afv.AFV_PHI, oracle_var(vot, O.I_PHI, s1["n_cell"]))
+    d = tempfile.mkdtemp(prefix="afv_vtk_")
+    try:
+        g_ms = timed(lambda: vf.write_vtk(0, os.path.join(d, "gpu"), [afv.AFV_PHI], ["phi"]), lambda: None)
+        o_ms = once(lambda: vot.write_vtk(os.path.join(d, "orc.vtu"), [O.I_PHI], ["phi"]))
+        a = open(os.path.join(d, "gpu.vtu"), "rb").read()
+        b = open(os.path.join(d, "orc.vtu"), "rb").read()
+        out["vtk"] = {"workload": s1["name"], "bytes": len(a), "gpu_ms": round(g_ms, 2), "oracle_ms": round(o_ms, 2),
+                      "byte_identical": a == b}
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+    vf.close()
+    return out
+
+
 def cpu_serving_sample(reqs, threads, picks, served_phi):
     """The oracle's FP64 solve of a sample of the requests on the host cores
     (one after another, as a CPU server would): its time per request, and the
@@ -525,6 +691,8 @@ def main():
     ap.add_argument("--no-batched", action="store_true", help="skip the 256-tree batched solve")
     ap.add_argument("--no-serving", action="store_true", help="skip the served request stream")
     ap.add_argument("--no-uniform", action="store_true", help="skip the 4096^2 periodic case")
+    ap.add_argument("--no-next-rows", action="store_true",
+                    help="skip the device tree build, operator, transfer and VTK measurements")
     ap.add_argument("--profile-solves", type=int, default=0,
                     help="only run this many mixed solves, untimed (a short command to profile)")
     args = ap.parse_args()
@@ -726,6 +894,9 @@ def main():
     served, reqs, served_phi = (None, None, {}) if args.no_serving else run_serving(
         afv, W, local, rank, world, keep_ids=set(picks) if check else ())
     uniform = None if args.no_uniform else run_uniform(afv, W, local, rank, world, check_errors=check)
+    next_rows = None
+    if check and not args.no_next_rows:
+        next_rows = run_next_rows(afv, W, local, os.cpu_count() or 1)
 
     peak, peak_kind = load_peaks()
     achieved = sweep_bytes / (sweep_ms / 1e3) / 1e9 if sweep_ms > 0 else None
@@ -783,6 +954,7 @@ def main():
         "batched": batched,
         "serving": served,
         "uniform_periodic": uniform,
+        "next_rows": next_rows,
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": "unknowns/s", "h2d_bytes_per_step": n_in * 8,
                 "d2h_bytes_per_step": n_in * 8,
