@@ -143,8 +143,12 @@ class Forest {
   int i_eps = -1, i_lsf = -1, i_bval = -1;
   int* d_tags = nullptr;
   int* d_ix = nullptr;  // [slot*D + d] the boxes' ix (cylindrical radial factors)
+  // eps_0 eps_f / (eps_0 + eps_f) per interior cell and face (the lpld
+  // operators' face weights, [(offi + q) * 2D + f]), taken with the operator
+  double* d_coef = nullptr;
   int set_operator(int new_op, int new_i_eps, int new_i_lsf, int new_i_bval, std::string& err);
   const double* eps_ptr() const;
+  void gen_coef();
   opdev::Op op_args() const;  // what the generic kernels read
   // The FP64 routines take the generic kernels of operators.cu: an operator
   // other than the Laplacian, or cylindrical coordinates (whose restriction

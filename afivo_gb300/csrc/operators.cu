@@ -46,6 +46,7 @@ struct Op {
   const double* bval;     // ghosted boundary value at the interface
   const int* ix;          // [slot*D + d]
   const double* rmin;     // [slot*D + d]
+  const double* coef;     // lpld face weights eps_0 eps / (eps_0 + eps), [(offi + q) * 2D + f], or null
 };
 
 // The operator a box takes (mg%box_* hooks, or the auto dispatch by tag).
@@ -107,7 +108,7 @@ __device__ __forceinline__ void lsf_stencil(const double* u, const double* l, co
 // g: mg$D_box_lpl, mg$D_box_lpld, mg2_box_clpl, mg2_box_clpld, mg$D_box_lpllsf.
 template <int D, int NC>
 __device__ __forceinline__ double op_at(const Op& o, int kind, const double* __restrict__ phi, long long g, int s,
-                                        int c, int i, double inv_dr_sq) {
+                                        int c, int i, double inv_dr_sq, long long qi) {
   const double* u = phi + g;
   constexpr int NG = NC + 2;
   switch (kind) {
@@ -135,6 +136,13 @@ __device__ __forceinline__ double op_at(const Op& o, int kind, const double* __r
       const double* e = o.eps + g;
       const double u0 = u[c], a0 = e[c];
       const bool cyl = kind == kClpld;
+      if (!cyl && o.coef) {  // the face weights of k_coef: the values of the division below
+        const double* w = o.coef + qi * (2 * D);
+        double sum = 0.0;
+#pragma unroll
+        for (int k = 0; k < 2 * D; ++k) sum = sum + w[k] * (u[c + nb_off<D, NC>(k)] - u0);
+        return inv_dr_sq * 2 * sum;
+      }
       double r1 = 1, r2 = 1;
       if (cyl) rfac(i, (o.ix[(size_t)s * D] - 1) * NC, r1, r2);
       double sum = 0.0;
@@ -194,6 +202,30 @@ __global__ void k_tags(BoxSet bs, const long long* __restrict__ offg, const doub
       tags[s] = t;
       if ((int)is_lsf + (int)is_eps + (int)is_deps > 1) atomicExch(conflict, 1);
     }
+  }
+}
+
+// The face weights of the lpld operators, eps_0 eps_f / (eps_0 + eps_f)
+// for every interior cell and face of a set of boxes (the reference's
+// expression; ghost cells read as stored), taken once per call so that the
+// sweeps, residuals and restrictions of its cycles do not divide per face and
+// cell.
+template <int D, int NC>
+__global__ void k_coef(BoxSet bs, const long long* __restrict__ offg, const long long* __restrict__ offi,
+                       const double* __restrict__ eps, double* __restrict__ coef) {
+  using G = Geo<D, NC>;
+  const long long total = (long long)bs.n * G::SI * (2 * D);
+  for (long long it = blockIdx.x * (long long)blockDim.x + threadIdx.x; it < total;
+       it += (long long)gridDim.x * blockDim.x) {
+    const int k = (int)(it % (2 * D));
+    const long long cell = it / (2 * D);
+    const int b = (int)(cell / G::SI), q = (int)(cell % G::SI);
+    const int s = bs.lo + b;
+    const int i = q % NC + 1, j = (q / NC) % NC + 1, kz = D == 3 ? q / (NC * NC) + 1 : 0;
+    const double* e = eps + offg[s];
+    const int c = G::g(i, j, kz);
+    const double a0 = e[c], a = e[c + nb_off<D, NC>(k)];
+    coef[(offi[s] + q) * (2 * D) + k] = a0 * a / (a0 + a);
   }
 }
 
@@ -259,12 +291,16 @@ __global__ void k_gsrb(Meta m, Op o, BoxSet bs, double* __restrict__ phi, const 
         const double a0 = e[c];
         double r1 = 1, r2 = 1;
         if (cyl) rfac(i, (o.ix[(size_t)s * D] - 1) * NC, r1, r2);
+        // 2 eps_0 eps / (eps_0 + eps) is exactly twice k_coef's weight: a
+        // factor 2 commutes with the rounding of the product and the quotient
+        // (for products and quotients in the normal range)
+        const double* w = (!cyl && o.coef) ? o.coef + (d.offi + G::in(i, j, D == 3 ? k : 1)) * (2 * D) : nullptr;
         double cu = 0.0, cs = 0.0;
 #pragma unroll
         for (int kk = 0; kk < 2 * D; ++kk) {
           const int of = nb_off<D, NC>(kk);
           const double a = e[c + of];
-          const double ck = 2 * a0 * a / (a0 + a);
+          const double ck = w ? 2 * w[kk] : 2 * a0 * a / (a0 + a);
           if (cyl) {
             const double rf = kk == 0 ? r1 : kk == 1 ? r2 : 1.0;
             cu = cu + ck * rf * u[c + of];
@@ -296,7 +332,7 @@ __global__ void k_residual(Meta m, Op o, BoxSet bs, const double* __restrict__ p
     const SlotDesc& d = m.desc[s];
     const int i = q % NC + 1, j = (q / NC) % NC + 1, k = D == 3 ? q / (NC * NC) + 1 : 0;
     const int c = G::g(i, j, k);
-    const double l = op_at<D, NC>(o, kind_of(o, s), phi, d.offg, s, c, i, d.inv_dx2);
+    const double l = op_at<D, NC>(o, kind_of(o, s), phi, d.offg, s, c, i, d.inv_dx2, d.offi + q);
     tmp[d.offg + c] = rhs[d.offi + q] - l;
   }
 }
@@ -381,7 +417,8 @@ __global__ void k_restrict(Meta m, Op o, BoxSet bs, double* __restrict__ phi, co
         for (int ii = 0; ii < 2; ++ii, ++e) {
           const int fi = 2 * i - 1 + ii, fj = 2 * j - 1 + jj, fk = D == 3 ? 2 * k - 1 + kk : 0;
           const int c = G::g(fi, fj, fk);
-          r[e] = rhs[d.offi + G::in(fi, fj, D == 3 ? fk : 1)] - op_at<D, NC>(o, kind, phi, d.offg, s, c, fi, d.inv_dx2);
+          const long long qf = d.offi + G::in(fi, fj, D == 3 ? fk : 1);
+          r[e] = rhs[qf] - op_at<D, NC>(o, kind, phi, d.offg, s, c, fi, d.inv_dx2, qf);
           if (store_res) tmp[d.offg + c] = r[e];
           p[e] = phi[d.offg + c];
           lc[e] = kind == kLsf ? o.lsf[d.offg + c] : 0.0;
@@ -456,8 +493,9 @@ __global__ void k_coarse(Meta m, Op o, BoxSet bs, const double* __restrict__ phi
     const int i = c % (NC + 2), j = (c / (NC + 2)) % (NC + 2), k = D == 3 ? c / ((NC + 2) * (NC + 2)) : 1;
     const bool inner = i >= 1 && i <= NC && j >= 1 && j <= NC && k >= 1 && k <= NC;
     if (inner) {
-      const double l = op_at<D, NC>(o, kind_of(o, s), phi, d.offg, s, c, i, d.inv_dx2);
-      rhs[d.offi + G::in(i, j, D == 3 ? k : 1)] = l + tmp[d.offg + c];
+      const long long qi = d.offi + G::in(i, j, D == 3 ? k : 1);
+      const double l = op_at<D, NC>(o, kind_of(o, s), phi, d.offg, s, c, i, d.inv_dx2, qi);
+      rhs[qi] = l + tmp[d.offg + c];
     }
     if (copy_tmp) tmp[d.offg + c] = phi[d.offg + c];
   }
@@ -639,6 +677,7 @@ opdev::Op Forest::op_args() const {
   o.bval = i_bval >= 0 ? var_ptr(i_bval) : d64.phi;
   o.ix = d_ix;
   o.rmin = meta.rmin;
+  o.coef = (i_eps >= 0 && d_coef && (op == AFV_OP_LPLD || op == AFV_OP_AUTO)) ? d_coef : nullptr;
   return o;
 }
 
@@ -700,6 +739,12 @@ int Forest::set_operator(int new_op, int new_i_eps, int new_i_lsf, int new_i_bva
       });
     }
   }
+  if (t_eps >= 0 && !d_coef) {  // room for the lpld face weights (gen_coef)
+    const size_t n = (size_t)std::max(1LL, plan.n_elem_i) * 2 * plan.dim;
+    if (cudaMallocAsync((void**)&d_coef, sizeof(double) * n, stream) != cudaSuccess)
+      return err = "device allocation failed", AFV_ERR_NOMEM;
+    bytes += sizeof(double) * n;
+  }
   int h_conflict = 0;
   if (conflict) {
     cudaMemcpyAsync(&h_conflict, conflict, sizeof(int), cudaMemcpyDeviceToHost, stream);
@@ -713,6 +758,25 @@ int Forest::set_operator(int new_op, int new_i_eps, int new_i_lsf, int new_i_bva
   i_lsf = t_lsf;
   i_bval = t_lsf >= 0 ? new_i_bval : -1;
   return AFV_OK;
+}
+
+// The lpld face weights from the current eps, on every level, enqueued at
+// the start of each FP64 routine (and in each solve's graph) so that a call
+// sees eps as it is when the call runs, as the reference's operators that
+// read eps at every use.
+void Forest::gen_coef() {
+  if (i_eps < 0 || !d_coef || (op != AFV_OP_LPLD && op != AFV_OP_AUTO)) return;
+  for (int l = plan.min_lvl; l <= plan.max_lvl; ++l) {
+    const int nbx = lvl_n(l);
+    if (!nbx) continue;
+    with_nc_op(plan.dim, plan.nc_at(l), [&](auto d_, auto nc_) {
+      constexpr int D = decltype(d_)::value, NC = decltype(nc_)::value;
+      using G = dev::Geo<D, NC>;
+      opdev::k_coef<D, NC><<<grid_n((long long)nbx * G::SI * 2 * D, n_sm), 256, 0, stream>>>(
+          level_set(l), meta.offg, meta.offi, var_ptr(i_eps), d_coef);
+      ++n_launches;
+    });
+  }
 }
 
 // gsrb_boxes (src/m_aX_mg.f90:397-420): each half-sweep, then the level's

@@ -162,7 +162,7 @@ Forest::~Forest() {
     if (p) cudaFreeAsync(p, stream);
   for (double* p : xcc)
     if (p) cudaFreeAsync(p, stream);
-  for (void* p : {(void*)fc, (void*)d_nb, (void*)d_lvl, (void*)d_qd, (void*)d_tags, (void*)d_ix})
+  for (void* p : {(void*)fc, (void*)d_nb, (void*)d_lvl, (void*)d_qd, (void*)d_tags, (void*)d_ix, (void*)d_coef})
     if (p) cudaFreeAsync(p, stream);
   if (stream) cudaStreamSynchronize(stream);
   for (const ProfEntry& p : prof) {
@@ -1020,6 +1020,7 @@ void Forest::fill64(int lvl) { fill(d64, lvl, false); }
 
 int Forest::gsrb_level(int lvl, int n_cycle, std::string& err) {
   if (generic()) {
+    gen_coef();
     gen_gsrb_boxes(lvl, n_cycle);
     if (int rc = check(err, "gsrb_level")) return rc;
     return check_device_error(err);
@@ -1034,10 +1035,12 @@ int Forest::fill_level(int lvl, std::string& err) {
 }
 int Forest::update_coarse(int lvl, std::string& err) {
   if (lvl <= plan.min_lvl || lvl > plan.max_lvl) return err = "level out of range", AFV_ERR_INVALID;
-  if (generic())
+  if (generic()) {
+    gen_coef();
     gen_update_coarse(lvl, true);
-  else
+  } else {
     update_coarse_t(d64, lvl, false, true);
+  }
   return check(err, "update_coarse");
 }
 int Forest::correct_children(int lp, std::string& err) {
@@ -1049,6 +1052,7 @@ int Forest::correct_children(int lp, std::string& err) {
   return check(err, "correct_children");
 }
 int Forest::residual_all(unsigned long long* norm, std::string& err) {
+  if (generic()) gen_coef();
   for (int l = plan.min_lvl; l <= plan.max_lvl; ++l)
     if (generic())
       gen_residual(l, norm);
@@ -1061,6 +1065,7 @@ int Forest::vcycle(const MgOpts& mg, int highest, bool set_residual, std::string
   if (highest < plan.min_lvl) return err = "highest_lvl below the coarsest level", AFV_ERR_INVALID;
   highest = std::min(highest, plan.max_lvl);
   if (generic()) {
+    gen_coef();
     gen_vcycle(mg, highest, set_residual);
   } else {
     vcycle_t(d64, mg, highest, false, false);
@@ -1242,6 +1247,7 @@ int Forest::fmg(const MgOpts& mg, bool set_residual, bool have_guess, std::strin
   std::vector<int> all(plan.n_trees, 1);
   set_active_host(all);
   Meta m = meta_of(meta);
+  if (generic()) gen_coef();
   if (have_guess) {
     for (int l = plan.max_lvl; l >= l0 + 1; --l) {
       // set_coarse_phi_rhs(l): trees with highest == l first fill level l.
@@ -1505,6 +1511,7 @@ void Forest::enqueue_solve_begin(int precision, double tol, int max_cycles, cons
   cudaMemcpyAsync(meta.active, d_solve_mask, sizeof(int) * nt, cudaMemcpyDeviceToDevice, stream);
   cudaMemsetAsync(d_cycles, 0, sizeof(int) * nt, stream);
   cudaMemsetAsync(d_failed, 0, sizeof(int) * nt, stream);
+  if (generic()) gen_coef();
   norm_reset();
   {
     // all leaves are on levels >= 1, with nc cells per side: one launch

@@ -135,3 +135,37 @@ def test_auto_with_unit_eps_is_the_laplacian(gpu):
             f.vcycle(set_residual=True)
         out.append(f.get_var(0, gpu.AFV_PHI))
     assert np.array_equal(out[0], out[1])
+
+
+def _scale_eps(ot, f, spec, factor):
+    """eps times factor on both sides (ghost cells and coarse levels included)."""
+    nc, dim = spec["n_cell"], spec["dim"]
+    parts = []
+    for lvl in range(ot.min_lvl, ot.highest_lvl + 1):
+        ncl = nc if lvl >= 1 else nc >> (1 - lvl)
+        e = factor * _eps(_centres(ot, lvl, ncl, dim))
+        ot.set_level(lvl, I_EPS, e)
+        parts.append(e.ravel())
+    f.set_var(0, I_EPS, np.concatenate(parts))
+
+
+def test_eps_changed_between_calls(gpu):
+    """The reference's lpld operators read eps at every use: eps changed
+    after the operator was set is seen by the next V-cycle and by the next
+    solve of a cached solve graph."""
+    spec, ot, f = _pair(gpu, "3d", 1)
+    for _ in range(2):
+        ot.vcycle(set_residual=True)
+        f.vcycle(set_residual=True)
+    _scale_eps(ot, f, spec, 3.0)
+    for _ in range(2):
+        ot.vcycle(set_residual=True)
+        f.vcycle(set_residual=True)
+    _check(gpu, f, ot, spec)
+    spec, ot, f = _pair(gpu, "2d", 1)
+    for factor in (1.0, 0.25):
+        _scale_eps(ot, f, spec, factor)
+        n = oracle_solve(ot, 1e-8)
+        cyc, rel, rc = f.solve(gpu.AFV_PREC_FP64, tol=1e-8, max_cycles=60)
+        assert rc == 0 and int(cyc[0]) == n
+        _check(gpu, f, ot, spec)
