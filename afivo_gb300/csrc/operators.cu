@@ -80,6 +80,19 @@ __device__ __forceinline__ void rfac(int i, int ioff, double& r1, double& r2) {
   r2 = (i + ioff) / (i + ioff - 0.5);
 }
 
+// x / y. When y is a power of two whose reciprocal is a normal number, x
+// times that (exact) reciprocal: the same correctly rounded quotient without
+// a division. The level-set and variable-coefficient formulas divide by 2 or
+// 4 away from interfaces and eps jumps (distances 1, equal eps), and GB300's
+// FP64 pipe makes each division costly.
+__device__ __forceinline__ double qdiv(double x, double y) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(y);
+  const unsigned e = (unsigned)(b >> 52) & 0x7ffu;
+  if ((b & 0xfffffffffffffull) == 0 && e >= 1 && e <= 2045)
+    return x * __longlong_as_double((long long)((b & 0x8000000000000000ull) | ((unsigned long long)(2046 - e) << 52)));
+  return x / y;
+}
+
 // lsf_dist_val (src/m_aX_mg.f90:993-1019): distance (0..1) to a neighbour and
 // the value there, or at the interface when the level set changes sign
 // between (boundary values interpolated).
@@ -126,10 +139,10 @@ __device__ __forceinline__ double op_at(const Op& o, int kind, const double* __r
       double dd[6], val[6];
       lsf_stencil<D, NC>(u, o.lsf + g, o.bval + g, c, dd, val);
       const double f0 = u[c];
-      double r = (dd[1] * val[0] + dd[0] * val[1] - (dd[0] + dd[1]) * f0) / ((dd[0] + dd[1]) * dd[0] * dd[1]) +
-                 (dd[3] * val[2] + dd[2] * val[3] - (dd[2] + dd[3]) * f0) / ((dd[2] + dd[3]) * dd[2] * dd[3]);
+      double r = qdiv(dd[1] * val[0] + dd[0] * val[1] - (dd[0] + dd[1]) * f0, (dd[0] + dd[1]) * dd[0] * dd[1]) +
+                 qdiv(dd[3] * val[2] + dd[2] * val[3] - (dd[2] + dd[3]) * f0, (dd[2] + dd[3]) * dd[2] * dd[3]);
       if constexpr (D == 3)
-        r = r + (dd[5] * val[4] + dd[4] * val[5] - (dd[4] + dd[5]) * f0) / ((dd[4] + dd[5]) * dd[4] * dd[5]);
+        r = r + qdiv(dd[5] * val[4] + dd[4] * val[5] - (dd[4] + dd[5]) * f0, (dd[4] + dd[5]) * dd[4] * dd[5]);
       return 2 * inv_dr_sq * r;
     }
     default: {  // kLpld, kClpld
@@ -152,9 +165,9 @@ __device__ __forceinline__ double op_at(const Op& o, int kind, const double* __r
         const double a = e[c + of];
         if (cyl) {
           const double rf = k == 0 ? r1 : k == 1 ? r2 : 1.0;
-          sum = sum + rf * a0 * a / (a0 + a) * (u[c + of] - u0);
+          sum = sum + qdiv(rf * a0 * a, a0 + a) * (u[c + of] - u0);
         } else {
-          sum = sum + a0 * a / (a0 + a) * (u[c + of] - u0);
+          sum = sum + qdiv(a0 * a, a0 + a) * (u[c + of] - u0);
         }
       }
       return inv_dr_sq * 2 * sum;
@@ -225,7 +238,7 @@ __global__ void k_coef(BoxSet bs, const long long* __restrict__ offg, const long
     const double* e = eps + offg[s];
     const int c = G::g(i, j, kz);
     const double a0 = e[c], a = e[c + nb_off<D, NC>(k)];
-    coef[(offi[s] + q) * (2 * D) + k] = a0 * a / (a0 + a);
+    coef[(offi[s] + q) * (2 * D) + k] = qdiv(a0 * a, a0 + a);
   }
 }
 
@@ -274,14 +287,14 @@ __global__ void k_gsrb(Meta m, Op o, BoxSet bs, double* __restrict__ phi, const 
         if constexpr (D == 2) {
           double prod = 1;
           for (int e = 0; e < 4; ++e) prod = prod * dd[e];
-          u[c] = 1 / (dd[0] * dd[1] + dd[2] * dd[3]) *
-                 ((dd[1] * val[0] + dd[0] * val[1]) * dd[2] * dd[3] / (dd[0] + dd[1]) +
-                  (dd[3] * val[2] + dd[2] * val[3]) * dd[0] * dd[1] / (dd[2] + dd[3]) - 0.5 * prod * d.dx2 * f);
+          u[c] = qdiv(1, dd[0] * dd[1] + dd[2] * dd[3]) *
+                 (qdiv((dd[1] * val[0] + dd[0] * val[1]) * dd[2] * dd[3], dd[0] + dd[1]) +
+                  qdiv((dd[3] * val[2] + dd[2] * val[3]) * dd[0] * dd[1], dd[2] + dd[3]) - 0.5 * prod * d.dx2 * f);
         } else {
-          u[c] = 1 / (1 / (dd[0] * dd[1]) + 1 / (dd[2] * dd[3]) + 1 / (dd[4] * dd[5])) *
-                 ((dd[1] * val[0] + dd[0] * val[1]) / ((dd[0] + dd[1]) * dd[0] * dd[1]) +
-                  (dd[3] * val[2] + dd[2] * val[3]) / ((dd[2] + dd[3]) * dd[2] * dd[3]) +
-                  (dd[5] * val[4] + dd[4] * val[5]) / ((dd[4] + dd[5]) * dd[4] * dd[5]) - 0.5 * d.dx2 * f);
+          u[c] = qdiv(1, qdiv(1, dd[0] * dd[1]) + qdiv(1, dd[2] * dd[3]) + qdiv(1, dd[4] * dd[5])) *
+                 (qdiv(dd[1] * val[0] + dd[0] * val[1], (dd[0] + dd[1]) * dd[0] * dd[1]) +
+                  qdiv(dd[3] * val[2] + dd[2] * val[3], (dd[2] + dd[3]) * dd[2] * dd[3]) +
+                  qdiv(dd[5] * val[4] + dd[4] * val[5], (dd[4] + dd[5]) * dd[4] * dd[5]) - 0.5 * d.dx2 * f);
         }
         break;
       }
@@ -300,7 +313,7 @@ __global__ void k_gsrb(Meta m, Op o, BoxSet bs, double* __restrict__ phi, const 
         for (int kk = 0; kk < 2 * D; ++kk) {
           const int of = nb_off<D, NC>(kk);
           const double a = e[c + of];
-          const double ck = w ? 2 * w[kk] : 2 * a0 * a / (a0 + a);
+          const double ck = w ? 2 * w[kk] : qdiv(2 * a0 * a, a0 + a);
           if (cyl) {
             const double rf = kk == 0 ? r1 : kk == 1 ? r2 : 1.0;
             cu = cu + ck * rf * u[c + of];
@@ -310,7 +323,7 @@ __global__ void k_gsrb(Meta m, Op o, BoxSet bs, double* __restrict__ phi, const 
             cs = cs + ck;
           }
         }
-        u[c] = (cu - d.dx2 * f) / cs;
+        u[c] = qdiv(cu - d.dx2 * f, cs);
         break;
       }
     }
@@ -597,7 +610,7 @@ __global__ void k_correct(Meta m, Op o, BoxSet parents, int nch, double* __restr
       double s1 = 0.0, s2 = 0.0;
       for (int e = 0; e <= D; ++e) s1 = s1 + cw[e] * val[e];
       for (int e = 0; e <= D; ++e) s2 = s2 + cw[e];
-      out = out + s1 / s2;
+      out = out + qdiv(s1, s2);
     } else {
       const double u0 = P_(tmp, c1[0], c1[1], c1[2]);
       const double a0 = P_(o.eps, c1[0], c1[1], c1[2]);
@@ -609,9 +622,9 @@ __global__ void k_correct(Meta m, Op o, BoxSet parents, int nch, double* __restr
         const double u = P_(tmp, cc[0], cc[1], cc[2]);
         const double a = P_(o.eps, cc[0], cc[1], cc[2]);
         if constexpr (D == 2)
-          sm = sm + (a0 * u0 + a * u) / (a0 + a);
+          sm = sm + qdiv(a0 * u0 + a * u, a0 + a);
         else
-          sm = sm + (a0 * u0 + a * (1.5 * u - 0.5 * u0)) / (a0 + a);
+          sm = sm + qdiv(a0 * u0 + a * (1.5 * u - 0.5 * u0), a0 + a);
       }
       out = out + (D == 2 ? 0.5 : 1 / 3.0) * sm;
     }
