@@ -42,10 +42,10 @@ AFV_REF_UNIFORM, AFV_REF_SOURCE, AFV_REF_RANDOM, AFV_REF_RANDOM_RM = 0, 1, 2, 3
 AFV_PREC_FP64, AFV_PREC_MIXED = 0, 1
 AFV_OPT_SWEEP_KERNEL, AFV_OPT_GRAPHS, AFV_OPT_RESTRICT_KERNEL, AFV_OPT_SMALL_SWEEPS = 0, 1, 2, 3
 AFV_OPT_PROFILE_LEAD_US, AFV_OPT_DEFECT_KERNEL, AFV_OPT_COARSE_END = 4, 5, 6
-AFV_OPT_WAIT_LIMIT_US, AFV_OPT_DIRECT_BOXES, AFV_OPT_ZERO_COPY = 7, 8, 9
+AFV_OPT_WAIT_LIMIT_US, AFV_OPT_DIRECT_BOXES, AFV_OPT_ZERO_COPY, AFV_OPT_DEFECT_CELLS = 7, 8, 9, 10
 OPTION_NAMES = ("sweep_kernel", "graphs", "restrict_kernel", "small_sweeps", "profile_lead_us",
                 "defect_kernel", "coarse_end", "wait_limit_us", "direct_boxes",
-                "zero_copy")  # AFV_OPT_* in order
+                "zero_copy", "defect_cells")  # AFV_OPT_* in order
 AFV_RB_MG, AFV_RB_PROLONG0, AFV_RB_INTERP, AFV_RB_INTERP_LIM = 0, 1, 2, 3
 AFV_BCM_TABLE, AFV_BCM_DIRICHLET_ZERO, AFV_BCM_NEUMANN_ZERO = 0, -1, -2
 AFV_OP_LPL, AFV_OP_LPLD, AFV_OP_AUTO = 0, 1, 2
@@ -147,6 +147,7 @@ def lib():
             "afv_forest_set_source_device": (I, [P, I, I, I, dp]),
             "afv_forest_autotune": (I, [P, ip, ctypes.POINTER(ctypes.c_float)]),
             "afv_forest_autotune_all": (I, [P, ip, ctypes.POINTER(ctypes.c_float)]),
+            "afv_forest_autotune_defect": (I, [P, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_float)]),
             "afv_forest_get_option": (I, [P, I, ip]),
             "afv_tree_max_abs_cc_noalloc": (I, [P, I, I, dp]),
             "afv_mg_solve": (I, [P, ctypes.POINTER(MgOpts), I, Dd, I, ip, dp]),
@@ -634,7 +635,17 @@ class Forest:
         times = {"sweep_kernel_%d" % k: ms[k] for k in range(6)}
         for k in range(4):
             times["small_%d_coarse_end_%d" % (k >> 1, k & 1)] = ms[6 + k]
-        return {"sweep_kernel": int(c[0]), "small_sweeps": int(c[1]), "coarse_end": int(c[2])}, times
+        return {"sweep_kernel": int(c[0]), "small_sweeps": int(c[1]), "coarse_end": int(c[2]),
+                "defect_cells": self.get_option(AFV_OPT_DEFECT_CELLS)}, times
+
+    def autotune_defect(self):
+        """Times the fixed-point defect with 1, 2 and 4 cells per thread and
+        keeps the fastest: (choice, {cells: ms per launch} of the shapes the
+        boxes allow)."""
+        c = ctypes.c_int(0)
+        ms = (ctypes.c_float * 3)()
+        _check(lib().afv_forest_autotune_defect(self.h, ctypes.byref(c), ms))
+        return int(c.value), {cr: ms[k] for k, cr in enumerate((1, 2, 4)) if ms[k] >= 0}
 
     def set_option(self, option, value):
         _check(lib().afv_forest_set_option(self.h, option, int(value)))

@@ -535,6 +535,12 @@ int afv_forest_set_option(afv_forest* f, int option, int value) {
       f->f.defect_fx = value != 0;
       f->f.drop_graphs();
       return AFV_OK;
+    case AFV_OPT_DEFECT_CELLS:
+      if (value != 0 && value != 1 && value != 2 && value != 4)
+        return fail(AFV_ERR_INVALID, "defect cells per thread must be 0, 1, 2 or 4");
+      f->f.defect_cells = value;
+      f->f.drop_graphs();
+      return AFV_OK;
     case AFV_OPT_COARSE_END:
       f->f.use_coarse_end = value != 0;
       f->f.drop_graphs();
@@ -566,6 +572,7 @@ int afv_forest_get_option(afv_forest* f, int option, int* value) {
     case AFV_OPT_SMALL_SWEEPS: *value = f->f.use_small_sweeps ? 1 : 0; return AFV_OK;
     case AFV_OPT_PROFILE_LEAD_US: *value = f->f.prof_lead_us; return AFV_OK;
     case AFV_OPT_DEFECT_KERNEL: *value = f->f.defect_fx ? 1 : 0; return AFV_OK;
+    case AFV_OPT_DEFECT_CELLS: *value = f->f.defect_cells; return AFV_OK;
     case AFV_OPT_COARSE_END: *value = f->f.use_coarse_end ? 1 : 0; return AFV_OK;
     case AFV_OPT_WAIT_LIMIT_US: *value = (int)(f->f.meta.wait_limit / 2000LL); return AFV_OK;
     case AFV_OPT_DIRECT_BOXES: *value = f->f.direct_boxes; return AFV_OK;
@@ -637,6 +644,10 @@ int afv_forest_autotune(afv_forest* f, int* choice, float* ms3) {
 int afv_forest_autotune_all(afv_forest* f, int* choice3, float* ms10) {
   if (!choice3) return fail(AFV_ERR_INVALID, "NULL argument");
   FOREST_CALL(f, return f->f.autotune_all(&choice3[0], &choice3[1], &choice3[2], ms10, err));
+}
+
+int afv_forest_autotune_defect(afv_forest* f, int* cells, float* ms3) {
+  FOREST_CALL(f, return f->f.autotune_defect(cells, ms3, err));
 }
 
 int afv_forest_set_source_device(afv_forest* f, int tree, int src_lpl, int n_gauss, const double* gauss) {

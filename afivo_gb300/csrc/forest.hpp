@@ -87,6 +87,7 @@ class Forest {
   int sweep_kernel = 1;  // 0: block-pipelined k_level_tma, 1: warp-per-box k_sweep_warp, 2: its async variant
   bool use_restrict_warp = true;  // warp-per-box restriction on levels >= 2
   bool defect_fx = true;          // mixed defect: fixed-point Laplacian (false: FP64 sum)
+  int defect_cells = 0;           // its cells per thread (1, 2, 4; 0: the default per box shape)
   bool use_coarse_end = true;     // correction cycle's levels l0..1 in one launch (k_coarse_end)
   int coarse_end_levels = -1;     // levels k_coarse_end covers (0: not eligible; -1: not yet known)
   int coarse_end_depth(int highest);
@@ -299,6 +300,10 @@ class Forest {
   // a loop handle: the loop-entry decision) and its finish.
   void enqueue_iteration(const MgOpts& mg, int precision, double tol);
   void enqueue_residual_check(int precision, double tol, int count_cycle = 1);
+  void launch_defect();
+  int defect_cr(int si) const;
+  void tune_defect(cudaEvent_t e0, cudaEvent_t e1, float* ms3);
+  int autotune_defect(int* cells, float* ms3, std::string& err);
   void enqueue_solve_begin(int precision, double tol, int max_cycles, const cudaGraphConditionalHandle* h);
   void enqueue_solve_end(int precision);
   int build_solve_graph(GraphCache& gc, const MgOpts& mg, int precision, double tol, int max_cycles,

@@ -2549,70 +2549,87 @@ k_defect(Meta m, BoxSet bs, const double* __restrict__ u, const double* __restri
 }
 
 // ---------------------------------------------------------------------------
-// k_defect_fx: k_defect with the fixed-point Laplacian, one leaf per
-// iteration of a 256-thread block and a three-deep software pipeline, so that
-// every load of a leaf is in flight while the block computes the leaf before
-// it: at iteration k the block waits for the copies issued at k - 1 (leaf k's
-// u, interior rows only, leaf k + 1's descriptor), issues leaf k + 1's u and leaf k + 2's
-// descriptor (cp.async), loads leaf k + 1's ghost sources and f into
-// registers, and computes leaf k: ghost cells from the sources and its own
-// cells, the largest exponent of the cells the stencil reads, those cells in
+// k_defect_fx: k_defect with the fixed-point Laplacian. A 256-thread block
+// takes LPB leaves per iteration (one group of LT = SI / CR threads per leaf,
+// at most 256: CR cells per thread, more in boxes of over 256 CR cells) in a
+// three-deep software
+// pipeline, so that every load of an iteration's leaves is in flight while
+// the block computes the iteration before: at iteration k the block waits for
+// the copies issued at k - 1 (the leaves' u, interior rows only, and the next
+// leaves' descriptors), issues iteration k + 1's u and k + 2's descriptors
+// (cp.async), loads k + 1's ghost sources and f into registers, and computes
+// iteration k: ghost cells from the sources and each leaf's own cells, each
+// leaf's largest exponent of the cells the stencil reads, those cells in
 // fixed point in place, then r = f - S/dx^2 for its cells. A leaf holding an
 // infinity or NaN takes the FP64 sum instead. Boxes of at least 32 cells
 // (smaller ones use k_defect).
 // ---------------------------------------------------------------------------
-template <int D, int NC>
+template <int D, int NC, int CR>
 struct DefectFxCfg {
   using G = Geo<D, NC>;
-  static constexpr int T = G::SI < 256 ? G::SI : 256;  // threads of a block
-  static constexpr int CPT = G::SI / T;               // interior cells per thread
-  static constexpr int NEED = 2 * D * G::NF;          // face ghosts
-  static constexpr int IPT = (NEED + T - 1) / T;      // face ghosts per thread
-  static constexpr int SPT = (G::SG + T - 1) / T;     // ghosted cells per thread
-  static constexpr int NPL = D == 3 ? NC : 1;         // interior planes of a box
-  static constexpr int PCH = NC * G::NG * 8 / 16;     // 16-byte chunks of a plane's interior rows
-  static constexpr bool OK = T % 32 == 0 && G::SI % T == 0 && (G::NG * 8) % 16 == 0 && SPT <= 32;
+  static constexpr int LT = G::SI / CR < 256 ? G::SI / CR : 256;  // threads of a leaf
+  static constexpr int LPB = 256 / LT;                  // leaves of an iteration
+  static constexpr int T = LT * LPB;                    // threads of a block
+  static constexpr int WPL = LT / 32;                   // warps of a leaf
+  static constexpr int CPT = G::SI / LT;                // interior cells per thread
+  static constexpr int NEED = 2 * D * G::NF;            // face ghosts of a leaf
+  static constexpr int IPT = (NEED + LT - 1) / LT;      // face ghosts per thread
+  static constexpr int SPT = (G::SG + LT - 1) / LT;     // ghosted cells per thread
+  static constexpr int NPL = D == 3 ? NC : 1;           // interior planes of a box
+  static constexpr int PCH = NC * G::NG * 8 / 16;       // 16-byte chunks of a plane's interior rows
+  static constexpr bool OK = LT >= 32 && LT % 32 == 0 && 256 % LT == 0 && G::SI % LT == 0 &&
+                             (G::NG * 8) % 16 == 0 && SPT <= 32;
 };
 
-template <int D, int NC>
-__global__ void __launch_bounds__(256, 5)
+template <int D, int NC, int CR>
+__global__ void __launch_bounds__(256, CR >= 4 ? 4 : 5)
 k_defect_fx(Meta m, BoxSet bs, const double* __restrict__ u, const double* __restrict__ f,
             float* __restrict__ r32, unsigned long long* __restrict__ norm_per_tree) {
   pdl_trigger();  // the first descriptors are copied before pdl_wait() (they never change)
-  using C = DefectFxCfg<D, NC>;
+  using C = DefectFxCfg<D, NC, CR>;
   using G = Geo<D, NC>;
   static_assert(C::OK, "k_defect_fx block shape");
-  __shared__ __align__(16) double sb[2][G::SG];
-  __shared__ __align__(16) SlotDesc sd[3];
+  constexpr int L = C::LPB;
+  __shared__ __align__(16) double sb[2][L][G::SG];
+  __shared__ __align__(16) SlotDesc sd[3][L];
   __shared__ int s_em[2][C::T / 32];
   __shared__ float s_mx[2][C::T / 32];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int lb = tid / C::LT, lt = tid % C::LT;  // this thread's leaf in an iteration, its thread there
+  const int groups = (bs.n + L - 1) / L;
   const int first = blockIdx.x, step = gridDim.x;
-  const int my = first < bs.n ? (bs.n - 1 - first) / step + 1 : 0;
+  const int my = first < groups ? (groups - 1 - first) / step + 1 : 0;
   if (my == 0) {
     pdl_wait();
     return;
   }
-  unsigned rmask = 0;  // ghosted cells tid + T j that the stencil reads
+  unsigned rmask = 0;  // ghosted cells lt + LT j that the stencil reads
 #pragma unroll
   for (int j = 0; j < C::SPT; ++j) {
-    const int e = tid + C::T * j;
+    const int e = lt + C::LT * j;
     if (e < G::SG && stencil_reads<D, NC>(e)) rmask |= 1u << j;
   }
-  auto slot_of = [&](int k) { return box_at(bs, first + k * step); };
-  auto copy_desc = [&](int k, int s) {
-    if (tid < (int)sizeof(SlotDesc) / 16)
-      cp_async16(reinterpret_cast<char*>(&sd[k % 3]) + 16 * tid,
-                 reinterpret_cast<const char*>(m.desc + s) + 16 * tid);
+  // index in the set of this thread's leaf at iteration k, and its slot
+  // (-1 past the end of the set)
+  auto leaf_of = [&](int k) { return (first + k * step) * L + lb; };
+  auto slot_of = [&](int k) {
+    const int li = leaf_of(k);
+    return li < bs.n ? box_at(bs, li) : -1;
   };
-  // Leaf k's rows j = 1..NC of the planes k = 1..NC (the one plane in 2-D):
+  auto copy_desc = [&](int k, int s) {
+    if (s >= 0 && lt < (int)sizeof(SlotDesc) / 16)
+      cp_async16(reinterpret_cast<char*>(&sd[k % 3][lb]) + 16 * lt,
+                 reinterpret_cast<const char*>(m.desc + s) + 16 * lt);
+  };
+  // A leaf's rows j = 1..NC of the planes k = 1..NC (the one plane in 2-D):
   // its interior with the x ghosts between the rows, contiguous per plane.
   // The ghost planes and rows are not read: every face ghost the stencil
   // reads is computed from its sources below, edges and corners are unused.
-  auto copy_box = [&](int k) {
-    const char* src = reinterpret_cast<const char*>(u + sd[k % 3].offg);
-    char* dst = reinterpret_cast<char*>(sb[k & 1]);
-    for (int c = tid; c < C::NPL * C::PCH; c += C::T) {
+  auto copy_box = [&](int k, int s) {
+    if (s < 0) return;
+    const char* src = reinterpret_cast<const char*>(u + sd[k % 3][lb].offg);
+    char* dst = reinterpret_cast<char*>(sb[k & 1][lb]);
+    for (int c = lt; c < C::NPL * C::PCH; c += C::LT) {
       const int off = 8 * (G::NG + (D == 3 ? (c / C::PCH + 1) * G::NG * G::NG : 0)) + 16 * (c % C::PCH);
       cp_async16(dst + off, src + off);
     }
@@ -2622,7 +2639,7 @@ k_defect_fx(Meta m, BoxSet bs, const double* __restrict__ u, const double* __res
   int it_f[C::IPT], it_g[C::IPT], it_n[C::IPT], it_a[C::IPT], it_lin[C::IPT];
 #pragma unroll
   for (int j = 0; j < C::IPT; ++j) {
-    const int r = tid + C::T * j;
+    const int r = lt + C::LT * j;
     const int rr = r < C::NEED ? r : 0;
     const int fc = rr / G::NF, lin = rr % G::NF;
     const Face<D, NC> F(fc, lin % NC + 1, lin / NC + 1);
@@ -2635,15 +2652,20 @@ k_defect_fx(Meta m, BoxSet bs, const double* __restrict__ u, const double* __res
   int cpos[C::CPT];
 #pragma unroll
   for (int c = 0; c < C::CPT; ++c) {
-    const int q = tid + C::T * c;
+    const int q = lt + C::LT * c;
     cpos[c] = G::g(q % NC + 1, (q / NC) % NC + 1, (D == 3) ? q / (NC * NC) + 1 : 0);
   }
-  // Ghost sources and f of leaf k (its descriptor has landed) and its slot.
+  // Ghost sources and f of this thread's leaf at iteration k (its
+  // descriptor has landed), slot s (-1: none).
   auto fetch = [&](int k, int s, double (&gv)[C::IPT], double (&fv)[C::CPT]) {
-    const SlotDesc& d = sd[k % 3];
+#pragma unroll
+    for (int j = 0; j < C::IPT; ++j) gv[j] = 0.0;
+#pragma unroll
+    for (int c = 0; c < C::CPT; ++c) fv[c] = 0.0;
+    if (s < 0) return;
+    const SlotDesc& d = sd[k % 3][lb];
 #pragma unroll
     for (int j = 0; j < C::IPT; ++j) {
-      gv[j] = 0.0;
       const int fc = it_f[j];
       if (fc < 0) continue;
       const int code = d.code[fc];
@@ -2657,21 +2679,21 @@ k_defect_fx(Meta m, BoxSet bs, const double* __restrict__ u, const double* __res
       }
     }
 #pragma unroll
-    for (int c = 0; c < C::CPT; ++c) fv[c] = f[d.offi + tid + C::T * c];
+    for (int c = 0; c < C::CPT; ++c) fv[c] = f[d.offi + lt + C::LT * c];
   };
-  // max |r| of leaf k (per-warp maxima in s_mx[k & 1]) into the stripe of its
-  // tree (tree < 0: inactive, nothing to add); thread 0 only
+  // max |r| of this thread's leaf at iteration k (per-warp maxima in
+  // s_mx[k & 1]) into the stripe of its tree (tree < 0: inactive, nothing to
+  // add); the leaf's first thread only
   auto commit_norm = [&](int k, int tree) {
-    if (tid == 0 && tree >= 0) {
+    if (lt == 0 && tree >= 0) {
       float mx = 0.f;
 #pragma unroll
-      for (int w = 0; w < C::T / 32; ++w) mx = nanmaxf(mx, s_mx[k & 1][w]);
-      atomicMax(norm_per_tree + (size_t)tree * kStripes + ((first + k * step) & (kStripes - 1)),
-                dbits(f2d_exact(mx)));
+      for (int w = 0; w < C::WPL; ++w) mx = nanmaxf(mx, s_mx[k & 1][lb * C::WPL + w]);
+      atomicMax(norm_per_tree + (size_t)tree * kStripes + (leaf_of(k) & (kStripes - 1)), dbits(f2d_exact(mx)));
     }
   };
 
-  // prologue: descriptor of leaf 0, then its u and the descriptor of leaf 1
+  // prologue: descriptors of iteration 0, then its u and the descriptors of iteration 1
   int s_cur = slot_of(0);
   copy_desc(0, s_cur);
   int s_next = my > 1 ? slot_of(1) : -1;
@@ -2681,26 +2703,26 @@ k_defect_fx(Meta m, BoxSet bs, const double* __restrict__ u, const double* __res
   cp_async_wait<0>();
   __syncthreads();
   pdl_wait();  // u and the flags may have been written by the previous kernel
-  copy_box(0);
+  copy_box(0, s_cur);
   cp_async_commit();
   double gc[C::IPT], gn[C::IPT], fcv[C::CPT], fnv[C::CPT];
   fetch(0, s_cur, gc, fcv);
-  int tree_prev = -1;  // tree of the previous leaf if it was active (thread 0)
+  int tree_prev = -1;  // tree of this thread's previous leaf if it was active (a leaf's first thread)
 
   for (int k = 0; k < my; ++k) {
     cp_async_wait<0>();
-    __syncthreads();  // leaf k's u and leaf k + 1's descriptor have landed; leaf k - 1 is done
+    __syncthreads();  // iteration k's u and k + 1's descriptors have landed; iteration k - 1 is done
     if (k > 0) commit_norm(k - 1, tree_prev);
-    if (k + 1 < my) copy_box(k + 1);
+    if (k + 1 < my) copy_box(k + 1, s_next);
     if (k + 2 < my) copy_desc(k + 2, s_after);
     cp_async_commit();
     const int s_far = k + 3 < my ? slot_of(k + 3) : -1;
     if (k + 1 < my) fetch(k + 1, s_next, gn, fnv);
-    const SlotDesc& d = sd[k % 3];
-    double* bx = sb[k & 1];
-    const bool act = m.active[d.tree] != 0;
+    const SlotDesc& d = sd[k % 3][lb];
+    double* bx = sb[k & 1][lb];
+    // uniform over a warp (a leaf's threads are whole warps)
+    const bool act = s_cur >= 0 && m.active[d.tree] != 0;
     tree_prev = act ? d.tree : -1;
-    float mx = 0.f;
     if (act) {
 #pragma unroll
       for (int j = 0; j < C::IPT; ++j) {
@@ -2719,30 +2741,38 @@ k_defect_fx(Meta m, BoxSet bs, const double* __restrict__ u, const double* __res
       }
     }
     __syncthreads();
-    int em = 0;
     if (act) {
+      int em = 0;
 #pragma unroll
       for (int j = 0; j < C::SPT; ++j)
-        if (rmask & (1u << j)) em = max(em, dexp(bx[tid + C::T * j]));
+        if (rmask & (1u << j)) em = max(em, dexp(bx[lt + C::LT * j]));
       em = __reduce_max_sync(0xffffffffu, em);
       if (lane == 0) s_em[k & 1][warp] = em;
     }
     __syncthreads();
+    int emax = 0;
     if (act) {
-      int emax = 0;
 #pragma unroll
-      for (int w = 0; w < C::T / 32; ++w) emax = max(emax, s_em[k & 1][w]);
+      for (int w = 0; w < C::WPL; ++w) emax = max(emax, s_em[k & 1][lb * C::WPL + w]);
+    }
+    // the leaf's cells in fixed point in place (a leaf with an infinity or
+    // NaN keeps its doubles); every thread reaches the barrier
+    const bool fx = act && emax != 0x7ff;
+    long long* X = reinterpret_cast<long long*>(bx);
+    if (fx) {
+#pragma unroll
+      for (int j = 0; j < C::SPT; ++j)
+        if (rmask & (1u << j)) X[lt + C::LT * j] = to_fx(bx[lt + C::LT * j], emax);
+    }
+    __syncthreads();
+    if (act) {
+      float mx = 0.f;
       const double ninv = -d.inv_dx2;
       float* rb = r32 + d.offi;
-      if (emax != 0x7ff) {
-        long long* X = reinterpret_cast<long long*>(bx);
-#pragma unroll
-        for (int j = 0; j < C::SPT; ++j)
-          if (rmask & (1u << j)) X[tid + C::T * j] = to_fx(bx[tid + C::T * j], emax);
-        __syncthreads();
+      if (fx) {
 #pragma unroll
         for (int c = 0; c < C::CPT; ++c) {
-          const int q = tid + C::T * c;
+          const int q = lt + C::LT * c;
           const long long* x = X + cpos[c];
           constexpr int OY = G::NG, OZ = G::NG * G::NG;
           const long long xc = x[0];
@@ -2758,7 +2788,7 @@ k_defect_fx(Meta m, BoxSet bs, const double* __restrict__ u, const double* __res
       } else {
 #pragma unroll
         for (int c = 0; c < C::CPT; ++c) {
-          const int q = tid + C::T * c;
+          const int q = lt + C::LT * c;
           const int i = q % NC + 1, j = (q / NC) % NC + 1, kz = (D == 3) ? q / (NC * NC) + 1 : 0;
           double sum;
           if constexpr (D == 2)

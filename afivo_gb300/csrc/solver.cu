@@ -1132,6 +1132,7 @@ int Forest::autotune_all(int* sweep_out, int* small_out, int* coarse_out, float*
   use_small_sweeps = best_small;
   use_coarse_end = best_ce;
   coarse_end_levels = -1;
+  tune_defect(e0, e1, nullptr);
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   prof_mask = saved_mask;
@@ -1143,14 +1144,70 @@ int Forest::autotune_all(int* sweep_out, int* small_out, int* coarse_out, float*
   return check_device_error(err);
 }
 
+// The fixed-point defect's cells per thread, 1, 2 and 4 (those that exist
+// for the forest's box shape; ms3[k] = -1 for the others): five launches of
+// each alone, timed between e0 and e1 on the forest's stream; the fastest is
+// kept. The defect writes only the correction's right-hand side and the
+// norms, which every solve recomputes.
+void Forest::tune_defect(cudaEvent_t e0, cudaEvent_t e1, float* ms3) {
+  const int cands[3] = {1, 2, 4};
+  for (int k = 0; k < 3; ++k)
+    if (ms3) ms3[k] = -1.f;
+  if (!defect_fx || n_all_leaves() == 0) return;
+  int si = 1;
+  for (int d = 0; d < plan.dim; ++d) si *= plan.nc;
+  const int saved_mask = prof_mask;
+  prof_mask = 0;
+  float best_ms = 1e30f;
+  int best = defect_cells;
+  for (int k = 0; k < 3; ++k) {
+    defect_cells = cands[k];
+    if (defect_cr(si) != cands[k]) continue;
+    norm_reset();
+    launch_defect();  // warm-up
+    cudaEventRecord(e0, stream);
+    for (int r = 0; r < 5; ++r) {
+      norm_reset();
+      launch_defect();
+    }
+    cudaEventRecord(e1, stream);
+    cudaEventSynchronize(e1);
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms3) ms3[k] = ms / 5;
+    if (ms < best_ms) {
+      best_ms = ms;
+      best = cands[k];
+    }
+  }
+  defect_cells = best;
+  prof_mask = saved_mask;
+  drop_graphs();
+}
+
+int Forest::autotune_defect(int* cells, float* ms3, std::string& err) {
+  if (!mixed) return err = "autotune needs a forest created with mixed_buffers", AFV_ERR_STATE;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  tune_defect(e0, e1, ms3);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (cells) *cells = defect_cells;
+  if (int rc = check(err, "autotune_defect")) return rc;
+  return check_device_error(err);
+}
+
 // The sweep kernel alone (the first part of autotune_all): variants 1, 2, 0.
 int Forest::autotune(int* choice, float* ms_out, std::string& err) {
   if (!mixed) return err = "autotune needs a forest created with mixed_buffers", AFV_ERR_STATE;
   float ms[10];
   const bool small = use_small_sweeps, ce = use_coarse_end;
+  const int dc = defect_cells;
   int rc = autotune_all(choice, nullptr, nullptr, ms, err);
   use_small_sweeps = small;  // this entry point tunes the sweep kernel only
   use_coarse_end = ce;
+  defect_cells = dc;
   coarse_end_levels = -1;
   if (ms_out) {
     ms_out[0] = ms[1];
@@ -1389,36 +1446,61 @@ void Forest::restrict_tree_phi64() {
 // residual, or the FP64 defect written as the FP32 right-hand side of the
 // mixed cycle), the convergence flags, each active tree's cycle count and
 // last norm, and (readback) the active count copied to pinned host memory.
+// The cells per thread of the fixed-point defect for boxes of si cells: the
+// forest's choice when that shape exists for them, else the most of 4, 2, 1
+// that does (fewer, larger iterations: 4 in 16x16 and 8x8x8 boxes, 2 in 8x8
+// and 4x4x4 ones, the fastest of the three in each on GB300).
+int Forest::defect_cr(int si) const {
+  auto ok = [&](int cr) { return si / cr >= 32 && (si / cr >= 256 || 256 % (si / cr) == 0); };
+  if (defect_cells > 0 && ok(defect_cells)) return defect_cells;
+  return ok(4) ? 4 : ok(2) ? 2 : 1;
+}
+
+// The mixed solve's FP64 defect on the leaves into the FP32 right-hand side,
+// with max |r| per tree into the striped norms; ghost cells are pulled inside
+// the kernel.
+void Forest::launch_defect() {
+  Meta m = meta_of(meta);
+  const int nl = n_all_leaves();
+  BoxSet bs{d_lists + all_leaves_off, 0, nl};
+  with_nc(plan.dim, plan.nc, [&](auto d_, auto nc_) {
+    constexpr int D = decltype(d_)::value, NC = decltype(nc_)::value;
+    using G = dev::Geo<D, NC>;
+    constexpr int PER_BOX = G::SI < dev::kThreads ? G::SI : dev::kThreads;
+    constexpr int BPC = dev::boxes_per_cta<G::SG, PER_BOX, double>(1);
+    // read u (8 B), f (8 B); write r (4 B)
+    ProfScope ps(this, kProfDefect, 20.0 * nl * G::SI);
+    bool done = false;
+    auto fx = [&](auto cr_) {
+      constexpr int CR = decltype(cr_)::value;
+      using FC = dev::DefectFxCfg<D, NC, CR>;
+      if constexpr (FC::OK) {
+        const int occ = kernel_occupancy((const void*)dev::k_defect_fx<D, NC, CR>, FC::T, 0);
+        const long long groups = ((long long)nl + FC::LPB - 1) / FC::LPB;
+        const int grid = (int)std::max(1LL, std::min(groups, (long long)n_sm * occ));
+        launch_k(dev::k_defect_fx<D, NC, CR>, grid, FC::T, 0, stream, m, bs, (const double*)d64.phi,
+                 (const double*)d64.rhs, d32.rhs, d_norm);
+        done = true;
+      }
+    };
+    if (defect_fx) {
+      switch (defect_cr(G::SI)) {
+        case 1: fx(std::integral_constant<int, 1>{}); break;
+        case 4: fx(std::integral_constant<int, 4>{}); break;
+        default: fx(std::integral_constant<int, 2>{}); break;
+      }
+    }
+    if (!done)
+      launch_k(dev::k_defect<D, NC>, grid_for((nl + BPC - 1) / BPC, n_sm * 4), dev::kThreads, 0, stream, m, bs,
+               d64.phi, d64.rhs, d32.rhs, d_norm);
+  });
+}
+
 void Forest::enqueue_residual_check(int precision, double tol, int count_cycle) {
   const int nt = plan.n_trees;
-  Meta m = meta_of(meta);
   norm_reset();
   if (precision == AFV_PREC_MIXED) {
-    // FP64 defect on the leaves; ghost cells are pulled inside the kernel.
-    int nl = n_all_leaves();
-    BoxSet bs{d_lists + all_leaves_off, 0, nl};
-    with_nc(plan.dim, plan.nc, [&](auto d_, auto nc_) {
-      constexpr int D = decltype(d_)::value, NC = decltype(nc_)::value;
-      using G = dev::Geo<D, NC>;
-      constexpr int PER_BOX = G::SI < dev::kThreads ? G::SI : dev::kThreads;
-      constexpr int BPC = dev::boxes_per_cta<G::SG, PER_BOX, double>(1);
-      // read u (8 B), f (8 B); write r (4 B)
-      ProfScope ps(this, kProfDefect, 20.0 * nl * G::SI);
-      if constexpr (dev::DefectFxCfg<D, NC>::OK) {
-        if (defect_fx) {
-          constexpr int T = dev::DefectFxCfg<D, NC>::T;
-          const int occ = kernel_occupancy((const void*)dev::k_defect_fx<D, NC>, T, 0);
-          const int grid = (int)std::max(1LL, std::min((long long)nl, (long long)n_sm * occ));
-          launch_k(dev::k_defect_fx<D, NC>, grid, T, 0, stream, m, bs, (const double*)d64.phi,
-                   (const double*)d64.rhs, d32.rhs, d_norm);
-          return;
-        }
-      }
-      {
-        launch_k(dev::k_defect<D, NC>, grid_for((nl + BPC - 1) / BPC, n_sm * 4), dev::kThreads, 0, stream, m, bs,
-                 d64.phi, d64.rhs, d32.rhs, d_norm);
-      }
-    });
+    launch_defect();
   } else if (generic()) {
     for (int l = plan.min_lvl; l <= plan.max_lvl; ++l) gen_residual(l, d_norm);
   } else {

@@ -419,7 +419,12 @@ int afv_forest_profile_read(afv_forest* f, int kind, long long* launches, double
  * exchanges page-locked host arrays (afv_forest_set_var / get_var) by kernel
  * loads and stores over the host link, without the device staging buffer;
  * 0 copies through the staging buffer with the copy engines, which leaves
- * the SMs to other work (another forest's solve) during the transfer. */
+ * the SMs to other work (another forest's solve) during the transfer.
+ * AFV_OPT_DEFECT_CELLS: cells per thread of the fixed-point defect (1, 2 or
+ * 4: a block of 256 threads takes 256 / (cells / this) leaves of a small box
+ * shape at a time), 0 (default) the most of 4, 2, 1 that the box shape
+ * allows; the same values for every setting. afv_forest_autotune_all sets
+ * it. */
 enum {
   AFV_OPT_SWEEP_KERNEL = 0,
   AFV_OPT_GRAPHS = 1,
@@ -430,7 +435,8 @@ enum {
   AFV_OPT_COARSE_END = 6,
   AFV_OPT_WAIT_LIMIT_US = 7,
   AFV_OPT_DIRECT_BOXES = 8,
-  AFV_OPT_ZERO_COPY = 9
+  AFV_OPT_ZERO_COPY = 9,
+  AFV_OPT_DEFECT_CELLS = 10
 };
 int afv_forest_set_option(afv_forest* f, int option, int value);
 int afv_forest_get_option(afv_forest* f, int option, int* value);
@@ -447,8 +453,18 @@ int afv_forest_autotune(afv_forest* f, int* choice, float* ms3);
  * and AFV_OPT_COARSE_END on and off with it and keeps the fastest pair.
  * choice3 receives (sweep kernel, small sweeps, coarse end); ms10 (may be
  * NULL) the ms per FP32 V-cycle of sweep kernels 0..5, then of the (small,
- * coarse end) settings (0,0), (0,1), (1,0), (1,1). Needs mixed_buffers. */
+ * coarse end) settings (0,0), (0,1), (1,0), (1,1). Last it times the
+ * fixed-point defect's cells per thread as afv_forest_autotune_defect does
+ * and keeps the fastest (AFV_OPT_DEFECT_CELLS). Needs mixed_buffers. */
 int afv_forest_autotune_all(afv_forest* f, int* choice3, float* ms10);
+/* No counterpart in the reference: times the mixed solve's fixed-point defect
+ * with 1, 2 and 4 cells per thread (five launches each on the current state;
+ * it writes only the correction's right-hand side and the norms, which every
+ * solve recomputes) and sets AFV_OPT_DEFECT_CELLS to the fastest. cells
+ * receives it; ms3 (may be NULL) the ms per launch of 1, 2 and 4, -1 for a
+ * shape the forest's boxes do not allow (and all three -1 with
+ * AFV_OPT_DEFECT_KERNEL 0). Needs mixed_buffers. */
+int afv_forest_autotune_defect(afv_forest* f, int* cells, float* ms3);
 
 /* No counterpart in the reference: the profiled event pairs one by one (up
  * to max; n_total receives how many were recorded): kernel kind, level,

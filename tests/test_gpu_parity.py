@@ -407,6 +407,41 @@ def test_defect_kernels_agree(gpu, which):
     assert compare_var(p1, ref, ot, spec["n_cell"], spec["dim"], True) < 1e-6
 
 
+@pytest.mark.parametrize("which", ["c1", "3d", "3d_nc4", "batch"])
+def test_defect_cells_agree(gpu, which):
+    """The fixed-point defect with 1, 2 and 4 cells per thread (one leaf or
+    several per block iteration) gives the same bits: each leaf's sums and
+    exponent do not depend on how its cells are spread over threads. The
+    autotuner keeps one of the shapes the boxes allow."""
+    if which == "batch":
+        specs = W.c4_random_2d(3, small=True)
+    elif which == "c1":
+        specs = [W.c1_poisson_2d()]
+    elif which == "3d_nc4":
+        specs = [dict(W.c2_poisson_3d(thr=3e-3, lvl_max=6), n_cell=4, dr=0.25)]
+    else:
+        specs = [W.c2_poisson_3d(thr=3e-3, lvl_max=5)]
+    out = []
+    for cells in (1, 2, 4):
+        g = gpu.Forest([W.build_tree(s) for s in specs], mixed=True)
+        for t, s in enumerate(specs):
+            g.set_source(t, s["gauss"], lpl=True)
+        g.set_option(gpu.AFV_OPT_DEFECT_CELLS, cells)
+        assert g.get_option(gpu.AFV_OPT_DEFECT_CELLS) == cells
+        cyc, rel, rc = g.solve(gpu.AFV_PREC_MIXED, tol=1e-8, max_cycles=60)
+        assert rc == 0 and max(rel) <= 1e-8
+        out.append((list(cyc), list(rel), [g.get_var(t, gpu.AFV_PHI) for t in range(len(specs))]))
+        if cells == 4:
+            choice, ms = g.autotune_defect()
+            assert choice in ms and g.get_option(gpu.AFV_OPT_DEFECT_CELLS) == choice
+            assert all(v > 0 for v in ms.values())
+        g.close()
+    for o in out[1:]:
+        assert o[0] == out[0][0] and o[1] == out[0][1]
+        for a, b in zip(o[2], out[0][2]):
+            assert np.array_equal(a, b)
+
+
 def test_mixed_solve_scale_invariant(gpu):
     """Scaling the right-hand side by 2^k scales every value of the mixed
     solve exactly (the fixed-point defect shifts its scale with the box's
@@ -430,17 +465,19 @@ def test_mixed_solve_scale_invariant(gpu):
 
 def test_defect_nonfinite_reports_divergence(gpu):
     """A box holding a NaN takes the FP64 sum, which carries the NaN into the
-    residual: both defect kernels report the solve as diverged."""
+    residual: both defect kernels report the solve as diverged (the fixed-
+    point one also with several leaves per block, the others in fixed point)."""
     spec = W.c1_poisson_2d()
     f, ot, _ = setup_pair(gpu, spec)
     rhs = f.get_var(0, gpu.AFV_RHS)
     phi = np.zeros_like(f.get_var(0, gpu.AFV_PHI, interior_only=True))
     phi[-1] = np.nan  # a cell of the last box, a leaf on the finest level
-    for opt in (1, 0):
+    for opt, cells in ((1, 1), (1, 2), (0, 0)):
         g = gpu.Forest([W.build_tree(spec)], mixed=True)
         g.set_var(0, gpu.AFV_RHS, rhs)
         g.set_var(0, gpu.AFV_PHI, phi, interior_only=True)
         g.set_option(gpu.AFV_OPT_DEFECT_KERNEL, opt)
+        g.set_option(gpu.AFV_OPT_DEFECT_CELLS, cells)
         cyc, rel, rc = g.solve(gpu.AFV_PREC_MIXED, tol=1e-8, max_cycles=5, check=False)
         assert rc == gpu.AFV_ERR_DIVERGED
         g.close()
