@@ -290,12 +290,13 @@ def test_mixed_batch_alone_vs_mix(gpu):
     assert max(outs) <= 1e-8
 
 
-@pytest.mark.parametrize("which", ["c1", "3d"])
+@pytest.mark.parametrize("which", ["c1", "c1_nc16", "3d"])
 def test_sweep_kernel_variants_agree(gpu, which):
     """Every sweep kernel variant (block-pipelined, warp-per-box with bulk
     copies in four warp / stage shapes, warp-per-box with per-lane copies)
     gives the oracle's bits, FP64 and mixed."""
-    spec = W.c1_poisson_2d() if which == "c1" else W.c2_poisson_3d(thr=3e-3, lvl_max=5)
+    spec = {"c1": W.c1_poisson_2d, "c1_nc16": lambda: dict(W.c1_poisson_2d(), n_cell=16, dr=1 / 16, lvl_max=6),
+            "3d": lambda: W.c2_poisson_3d(thr=3e-3, lvl_max=5)}[which]()
     f, ot, _ = setup_pair(gpu, spec)
     for _ in range(2):
         ot.vcycle()
@@ -315,6 +316,32 @@ def test_sweep_kernel_variants_agree(gpu, which):
         g.close()
     for m in mixed[1:]:
         assert np.array_equal(mixed[0], m)
+
+
+def test_sweep_kernel_variants_agree_batch(gpu):
+    """A forest of trees of different depths (a warp's boxes from several
+    trees): every sweep variant gives the same bits in FP64 V-cycles and
+    mixed solves, per tree."""
+    specs = W.c4_random_2d(5, small=True)
+    out = []
+    for sk in (0, 1, 2, 3, 4, 5):
+        g = gpu.Forest([W.build_tree(s) for s in specs], mixed=True)
+        for t, s in enumerate(specs):
+            g.set_source(t, s["gauss"], lpl=True)
+        g.set_option(gpu.AFV_OPT_SWEEP_KERNEL, sk)
+        for _ in range(2):
+            g.vcycle()
+        v = [g.get_var(t, gpu.AFV_PHI) for t in range(len(specs))]
+        g.zero(gpu.AFV_PHI)
+        cyc, rel, rc = g.solve(gpu.AFV_PREC_MIXED, tol=1e-8, max_cycles=60)
+        assert rc == 0 and max(rel) <= 1e-8
+        v += [g.get_var(t, gpu.AFV_PHI) for t in range(len(specs))]
+        out.append((list(cyc), v))
+        g.close()
+    for cyc, v in out[1:]:
+        assert cyc == out[0][0]
+        for a, b in zip(v, out[0][1]):
+            assert np.array_equal(a, b)
 
 
 @pytest.mark.parametrize("which", ["c1", "3d"])
