@@ -238,7 +238,15 @@ __global__ void k_coef(BoxSet bs, const long long* __restrict__ offg, const long
     const double* e = eps + offg[s];
     const int c = G::g(i, j, kz);
     const double a0 = e[c], a = e[c + nb_off<D, NC>(k)];
-    coef[(offi[s] + q) * (2 * D) + k] = qdiv(a0 * a, a0 + a);
+    const double p = a0 * a;
+    // Equal eps of a moderate size (2^-400 <= |eps| <= 2^500, so eps^2 is a
+    // normal number and a non-zero rounding error of it is at least 2^-904,
+    // which the fused multiply-add shows) whose square is exact: p / (2 eps)
+    // is eps / 2 in exact arithmetic, and the quotient and eps * 0.5 both
+    // round it the same way. Other values (0, tiny, huge, non-finite) divide.
+    const double ma = fabs(a0);
+    const bool exact_half = a0 == a && ma >= 0x1p-400 && ma <= 0x1p500 && fma(a0, a0, -p) == 0.0;
+    coef[(offi[s] + q) * (2 * D) + k] = exact_half ? a0 * 0.5 : qdiv(p, a0 + a);
   }
 }
 

@@ -73,7 +73,13 @@ def compare_var(gpu_flat, ora_flat, t, n_cell, dim, interior_only):
     for l in g:
         nc = n_cell if l >= 1 else n_cell >> (1 - l)
         m = interior_mask(nc, dim) if interior_only else face_mask(nc, dim)
-        d = np.abs(g[l] - o[l])[:, m]
+        a, b = g[l][:, m], o[l][:, m]
+        # identical values (infinities and NaNs included) differ by 0; a
+        # non-finite value against another value by infinity
+        same = (a == b) | (np.isnan(a) & np.isnan(b))
+        with np.errstate(invalid="ignore"):
+            d = np.where(same, 0.0, np.abs(a - b))
+        d[np.isnan(d)] = np.inf
         if d.size:
             worst = max(worst, float(d.max()) / scale)
     return worst

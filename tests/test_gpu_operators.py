@@ -36,7 +36,8 @@ def _eps(r):
 SPECS = {"2d": W.c1_poisson_2d(), "3d": W.c2_poisson_3d(thr=3e-3, lvl_max=5)}
 
 
-def _pair(afv, which, op):
+def _pair(afv, which, op, eps_fn=None):
+    eps_fn = eps_fn or _eps
     spec = SPECS[which]
     nc, dim = spec["n_cell"], spec["dim"]
     ot = oracle_tree(spec)
@@ -48,7 +49,7 @@ def _pair(afv, which, op):
     parts = []
     for lvl in range(ot.min_lvl, ot.highest_lvl + 1):
         ncl = nc if lvl >= 1 else nc >> (1 - lvl)
-        e = _eps(_centres(ot, lvl, ncl, dim))
+        e = eps_fn(_centres(ot, lvl, ncl, dim))
         ot.set_level(lvl, I_EPS, e)
         parts.append(e.ravel())
     f.set_var(0, I_EPS, np.concatenate(parts))
@@ -169,3 +170,23 @@ def test_eps_changed_between_calls(gpu):
         cyc, rel, rc = f.solve(gpu.AFV_PREC_FP64, tol=1e-8, max_cycles=60)
         assert rc == 0 and int(cyc[0]) == n
         _check(gpu, f, ot, spec)
+
+
+@pytest.mark.parametrize("scale", [1.0, 2.0 ** -450], ids=["unit", "tiny"])
+@pytest.mark.parametrize("which", ["2d", "3d"])
+def test_lpld_face_weights_all_branches(gpu, which, scale):
+    """eps of 0.1 (its square is inexact: the face weight divides), 3 (an
+    exact square: eps / 2 directly) and a smooth eps (unequal neighbours) in
+    one tree, and the same times 2^-450 (below the range of the shortcut):
+    V-cycles give the oracle's values, all finite."""
+    def eps(r):
+        x = r[..., 0]
+        return scale * np.where(x < 0.3, 0.1, np.where(x < 0.6, 3.0, 1.0 + r[..., 1]))
+    spec, ot, f = _pair(gpu, which, 1, eps_fn=eps)
+    for _ in range(2):
+        ot.vcycle(set_residual=True)
+        f.vcycle(set_residual=True)
+        _check(gpu, f, ot, spec)
+    for v in (gpu.AFV_PHI, gpu.AFV_TMP):
+        assert np.isfinite(f.get_var(0, v, interior_only=True)).all()
+    assert np.isfinite(f.get_var(0, gpu.AFV_RHS)).all()
