@@ -116,17 +116,21 @@ class _Resident:
 
 class Server:
     """Solve requests with resident per-shape forests under a device-memory
-    budget; `slots` workers run batches of at most `max_batch` requests."""
+    budget; `slots` workers run batches of at most `max_batch` requests, and
+    of at most `max_batch_cells` leaf cells where that is set (a batch of
+    large trees takes about as long per request as one of two, so a smaller
+    batch shortens the large requests' latency at little cost in rate)."""
 
     def __init__(self, device=0, budget_bytes=8 << 30, slots=4, max_batch=8,
                  precision=AFV_PREC_MIXED, tol=1e-8, max_cycles=60, keep_phi=False,
-                 forest_cls=Forest, build_tree=W.build_tree, max_per_shape=2):
+                 forest_cls=Forest, build_tree=W.build_tree, max_per_shape=2, max_batch_cells=None):
         self.device = device
         self.forest_cls = forest_cls  # the device forest type (a stand-in in host-only tests)
         self.build_tree = build_tree
         self.budget = int(budget_bytes)
         self.slots = slots
         self.max_batch = max_batch
+        self.max_batch_cells = max_batch_cells
         self.max_per_shape = max_per_shape  # resident forests of one shape at most
         self.precision = precision
         self.tol = tol
@@ -143,6 +147,12 @@ class Server:
 
     def resident_bytes(self):
         return sum(r.bytes for r in self.pool)
+
+    def _batch_cap(self, cells):
+        """Requests per batch for trees of `cells` leaf cells."""
+        if not self.max_batch_cells:
+            return self.max_batch
+        return max(1, min(self.max_batch, int(self.max_batch_cells // max(1, cells))))
 
     def _keep(self, rid):
         return self.keep_phi is True or (self.keep_phi and rid in self.keep_phi)
@@ -162,7 +172,7 @@ class Server:
                 res = None
                 per = self.tree_bytes.get(key)
                 if per is not None:
-                    k = max(1, min(self.max_batch, self.budget // per[0]))
+                    k = max(1, min(self._batch_cap(per[1]), self.budget // per[0]))
                     need = k * per[0]
                 else:
                     k, need = self.max_batch, 0  # sized once the tree is built
@@ -199,7 +209,7 @@ class Server:
             self.tree_bytes[res.key] = (per, tree.leaf_cells())
             while True:
                 others = self.resident_bytes() - res.bytes
-                k = min(self.max_batch, (self.budget - others) // per)
+                k = min(self._batch_cap(tree.leaf_cells()), (self.budget - others) // per)
                 if k < 1 and self._make_room(max(0, per - res.bytes)):
                     continue
                 if k >= 1:
@@ -240,7 +250,7 @@ class Server:
                                 res = _Resident(batch[0]["key"], None, 0, 0, 0)
                                 per = self.tree_bytes.get(res.key)
                                 if per is not None:
-                                    res.k = max(1, min(self.max_batch, self.budget // per[0]))
+                                    res.k = max(1, min(self._batch_cap(per[1]), self.budget // per[0]))
                                     res.bytes = res.k * per[0]
                                 self.pool.append(res)
                             res.busy = True

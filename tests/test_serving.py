@@ -111,6 +111,19 @@ def test_continuous_batching_overlaps_forests(monkeypatch):
     assert summ["queue_p50_ms"] >= 0 and summ["service_p50_ms"] > 0
 
 
+def test_batch_cell_cap(monkeypatch):
+    """With max_batch_cells, a shape's forests hold at most that many leaf
+    cells of trees (at least one tree): 3000-cell trees under a 7000-cell cap
+    go two per batch, 1000-cell trees take the request cap of 4."""
+    srv = _server(monkeypatch, 10, budget_bytes=10000, slots=2, max_batch=4, max_batch_cells=7000)
+    reqs = [dict(r, lvl_max=3 if k % 2 else 1) for k, r in enumerate(fake_requests(16, 0.0, 1))]
+    res = srv.serve(reqs, realtime=False)
+    big = [r.batch for r, q in zip(res, reqs) if q["lvl_max"] == 3]
+    small = [r.batch for r, q in zip(res, reqs) if q["lvl_max"] == 1]
+    assert max(big) <= 2 and max(small) <= 4 and max(small) > 2
+    assert S.summary(res)["requests"] == 16
+
+
 def test_oversized_request_is_refused(monkeypatch):
     srv = _server(monkeypatch, 10 ** 12, budget_bytes=1000)
     with pytest.raises(ValueError, match="over the budget"):
