@@ -127,6 +127,30 @@ class Clocks:
                 "samples": len(sm)}
 
 
+def cpu_model():
+    """The host CPU's model name and architecture (lscpu, else /proc/cpuinfo)."""
+    import platform
+    name = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().startswith("Model name:"):
+                name = line.split(":", 1)[1].strip()
+                break
+    except (OSError, subprocess.SubprocessError):
+        pass
+    if not name:
+        try:
+            with open("/proc/cpuinfo") as f:
+                for line in f:
+                    if line.lower().startswith(("model name", "cpu model")):
+                        name = line.split(":", 1)[1].strip()
+                        break
+        except OSError:
+            pass
+    return "%s (%s)" % (name or "unknown", platform.machine())
+
+
 def load_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -247,6 +271,7 @@ def run_reference(args, spec):
                   "ms_p50": float(np.percentile(secs, 50)) * 1e3,
                   "ms_p99": float(np.percentile(secs, 99)) * 1e3},
         "cpu_baseline": {"value": value, "unit": "unknowns/s", "cores": cores, "kind": "port",
+                         "cpu": cpu_model(),
                          "sample": f"{args.steps} FP64 solves of the full tree to {TOL:g} "
                                    f"(oracle: C++/OpenMP restatement of the reference solver, "
                                    f"{cores} threads)"},
@@ -905,7 +930,7 @@ def main():
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cores = os.cpu_count() or 1
         v, dt, n, osolve = cpu_baseline_sample(spec, cores)
-        cpu = {"value": v, "unit": "unknowns/s", "cores": cores, "kind": "port",
+        cpu = {"value": v, "unit": "unknowns/s", "cores": cores, "kind": "port", "cpu": cpu_model(),
                "sample": f"{n} FP64 solves of the full tree to {TOL:g} on the oracle "
                          f"({dt:.1f} s, {cores} threads; median rate)"}
         # the headline's solution (the last end-to-end mixed solve) and a GPU
