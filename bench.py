@@ -127,6 +127,49 @@ class Clocks:
                 "samples": len(sm)}
 
 
+def vcycle_bytes(trees, w=4):
+    """Algorithmic bytes of one FAS V(2,2) cycle over a set of trees, per
+    operator of the reference's schedule (src/m_aX_mg.f90:208-255), each
+    input read once and each output written once over its interior, ghost
+    fills 2w per face-ghost cell (no edges or corners). On level l above the
+    coarsest, with N_l interior cells and G_l face-ghost cells of all its
+    boxes: 8 half-sweeps 24 N_l w, their fills 16 G_l w, residual 3 N_l w,
+    restriction (2 + 2/2^D) N_l w, fills after restriction and correction
+    2 (G_{l-1} + G_l) w, coarse rhs 4 N_l/2^D w, parent difference
+    3 N_l/2^D w, correction (2 + 1/2^D) N_l w; the coarsest level's 4
+    half-sweeps and fills (12 N + 8 G) w."""
+    total = 0.0
+    for t in trees:
+        inf = t.info()
+        D, nc, l0, top = inf["dim"], inf["n_cell"], inf["min_lvl"], inf["highest_lvl"]
+        N, G = {}, {}
+        for l in range(l0, top + 1):
+            ncl = nc if l >= 1 else nc >> (1 - l)
+            nb = len(t.level(l)[0])
+            N[l], G[l] = nb * ncl ** D, nb * 2 * D * ncl ** (D - 1)
+        f = 1.0 / (1 << D)
+        total += (12 * N[l0] + 8 * G[l0]) * w
+        for l in range(l0 + 1, top + 1):
+            total += ((24 + 3 + (2 + 2 * f) + 4 * f + 3 * f + (2 + f)) * N[l] + 16 * G[l]
+                      + 2 * (G[l - 1] + G[l])) * w
+    return total
+
+
+def solve_roofline(trees, leaf_cells, cycles, ms, peak, peak_kind):
+    """Whole-solve roofline of a mixed solve: per outer iteration the FP32
+    V-cycle's algorithmic bytes plus the FP64 defect and accumulate (read u,
+    f, write r; read e, read and write u: 48 B per leaf cell), over the
+    solve's time."""
+    per_iter = vcycle_bytes(trees) + 48.0 * leaf_cells
+    total = per_iter * cycles
+    achieved = total / (ms / 1e3) / 1e9
+    return {"bound": "hbm", "algorithmic_bytes_per_iteration": per_iter, "iterations": cycles,
+            "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "peak_kind": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
+            "counts": "FP32 V(2,2) cycle by operator (vcycle_bytes) + 48 B per leaf cell of FP64 "
+                      "defect and accumulate, per iteration; the solve's own CUDA-event time"}
+
+
 def cpu_model():
     """The host CPU's model name and architecture (lscpu, else /proc/cpuinfo)."""
     import platform
@@ -281,6 +324,22 @@ def run_reference(args, spec):
     print(json.dumps(line))
 
 
+def _batched_solve_roofline(trees, mine, forest, cyc, ms):
+    """solve_roofline of a batch: trees converge after their own number of
+    iterations (the solve stops a tree's work when it converges), so each
+    tree's bytes count for its own cycles."""
+    peak, peak_kind = load_peaks()
+    total = 0.0
+    for k, i in enumerate(mine):
+        t = trees[i]
+        total += (vcycle_bytes([t]) + 48.0 * t.leaf_cells()) * int(cyc[k])
+    achieved = total / (ms / 1e3) / 1e9
+    return {"bound": "hbm", "algorithmic_bytes": total, "achieved": round(achieved, 1), "peak": peak,
+            "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
+            "counts": "per tree: FP32 V(2,2) cycle by operator (vcycle_bytes) + 48 B per leaf cell of FP64 "
+                      "defect and accumulate, times the tree's iterations; the batch solve's CUDA-event time"}
+
+
 def run_batched(afv, W, local, rank, world, n_trees=256, check_errors=False):
     """Batched 2-D solves: 256 independent random quadtrees in one forest per
     GPU (trees placed over the ranks), one launch per level and operator for
@@ -353,6 +412,7 @@ def run_batched(afv, W, local, rank, world, n_trees=256, check_errors=False):
            "cycles_min": int(min(cyc)), "cycles_max": int(max(cyc)), "rel_res_max": float(max(rel)),
            "autotune_choice": choice, "autotune_ms_per_vcycle": {k: round(v, 3) for k, v in tune_ms.items()},
            "kernels_mixed_solve": kern, "roofline": roof,
+           "solve_roofline": _batched_solve_roofline(trees, mine, forest, cyc, ms),
            "tree_build_s": round(t_build, 2), "err_vs_fp64_oracle": errors}
     forest.close()
     return out
@@ -957,6 +1017,7 @@ def main():
         "fp64": {"value": value64, "unit": "unknowns/s", "cycles": cyc64, "rel_res": max(rels64),
                  "ms_per_solve": ms64 / len(cyc64), **errs64},
         "mixed_vs_fp64_solve_speedup": (ms64 / len(cyc64)) / (ms / args.steps),
+        "solve_roofline": solve_roofline([tree], cells, max(cyc), ms / args.steps, peak, peak_kind),
         "roofline": {"bound": "hbm", "kernel": "k_sweep_warp<3,8,float>",
                      "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None,
