@@ -337,7 +337,12 @@ def _batched_solve_roofline(trees, mine, forest, cyc, ms):
     return {"bound": "hbm", "algorithmic_bytes": total, "achieved": round(achieved, 1), "peak": peak,
             "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
             "counts": "per tree: FP32 V(2,2) cycle by operator (vcycle_bytes) + 48 B per leaf cell of FP64 "
-                      "defect and accumulate, times the tree's iterations; the batch solve's CUDA-event time"}
+                      "defect and accumulate, times the tree's iterations; the batch solve's CUDA-event time",
+            "gap": "below 0.6: the 8x8 boxes' half-sweep is bound by the warp's per-box work (about 291 "
+                   "warp instructions per box for 32 updated cells, 56-64 % issue active; "
+                   "profiles/k_sweep_warp_random2d_c4.md) and by the per-launch latency of levels that give "
+                   "each resident warp two boxes; the FP64 defect (650 us per launch, 2 cells per thread) is "
+                   "bound by instruction issue too"}
 
 
 def run_batched(afv, W, local, rank, world, n_trees=256, check_errors=False):
@@ -765,6 +770,29 @@ def profile_solves(spec, n):
             raise SystemExit(1)
 
 
+def profile_batched(n_trees, sweep_kernel=4):
+    """One mixed solve of the first n_trees trees of the 256-tree batch in one
+    forest, with the sweep variant the tuning pass picks for that batch (12
+    warps x 3 stages) and stream launches: the command the 2-D kernel
+    profiles are taken on."""
+    from afivo_gb300 import build as B
+    B.build()
+    import afivo_gb300 as afv
+    from afivo_gb300 import workloads as W
+    specs = W.c4_random_2d(256)[:n_trees]
+    forest = afv.Forest([W.build_tree(s) for s in specs], mixed=True)
+    for t, s in enumerate(specs):
+        forest.set_source(t, s["gauss"], lpl=True)
+    forest.set_option(afv.AFV_OPT_SWEEP_KERNEL, sweep_kernel)
+    forest.set_option(afv.AFV_OPT_GRAPHS, 0)
+    cyc, rel, rc = forest.solve(afv.AFV_PREC_MIXED, tol=TOL, max_cycles=60, check=False)
+    info = forest.info()
+    print(f"batch of {n_trees}: rc {rc}, leaf cells {info['leaf_cells']}, boxes {info['n_boxes']}, "
+          f"cycles {int(min(cyc))}..{int(max(cyc))}", flush=True)
+    if rc != 0:
+        raise SystemExit(1)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -780,6 +808,8 @@ def main():
                     help="skip the device tree build, operator, transfer and VTK measurements")
     ap.add_argument("--profile-solves", type=int, default=0,
                     help="only run this many mixed solves, untimed (a short command to profile)")
+    ap.add_argument("--profile-batched", type=int, default=0,
+                    help="only run one mixed solve of this many trees of the batch, untimed")
     args = ap.parse_args()
     from afivo_gb300 import workloads as W
     spec = W.c2_poisson_3d(thr=3e-3, lvl_max=7) if args.small else W.c2_poisson_3d()
@@ -789,6 +819,8 @@ def main():
         return run_reference(args, spec)
     if args.profile_solves:
         return profile_solves(spec, args.profile_solves)
+    if args.profile_batched:
+        return profile_batched(args.profile_batched)
 
     rank, world, local = dist_setup(args.gpus)
     import torch
