@@ -190,3 +190,31 @@ def test_lpld_face_weights_all_branches(gpu, which, scale):
     for v in (gpu.AFV_PHI, gpu.AFV_TMP):
         assert np.isfinite(f.get_var(0, v, interior_only=True)).all()
     assert np.isfinite(f.get_var(0, gpu.AFV_RHS)).all()
+
+
+def test_lpld_masked_solves(gpu):
+    """Masked FP64 solves with the variable-coefficient operator on a forest
+    of two copies of a tree: the leading tree alone (the solve limited to the
+    leading slots, face weights of those trees only) and the trailing tree
+    alone each give the solo forest's bits, and leave the other tree as it
+    was."""
+    spec, ot, solo = _pair(gpu, "2d", 1)
+    eps, rhs = solo.get_var(0, I_EPS), solo.get_var(0, gpu.AFV_RHS)
+    cyc, rel, rc = solo.solve(gpu.AFV_PREC_FP64, tol=1e-8, max_cycles=60)
+    assert rc == 0
+    ref = solo.get_var(0, gpu.AFV_PHI)
+    for mask in ([1, 0], [0, 1]):
+        g = gpu.Forest([W.build_tree(spec), W.build_tree(spec)])
+        g.add_vars(1, 0)
+        for t in (0, 1):
+            g.set_var(t, I_EPS, eps)
+            g.set_var(t, gpu.AFV_RHS, rhs)
+        g.set_operator(1, I_EPS)
+        before = [g.get_var(t, gpu.AFV_PHI) for t in (0, 1)]
+        c, r, rc = g.solve(gpu.AFV_PREC_FP64, tol=1e-8, max_cycles=60, mask=mask)
+        assert rc == 0
+        on, off = mask.index(1), mask.index(0)
+        assert int(c[on]) == int(cyc[0])
+        assert np.array_equal(g.get_var(on, gpu.AFV_PHI), ref)
+        assert np.array_equal(g.get_var(off, gpu.AFV_PHI), before[off])
+        g.close()
