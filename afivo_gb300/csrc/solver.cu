@@ -1442,10 +1442,6 @@ void Forest::restrict_tree_phi64() {
   fill_all64(false);
 }
 
-// One residual check, enqueued only: per-tree max |r| over the leaves (the FP64
-// residual, or the FP64 defect written as the FP32 right-hand side of the
-// mixed cycle), the convergence flags, each active tree's cycle count and
-// last norm, and (readback) the active count copied to pinned host memory.
 // The cells per thread of the fixed-point defect for boxes of si cells: the
 // forest's choice when that shape exists for them, else the most of 4, 2, 1
 // that does (fewer, larger iterations: 4 in 16x16 and 8x8x8 boxes, 2 in 8x8
@@ -1496,6 +1492,10 @@ void Forest::launch_defect() {
   });
 }
 
+// One residual check, enqueued only: per-tree max |r| over the leaves (the FP64
+// residual, or the FP64 defect written as the FP32 right-hand side of the
+// mixed cycle), the convergence flags, each active tree's cycle count and
+// last norm, and (readback) the active count copied to pinned host memory.
 void Forest::enqueue_residual_check(int precision, double tol, int count_cycle) {
   const int nt = plan.n_trees;
   norm_reset();
