@@ -312,16 +312,22 @@ __global__ void k_gsrb(Meta m, Op o, BoxSet bs, double* __restrict__ phi, const 
         const double a0 = e[c];
         double r1 = 1, r2 = 1;
         if (cyl) rfac(i, (o.ix[(size_t)s * D] - 1) * NC, r1, r2);
-        // 2 eps_0 eps / (eps_0 + eps) is exactly twice k_coef's weight: a
-        // factor 2 commutes with the rounding of the product and the quotient
-        // (for products and quotients in the normal range)
-        const double* w = (!cyl && o.coef) ? o.coef + (d.offi + G::in(i, j, D == 3 ? k : 1)) * (2 * D) : nullptr;
+        // 2 eps_0 eps / (eps_0 + eps) is exactly twice k_coef's weight when
+        // both eps lie within 2^-500..2^500 (by their exponents): the product
+        // and the quotient are then normal numbers, and a factor 2 commutes
+        // with their rounding. Other pairs divide as the reference does.
+        auto mid = [](double v) {
+          const unsigned ex = (unsigned)((unsigned long long)__double_as_longlong(v) >> 52) & 0x7ffu;
+          return ex >= 1023u - 500u && ex <= 1023u + 500u;
+        };
+        const double* w = (!cyl && o.coef && mid(a0)) ? o.coef + (d.offi + G::in(i, j, D == 3 ? k : 1)) * (2 * D)
+                                                       : nullptr;
         double cu = 0.0, cs = 0.0;
 #pragma unroll
         for (int kk = 0; kk < 2 * D; ++kk) {
           const int of = nb_off<D, NC>(kk);
           const double a = e[c + of];
-          const double ck = w ? 2 * w[kk] : qdiv(2 * a0 * a, a0 + a);
+          const double ck = (w && mid(a)) ? 2 * w[kk] : qdiv(2 * a0 * a, a0 + a);
           if (cyl) {
             const double rf = kk == 0 ? r1 : kk == 1 ? r2 : 1.0;
             cu = cu + ck * rf * u[c + of];

@@ -172,13 +172,15 @@ def test_eps_changed_between_calls(gpu):
         _check(gpu, f, ot, spec)
 
 
-@pytest.mark.parametrize("scale", [1.0, 2.0 ** -450], ids=["unit", "tiny"])
+@pytest.mark.parametrize("scale", [1.0, 2.0 ** -450, 1e-160], ids=["unit", "tiny", "subnormal_products"])
 @pytest.mark.parametrize("which", ["2d", "3d"])
 def test_lpld_face_weights_all_branches(gpu, which, scale):
     """eps of 0.1 (its square is inexact: the face weight divides), 3 (an
     exact square: eps / 2 directly) and a smooth eps (unequal neighbours) in
-    one tree, and the same times 2^-450 (below the range of the shortcut):
-    V-cycles give the oracle's values, all finite."""
+    one tree, and the same times 2^-450 (below the range of the shortcut)
+    and times 1e-160 (products of neighbouring eps below the normal range,
+    where the sweep divides instead of doubling the stored weight): V-cycles
+    give the oracle's values, all finite."""
     def eps(r):
         x = r[..., 0]
         return scale * np.where(x < 0.3, 0.1, np.where(x < 0.6, 3.0, 1.0 + r[..., 1]))
