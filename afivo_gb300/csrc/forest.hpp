@@ -301,7 +301,8 @@ class Forest {
   void enqueue_iteration(const MgOpts& mg, int precision, double tol);
   void enqueue_residual_check(int precision, double tol, int count_cycle = 1);
   void launch_defect();
-  int defect_cr(int si) const;
+  int defect_shapes() const;
+  int defect_cr() const;
   void tune_defect(cudaEvent_t e0, cudaEvent_t e1, float* ms3);
   int autotune_defect(int* cells, float* ms3, std::string& err);
   void enqueue_solve_begin(int precision, double tol, int max_cycles, const cudaGraphConditionalHandle* h);

@@ -2570,15 +2570,20 @@ struct DefectFxCfg {
   static constexpr int LT = G::SI / CR < 256 ? G::SI / CR : 256;  // threads of a leaf
   static constexpr int LPB = 256 / LT;                  // leaves of an iteration
   static constexpr int T = LT * LPB;                    // threads of a block
-  static constexpr int WPL = LT / 32;                   // warps of a leaf
+  static constexpr int SEG = LT < 32 ? LT : 32;         // lanes of a reduction segment (one leaf's, or a warp)
+  static constexpr int SPL = LT / SEG;                  // segments of a leaf
+  static constexpr int NSEG = T / SEG;                  // segments of a block
   static constexpr int CPT = G::SI / LT;                // interior cells per thread
   static constexpr int NEED = 2 * D * G::NF;            // face ghosts of a leaf
   static constexpr int IPT = (NEED + LT - 1) / LT;      // face ghosts per thread
   static constexpr int SPT = (G::SG + LT - 1) / LT;     // ghosted cells per thread
   static constexpr int NPL = D == 3 ? NC : 1;           // interior planes of a box
   static constexpr int PCH = NC * G::NG * 8 / 16;       // 16-byte chunks of a plane's interior rows
-  static constexpr bool OK = LT >= 32 && LT % 32 == 0 && 256 % LT == 0 && G::SI % LT == 0 &&
-                             (G::NG * 8) % 16 == 0 && SPT <= 32;
+  // static shared memory: two staged leaves per iteration slot, three
+  // descriptor slots, the segments' exponents and maxima (at most 48 KB)
+  static constexpr int SMEM = 2 * LPB * G::SG * 8 + 3 * LPB * (int)sizeof(SlotDesc) + 2 * NSEG * 8;
+  static constexpr bool OK = LT >= 16 && (LT % 32 == 0 || 32 % LT == 0) && 256 % LT == 0 &&
+                             G::SI % LT == 0 && (G::NG * 8) % 16 == 0 && SPT <= 32 && SMEM <= 48 * 1024;
 };
 
 template <int D, int NC, int CR>
@@ -2592,9 +2597,10 @@ k_defect_fx(Meta m, BoxSet bs, const double* __restrict__ u, const double* __res
   constexpr int L = C::LPB;
   __shared__ __align__(16) double sb[2][L][G::SG];
   __shared__ __align__(16) SlotDesc sd[3][L];
-  __shared__ int s_em[2][C::T / 32];
-  __shared__ float s_mx[2][C::T / 32];
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  __shared__ int s_em[2][C::NSEG];
+  __shared__ float s_mx[2][C::NSEG];
+  const int tid = threadIdx.x;
+  const int seg = tid / C::SEG, first_of_seg = (tid % C::SEG) == 0;
   const int lb = tid / C::LT, lt = tid % C::LT;  // this thread's leaf in an iteration, its thread there
   const int groups = (bs.n + L - 1) / L;
   const int first = blockIdx.x, step = gridDim.x;
@@ -2681,14 +2687,14 @@ k_defect_fx(Meta m, BoxSet bs, const double* __restrict__ u, const double* __res
 #pragma unroll
     for (int c = 0; c < C::CPT; ++c) fv[c] = f[d.offi + lt + C::LT * c];
   };
-  // max |r| of this thread's leaf at iteration k (per-warp maxima in
+  // max |r| of this thread's leaf at iteration k (per-segment maxima in
   // s_mx[k & 1]) into the stripe of its tree (tree < 0: inactive, nothing to
   // add); the leaf's first thread only
   auto commit_norm = [&](int k, int tree) {
     if (lt == 0 && tree >= 0) {
       float mx = 0.f;
 #pragma unroll
-      for (int w = 0; w < C::WPL; ++w) mx = nanmaxf(mx, s_mx[k & 1][lb * C::WPL + w]);
+      for (int w = 0; w < C::SPL; ++w) mx = nanmaxf(mx, s_mx[k & 1][lb * C::SPL + w]);
       atomicMax(norm_per_tree + (size_t)tree * kStripes + (leaf_of(k) & (kStripes - 1)), dbits(f2d_exact(mx)));
     }
   };
@@ -2720,7 +2726,7 @@ k_defect_fx(Meta m, BoxSet bs, const double* __restrict__ u, const double* __res
     if (k + 1 < my) fetch(k + 1, s_next, gn, fnv);
     const SlotDesc& d = sd[k % 3][lb];
     double* bx = sb[k & 1][lb];
-    // uniform over a warp (a leaf's threads are whole warps)
+    // uniform over a leaf's threads (whole warps, or a segment of a warp)
     const bool act = s_cur >= 0 && m.active[d.tree] != 0;
     tree_prev = act ? d.tree : -1;
     if (act) {
@@ -2741,19 +2747,28 @@ k_defect_fx(Meta m, BoxSet bs, const double* __restrict__ u, const double* __res
       }
     }
     __syncthreads();
-    if (act) {
+    {
+      // every lane reduces (0 for an inactive leaf): a segment may be half
+      // a warp whose other half is another leaf
       int em = 0;
+      if (act) {
 #pragma unroll
-      for (int j = 0; j < C::SPT; ++j)
-        if (rmask & (1u << j)) em = max(em, dexp(bx[lt + C::LT * j]));
-      em = __reduce_max_sync(0xffffffffu, em);
-      if (lane == 0) s_em[k & 1][warp] = em;
+        for (int j = 0; j < C::SPT; ++j)
+          if (rmask & (1u << j)) em = max(em, dexp(bx[lt + C::LT * j]));
+      }
+      if constexpr (C::SEG == 32) {
+        em = __reduce_max_sync(0xffffffffu, em);
+      } else {
+#pragma unroll
+        for (int o = C::SEG / 2; o > 0; o >>= 1) em = max(em, __shfl_xor_sync(0xffffffffu, em, o));
+      }
+      if (act && first_of_seg) s_em[k & 1][seg] = em;
     }
     __syncthreads();
     int emax = 0;
     if (act) {
 #pragma unroll
-      for (int w = 0; w < C::WPL; ++w) emax = max(emax, s_em[k & 1][lb * C::WPL + w]);
+      for (int w = 0; w < C::SPL; ++w) emax = max(emax, s_em[k & 1][lb * C::SPL + w]);
     }
     // the leaf's cells in fixed point in place (a leaf with an infinity or
     // NaN keeps its doubles); every thread reaches the barrier
@@ -2765,8 +2780,8 @@ k_defect_fx(Meta m, BoxSet bs, const double* __restrict__ u, const double* __res
         if (rmask & (1u << j)) X[lt + C::LT * j] = to_fx(bx[lt + C::LT * j], emax);
     }
     __syncthreads();
+    float mx = 0.f;
     if (act) {
-      float mx = 0.f;
       const double ninv = -d.inv_dx2;
       float* rb = r32 + d.offi;
       if (fx) {
@@ -2802,10 +2817,11 @@ k_defect_fx(Meta m, BoxSet bs, const double* __restrict__ u, const double* __res
           mx = nanmaxf(mx, fabsf(r));
         }
       }
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) mx = nanmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-      if (lane == 0) s_mx[k & 1][warp] = mx;
     }
+    // every lane reduces within its segment (0 for an inactive leaf)
+#pragma unroll
+    for (int o = C::SEG / 2; o > 0; o >>= 1) mx = nanmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if (act && first_of_seg) s_mx[k & 1][seg] = mx;
 #pragma unroll
     for (int j = 0; j < C::IPT; ++j) gc[j] = gn[j];
 #pragma unroll

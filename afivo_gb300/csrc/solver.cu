@@ -1154,15 +1154,14 @@ void Forest::tune_defect(cudaEvent_t e0, cudaEvent_t e1, float* ms3) {
   for (int k = 0; k < 3; ++k)
     if (ms3) ms3[k] = -1.f;
   if (!defect_fx || n_all_leaves() == 0) return;
-  int si = 1;
-  for (int d = 0; d < plan.dim; ++d) si *= plan.nc;
+  const int shapes = defect_shapes();
   const int saved_mask = prof_mask;
   prof_mask = 0;
   float best_ms = 1e30f;
   int best = defect_cells;
   for (int k = 0; k < 3; ++k) {
+    if (!(shapes & cands[k])) continue;
     defect_cells = cands[k];
-    if (defect_cr(si) != cands[k]) continue;
     norm_reset();
     launch_defect();  // warm-up
     cudaEventRecord(e0, stream);
@@ -1442,14 +1441,26 @@ void Forest::restrict_tree_phi64() {
   fill_all64(false);
 }
 
-// The cells per thread of the fixed-point defect for boxes of si cells: the
-// forest's choice when that shape exists for them, else the most of 4, 2, 1
-// that does (fewer, larger iterations: 4 in 16x16 and 8x8x8 boxes, 2 in 8x8
-// and 4x4x4 ones, the fastest of the three in each on GB300).
-int Forest::defect_cr(int si) const {
-  auto ok = [&](int cr) { return si / cr >= 32 && (si / cr >= 256 || 256 % (si / cr) == 0); };
-  if (defect_cells > 0 && ok(defect_cells)) return defect_cells;
-  return ok(4) ? 4 : ok(2) ? 2 : 1;
+// The fixed-point defect's shapes for the forest's leaf boxes: bit c set
+// when c cells per thread (1, 2, 4) exist for them.
+int Forest::defect_shapes() const {
+  int bits = 0;
+  with_nc(plan.dim, plan.nc, [&](auto d_, auto nc_) {
+    constexpr int D = decltype(d_)::value, NC = decltype(nc_)::value;
+    if constexpr (dev::DefectFxCfg<D, NC, 1>::OK) bits |= 1;
+    if constexpr (dev::DefectFxCfg<D, NC, 2>::OK) bits |= 2;
+    if constexpr (dev::DefectFxCfg<D, NC, 4>::OK) bits |= 4;
+  });
+  return bits;
+}
+
+// Cells per thread of the fixed-point defect: the forest's choice when that
+// shape exists, else the most of 4, 2, 1 that does (fewer, larger
+// iterations); 0 when none does (the FP64 sum, k_defect).
+int Forest::defect_cr() const {
+  const int bits = defect_shapes();
+  if (defect_cells > 0 && (bits & defect_cells)) return defect_cells;
+  return (bits & 4) ? 4 : (bits & 2) ? 2 : (bits & 1) ? 1 : 0;
 }
 
 // The mixed solve's FP64 defect on the leaves into the FP32 right-hand side,
@@ -1480,10 +1491,11 @@ void Forest::launch_defect() {
       }
     };
     if (defect_fx) {
-      switch (defect_cr(G::SI)) {
+      switch (defect_cr()) {
         case 1: fx(std::integral_constant<int, 1>{}); break;
+        case 2: fx(std::integral_constant<int, 2>{}); break;
         case 4: fx(std::integral_constant<int, 4>{}); break;
-        default: fx(std::integral_constant<int, 2>{}); break;
+        default: break;  // no shape for these boxes: the FP64 sum
       }
     }
     if (!done)

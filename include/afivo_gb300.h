@@ -422,9 +422,9 @@ int afv_forest_profile_read(afv_forest* f, int kind, long long* launches, double
  * the SMs to other work (another forest's solve) during the transfer.
  * AFV_OPT_DEFECT_CELLS: cells per thread of the fixed-point defect (1, 2 or
  * 4: a block of 256 threads takes 256 / (cells / this) leaves of a small box
- * shape at a time), 0 (default) the most of 4, 2, 1 that the box shape
- * allows; the same values for every setting. afv_forest_autotune_all sets
- * it. */
+ * shape at a time, at least 16 threads per leaf, within 48 KB of shared
+ * memory), 0 (default) the most of 4, 2, 1 that the box shape allows; the
+ * same values for every setting. afv_forest_autotune_all sets it. */
 enum {
   AFV_OPT_SWEEP_KERNEL = 0,
   AFV_OPT_GRAPHS = 1,

@@ -403,13 +403,14 @@ def _steep_spec(dim):
                 crit=W.AFV_REF_UNIFORM, lvl_max=4 if dim == 2 else 3)
 
 
-@pytest.mark.parametrize("which", ["c1", "3d", "steep2d", "steep3d"])
+@pytest.mark.parametrize("which", ["c1", "c1_nc4", "3d", "steep2d", "steep3d"])
 def test_defect_kernels_agree(gpu, which):
     """The mixed solve's defect with the fixed-point Laplacian (default) and
     with the FP64 sum: same cycle counts, residuals within float rounding,
     solutions within the solve tolerance of each other and of the oracle,
     also for a source with steep jumps inside boxes."""
-    spec = {"c1": W.c1_poisson_2d, "3d": lambda: W.c2_poisson_3d(thr=3e-3, lvl_max=5),
+    spec = {"c1": W.c1_poisson_2d, "c1_nc4": lambda: dict(W.c1_poisson_2d(), n_cell=4, dr=0.25, lvl_max=8, thr=1e-6),
+            "3d": lambda: W.c2_poisson_3d(thr=3e-3, lvl_max=5),
             "steep2d": lambda: _steep_spec(2), "steep3d": lambda: _steep_spec(3)}[which]()
     f, ot, _ = setup_pair(gpu, spec)
     rhs = f.get_var(0, gpu.AFV_RHS)
@@ -434,16 +435,19 @@ def test_defect_kernels_agree(gpu, which):
     assert compare_var(p1, ref, ot, spec["n_cell"], spec["dim"], True) < 1e-6
 
 
-@pytest.mark.parametrize("which", ["c1", "3d", "3d_nc4", "batch"])
+@pytest.mark.parametrize("which", ["c1", "c1_nc4", "3d", "3d_nc4", "batch"])
 def test_defect_cells_agree(gpu, which):
     """The fixed-point defect with 1, 2 and 4 cells per thread (one leaf or
-    several per block iteration) gives the same bits: each leaf's sums and
-    exponent do not depend on how its cells are spread over threads. The
-    autotuner keeps one of the shapes the boxes allow."""
+    several per block iteration, 16 or more threads per leaf: two leaves per
+    warp at 16) gives the same bits: each leaf's sums and exponent do not
+    depend on how its cells are spread over threads. The autotuner keeps one
+    of the shapes the boxes allow."""
     if which == "batch":
         specs = W.c4_random_2d(3, small=True)
     elif which == "c1":
         specs = [W.c1_poisson_2d()]
+    elif which == "c1_nc4":
+        specs = [dict(W.c1_poisson_2d(), n_cell=4, dr=0.25, lvl_max=8, thr=1e-6)]
     elif which == "3d_nc4":
         specs = [dict(W.c2_poisson_3d(thr=3e-3, lvl_max=6), n_cell=4, dr=0.25)]
     else:
