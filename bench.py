@@ -341,7 +341,7 @@ def _batched_solve_roofline(trees, mine, forest, cyc, ms):
             "gap": "below 0.6: the 8x8 boxes' half-sweep is bound by the warp's per-box work (about 291 "
                    "warp instructions per box for 32 updated cells, 56-64 % issue active; "
                    "profiles/k_sweep_warp_random2d_c4.md) and by the per-launch latency of levels that give "
-                   "each resident warp two boxes; the FP64 defect (650 us per launch, 2 cells per thread) is "
+                   "each resident warp two boxes; the FP64 defect (520 us per launch, 4 cells per thread) is "
                    "bound by instruction issue too"}
 
 
