@@ -985,20 +985,29 @@ def main():
         f.set_option(afv.AFV_OPT_ZERO_COPY, 0)
     for k in (0, 1):  # the staging buffers
         e2e_step(k)
-    barrier(world)
-    torch.cuda.synchronize()
-    first_in.clear()
-    t0 = time.perf_counter()
-    threads = [threading.Thread(target=worker, args=(k, (args.steps + 1 - k) // 2)) for k in (0, 1)]
-    for th in threads:
-        th.start()
-    for th in threads:
-        th.join()
-    torch.cuda.synchronize()
-    if errors:
-        raise errors[0]
-    e2e_s = max_over_ranks(time.perf_counter() - t0, world)
-    e2e_value = cells * sum_over_ranks(float(sum(done)), world) / e2e_s
+
+    def pipelined():
+        """One timed run of `steps` steps over the two threads; its rate."""
+        done[0] = done[1] = 0
+        barrier(world)
+        torch.cuda.synchronize()
+        first_in.clear()
+        t0 = time.perf_counter()
+        threads = [threading.Thread(target=worker, args=(k, (args.steps + 1 - k) // 2)) for k in (0, 1)]
+        for th in threads:
+            th.start()
+        for th in threads:
+            th.join()
+        torch.cuda.synchronize()
+        if errors:
+            raise errors[0]
+        secs = max_over_ranks(time.perf_counter() - t0, world)
+        return cells * sum_over_ranks(float(sum(done)), world) / secs
+
+    # three timed runs, the median reported: a run of a few steps over two
+    # host threads is exposed to the host's scheduling
+    e2e_runs = [pipelined() for _ in range(3)]
+    e2e_value = float(np.median(e2e_runs))
     e2e_same = bool(np.array_equal(host_phi[0].numpy(), host_phi[1].numpy()))
     forest.set_option(afv.AFV_OPT_ZERO_COPY, zero_copy)
     twin.close()
@@ -1080,6 +1089,7 @@ def main():
                             "engines, through a staging buffer) overlap the other forest's solve; every "
                             "step copies rhs in and phi out",
                 "solutions_identical": e2e_same,
+                "runs": [round(v, 1) for v in e2e_runs], "of_runs": "median of three timed runs",
                 "note": "with two solves in flight each fills the other's idle gaps on the coarse "
                         "levels, so the pipelined rate can exceed the single-solve device rate",
                 "serial": {"value": e2e_serial, "ms_per_step": 1e3 * e2e_serial_s / args.steps}},
